@@ -1,0 +1,137 @@
+/*
+ * qkgw.h -- C ABI of the GB300-native restricted G0W0 / evGW library (libqkgw.so).
+ *
+ * Conventions (the same as QuAcK's existing GPU module, src/cuda/src/ph_drpa_sing.c:17-18
+ * bound from Fortran in src/GPU/cu_quack_module.f90:25-36):
+ *   - every integer is a C int passed by value (Fortran: integer(c_int), value);
+ *   - every array is a double* into a Fortran column-major array, caller-owned;
+ *   - host-pointer entry points copy in, compute on the GPU, copy out and return when done;
+ *   - *_dev entry points take device pointers and return once the work is complete;
+ *   - every function returns a status (QK_OK = 0).  Unlike the reference module, which prints and
+ *     calls exit() on a CUDA error (src/cuda/src/utils.cu:10-16), nothing here exits the host.
+ *
+ * Array meanings (0-based C offsets of the Fortran arrays):
+ *   ERI(p,q,r,s) = <pq|rs> at p + N*(q + N*(r + N*s))               (N = nOrb)
+ *   Aph/Bph(ia,jb), ia = (i-nC)*nv + (a-nO), at ia + nS*jb          (nv = nOrb-nO-nR)
+ *   XpY/XmY(m,ia) at m + nS*ia  (row m = excitation, CPU orientation of LR/phRLR.f90:77-81)
+ *   rho(p,q,m) at p + N*(q + N*m)
+ *
+ * A context is single-stream and not thread-safe: use one per host thread.
+ */
+#ifndef QKGW_H
+#define QKGW_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct qk_ctx qk_ctx;
+
+enum {
+  QK_OK = 0,
+  QK_ERR_ARG = 1,          /* invalid sizes / unsupported option values */
+  QK_ERR_CUDA = 2,         /* a CUDA runtime call failed (see qk_last_error_string) */
+  QK_ERR_NOMEM = 3,        /* device allocation failed */
+  QK_ERR_NOT_PD = 4,       /* reserved: A-B not positive definite (reported as warning flag) */
+  QK_ERR_NO_CONV = 5,      /* evGW did not converge in maxSCF cycles (evRGW.f90:190-198 stops) */
+  QK_ERR_UNSUPPORTED = 6,  /* option outside the supported path (e.g. TDA_W, triplet W in drivers) */
+  QK_ERR_DEVICE = 7,       /* a device-side check failed (bounded wait expired, bad index) */
+  QK_ERR_NO_DEVICE = 8     /* no CUDA device / library not built for this GPU */
+};
+
+/* precision tiers for the O(N^2 nS^2) contractions (excitation density, ERI slabs) */
+enum {
+  QK_PREC_FP64 = 0,        /* FP64 throughout (plain form) */
+  QK_PREC_BF16X3 = 1       /* BF16x3 split products on tcgen05, FP32 accumulation */
+};
+
+/* Options of the GW line of QuAcK's input/options (QuAcK/read_options.f90:242-267). */
+typedef struct qk_gw_params {
+  double eta;        /* eta_GW */
+  int linearize;     /* lin_GW */
+  int doSRG;         /* reg_GW  (SRG regularisation, flow s = 500, RG0W0.f90:98) */
+  int TDA_W;         /* must be 0: TDA screening is rejected with QK_ERR_UNSUPPORTED */
+  int maxSCF;        /* maxSCF_GW (evGW) */
+  double thresh;     /* thresh_GW (evGW) */
+  int max_diis;      /* max_diis_GW (evGW) */
+  int precision;     /* QK_PREC_* */
+} qk_gw_params;
+
+/* ---- context ------------------------------------------------------------------------------ */
+int qk_init(int device, qk_ctx** ctx);
+int qk_finalize(qk_ctx* ctx);
+const char* qk_last_error_string(const qk_ctx* ctx);
+/* Per-stage device times (ms) of the last driver call; names in qk_timing_name(i). */
+int qk_get_timings(const qk_ctx* ctx, double* ms, int n);
+const char* qk_timing_name(int i);
+int qk_num_timings(void);
+/* Count of this library's kernel launches since qk_init (diagnostics). */
+long long qk_launch_count(const qk_ctx* ctx);
+/* Release cached device workspace. */
+int qk_trim(qk_ctx* ctx);
+
+/* ---- stage-level drop-ins (host pointers) ------------------------------------------------- */
+/* LR/phRLR_A.f90:1-138 */
+int qk_phRLR_A(qk_ctx* ctx, int ispin, int dRPA, int nBas, int nC, int nO, int nV, int nR, int nS,
+               double lambda, const double* e, const double* ERI, double* Aph);
+/* LR/phRLR_B.f90:1-98 */
+int qk_phRLR_B(qk_ctx* ctx, int ispin, int dRPA, int nBas, int nC, int nO, int nV, int nR, int nS,
+               double lambda, const double* ERI, double* Bph);
+/* LR/phRLR.f90:1-97 (TDA must be 0) */
+int qk_phRLR(qk_ctx* ctx, int TDA, int nS, const double* Aph, const double* Bph,
+             double* EcRPA, double* Om, double* XpY, double* XmY);
+/* GW/RGW_excitation_density.f90:1-80 */
+int qk_RGW_excitation_density(qk_ctx* ctx, int nOrb, int nC, int nO, int nR, int nS,
+                              const double* ERI, const double* XpY, double* rho);
+/* GW/RGW_self_energy_diag.f90:1-113 */
+int qk_RGW_self_energy_diag(qk_ctx* ctx, double eta, int nBas, int nOrb, int nC, int nO, int nV,
+                            int nR, int nS, const double* e, const double* Om, const double* rho,
+                            double* EcGM, double* Sig, double* Z);
+/* GW/RGW_SRG_self_energy_diag.f90:1-160 */
+int qk_RGW_SRG_self_energy_diag(qk_ctx* ctx, double flow, int nBas, int nOrb, int nC, int nO,
+                                int nV, int nR, int nS, const double* e, const double* Om,
+                                const double* rho, double* EcGM, double* SigC, double* Z);
+/* GW/RGW_QP_graph.f90:1-97 (+ RGW_Re_SigC / RGW_Re_dSigC and their SRG twins).
+ * Z is in/out: orbitals whose Newton search fails keep their Z, as in the reference. */
+int qk_RGW_QP_graph(qk_ctx* ctx, int doSRG, double eta, double flow, int nBas, int nC, int nO,
+                    int nV, int nR, int nS, const double* eHF, const double* Om, const double* rho,
+                    const double* eGWlin, const double* eOld, double* eGW, double* Z);
+/* AOtoMO/AOtoMO_ERI_RHF.f90:1-55 */
+int qk_AOtoMO_ERI_RHF(qk_ctx* ctx, int nBas, int nOrb, const double* c, const double* ERI_AO,
+                      double* ERI_MO);
+/* utils/DIIS_extrapolation.f90:1-61: error/e are (n,max_diis) histories, updated in place;
+ * n_diis is the history length after this call's increment. */
+int qk_DIIS_extrapolation(qk_ctx* ctx, double* rcond, int n_err, int n_e, int n_diis,
+                          double* error, double* e, const double* error_in, double* e_inout);
+
+/* ---- driver-level (host pointers) --------------------------------------------------------- */
+/* GW/RG0W0.f90:109-233.  Om receives the screening (first Casida) energies; EcRPA the
+ * correlation energy of the second Casida at eGW (the dumped "G0W0 correlation energy"). */
+int qk_RG0W0(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
+             int nR, int nS, const double* eHF, const double* ERI, double* eGW, double* SigC,
+             double* Z, double* Om, double* EcRPA, double* EcGM);
+/* GW/evRGW.f90:110-198.  Returns QK_ERR_NO_CONV (results still written) when maxSCF is hit. */
+int qk_evRGW(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
+             int nR, int nS, const double* eHF, const double* ERI, double* eGW, double* SigC,
+             double* Z, double* EcRPA, double* EcGM, int* nSCF, double* Conv);
+
+/* ---- driver-level (device pointers; inputs resident in HBM) ------------------------------- */
+int qk_RG0W0_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
+                 int nR, int nS, const double* d_eHF, const double* d_ERI, double* d_eGW,
+                 double* d_SigC, double* d_Z, double* d_Om, double* EcRPA, double* EcGM);
+int qk_evRGW_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
+                 int nR, int nS, const double* d_eHF, const double* d_ERI, double* d_eGW,
+                 double* d_SigC, double* d_Z, double* EcRPA, double* EcGM, int* nSCF,
+                 double* Conv);
+
+/* ---- dense symmetric eigensolver (device pointers; replaces dsyev('V','U') of
+ *      utils/wrap_lapack.f90:99-136 on the GPU).  A (n x n, lda) is destroyed; w ascending;
+ *      if want_vectors, Zt receives the eigenvectors as ROWS: Zt[j + n*i] = component i of
+ *      eigenvector j. ------------------------------------------------------------------------ */
+int qk_dsyev_dev(qk_ctx* ctx, int n, double* d_A, int lda, double* d_w, double* d_Zt,
+                 int want_vectors);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QKGW_H */

@@ -1,0 +1,451 @@
+"""CPU oracle for the restricted G0W0 / evGW call chain of QuAcK.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker that the CUDA library
+is compared against; it is imported only by ``tests/``, by
+``__graft_entry__.smoke()`` and by the ``cpu_baseline`` / ``--impl reference``
+legs of ``bench.py``.  Nothing in ``quack_gb300`` imports it and no product
+path routes through it.
+
+It restates QuAcK's Fortran (pfloos/QuAcK, ``src/``) in NumPy/SciPy, one
+function per reference routine, with the same loop bounds, index maps and
+product order (LAPACK ``dsyev('V','U')`` and ``dsysvx('N','U')`` through
+``scipy.linalg.lapack``).  Arrays follow the Fortran meaning of the reference
+arguments with 0-based indices: ``ERI[p,q,r,s]`` is ``ERI(p+1,q+1,r+1,s+1)``
+= <pq|rs> = (pr|qs) (physicist layout, PyDuck.py:342 + read_2e_integrals.f90:61),
+``rho[p,q,m]`` is ``rho(p+1,q+1,m+1)``, ``XpY[m,ia]`` is ``XpY(m+1,ia+1)``.
+
+Parity status: pinned end to end by the He/6-31G FeatherBench goldens
+(tests/feather_bench.py:86-91 of the reference) through ``oracle/he631g.py``.
+Eigenvectors are compared only up to sign / degenerate rotation.
+"""
+from __future__ import annotations
+
+import numpy as np
+from scipy.linalg import lapack
+
+HaToeV = 27.211386245988          # include/parameters.h:16
+
+
+# ---------------------------------------------------------------------------
+# LAPACK wrappers (src/utils/wrap_lapack.f90)
+# ---------------------------------------------------------------------------
+def diagonalize_matrix(A):
+    """dsyev('V','U') -- wrap_lapack.f90:99-136.  Returns (eigvecs, eigvals)."""
+    w, v, info = lapack.dsyev(np.asfortranarray(A), compute_v=1, lower=0)
+    if info != 0:
+        raise RuntimeError("Problem in diagonalize_matrix (dsyev)!! info=%d" % info)
+    return v, w
+
+
+def linear_solve(A, b):
+    """dsysvx('N','U') -- wrap_lapack.f90:560-598.  Returns (x, rcond)."""
+    out = lapack.dsysvx(np.asfortranarray(A), np.asfortranarray(b.reshape(-1, 1)), lower=0)
+    # scipy returns (a_s, udut, ipiv, b_s, x, rcond, ferr, berr, info)
+    x, rcond = out[4], out[5]
+    return np.asarray(x).reshape(-1), float(rcond)
+
+
+# ---------------------------------------------------------------------------
+# small matrix helpers (src/utils/utils.f90)
+# ---------------------------------------------------------------------------
+def ADAt(A, D):
+    """B = A.diag(D).A^T -- utils.f90:634-678 (tmp(i,j)=D(i)*A(j,i); dgemm(A,tmp))."""
+    tmp = D[:, None] * A.T
+    return A @ tmp
+
+
+def DA(D, A):
+    """A <- diag(D).A (row scaling) -- utils.f90:680-699."""
+    return D[:, None] * A
+
+
+def trace_matrix(A):
+    """utils.f90:328-352."""
+    return float(np.sum(np.diag(A)))
+
+
+def prepend(A, b):
+    """Shift columns right by one and put b in column 1 -- utils.f90:506-536."""
+    out = np.empty_like(A)
+    out[:, 1:] = A[:, :-1]
+    out[:, 0] = b
+    return out
+
+
+# ---------------------------------------------------------------------------
+# index helpers
+# ---------------------------------------------------------------------------
+def _ov(nBas, nC, nO, nR):
+    occ = np.arange(nC, nO)
+    vir = np.arange(nO, nBas - nR)
+    return occ, vir
+
+
+# ---------------------------------------------------------------------------
+# Linear response (src/LR)
+# ---------------------------------------------------------------------------
+def phRLR_A(ispin, dRPA, nBas, nC, nO, nV, nR, nS, lam, e, ERI):
+    """Resonant ph block -- LR/phRLR_A.f90:43-72 (singlet), :92-118 (triplet).
+
+    A(ia,jb) = ct1*ERI(b,i,j,a) + ct2*ERI(b,j,a,i) + delta_ij delta_ab (e_a - e_i),
+    ia = a - nO + (i-nC-1)*nn  (0-based: ia = (i-nC)*nn + (a-nO)).
+    """
+    occ, vir = _ov(nBas, nC, nO, nR)
+    no, nv = len(occ), len(vir)
+    assert no * nv == nS
+    delta = 1.0 if dRPA else 0.0
+    ct2 = -(1.0 - delta) * lam
+    if ispin == 1:
+        ct1 = 2.0 * lam
+        T1 = ERI[np.ix_(vir, occ, occ, vir)]          # [b,i,j,a]
+        A4 = ct1 * T1.transpose(1, 3, 2, 0)           # [i,a,j,b]
+    elif ispin == 2:
+        A4 = np.zeros((no, nv, no, nv))
+    else:
+        raise ValueError("ispin must be 1 or 2")
+    if ct2 != 0.0:
+        T2 = ERI[np.ix_(vir, occ, vir, occ)]          # [b,j,a,i]
+        A4 = A4 + ct2 * T2.transpose(3, 2, 1, 0)      # [i,a,j,b]
+    A = A4.reshape(nS, nS).copy()
+    ea = np.broadcast_to(e[vir][None, :], (no, nv)).reshape(nS)
+    ei = np.broadcast_to(e[occ][:, None], (no, nv)).reshape(nS)
+    di = np.diag_indices(nS)
+    A[di] = (A[di] + ea) - ei           # Aph(ia,jb) + e(a) - e(i), evaluated left to right
+    return A
+
+
+def phRLR_B(ispin, dRPA, nBas, nC, nO, nV, nR, nS, lam, ERI):
+    """Coupling ph block -- LR/phRLR_B.f90:34-59 (singlet), :78-98 (triplet).
+
+    B(ia,jb) = ct1*ERI(b,i,j,a) + ct2*ERI(b,j,i,a).
+    """
+    occ, vir = _ov(nBas, nC, nO, nR)
+    no, nv = len(occ), len(vir)
+    assert no * nv == nS
+    delta = 1.0 if dRPA else 0.0
+    ct2 = -(1.0 - delta) * lam
+    if ispin == 1:
+        T1 = ERI[np.ix_(vir, occ, occ, vir)]          # [b,i,j,a]
+        B4 = 2.0 * lam * T1.transpose(1, 3, 2, 0)
+    elif ispin == 2:
+        B4 = np.zeros((no, nv, no, nv))
+    else:
+        raise ValueError("ispin must be 1 or 2")
+    if ct2 != 0.0:
+        T2 = ERI[np.ix_(vir, occ, occ, vir)]          # [b,j,i,a]
+        B4 = B4 + ct2 * T2.transpose(2, 3, 1, 0)      # [i,a,j,b]
+    return B4.reshape(nS, nS).copy()
+
+
+def phRLR(TDA, nS, Aph, Bph):
+    """Casida solve -- LR/phRLR.f90:45-95.
+
+    Returns (EcRPA, Om, XpY, XmY) with XpY[m, ia] (row m = excitation).
+    """
+    if TDA:
+        Zv, Om = diagonalize_matrix(Aph)
+        XpY = Zv.T.copy()
+        XmY = XpY.copy()
+    else:
+        ApB = Aph + Bph
+        AmB = Aph - Bph
+        U, lam = diagonalize_matrix(AmB)                      # phRLR.f90:54
+        AmBSq = ADAt(U, 1.0 * np.sqrt(lam))                   # :59
+        AmBIv = ADAt(U, 1.0 / np.sqrt(lam))                   # :60
+        tmp = ApB @ AmBSq                                     # :62
+        Zm = AmBSq @ tmp                                      # :63
+        Zv, Om = diagonalize_matrix(Zm)                       # :67
+        Om = np.sqrt(np.abs(Om))                              # :76
+        XpY = DA(1.0 / np.sqrt(Om), Zv.T @ AmBSq)             # :77-78
+        XmY = DA(1.0 * np.sqrt(Om), Zv.T @ AmBIv)             # :80-81
+    EcRPA = 0.5 * (float(np.sum(Om)) - trace_matrix(Aph))     # :95
+    return EcRPA, Om, XpY, XmY
+
+
+# ---------------------------------------------------------------------------
+# GW kernels (src/GW)
+# ---------------------------------------------------------------------------
+def RGW_excitation_density(nOrb, nC, nO, nR, nS, ERI, XpY):
+    """rho(p,q,m) = sum_jb ERI(p,j,q,b) XpY(m,jb) -- GW/RGW_excitation_density.f90:30-50.
+
+    jb runs j = nC+1..nO (outer), b = nO+1..nOrb-nR (inner).  The reference
+    gathers tmp(p,q,jb) over all p,q and multiplies by XpY^T (dgemm 'N','T').
+    """
+    occ, vir = _ov(nOrb, nC, nO, nR)
+    tmp = ERI[:, occ][:, :, :, vir]                          # [p,j,q,b]
+    tmp = tmp.transpose(0, 2, 1, 3).reshape(nOrb, nOrb, nS)  # [p,q,jb]
+    rho = (tmp.reshape(nOrb * nOrb, nS) @ XpY.T).reshape(nOrb, nOrb, nS)
+    return rho
+
+
+def RGW_self_energy_diag(eta, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho):
+    """Diagonal Sigma_c, Z and EcGM -- GW/RGW_self_energy_diag.f90:35-111.
+
+    Returns (EcGM, Sig, Z).
+    """
+    occ, vir = _ov(nBas, nC, nO, nR)
+    act = np.arange(nC, nBas - nR)
+    Sig = np.zeros(nBas)
+    dZ = np.zeros(nBas)
+    eta2 = eta * eta
+    for p in act:
+        # occupied part (:44-62): eps = e(p) - e(i) + Om(m)
+        eps = e[p] - e[occ][:, None] + Om[None, :]           # [i,m]
+        num = 2.0 * rho[p, occ, :] ** 2
+        Sig[p] += np.sum(num * eps / (eps ** 2 + eta2))
+        dZ[p] -= np.sum(num * (eps ** 2 - eta2) / (eps ** 2 + eta2) ** 2)
+        # virtual part (:66-84): eps = e(p) - e(a) - Om(m)
+        eps = e[p] - e[vir][:, None] - Om[None, :]
+        num = 2.0 * rho[p, vir, :] ** 2
+        Sig[p] += np.sum(num * eps / (eps ** 2 + eta2))
+        dZ[p] -= np.sum(num * (eps ** 2 - eta2) / (eps ** 2 + eta2) ** 2)
+    # Galitskii-Migdal (:88-107): eps = e(a) - e(i) + Om(m)
+    eps = e[vir][:, None, None] - e[occ][None, :, None] + Om[None, None, :]
+    num = 4.0 * rho[np.ix_(vir, occ, np.arange(nS))] ** 2
+    EcGM = -float(np.sum(num * eps / (eps ** 2 + eta2)))
+    Z = 1.0 / (1.0 - dZ)                                      # :111
+    return EcGM, Sig, Z
+
+
+def RGW_SRG_self_energy_diag(flow, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho):
+    """SRG-regularised diagonal Sigma_c, Z, EcGM -- GW/RGW_SRG_self_energy_diag.f90:55-158."""
+    occ, vir = _ov(nOrb, nC, nO, nR)
+    act = np.arange(nC, nOrb - nR)
+    s = flow
+    SigC = np.zeros(nOrb)
+    dZ = np.zeros(nOrb)
+    for p in act:
+        D = e[p] - e[occ][:, None] + Om[None, :]
+        r2 = 2.0 * rho[p, occ, :] ** 2
+        reg = 1.0 - np.exp(-2.0 * s * D * D)
+        SigC[p] += np.sum(r2 * reg / D)
+        dZ[p] -= np.sum(r2 * reg / D ** 2)
+        D = e[p] - e[vir][:, None] - Om[None, :]
+        r2 = 2.0 * rho[p, vir, :] ** 2
+        reg = 1.0 - np.exp(-2.0 * s * D * D)
+        SigC[p] += np.sum(r2 * reg / D)
+        dZ[p] -= np.sum(r2 * reg / D ** 2)
+    Z = 1.0 / (1.0 - dZ)
+    D = e[vir][:, None, None] - e[occ][None, :, None] + Om[None, None, :]
+    r = rho[np.ix_(vir, occ, np.arange(nS))]
+    EcGM = -float(np.sum(4.0 * r * r * (1.0 - np.exp(-2.0 * s * D * D)) / D))
+    return EcGM, SigC, Z
+
+
+def RGW_Re_SigC(p, w, eta, nBas, nC, nO, nV, nR, nS, e, Om, rho):
+    """GW/RGW_Re_SigC.f90:30-50."""
+    occ, vir = _ov(nBas, nC, nO, nR)
+    eta2 = eta * eta
+    eps = w - e[occ][:, None] + Om[None, :]
+    num = 2.0 * rho[p, occ, :] ** 2
+    s = np.sum(num * eps / (eps ** 2 + eta2))
+    eps = w - e[vir][:, None] - Om[None, :]
+    num = 2.0 * rho[p, vir, :] ** 2
+    return float(s + np.sum(num * eps / (eps ** 2 + eta2)))
+
+
+def RGW_Re_dSigC(p, w, eta, nBas, nC, nO, nV, nR, nS, e, Om, rho):
+    """GW/RGW_Re_dSigC.f90:30-50."""
+    occ, vir = _ov(nBas, nC, nO, nR)
+    eta2 = eta * eta
+    eps = w - e[occ][:, None] + Om[None, :]
+    num = 2.0 * rho[p, occ, :] ** 2
+    s = -np.sum(num * (eps ** 2 - eta2) / (eps ** 2 + eta2) ** 2)
+    eps = w - e[vir][:, None] - Om[None, :]
+    num = 2.0 * rho[p, vir, :] ** 2
+    return float(s - np.sum(num * (eps ** 2 - eta2) / (eps ** 2 + eta2) ** 2))
+
+
+def RGW_SRG_Re_SigC(p, w, flow, nBas, nC, nO, nV, nR, nS, e, Om, rho):
+    """GW/RGW_SRG_Re_SigC.f90."""
+    occ, vir = _ov(nBas, nC, nO, nR)
+    s = flow
+    D = w - e[occ][:, None] + Om[None, :]
+    v = np.sum(2.0 * rho[p, occ, :] ** 2 * (1.0 - np.exp(-2.0 * s * D * D)) / D)
+    D = w - e[vir][:, None] - Om[None, :]
+    return float(v + np.sum(2.0 * rho[p, vir, :] ** 2 * (1.0 - np.exp(-2.0 * s * D * D)) / D))
+
+
+def RGW_SRG_Re_dSigC(p, w, flow, nBas, nC, nO, nV, nR, nS, e, Om, rho):
+    """GW/RGW_SRG_Re_dSigC.f90."""
+    occ, vir = _ov(nBas, nC, nO, nR)
+    s = flow
+    D = w - e[occ][:, None] + Om[None, :]
+    v = -np.sum(2.0 * rho[p, occ, :] ** 2 * (1.0 - np.exp(-2.0 * s * D * D)) / D ** 2)
+    D = w - e[vir][:, None] - Om[None, :]
+    return float(v - np.sum(2.0 * rho[p, vir, :] ** 2 * (1.0 - np.exp(-2.0 * s * D * D)) / D ** 2))
+
+
+QP_MAXIT = 64        # RGW_QP_graph.f90:38
+QP_THRESH = 1e-6     # RGW_QP_graph.f90:39
+
+
+def RGW_QP_graph(doSRG, eta, flow, nBas, nC, nO, nV, nR, nS, eHF, Om, rho, eGWlin, eOld, Z_in,
+                 return_iters=False):
+    """Newton root search of w - eHF(p) - SigC(w) = 0 -- GW/RGW_QP_graph.f90:50-92.
+
+    ``Z_in`` is the renormalisation factor on entry: the reference leaves Z(p)
+    untouched for orbitals whose Newton search fails (:78-81).  Returns
+    (eGW, Z) and, if asked, the per-orbital iteration counts.
+    """
+    eGW = np.array(eGWlin, dtype=np.float64, copy=True)
+    Z = np.array(Z_in, dtype=np.float64, copy=True)
+    iters = np.zeros(nBas, dtype=np.int64)
+    for p in range(nC, nBas - nR):
+        w = eGWlin[p]
+        nIt = 0
+        f = 1.0
+        df = 1.0
+        while abs(f) > QP_THRESH and nIt < QP_MAXIT:
+            nIt += 1
+            if doSRG:
+                SigC = RGW_SRG_Re_SigC(p, w, flow, nBas, nC, nO, nV, nR, nS, eOld, Om, rho)
+                dSigC = RGW_SRG_Re_dSigC(p, w, flow, nBas, nC, nO, nV, nR, nS, eOld, Om, rho)
+            else:
+                SigC = RGW_Re_SigC(p, w, eta, nBas, nC, nO, nV, nR, nS, eOld, Om, rho)
+                dSigC = RGW_Re_dSigC(p, w, eta, nBas, nC, nO, nV, nR, nS, eOld, Om, rho)
+            f = w - eHF[p] - SigC
+            df = 1.0 / (1.0 - dSigC)
+            w = w - df * f
+        iters[p] = nIt
+        if nIt == QP_MAXIT:
+            eGW[p] = eGWlin[p]
+        else:
+            eGW[p] = w
+            Z[p] = df
+    if return_iters:
+        return eGW, Z, iters
+    return eGW, Z
+
+
+# ---------------------------------------------------------------------------
+# DIIS (src/utils/DIIS_extrapolation.f90:1-61)
+# ---------------------------------------------------------------------------
+def DIIS_extrapolation(n_diis, error, e, error_in, e_inout):
+    """Returns (rcond, error, e, e_out).  ``error``/``e`` hold the history in
+    columns 0..n_diis-1 (column 0 = newest after prepend)."""
+    error = error.copy()
+    e = e.copy()
+    error[:, :n_diis] = prepend(error[:, :n_diis], error_in)        # :30
+    e[:, :n_diis] = prepend(e[:, :n_diis], e_inout)                 # :31
+    A = np.zeros((n_diis + 1, n_diis + 1))
+    A[:n_diis, :n_diis] = error[:, :n_diis].T @ error[:, :n_diis]   # :36
+    A[:n_diis, n_diis] = -1.0
+    A[n_diis, :n_diis] = -1.0
+    A[n_diis, n_diis] = 0.0
+    b = np.zeros(n_diis + 1)
+    b[n_diis] = -1.0
+    w, rcond = linear_solve(A, b)                                   # :50
+    e_out = np.array(e_inout, copy=True)
+    if rcond > 10e-14:                                              # :54
+        e_out = e[:, :n_diis] @ w[:n_diis]
+    return rcond, error, e, e_out
+
+
+# ---------------------------------------------------------------------------
+# AO -> MO (src/AOtoMO/AOtoMO_ERI_RHF.f90:26-53)
+# ---------------------------------------------------------------------------
+def AOtoMO_ERI_RHF(nBas, nOrb, c, ERI_AO):
+    """Four successive dgemm('T','N') quarter transforms.
+
+    In Fortran order each step contracts the first index and appends the new
+    MO index last; after four steps ERI_MO(p,q,r,s) = sum c(mu,p)...ERI_AO.
+    """
+    X = np.asfortranarray(ERI_AO)
+    for _ in range(4):
+        n0 = X.shape[0]
+        rest = X.shape[1:]
+        M = X.reshape(n0, -1, order="F")           # (nBas, prod(rest))
+        Y = M.T @ c                                # (prod(rest), nOrb)
+        X = Y.reshape(rest + (c.shape[1],), order="F")
+    return np.ascontiguousarray(X)
+
+
+# ---------------------------------------------------------------------------
+# Drivers (src/GW/RG0W0.f90, src/GW/evRGW.f90)
+# ---------------------------------------------------------------------------
+def RG0W0(linearize, eta, doSRG, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eHF, TDA_W=False):
+    """G0W0@RHF -- GW/RG0W0.f90:109-233 (dRPA singlet screening).
+
+    Returns a dict with eGW, SigC, Z, Om, XpY, rho, EcRPA (second Casida at
+    eGW, :222-225), EcGM, eGWlin and the first-Casida EcRPA.
+    """
+    if TDA_W:
+        raise NotImplementedError("TDA_W screening is not on the supported path")
+    flow = 500.0                                                     # :98
+    isp_W, dRPA_W = 1, True
+    Aph = phRLR_A(isp_W, dRPA_W, nOrb, nC, nO, nV, nR, nS, 1.0, eHF, ERI)
+    Bph = phRLR_B(isp_W, dRPA_W, nOrb, nC, nO, nV, nR, nS, 1.0, ERI)
+    EcRPA0, Om, XpY, XmY = phRLR(False, nS, Aph, Bph)
+    rho = RGW_excitation_density(nOrb, nC, nO, nR, nS, ERI, XpY)
+    if doSRG:
+        EcGM, SigC, Z = RGW_SRG_self_energy_diag(flow, nBas, nOrb, nC, nO, nV, nR, nS, eHF, Om, rho)
+    else:
+        EcGM, SigC, Z = RGW_self_energy_diag(eta, nBas, nOrb, nC, nO, nV, nR, nS, eHF, Om, rho)
+    eGWlin = eHF + Z * SigC                                          # :188
+    iters = None
+    if linearize:
+        eGW = eGWlin.copy()
+    else:
+        eGW, Z, iters = RGW_QP_graph(doSRG, eta, flow, nOrb, nC, nO, nV, nR, nS, eHF, Om, rho,
+                                     eGWlin, eHF, Z, return_iters=True)
+    Aph2 = phRLR_A(isp_W, dRPA_W, nOrb, nC, nO, nV, nR, nS, 1.0, eGW, ERI)
+    Bph2 = phRLR_B(isp_W, dRPA_W, nOrb, nC, nO, nV, nR, nS, 1.0, ERI)
+    EcRPA, Om2, _, _ = phRLR(False, nS, Aph2, Bph2)
+    return dict(eGW=eGW, SigC=SigC, Z=Z, Om=Om, XpY=XpY, XmY=XmY, rho=rho, EcRPA=EcRPA,
+                EcRPA_HF=EcRPA0, EcGM=EcGM, eGWlin=eGWlin, Om_GW=Om2, qp_iters=iters)
+
+
+def evRGW(maxSCF, thresh, max_diis, linearize, eta, doSRG, nBas, nOrb, nC, nO, nV, nR, nS,
+          ERI, eHF, TDA_W=False, raise_on_fail=True):
+    """evGW@RHF -- GW/evRGW.f90:110-198.
+
+    Returns a dict with eGW (after the last DIIS step), EcRPA (Casida of the
+    last cycle), SigC, Z, Conv, nSCF and the per-cycle Conv history.
+    """
+    if TDA_W:
+        raise NotImplementedError("TDA_W screening is not on the supported path")
+    flow = 500.0
+    ispin, dRPA = 1, True
+    nSCF = 0
+    n_diis = 0
+    Conv = 1.0
+    e_diis = np.zeros((nOrb, max(max_diis, 1)))
+    error_diis = np.zeros((nOrb, max(max_diis, 1)))
+    eGW = eHF.copy()
+    eOld = eGW.copy()
+    Z = np.ones(nOrb)
+    hist = []
+    EcRPA = EcGM = 0.0
+    SigC = np.zeros(nOrb)
+    while Conv > thresh and nSCF <= maxSCF:                          # :119
+        Aph = phRLR_A(ispin, dRPA, nOrb, nC, nO, nV, nR, nS, 1.0, eGW, ERI)
+        Bph = phRLR_B(ispin, dRPA, nOrb, nC, nO, nV, nR, nS, 1.0, ERI)
+        EcRPA, Om, XpY, XmY = phRLR(False, nS, Aph, Bph)
+        rho = RGW_excitation_density(nOrb, nC, nO, nR, nS, ERI, XpY)
+        if doSRG:
+            EcGM, SigC, Z = RGW_SRG_self_energy_diag(flow, nBas, nOrb, nC, nO, nV, nR, nS, eGW, Om, rho)
+        else:
+            EcGM, SigC, Z = RGW_self_energy_diag(eta, nBas, nOrb, nC, nO, nV, nR, nS, eGW, Om, rho)
+        if linearize:
+            eGW = eHF + SigC                                         # :147
+        else:
+            eGW, Z = RGW_QP_graph(doSRG, eta, flow, nOrb, nC, nO, nV, nR, nS, eHF, Om, rho,
+                                  eOld, eOld, Z)                     # :154
+        Conv = float(np.max(np.abs(eGW - eOld)))                     # :160
+        hist.append(Conv)
+        if max_diis > 1:                                             # :166-171
+            n_diis = min(n_diis + 1, max_diis)
+            _, error_diis, e_diis, eGW = DIIS_extrapolation(n_diis, error_diis, e_diis, eGW - eOld, eGW)
+        eOld = eGW.copy()                                            # :177
+        nSCF += 1
+    failed = (nSCF == maxSCF + 1)
+    if failed and raise_on_fail:
+        raise RuntimeError("evGW convergence failed")               # :190-198
+    return dict(eGW=eGW, EcRPA=EcRPA, EcGM=EcGM, SigC=SigC, Z=Z, Conv=Conv, nSCF=nSCF,
+                conv_hist=hist, failed=failed)
+
+
+def homo_lumo(eGW, nO):
+    """print_RG0W0.f90:27-29."""
+    return float(np.max(eGW[:nO])), float(np.min(eGW[nO:]))

@@ -1,0 +1,295 @@
+"""Python mirror of QuAcK's restricted G0W0/evGW call chain on top of libqkgw.so.
+
+Each function has the name, argument order and meaning of the Fortran subroutine it replaces
+(the C ABI in include/qkgw.h cites the reference file:line of each).  Arrays are numpy arrays
+indexed like the Fortran ones with 0-based indices (ERI[p,q,r,s] = ERI(p+1,q+1,r+1,s+1)); they
+are handed to the library in Fortran (column-major) memory order.  Every call runs on the GPU;
+there is no CPU fallback -- if the CUDA library is missing or no GB300 is visible the calls
+raise :class:`QkError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIBPATH = os.path.join(_HERE, "libqkgw.so")
+_lib = None
+
+QK_OK, QK_ERR_ARG, QK_ERR_CUDA, QK_ERR_NOMEM, QK_ERR_NOT_PD, QK_ERR_NO_CONV = 0, 1, 2, 3, 4, 5
+QK_ERR_UNSUPPORTED, QK_ERR_DEVICE, QK_ERR_NO_DEVICE = 6, 7, 8
+QK_PREC_FP64, QK_PREC_BF16X3 = 0, 1
+
+_dp = C.POINTER(C.c_double)
+
+
+class QkError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("qkgw error %d: %s" % (code, msg))
+        self.code = code
+
+
+class qk_gw_params(C.Structure):
+    _fields_ = [("eta", C.c_double), ("linearize", C.c_int), ("doSRG", C.c_int),
+                ("TDA_W", C.c_int), ("maxSCF", C.c_int), ("thresh", C.c_double),
+                ("max_diis", C.c_int), ("precision", C.c_int)]
+
+
+def lib():
+    """Load libqkgw.so (built in-tree by quack_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIBPATH):
+            raise QkError(QK_ERR_NO_DEVICE, "libqkgw.so not built (run quack_gb300.build.build())")
+        _lib = C.CDLL(_LIBPATH)
+        _lib.qk_last_error_string.restype = C.c_char_p
+        _lib.qk_timing_name.restype = C.c_char_p
+        _lib.qk_launch_count.restype = C.c_longlong
+        for name in ("qk_RGW_self_energy_diag", "qk_RGW_SRG_self_energy_diag", "qk_RGW_QP_graph",
+                     "qk_phRLR_A", "qk_phRLR_B"):
+            getattr(_lib, name).restype = C.c_int
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _f(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+class Context:
+    """A qk_ctx: one CUDA stream plus cached device workspace on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        rc = lib().qk_init(C.c_int(device), C.byref(self._h))
+        if rc != QK_OK:
+            raise QkError(rc, "qk_init failed (no usable sm_103a device?)")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, rc, allow=()):
+        if rc != QK_OK and rc not in allow:
+            raise QkError(rc, lib().qk_last_error_string(self._h).decode())
+        return rc
+
+    def timings(self):
+        L = lib()
+        n = L.qk_num_timings()
+        buf = (C.c_double * n)()
+        L.qk_get_timings(self._h, buf, n)
+        return {L.qk_timing_name(i).decode(): buf[i] for i in range(n)}
+
+    def launches(self) -> int:
+        return int(lib().qk_launch_count(self._h))
+
+    def close(self):
+        if self._h:
+            lib().qk_finalize(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default = None
+
+
+def default_context() -> Context:
+    global _default
+    if _default is None:
+        _default = Context(0)
+    return _default
+
+
+def _ctx(ctx):
+    return ctx if ctx is not None else default_context()
+
+
+# ------------------------------------------------------------------------------------------
+# stage-level drop-ins (same names/arguments as the Fortran subroutines)
+# ------------------------------------------------------------------------------------------
+def phRLR_A(ispin, dRPA, nBas, nC, nO, nV, nR, nS, lam, e, ERI, ctx=None):
+    """LR/phRLR_A.f90.  Returns Aph (nS, nS)."""
+    c = _ctx(ctx)
+    e, ERI = _f(e), _f(ERI)
+    out = np.empty((nS, nS), order="F")
+    c.check(lib().qk_phRLR_A(c.handle, ispin, int(bool(dRPA)), nBas, nC, nO, nV, nR, nS,
+                             C.c_double(lam), _ptr(e), _ptr(ERI), _ptr(out)))
+    return out
+
+
+def phRLR_B(ispin, dRPA, nBas, nC, nO, nV, nR, nS, lam, ERI, ctx=None):
+    """LR/phRLR_B.f90.  Returns Bph (nS, nS)."""
+    c = _ctx(ctx)
+    ERI = _f(ERI)
+    out = np.empty((nS, nS), order="F")
+    c.check(lib().qk_phRLR_B(c.handle, ispin, int(bool(dRPA)), nBas, nC, nO, nV, nR, nS,
+                             C.c_double(lam), _ptr(ERI), _ptr(out)))
+    return out
+
+
+def phRLR(TDA, nS, Aph, Bph, ctx=None):
+    """LR/phRLR.f90.  Returns (EcRPA, Om, XpY, XmY) with XpY[m, ia]."""
+    c = _ctx(ctx)
+    Aph, Bph = _f(Aph), _f(Bph)
+    Om = np.empty(nS)
+    XpY = np.empty((nS, nS), order="F")
+    XmY = np.empty((nS, nS), order="F")
+    Ec = C.c_double()
+    c.check(lib().qk_phRLR(c.handle, int(bool(TDA)), nS, _ptr(Aph), _ptr(Bph), C.byref(Ec),
+                           _ptr(Om), _ptr(XpY), _ptr(XmY)))
+    return Ec.value, Om, XpY, XmY
+
+
+def RGW_excitation_density(nOrb, nC, nO, nR, nS, ERI, XpY, ctx=None):
+    """GW/RGW_excitation_density.f90.  Returns rho (nOrb, nOrb, nS)."""
+    c = _ctx(ctx)
+    ERI, XpY = _f(ERI), _f(XpY)
+    rho = np.empty((nOrb, nOrb, nS), order="F")
+    c.check(lib().qk_RGW_excitation_density(c.handle, nOrb, nC, nO, nR, nS, _ptr(ERI), _ptr(XpY),
+                                            _ptr(rho)))
+    return rho
+
+
+def RGW_self_energy_diag(eta, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho, ctx=None):
+    """GW/RGW_self_energy_diag.f90.  Returns (EcGM, Sig, Z)."""
+    c = _ctx(ctx)
+    e, Om, rho = _f(e), _f(Om), _f(rho)
+    Sig = np.empty(nBas)
+    Z = np.empty(nBas)
+    gm = C.c_double()
+    c.check(lib().qk_RGW_self_energy_diag(c.handle, C.c_double(eta), nBas, nOrb, nC, nO, nV, nR,
+                                          nS, _ptr(e), _ptr(Om), _ptr(rho), C.byref(gm),
+                                          _ptr(Sig), _ptr(Z)))
+    return gm.value, Sig, Z
+
+
+def RGW_SRG_self_energy_diag(flow, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho, ctx=None):
+    """GW/RGW_SRG_self_energy_diag.f90.  Returns (EcGM, SigC, Z)."""
+    c = _ctx(ctx)
+    e, Om, rho = _f(e), _f(Om), _f(rho)
+    Sig = np.empty(nOrb)
+    Z = np.empty(nOrb)
+    gm = C.c_double()
+    c.check(lib().qk_RGW_SRG_self_energy_diag(c.handle, C.c_double(flow), nBas, nOrb, nC, nO, nV,
+                                              nR, nS, _ptr(e), _ptr(Om), _ptr(rho), C.byref(gm),
+                                              _ptr(Sig), _ptr(Z)))
+    return gm.value, Sig, Z
+
+
+def RGW_QP_graph(doSRG, eta, flow, nBas, nC, nO, nV, nR, nS, eHF, Om, rho, eGWlin, eOld, Z,
+                 ctx=None):
+    """GW/RGW_QP_graph.f90.  ``Z`` is the entry renormalisation factor (kept for orbitals whose
+    Newton search fails).  Returns (eGW, Z)."""
+    c = _ctx(ctx)
+    eHF, Om, rho, eGWlin, eOld = _f(eHF), _f(Om), _f(rho), _f(eGWlin), _f(eOld)
+    Zio = np.array(Z, dtype=np.float64, copy=True)
+    eGW = np.empty(nBas)
+    c.check(lib().qk_RGW_QP_graph(c.handle, int(bool(doSRG)), C.c_double(eta), C.c_double(flow),
+                                  nBas, nC, nO, nV, nR, nS, _ptr(eHF), _ptr(Om), _ptr(rho),
+                                  _ptr(eGWlin), _ptr(eOld), _ptr(eGW), _ptr(Zio)))
+    return eGW, Zio
+
+
+def AOtoMO_ERI_RHF(nBas, nOrb, c_mo, ERI_AO, ctx=None):
+    """AOtoMO/AOtoMO_ERI_RHF.f90.  Returns ERI_MO (nOrb,)*4."""
+    c = _ctx(ctx)
+    cm, E = _f(c_mo), _f(ERI_AO)
+    out = np.empty((nOrb,) * 4, order="F")
+    c.check(lib().qk_AOtoMO_ERI_RHF(c.handle, nBas, nOrb, _ptr(cm), _ptr(E), _ptr(out)))
+    return out
+
+
+def DIIS_extrapolation(n_err, n_e, n_diis, error, e, error_in, e_inout, ctx=None):
+    """utils/DIIS_extrapolation.f90.  ``error``/``e`` hold at least n_diis columns; they are
+    updated in place (prepend).  Returns (rcond, e_out)."""
+    c = _ctx(ctx)
+    assert error.flags.f_contiguous and e.flags.f_contiguous
+    err_in = _f(error_in)
+    eio = np.array(e_inout, dtype=np.float64, copy=True)
+    rc = C.c_double()
+    c.check(lib().qk_DIIS_extrapolation(c.handle, C.byref(rc), n_err, n_e, n_diis, _ptr(error),
+                                        _ptr(e), _ptr(err_in), _ptr(eio)))
+    return rc.value, eio
+
+
+# ------------------------------------------------------------------------------------------
+# drivers
+# ------------------------------------------------------------------------------------------
+@dataclass
+class GWOptions:
+    """GW line of QuAcK's options file (QuAcK/read_options.f90:242-267)."""
+    maxSCF: int = 64
+    thresh: float = 1e-5
+    max_diis: int = 1
+    linearize: bool = False
+    eta: float = 0.0
+    TDA_W: bool = False
+    reg: bool = False
+    precision: int = QK_PREC_FP64
+
+    def c(self):
+        return qk_gw_params(self.eta, int(self.linearize), int(self.reg), int(self.TDA_W),
+                            self.maxSCF, self.thresh, self.max_diis, self.precision)
+
+
+def RG0W0(opts: GWOptions, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eHF, ctx=None):
+    """GW/RG0W0.f90 (dRPA singlet W).  Returns dict(eGW, SigC, Z, Om, EcRPA, EcGM)."""
+    c = _ctx(ctx)
+    ERI, eHF = _f(ERI), _f(eHF)
+    eGW, SigC, Z, Om = np.empty(nOrb), np.empty(nOrb), np.empty(nOrb), np.empty(nS)
+    Ec, gm = C.c_double(), C.c_double()
+    prm = opts.c()
+    c.check(lib().qk_RG0W0(c.handle, C.byref(prm), nBas, nOrb, nC, nO, nV, nR, nS, _ptr(eHF),
+                           _ptr(ERI), _ptr(eGW), _ptr(SigC), _ptr(Z), _ptr(Om), C.byref(Ec),
+                           C.byref(gm)))
+    return dict(eGW=eGW, SigC=SigC, Z=Z, Om=Om, EcRPA=Ec.value, EcGM=gm.value)
+
+
+def evRGW(opts: GWOptions, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eHF, ctx=None, raise_on_fail=True):
+    """GW/evRGW.f90.  Returns dict(eGW, SigC, Z, EcRPA, EcGM, nSCF, Conv, failed)."""
+    c = _ctx(ctx)
+    ERI, eHF = _f(ERI), _f(eHF)
+    eGW, SigC, Z = np.empty(nOrb), np.empty(nOrb), np.empty(nOrb)
+    Ec, gm, conv = C.c_double(), C.c_double(), C.c_double()
+    nscf = C.c_int()
+    prm = opts.c()
+    rc = c.check(lib().qk_evRGW(c.handle, C.byref(prm), nBas, nOrb, nC, nO, nV, nR, nS, _ptr(eHF),
+                                _ptr(ERI), _ptr(eGW), _ptr(SigC), _ptr(Z), C.byref(Ec),
+                                C.byref(gm), C.byref(nscf), C.byref(conv)),
+                 allow=() if raise_on_fail else (QK_ERR_NO_CONV,))
+    return dict(eGW=eGW, SigC=SigC, Z=Z, EcRPA=Ec.value, EcGM=gm.value, nSCF=nscf.value,
+                Conv=conv.value, failed=(rc == QK_ERR_NO_CONV))
+
+
+def RG0W0_dev(opts: GWOptions, nOrb, nC, nO, nR, d_ERI, d_eHF, d_eGW, d_SigC, d_Z, d_Om,
+              ctx=None):
+    """Device-pointer driver: arguments are integer device addresses (e.g. tensor.data_ptr()).
+    Returns (EcRPA, EcGM)."""
+    c = _ctx(ctx)
+    nS = (nO - nC) * (nOrb - nO - nR)
+    Ec, gm = C.c_double(), C.c_double()
+    prm = opts.c()
+    c.check(lib().qk_RG0W0_dev(c.handle, C.byref(prm), nOrb, nOrb, nC, nO, nOrb - nO, nR, nS,
+                               C.c_void_p(d_eHF), C.c_void_p(d_ERI), C.c_void_p(d_eGW),
+                               C.c_void_p(d_SigC), C.c_void_p(d_Z), C.c_void_p(d_Om),
+                               C.byref(Ec), C.byref(gm)))
+    return Ec.value, gm.value
+
+
+def dsyev_dev(n, d_A, lda, d_w, d_Zt, want_vectors=True, ctx=None):
+    """GPU dsyev on device buffers (A destroyed; Zt rows are eigenvectors)."""
+    c = _ctx(ctx)
+    c.check(lib().qk_dsyev_dev(c.handle, n, C.c_void_p(d_A), lda, C.c_void_p(d_w),
+                               C.c_void_p(d_Zt), int(bool(want_vectors))))

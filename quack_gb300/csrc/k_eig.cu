@@ -1,0 +1,510 @@
+// k_eig.cu -- dense symmetric FP64 eigensolver, written for GB300.
+//
+// Replaces dsyev('V','U') (utils/wrap_lapack.f90:99-136) as used by LR/phRLR.f90:54,67.
+// Pipeline (all on the GPU, no vendor solver):
+//   1. k_sytrd: Householder tridiagonalisation (lower variant) in ONE persistent cooperative
+//      kernel.  Each iteration fuses the rank-2 update of step k with the symmetric mat-vec of
+//      step k+1, so the trailing matrix is streamed once per column (read+write); every CTA
+//      recomputes the O(n) vector work redundantly (bitwise identical in all CTAs), leaving
+//      one bounded grid barrier per column.
+//   2. k_stebz: Sturm-count bisection, one thread per eigenvalue, full FP64 precision.
+//   3. k_stein: inverse iteration on T - lambda I (tridiagonal GEPP), one thread per cluster of
+//      close eigenvalues, modified Gram-Schmidt inside clusters; eigenvectors written as rows.
+//   4. Blocked back-transformation E <- E * Q^T with compact-WY blocks of 64 reflectors on the
+//      DMMA GEMM.
+// Eigenvalues come out ascending (as dsyev).  Eigenvectors are defined up to sign/rotation in
+// degenerate subspaces, which every downstream GW quantity is invariant to.
+#include <cmath>
+#include <cfloat>
+#include "qk_internal.cuh"
+
+namespace {
+
+constexpr int TRI_THREADS = 512;
+constexpr int TRI_SMAX = 64;        // max column segments per row chunk
+constexpr int BT_NB = 64;           // reflectors per compact-WY block
+constexpr double CLUSTER_REL = 1e-7;  // eigenvalues closer than this * ||T||_1 share a cluster
+
+struct TriArgs {
+  double* A;
+  long long lda;
+  int n;
+  double* d;
+  double* e;
+  double* tau;
+  double* V;
+  long long ldv;
+  double* pbuf;  // 3*n
+  double* gvec;  // gridDim.x * 3 * n when vectors do not fit in shared memory
+  unsigned* bar;
+  int* status;
+  int use_smem;
+};
+
+__global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
+  extern __shared__ double sm[];
+  __shared__ double red[32];
+  const int n = a.n;
+  double *vk, *wk, *vk1;
+  if (a.use_smem) {
+    vk = sm;
+    wk = sm + n;
+    vk1 = sm + 2 * n;
+  } else {
+    double* base = a.gvec + (size_t)blockIdx.x * 3 * n;
+    vk = base;
+    wk = base + n;
+    vk1 = base + 2 * n;
+  }
+  unsigned epoch = 0;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+  const int gwarp = blockIdx.x * nwarps + warp, totwarps = gridDim.x * nwarps;
+  const int gthread = blockIdx.x * nt + tid, totthreads = gridDim.x * nt;
+  double tau_k = 0.0;
+
+  for (int k = -1; k <= n - 2; ++k) {
+    // ---- zero the p accumulator used two iterations ahead (triple buffering) ----
+    {
+      double* pz = a.pbuf + (size_t)((k + 2) % 3) * n;
+      for (int i = gthread; i < n; i += totthreads) __stcg(pz + i, 0.0);
+    }
+    // ---- small phase (redundant in every CTA) ----
+    if (k >= 0) {
+      const double* p = a.pbuf + (size_t)(k % 3) * n;
+      double dot = 0.0;
+      for (int i = k + 1 + tid; i < n; i += nt) {
+        const double pi = __ldcg(p + i);
+        wk[i] = pi;
+        dot += pi * vk[i];
+      }
+      dot = qk_block_sum(dot, red);
+      const double c = 0.5 * tau_k * tau_k * dot;
+      for (int i = k + 1 + tid; i < n; i += nt) wk[i] = tau_k * wk[i] - c * vk[i];
+      __syncthreads();
+    }
+    const int j = k + 1;
+    double tau1 = 0.0;
+    if (j <= n - 1) {
+      double wj = 0.0, vj = 0.0;
+      if (k >= 0) { wj = wk[j]; vj = vk[j]; }
+      for (int i = j + tid; i < n; i += nt) {
+        double x = __ldcg(a.A + i + a.lda * j);
+        if (k >= 0) x = x - vk[i] * wj - wk[i] * vj;
+        vk1[i] = x;
+      }
+      __syncthreads();
+      const double dj = vk1[j];
+      if (j <= n - 2) {
+        double ss = 0.0;
+        for (int i = j + 2 + tid; i < n; i += nt) ss += vk1[i] * vk1[i];
+        const double sigma = qk_block_sum(ss, red);
+        const double alpha = vk1[j + 1];
+        double beta, scal;
+        if (sigma == 0.0) {
+          tau1 = 0.0;
+          beta = alpha;
+          scal = 1.0;
+        } else {
+          beta = -copysign(sqrt(alpha * alpha + sigma), alpha);
+          tau1 = (beta - alpha) / beta;
+          scal = 1.0 / (alpha - beta);
+        }
+        for (int i = j + 2 + tid; i < n; i += nt) vk1[i] *= scal;
+        __syncthreads();
+        if (tid == 0) vk1[j + 1] = 1.0;
+        __syncthreads();
+        if (blockIdx.x == 0) {
+          if (tid == 0) { a.e[j] = beta; a.tau[j] = tau1; }
+          for (int i = j + 1 + tid; i < n; i += nt) a.V[i + a.ldv * j] = vk1[i];
+        }
+      }
+      if (blockIdx.x == 0 && tid == 0) a.d[j] = dj;
+    }
+    __syncthreads();
+    // ---- big pass: rank-2 update of step k fused with p_{k+1} = A' v_{k+1} ----
+    const int r0 = k + 2;
+    const int mm = n - r0;
+    if (mm > 0) {
+      const int nchunks = (mm + 31) >> 5;
+      int S = totwarps / nchunks;
+      S = S < 1 ? 1 : (S > TRI_SMAX ? TRI_SMAX : S);
+      const int smax2 = (mm + 7) / 8;
+      if (S > smax2) S = smax2;
+      const int L = (mm + S - 1) / S;
+      double* pnext = a.pbuf + (size_t)((k + 1) % 3) * n;
+      const bool upd = (k >= 0);
+      const bool wantp = (j <= n - 2);
+      const int items = nchunks * S;
+      for (int item = gwarp; item < items; item += totwarps) {
+        const int c = item / S, sgi = item - c * S;
+        const int i = r0 + c * 32 + lane;
+        const int cb = r0 + sgi * L;
+        const int ce = min(n, cb + L);
+        if (i < n && cb < ce) {
+          const double vi = upd ? vk[i] : 0.0, wi = upd ? wk[i] : 0.0;
+          double* col = a.A + i;
+          double acc = 0.0;
+          if (upd) {
+#pragma unroll 4
+            for (int cc = cb; cc < ce; ++cc) {
+              double* ptr = col + a.lda * cc;
+              double x = __ldcg(ptr);
+              x = x - vi * wk[cc] - wi * vk[cc];
+              __stcg(ptr, x);
+              acc += x * vk1[cc];
+            }
+          } else {
+#pragma unroll 4
+            for (int cc = cb; cc < ce; ++cc) acc += __ldcg(col + a.lda * cc) * vk1[cc];
+          }
+          if (wantp) atomicAdd(pnext + i, acc);
+        }
+      }
+    }
+    if (!qk_grid_barrier(a.bar, gridDim.x, epoch, a.status)) return;
+    // rotate vectors: v_{k+1} becomes v_k
+    double* t = vk;
+    vk = vk1;
+    vk1 = t;
+    tau_k = tau1;
+  }
+}
+
+// Gershgorin bounds, pivmin, ||T||_1 and e^2 (single block).
+__global__ void k_tri_prep(int n, const double* __restrict__ d, const double* __restrict__ e,
+                           double* __restrict__ e2, double* __restrict__ out /* gl, gu, pivmin, tnrm */) {
+  __shared__ double red[32];
+  double gl = INFINITY, gu = -INFINITY, emax = 0.0, tn = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double el = i > 0 ? fabs(e[i - 1]) : 0.0;
+    const double er = i < n - 1 ? fabs(e[i]) : 0.0;
+    gl = fmin(gl, d[i] - el - er);
+    gu = fmax(gu, d[i] + el + er);
+    tn = fmax(tn, fabs(d[i]) + el + er);
+    if (i < n - 1) {
+      e2[i] = e[i] * e[i];
+      emax = fmax(emax, e[i] * e[i]);
+    }
+  }
+  // max/min reductions via shuffles
+  for (int o = 16; o > 0; o >>= 1) {
+    gl = fmin(gl, __shfl_xor_sync(0xffffffffu, gl, o));
+    gu = fmax(gu, __shfl_xor_sync(0xffffffffu, gu, o));
+    emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    tn = fmax(tn, __shfl_xor_sync(0xffffffffu, tn, o));
+  }
+  __shared__ double s4[4][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) { s4[0][wid] = gl; s4[1][wid] = gu; s4[2][wid] = emax; s4[3][wid] = tn; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < nw; ++w) {
+      gl = fmin(gl, s4[0][w]);
+      gu = fmax(gu, s4[1][w]);
+      emax = fmax(emax, s4[2][w]);
+      tn = fmax(tn, s4[3][w]);
+    }
+    const double safmin = DBL_MIN;
+    const double pivmin = safmin * fmax(1.0, emax);
+    const double tnorm = fmax(fabs(gl), fabs(gu));
+    const double fudge = 2.0 * DBL_EPSILON * tnorm * n + 4.0 * pivmin;
+    out[0] = gl - fudge - 2.0 * DBL_EPSILON * fabs(gl);
+    out[1] = gu + fudge + 2.0 * DBL_EPSILON * fabs(gu);
+    out[2] = pivmin;
+    out[3] = tn > 0.0 ? tn : 1.0;
+  }
+  (void)red;
+}
+
+__device__ __forceinline__ int sturm_count(int n, const double* __restrict__ d,
+                                           const double* __restrict__ e2, double x, double pivmin) {
+  double q = d[0] - x;
+  if (fabs(q) <= pivmin) q = -pivmin;
+  int c = q < 0.0;
+  for (int i = 1; i < n; ++i) {
+    q = (d[i] - x) - __ldg(e2 + i - 1) / q;
+    if (fabs(q) <= pivmin) q = -pivmin;
+    c += q < 0.0;
+  }
+  return c;
+}
+
+// one thread per eigenvalue index j: bisection to full precision on the Sturm count
+__global__ void k_stebz(int n, const double* __restrict__ d, const double* __restrict__ e2,
+                        const double* __restrict__ prep, double* __restrict__ w) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double lo = prep[0], hi = prep[1];
+  const double pivmin = prep[2];
+  for (int it = 0; it < 160; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (!(mid > lo && mid < hi)) break;
+    if (hi - lo <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + 2.0 * pivmin) break;
+    const int c = sturm_count(n, d, e2, mid, pivmin);
+    if (c <= j) lo = mid; else hi = mid;
+  }
+  w[j] = 0.5 * (lo + hi);
+}
+
+__device__ __forceinline__ double rand_pm1(unsigned long long i, unsigned long long j) {
+  unsigned long long z = (i * 0x9E3779B97F4A7C15ull) ^ (j + 0x632BE59BD9B4E019ull);
+  z ^= z >> 30; z *= 0xBF58476D1CE4E5B9ull;
+  z ^= z >> 27; z *= 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return ((double)(z >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;
+}
+
+// Inverse iteration.  Thread j leads the cluster that starts at eigenvalue j (clusters are
+// maximal runs with consecutive gaps <= CLUSTER_REL*||T||_1).  Workspace W holds five
+// interleaved arrays (U0,U1,U2,mult,swap) of n entries per thread: W[(arr*n + i)*n + j].
+// The iterate lives directly in the output row Zt[jj + n*i].
+__global__ void k_stein(int n, const double* __restrict__ d, const double* __restrict__ e,
+                        const double* __restrict__ w, const double* __restrict__ prep,
+                        double* __restrict__ W, double* __restrict__ Zt) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double tnrm = prep[3];
+  const double ortol = CLUSTER_REL * tnrm;
+  if (j > 0 && w[j] - w[j - 1] <= ortol) return;  // not a cluster leader
+  int jend = j;
+  while (jend + 1 < n && w[jend + 1] - w[jend] <= ortol) ++jend;
+
+  const size_t N = (size_t)n;
+  double* U0 = W + 0 * N * N;
+  double* U1 = W + 1 * N * N;
+  double* U2 = W + 2 * N * N;
+  double* ML = W + 3 * N * N;
+  double* SW = W + 4 * N * N;
+  auto at = [&](double* arr, int i) -> double& { return arr[(size_t)i * N + j]; };
+  const double tiny = DBL_EPSILON * tnrm;
+  double xprev = -INFINITY;
+
+  for (int jj = j; jj <= jend; ++jj) {
+    double x = w[jj];
+    if (jj > j) {
+      const double pertol = 10.0 * fabs(DBL_EPSILON * x) + tiny;
+      if (x - xprev < pertol) x = xprev + pertol;
+    }
+    xprev = x;
+    // ---- GEPP of T - x I ----
+    double r0 = d[0] - x, r1 = n > 1 ? e[0] : 0.0, r2 = 0.0;
+    for (int k = 0; k < n - 1; ++k) {
+      const double ck = e[k];
+      const double ak1 = d[k + 1] - x;
+      const double bk1 = (k + 1 < n - 1) ? e[k + 1] : 0.0;
+      if (fabs(ck) <= fabs(r0)) {
+        const double m = (r0 != 0.0) ? ck / r0 : 0.0;
+        at(U0, k) = r0; at(U1, k) = r1; at(U2, k) = r2; at(ML, k) = m; at(SW, k) = 0.0;
+        r0 = ak1 - m * r1;
+        r1 = bk1 - m * r2;
+        r2 = 0.0;
+      } else {
+        const double m = r0 / ck;
+        at(U0, k) = ck; at(U1, k) = ak1; at(U2, k) = bk1; at(ML, k) = m; at(SW, k) = 1.0;
+        const double n0 = r1 - m * ak1;
+        const double n1 = r2 - m * bk1;
+        r0 = n0;
+        r1 = n1;
+        r2 = 0.0;
+      }
+    }
+    at(U0, n - 1) = r0; at(U1, n - 1) = 0.0; at(U2, n - 1) = 0.0;
+    // ---- start vector ----
+    for (int i = 0; i < n; ++i) Zt[(size_t)jj + N * i] = rand_pm1(i, jj);
+    for (int it = 0; it < 3; ++it) {
+      // scale to unit inf-norm
+      double mx = 0.0;
+      for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(Zt[(size_t)jj + N * i]));
+      const double sc = mx > 0.0 ? 1.0 / mx : 1.0;
+      // forward: apply P and L^{-1}
+      double yk = Zt[jj] * sc;
+      for (int k = 0; k < n - 1; ++k) {
+        double yk1 = Zt[(size_t)jj + N * (k + 1)] * sc;
+        const double m = at(ML, k);
+        if (at(SW, k) != 0.0) {
+          const double t = yk;
+          yk = yk1;
+          yk1 = t - m * yk;
+        } else {
+          yk1 = yk1 - m * yk;
+        }
+        Zt[(size_t)jj + N * k] = yk;
+        yk = yk1;
+      }
+      Zt[(size_t)jj + N * (n - 1)] = yk;
+      // back substitution with U (tiny pivots perturbed)
+      double y1 = 0.0, y2 = 0.0;
+      for (int k = n - 1; k >= 0; --k) {
+        double u = at(U0, k);
+        if (fabs(u) < tiny) u = (u < 0.0) ? -tiny : tiny;
+        const double yv = (Zt[(size_t)jj + N * k] - at(U1, k) * y1 - at(U2, k) * y2) / u;
+        Zt[(size_t)jj + N * k] = yv;
+        y2 = y1;
+        y1 = yv;
+      }
+      // MGS against earlier members of the cluster
+      for (int kk = j; kk < jj; ++kk) {
+        double dot = 0.0;
+        for (int i = 0; i < n; ++i) dot += Zt[(size_t)jj + N * i] * Zt[(size_t)kk + N * i];
+        for (int i = 0; i < n; ++i) Zt[(size_t)jj + N * i] -= dot * Zt[(size_t)kk + N * i];
+      }
+    }
+    // normalise (2-norm), largest component positive
+    double mx = 0.0, s2 = 0.0;
+    int imx = 0;
+    for (int i = 0; i < n; ++i) {
+      const double v = Zt[(size_t)jj + N * i];
+      if (fabs(v) > mx) { mx = fabs(v); imx = i; }
+    }
+    const double sc0 = mx > 0.0 ? 1.0 / mx : 1.0;
+    for (int i = 0; i < n; ++i) {
+      const double v = Zt[(size_t)jj + N * i] * sc0;
+      s2 += v * v;
+    }
+    double sc = sc0 / sqrt(s2);
+    if (Zt[(size_t)jj + N * imx] < 0.0) sc = -sc;
+    for (int i = 0; i < n; ++i) Zt[(size_t)jj + N * i] *= sc;
+  }
+}
+
+// Forward compact-WY T factor (upper triangular) for nb reflectors from G = V^T V.
+__global__ void k_larft(int nb, const double* __restrict__ G, const double* __restrict__ tau,
+                        double* __restrict__ T) {
+  // single block, nb <= 64 threads used
+  __shared__ double sT[BT_NB][BT_NB + 1];
+  __shared__ double z[BT_NB];
+  const int t = threadIdx.x;
+  for (int idx = t; idx < BT_NB * (BT_NB + 1); idx += blockDim.x) (&sT[0][0])[idx] = 0.0;
+  __syncthreads();
+  for (int i = 0; i < nb; ++i) {
+    if (t < i) z[t] = G[t + nb * i];
+    __syncthreads();
+    if (t < i) {
+      double s = 0.0;
+      for (int c = t; c < i; ++c) s += sT[t][c] * z[c];
+      sT[t][i] = -tau[i] * s;
+    }
+    if (t == 0) sT[i][i] = tau[i];
+    __syncthreads();
+  }
+  for (int idx = t; idx < nb * nb; idx += blockDim.x) {
+    const int r = idx % nb, c = idx / nb;
+    T[idx] = sT[r][c];
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, int want_vectors) {
+  if (n <= 0) return QK_OK;
+  const size_t N = (size_t)n;
+  // workspace: V (n*n), small vectors (d, e, tau, e2, pbuf(3n), prep(8))
+  double *V = nullptr, *tri = nullptr;
+  QK_TRY(qk_wst(ctx, W_V, N * N, &V));
+  QK_TRY(qk_wst(ctx, W_TRI, 8 * N + 64, &tri));
+  double* d = tri;
+  double* e = tri + N;
+  double* tau = tri + 2 * N;
+  double* e2 = tri + 3 * N;
+  double* pbuf = tri + 4 * N;
+  double* prep = tri + 7 * N;
+  QK_CK(cudaMemsetAsync(V, 0, N * N * sizeof(double), ctx->stream));
+  QK_CK(cudaMemsetAsync(tri, 0, (8 * N + 64) * sizeof(double), ctx->stream));
+  QK_CK(cudaMemsetAsync(ctx->d_bar, 0, 16 * sizeof(unsigned), ctx->stream));
+
+  // ---- 1. tridiagonalisation ----
+  qk_tic(ctx, T_TRIDIAG);
+  {
+    const size_t smem_need = 3 * N * sizeof(double);
+    const int use_smem = smem_need <= 200 * 1024;
+    const size_t smem = use_smem ? smem_need : 0;
+    QK_CK(cudaFuncSetAttribute(k_sytrd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(use_smem ? smem : 0)));
+    int per_sm = 0;
+    QK_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sytrd, TRI_THREADS, smem));
+    if (per_sm < 1) return qk_fail(ctx, QK_ERR_CUDA, "k_sytrd cannot be resident");
+    if (per_sm > 2) per_sm = 2;
+    int grid = per_sm * ctx->num_sms;
+    // small problems do not need the whole GPU
+    const int want = (int)((N * N) / (32 * 64)) + 1;
+    if (grid > want) grid = want < 1 ? 1 : want;
+    double* gvec = nullptr;
+    if (!use_smem) QK_TRY(qk_wst(ctx, W_VEC, (size_t)grid * 3 * N, &gvec));
+    TriArgs ta;
+    ta.A = A;
+    ta.lda = lda;
+    ta.n = n;
+    ta.d = d;
+    ta.e = e;
+    ta.tau = tau;
+    ta.V = V;
+    ta.ldv = n;
+    ta.pbuf = pbuf;
+    ta.gvec = gvec;
+    ta.bar = ctx->d_bar;
+    ta.status = ctx->d_status;
+    ta.use_smem = use_smem;
+    void* args[] = {&ta};
+    QK_CK(cudaLaunchCooperativeKernel((void*)k_sytrd, dim3(grid), dim3(TRI_THREADS), args, smem,
+                                      ctx->stream));
+    ctx->launches++;
+  }
+  qk_toc(ctx, T_TRIDIAG);
+
+  // ---- 2. eigenvalues by bisection ----
+  qk_tic(ctx, T_TRIDIAG_EIGVEC);
+  k_tri_prep<<<1, 1024, 0, ctx->stream>>>(n, d, e, e2, prep);
+  QK_LAUNCHED();
+  k_stebz<<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, d, e2, prep, w);
+  QK_LAUNCHED();
+  if (!want_vectors) {
+    qk_toc(ctx, T_TRIDIAG_EIGVEC);
+    return QK_OK;
+  }
+  // ---- 3. eigenvectors of T by inverse iteration ----
+  double* Wst = nullptr;
+  QK_TRY(qk_wst(ctx, W_EIGWORK, 5 * N * N, &Wst));
+  k_stein<<<(n + 63) / 64, 64, 0, ctx->stream>>>(n, d, e, w, prep, Wst, Zt);
+  QK_LAUNCHED();
+  qk_toc(ctx, T_TRIDIAG_EIGVEC);
+
+  // ---- 4. back-transformation Zt <- Zt * Q^T, blocks from last to first ----
+  qk_tic(ctx, T_BACKTRANS);
+  const int nref = n - 2;  // reflectors 0..n-3 can be non-trivial
+  if (nref > 0) {
+    double *W1 = nullptr, *W2 = nullptr, *G = nullptr, *T = nullptr;
+    double* bt = nullptr;
+    QK_TRY(qk_wst(ctx, W_PART, 2 * N * BT_NB + 2 * BT_NB * BT_NB, &bt));
+    W1 = bt;
+    W2 = bt + N * BT_NB;
+    G = bt + 2 * N * BT_NB;
+    T = G + BT_NB * BT_NB;
+    const int nblk = (nref + BT_NB - 1) / BT_NB;
+    for (int b = nblk - 1; b >= 0; --b) {
+      const int kb = b * BT_NB;
+      const int nb = (nref - kb) < BT_NB ? (nref - kb) : BT_NB;
+      const int m = n - kb - 1;
+      const double* Vb = V + (kb + 1) + N * kb;
+      double* Es = Zt + N * (kb + 1);
+      QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, nb, m, 1.0, Vb, n, 0, Vb, n, 0, 0.0, G, nb, 0, 1));
+      k_larft<<<1, 64, 0, ctx->stream>>>(nb, G, tau + kb, T);
+      QK_LAUNCHED();
+      QK_TRY(qk_dgemm(ctx, 'N', 'N', n, nb, m, 1.0, Es, n, 0, Vb, n, 0, 0.0, W1, n, 0, 1));
+      QK_TRY(qk_dgemm(ctx, 'N', 'T', n, nb, nb, 1.0, W1, n, 0, T, nb, 0, 0.0, W2, n, 0, 1));
+      QK_TRY(qk_dgemm(ctx, 'N', 'T', n, m, nb, -1.0, W2, n, 0, Vb, n, 0, 1.0, Es, n, 0, 1));
+    }
+  }
+  qk_toc(ctx, T_BACKTRANS);
+  return QK_OK;
+}
+
+extern "C" int qk_dsyev_dev(qk_ctx* ctx, int n, double* d_A, int lda, double* d_w, double* d_Zt,
+                            int want_vectors) {
+  if (!ctx || n < 0 || lda < n) return QK_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  QK_TRY(qk_status_reset(ctx));
+  QK_TRY(qk_eig_sym(ctx, n, d_A, lda, d_w, d_Zt, want_vectors));
+  return qk_status_check(ctx, QKD_BARRIER_TIMEOUT | QKD_BAD_INDEX);
+}

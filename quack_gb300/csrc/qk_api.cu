@@ -1,0 +1,611 @@
+// qk_api.cu -- the extern "C" entry points: stage-level drop-ins for the Fortran subroutines of
+// the restricted G0W0/evGW call chain and the device-resident drivers.
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "qk_internal.cuh"
+
+namespace {
+
+struct Dims {
+  int N, nC, nO, nR, nS, no, nv;
+};
+
+int check_dims(qk_ctx* ctx, int nBas, int nOrb, int nC, int nO, int nV, int nR, int nS, Dims* d) {
+  (void)nV;
+  if (nBas != nOrb)
+    return qk_fail(ctx, QK_ERR_ARG, "nBas (%d) != nOrb (%d): the restricted GW path dimensions "
+                   "its arrays with nBas and nOrb interchangeably (RGW_self_energy_diag.f90:22-27)",
+                   nBas, nOrb);
+  const int N = nOrb;
+  const int no = nO - nC, nv = N - nO - nR;
+  if (N <= 0 || nC < 0 || nR < 0 || no <= 0 || nv <= 0)
+    return qk_fail(ctx, QK_ERR_ARG, "invalid orbital partition N=%d nC=%d nO=%d nR=%d", N, nC, nO, nR);
+  if ((long long)no * nv != nS)
+    return qk_fail(ctx, QK_ERR_ARG, "nS=%d does not equal (nO-nC)*(nOrb-nO-nR)=%lld", nS,
+                   (long long)no * nv);
+  d->N = N; d->nC = nC; d->nO = nO; d->nR = nR; d->nS = nS; d->no = no; d->nv = nv;
+  return QK_OK;
+}
+
+int h2d(qk_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  QK_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  return QK_OK;
+}
+int d2h(qk_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  QK_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return QK_OK;
+}
+
+// small elementwise helpers used by the general (non-diagonal A-B) Casida path
+__global__ void k_axpby(long long n, double a, const double* __restrict__ x, double b,
+                        const double* __restrict__ y, double* __restrict__ z) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    z[i] = a * x[i] + b * y[i];
+}
+// rows of X (n x n, column-major) scaled: X(r,c) *= f(d[r]); mode 0: sqrt, 1: 1/sqrt, 2: identity
+__global__ void k_rowscale(int n, const double* __restrict__ d, int mode, const double* __restrict__ X,
+                           double* __restrict__ Y) {
+  const long long total = (long long)n * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i % n);
+    double f = d[r];
+    if (mode == 0) f = 1.0 * sqrt(f);
+    else if (mode == 1) f = 1.0 / sqrt(f);
+    Y[i] = f * X[i];
+  }
+}
+__global__ void k_offdiag_maxabs(int n, const double* __restrict__ A, const double* __restrict__ B,
+                                 double* out) {
+  double m = 0.0;
+  const long long total = (long long)n * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i % n), c = (int)(i / n);
+    if (r != c) m = fmax(m, fabs(A[i] - B[i]));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0) {
+    // non-negative doubles order like their bit patterns
+    atomicMax((unsigned long long*)out, (unsigned long long)__double_as_longlong(m));
+  }
+}
+__global__ void k_trace(int n, const double* __restrict__ A, double* out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += A[(long long)i * n + i];
+  s = qk_block_sum(s, red);
+  if (threadIdx.x == 0) *out = s;
+}
+__global__ void k_xpy_general(int nS, const double* __restrict__ w, double* __restrict__ Om,
+                              double* __restrict__ XpY, double* __restrict__ XmY, int* status) {
+  const long long total = (long long)nS * nS;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int m = (int)(i % nS);
+    const double om = sqrt(fabs(w[m]));
+    XpY[i] *= 1.0 / sqrt(om);
+    XmY[i] *= 1.0 * sqrt(om);
+    if (i < nS) {
+      Om[m] = om;
+      if (w[m] < 0.0) atomicOr(status, QKD_NEG_OMEGA);
+    }
+  }
+}
+__global__ void k_ecrpa(const double* sumOm, const double* trA, double* out) {
+  *out = 0.5 * (*sumOm - *trA);
+}
+
+int grid_for(qk_ctx* ctx, long long total) {
+  long long b = (total + 255) / 256;
+  const long long cap = 64LL * ctx->num_sms;
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+// the excitation density rho = slab * XpY^T for the chosen precision tier
+int rho_gemm(qk_ctx* ctx, int prec, int N, int nS, const double* S, const double* XpY, double* rho) {
+  const long long N2 = (long long)N * N;
+  if (prec == QK_PREC_BF16X3)
+    return qk_gemm_bf16x3_nt(ctx, (int)N2, nS, nS, S, N2, XpY, nS, rho, N2);
+  return qk_dgemm(ctx, 'N', 'T', (int)N2, nS, nS, 1.0, S, N2, 0, XpY, nS, 0, 0.0, rho, N2, 0, 1);
+}
+
+// Casida with eigenvectors for the dRPA singlet screening at energies e.
+// Outputs: Om (nS), XpY (nS*nS), optional XmY, sumOm/trA (device scalars) for EcRPA.
+int casida_dev(qk_ctx* ctx, const Dims& d, const double* e, const double* ERI, double* Om,
+               double* XpY, double* XmY, double* scal /* [0]=trA [1]=sumOm [2]=EcRPA */,
+               int want_vectors) {
+  const size_t S2 = (size_t)d.nS * d.nS;
+  double *M = nullptr, *Zt = nullptr, *sq = nullptr;
+  QK_TRY(qk_wst(ctx, W_M, S2, &M));
+  QK_TRY(qk_wst(ctx, W_E, 2 * (size_t)d.nS + 64, &sq));
+  double* w = sq + d.nS;
+  qk_tic(ctx, T_BUILD);
+  QK_TRY(qk_launch_casida_M(ctx, d.N, d.nC, d.nO, d.nR, e, ERI, M, sq, scal + 0));
+  qk_toc(ctx, T_BUILD);
+  if (want_vectors) QK_TRY(qk_wst(ctx, W_ZT, S2, &Zt));
+  QK_TRY(qk_eig_sym(ctx, d.nS, M, d.nS, w, Zt, want_vectors));
+  if (want_vectors) QK_TRY(qk_launch_xpy(ctx, d.nS, w, Zt, sq, Om, XpY, XmY, XmY != nullptr));
+  QK_TRY(qk_launch_sum_sqrt(ctx, d.nS, w, scal + 1));
+  k_ecrpa<<<1, 1, 0, ctx->stream>>>(scal + 1, scal + 0, scal + 2);
+  QK_LAUNCHED();
+  return QK_OK;
+}
+
+int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* eHF,
+             const double* ERI, double* eGW, double* SigC, double* Z, double* Om, double* hEcRPA,
+             double* hEcGM) {
+  if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
+  const double flow = 500.0;  // RG0W0.f90:98
+  const int N = d.N, nS = d.nS;
+  const size_t S2 = (size_t)nS * nS, N2S = (size_t)N * N * nS;
+  double *XpY, *slab, *rho, *scal, *eGWlin;
+  QK_TRY(qk_wst(ctx, W_XPY, S2, &XpY));
+  QK_TRY(qk_wst(ctx, W_SLAB, N2S, &slab));
+  QK_TRY(qk_wst(ctx, W_RHO, N2S, &rho));
+  double* small = nullptr;
+  QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)2 * N + 16, &small));
+  scal = small;
+  eGWlin = small + 16;
+  double* EcGM_d = scal + 8;
+  qk_timings_clear(ctx);
+  // screening at eHF
+  QK_TRY(casida_dev(ctx, d, eHF, ERI, Om, XpY, nullptr, scal, 1));
+  // excitation densities
+  qk_tic(ctx, T_SLAB);
+  QK_TRY(qk_launch_slab_gather(ctx, N, d.nC, d.nO, d.nR, ERI, slab));
+  qk_toc(ctx, T_SLAB);
+  qk_tic(ctx, T_RHO);
+  QK_TRY(rho_gemm(ctx, prm->precision, N, nS, slab, XpY, rho));
+  qk_toc(ctx, T_RHO);
+  // self-energy
+  qk_tic(ctx, T_SIGMA);
+  QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho, SigC,
+                       Z, EcGM_d));
+  QK_TRY(qk_qp_linear(ctx, N, eHF, Z, SigC, 1, eGWlin));
+  qk_toc(ctx, T_SIGMA);
+  qk_tic(ctx, T_QP);
+  if (prm->linearize) {
+    QK_CK(cudaMemcpyAsync(eGW, eGWlin, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
+    QK_TRY(qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho,
+                        eGWlin, eHF, eGW, Z));
+  }
+  qk_toc(ctx, T_QP);
+  // second Casida at eGW for EcRPA (RG0W0.f90:222-225): eigenvalues only
+  qk_tic(ctx, T_CASIDA2);
+  QK_TRY(casida_dev(ctx, d, eGW, ERI, nullptr, nullptr, nullptr, scal + 3, 0));
+  qk_toc(ctx, T_CASIDA2);
+  double h[16];
+  QK_TRY(d2h(ctx, h, scal, 16 * sizeof(double)));
+  QK_CK(cudaStreamSynchronize(ctx->stream));
+  qk_timings_collect(ctx);
+  if (hEcRPA) *hEcRPA = h[5];
+  if (hEcGM) *hEcGM = h[8];
+  return QK_OK;
+}
+
+int evgw_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* eHF,
+             const double* ERI, double* eGW, double* SigC, double* Z, double* hEcRPA,
+             double* hEcGM, int* hnSCF, double* hConv) {
+  if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
+  const double flow = 500.0;
+  const int N = d.N, nS = d.nS;
+  const size_t S2 = (size_t)nS * nS, N2S = (size_t)N * N * nS;
+  const int maxd = prm->max_diis > 1 ? prm->max_diis : 1;
+  double *XpY, *slab, *rho, *small;
+  QK_TRY(qk_wst(ctx, W_XPY, S2, &XpY));
+  QK_TRY(qk_wst(ctx, W_SLAB, N2S, &slab));
+  QK_TRY(qk_wst(ctx, W_RHO, N2S, &rho));
+  QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)(6 + 2 * maxd) * N + nS + 64, &small));
+  double* scal = small;            // [0]=trA [1]=sumOm [2]=EcRPA [8]=EcGM [9]=Conv [10]=rcond
+  double* eOld = small + 64;
+  double* errv = eOld + N;
+  double* Om = errv + N;
+  double* err_hist = Om + nS;
+  double* e_hist = err_hist + (size_t)N * maxd;
+  QK_CK(cudaMemsetAsync(err_hist, 0, sizeof(double) * 2 * (size_t)N * maxd, ctx->stream));
+  QK_CK(cudaMemcpyAsync(eGW, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  QK_CK(cudaMemcpyAsync(eOld, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  qk_timings_clear(ctx);
+  // the slab of (pq|jb) does not depend on the energies: gather it once
+  qk_tic(ctx, T_SLAB);
+  QK_TRY(qk_launch_slab_gather(ctx, N, d.nC, d.nO, d.nR, ERI, slab));
+  qk_toc(ctx, T_SLAB);
+  int nSCF = 0, n_diis = 0;
+  double Conv = 1.0;
+  while (Conv > prm->thresh && nSCF <= prm->maxSCF) {  // evRGW.f90:119
+    QK_TRY(casida_dev(ctx, d, eGW, ERI, Om, XpY, nullptr, scal, 1));
+    qk_tic(ctx, T_RHO);
+    QK_TRY(rho_gemm(ctx, prm->precision, N, nS, slab, XpY, rho));
+    qk_toc(ctx, T_RHO);
+    qk_tic(ctx, T_SIGMA);
+    QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eGW, Om, rho,
+                         SigC, Z, scal + 8));
+    qk_toc(ctx, T_SIGMA);
+    qk_tic(ctx, T_QP);
+    if (prm->linearize) {
+      QK_TRY(qk_qp_linear(ctx, N, eHF, Z, SigC, 0, eGW));  // evRGW.f90:147
+    } else {
+      QK_TRY(qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho,
+                          eOld, eOld, eGW, Z));  // evRGW.f90:154
+    }
+    qk_toc(ctx, T_QP);
+    QK_TRY(qk_max_abs_diff(ctx, N, eGW, eOld, scal + 9));
+    if (prm->max_diis > 1) {  // evRGW.f90:166-171
+      n_diis = n_diis + 1 < prm->max_diis ? n_diis + 1 : prm->max_diis;
+      QK_TRY(qk_sub(ctx, N, eGW, eOld, errv));
+      QK_TRY(qk_diis_dev(ctx, N, N, n_diis, err_hist, e_hist, errv, eGW, scal + 10));
+    }
+    QK_CK(cudaMemcpyAsync(eOld, eGW, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    QK_TRY(d2h(ctx, &Conv, scal + 9, sizeof(double)));
+    QK_CK(cudaStreamSynchronize(ctx->stream));
+    nSCF++;
+  }
+  double h[16];
+  QK_TRY(d2h(ctx, h, scal, 16 * sizeof(double)));
+  QK_CK(cudaStreamSynchronize(ctx->stream));
+  qk_timings_collect(ctx);
+  if (hEcRPA) *hEcRPA = h[2];
+  if (hEcGM) *hEcGM = h[8];
+  if (hnSCF) *hnSCF = nSCF;
+  if (hConv) *hConv = Conv;
+  if (nSCF == prm->maxSCF + 1)  // evRGW.f90:190-198
+    return qk_fail(ctx, QK_ERR_NO_CONV, "evGW convergence failed after %d cycles (Conv=%g)", nSCF, Conv);
+  return QK_OK;
+}
+
+int begin(qk_ctx* ctx) {
+  if (!ctx) return QK_ERR_ARG;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return qk_cuda_fail(ctx, e, "cudaSetDevice", __FILE__, __LINE__);
+  ctx->err.clear();
+  return qk_status_reset(ctx);
+}
+
+constexpr int FATAL = QKD_BARRIER_TIMEOUT | QKD_BAD_INDEX | QKD_MBAR_TIMEOUT;
+
+int end(qk_ctx* ctx, int st) {
+  if (st != QK_OK && st != QK_ERR_NO_CONV) {
+    cudaStreamSynchronize(ctx->stream);
+    return st;
+  }
+  int s2 = qk_status_check(ctx, FATAL);
+  return s2 != QK_OK ? s2 : st;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------------------------------------
+// stage-level drop-ins
+// ---------------------------------------------------------------------------------------------
+int qk_phRLR_A(qk_ctx* ctx, int ispin, int dRPA, int nBas, int nC, int nO, int nV, int nR, int nS,
+               double lambda, const double* e, const double* ERI, double* Aph) {
+  QK_TRY(begin(ctx));
+  (void)nV;
+  if (ispin != 1 && ispin != 2) return qk_fail(ctx, QK_ERR_ARG, "ispin must be 1 or 2");
+  const int no = nO - nC, nv = nBas - nO - nR;
+  if (no <= 0 || nv <= 0 || (long long)no * nv != nS) return qk_fail(ctx, QK_ERR_ARG, "bad sizes");
+  const size_t N = nBas, N4 = N * N * N * N, S2 = (size_t)nS * nS;
+  double *dERI, *de, *dA;
+  QK_TRY(qk_wst(ctx, W_ERI, N4, &dERI));
+  QK_TRY(qk_wst(ctx, W_HOST_B, N + 16, &de));
+  QK_TRY(qk_wst(ctx, W_M, S2, &dA));
+  QK_TRY(h2d(ctx, dERI, ERI, N4 * 8));
+  QK_TRY(h2d(ctx, de, e, N * 8));
+  QK_TRY(qk_launch_build_AB(ctx, 0, ispin, dRPA, nBas, nC, nO, nR, lambda, de, dERI, dA));
+  QK_TRY(d2h(ctx, Aph, dA, S2 * 8));
+  return end(ctx, QK_OK);
+}
+
+int qk_phRLR_B(qk_ctx* ctx, int ispin, int dRPA, int nBas, int nC, int nO, int nV, int nR, int nS,
+               double lambda, const double* ERI, double* Bph) {
+  QK_TRY(begin(ctx));
+  (void)nV;
+  if (ispin != 1 && ispin != 2) return qk_fail(ctx, QK_ERR_ARG, "ispin must be 1 or 2");
+  const int no = nO - nC, nv = nBas - nO - nR;
+  if (no <= 0 || nv <= 0 || (long long)no * nv != nS) return qk_fail(ctx, QK_ERR_ARG, "bad sizes");
+  const size_t N = nBas, N4 = N * N * N * N, S2 = (size_t)nS * nS;
+  double *dERI, *dB;
+  QK_TRY(qk_wst(ctx, W_ERI, N4, &dERI));
+  QK_TRY(qk_wst(ctx, W_M, S2, &dB));
+  QK_TRY(h2d(ctx, dERI, ERI, N4 * 8));
+  QK_TRY(qk_launch_build_AB(ctx, 1, ispin, dRPA, nBas, nC, nO, nR, lambda, nullptr, dERI, dB));
+  QK_TRY(d2h(ctx, Bph, dB, S2 * 8));
+  return end(ctx, QK_OK);
+}
+
+int qk_phRLR(qk_ctx* ctx, int TDA, int nS, const double* Aph, const double* Bph, double* EcRPA,
+             double* Om, double* XpY, double* XmY) {
+  QK_TRY(begin(ctx));
+  if (TDA) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA screening is not supported");
+  if (nS <= 0) return qk_fail(ctx, QK_ERR_ARG, "nS must be positive");
+  const size_t S2 = (size_t)nS * nS;
+  double *dA, *dB, *dM, *dZt, *dX, *dY, *sm;
+  QK_TRY(qk_wst(ctx, W_HOST_A, 2 * S2, &dA));
+  dB = dA + S2;
+  QK_TRY(qk_wst(ctx, W_M, S2, &dM));
+  QK_TRY(qk_wst(ctx, W_ZT, S2, &dZt));
+  QK_TRY(qk_wst(ctx, W_XPY, S2, &dX));
+  QK_TRY(qk_wst(ctx, W_XMY, S2, &dY));
+  QK_TRY(qk_wst(ctx, W_E, 3 * (size_t)nS + 64, &sm));
+  double* sq = sm;
+  double* w = sm + nS;
+  double* dOm = sm + 2 * nS;
+  double* scal = sm + 3 * nS;  // [0] trA [1] sumOm [2] EcRPA [3] offdiag max
+  QK_TRY(h2d(ctx, dA, Aph, S2 * 8));
+  QK_TRY(h2d(ctx, dB, Bph, S2 * 8));
+  QK_CK(cudaMemsetAsync(scal, 0, 8 * sizeof(double), ctx->stream));
+  k_offdiag_maxabs<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, dA, dB, scal + 3);
+  QK_LAUNCHED();
+  double offmax = 0.0;
+  QK_TRY(d2h(ctx, &offmax, scal + 3, 8));
+  QK_CK(cudaStreamSynchronize(ctx->stream));
+  if (offmax == 0.0) {
+    // A-B diagonal (dRPA): M = AmBSq.(A+B).AmBSq directly
+    QK_TRY(qk_launch_casida_M_from_AB(ctx, nS, dA, dB, dM, sq, scal + 0));
+    QK_TRY(qk_eig_sym(ctx, nS, dM, nS, w, dZt, 1));
+    QK_TRY(qk_launch_xpy(ctx, nS, w, dZt, sq, dOm, dX, dY, 1));
+  } else {
+    // general A-B (phRLR.f90:50-81): eig(A-B), AmBSq = U sqrt(l) U^T, AmBIv = U l^-1/2 U^T
+    double *amb, *sqm, *ivm, *tmp;
+    QK_TRY(qk_wst(ctx, W_SLAB, 4 * S2, &amb));
+    sqm = amb + S2;
+    ivm = sqm + S2;
+    tmp = ivm + S2;
+    k_axpby<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>((long long)S2, 1.0, dA, -1.0, dB, amb);
+    QK_LAUNCHED();
+    k_trace<<<1, 1024, 0, ctx->stream>>>(nS, dA, scal + 0);
+    QK_LAUNCHED();
+    QK_TRY(qk_eig_sym(ctx, nS, amb, nS, w, dZt, 1));  // dZt = U^T
+    // AmBSq = U diag(sqrt l) U^T = Zt^T (D Zt)
+    k_rowscale<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, w, 0, dZt, tmp);
+    QK_LAUNCHED();
+    QK_TRY(qk_dgemm(ctx, 'T', 'N', nS, nS, nS, 1.0, dZt, nS, 0, tmp, nS, 0, 0.0, sqm, nS, 0, 1));
+    k_rowscale<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, w, 1, dZt, tmp);
+    QK_LAUNCHED();
+    QK_TRY(qk_dgemm(ctx, 'T', 'N', nS, nS, nS, 1.0, dZt, nS, 0, tmp, nS, 0, 0.0, ivm, nS, 0, 1));
+    // ApB into amb, tmp = ApB.AmBSq, M = AmBSq.tmp
+    k_axpby<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>((long long)S2, 1.0, dA, 1.0, dB, amb);
+    QK_LAUNCHED();
+    QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, amb, nS, 0, sqm, nS, 0, 0.0, tmp, nS, 0, 1));
+    QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, sqm, nS, 0, tmp, nS, 0, 0.0, dM, nS, 0, 1));
+    QK_TRY(qk_eig_sym(ctx, nS, dM, nS, w, dZt, 1));  // dZt = Z^T
+    QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, dZt, nS, 0, sqm, nS, 0, 0.0, dX, nS, 0, 1));
+    QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, dZt, nS, 0, ivm, nS, 0, 0.0, dY, nS, 0, 1));
+    k_xpy_general<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, w, dOm, dX, dY, ctx->d_status);
+    QK_LAUNCHED();
+  }
+  QK_TRY(qk_launch_sum_sqrt(ctx, nS, w, scal + 1));
+  k_ecrpa<<<1, 1, 0, ctx->stream>>>(scal + 1, scal + 0, scal + 2);
+  QK_LAUNCHED();
+  QK_TRY(d2h(ctx, Om, dOm, nS * 8));
+  QK_TRY(d2h(ctx, XpY, dX, S2 * 8));
+  QK_TRY(d2h(ctx, XmY, dY, S2 * 8));
+  QK_TRY(d2h(ctx, EcRPA, scal + 2, 8));
+  return end(ctx, QK_OK);
+}
+
+int qk_RGW_excitation_density(qk_ctx* ctx, int nOrb, int nC, int nO, int nR, int nS,
+                              const double* ERI, const double* XpY, double* rho) {
+  QK_TRY(begin(ctx));
+  Dims d;
+  QK_TRY(check_dims(ctx, nOrb, nOrb, nC, nO, nOrb - nO, nR, nS, &d));
+  const size_t N = nOrb, N4 = N * N * N * N, S2 = (size_t)nS * nS, N2S = N * N * nS;
+  double *dERI, *dX, *dS, *dR;
+  QK_TRY(qk_wst(ctx, W_ERI, N4, &dERI));
+  QK_TRY(qk_wst(ctx, W_XPY, S2, &dX));
+  QK_TRY(qk_wst(ctx, W_SLAB, N2S, &dS));
+  QK_TRY(qk_wst(ctx, W_RHO, N2S, &dR));
+  QK_TRY(h2d(ctx, dERI, ERI, N4 * 8));
+  QK_TRY(h2d(ctx, dX, XpY, S2 * 8));
+  QK_TRY(qk_launch_slab_gather(ctx, nOrb, nC, nO, nR, dERI, dS));
+  QK_TRY(rho_gemm(ctx, QK_PREC_FP64, nOrb, nS, dS, dX, dR));
+  QK_TRY(d2h(ctx, rho, dR, N2S * 8));
+  return end(ctx, QK_OK);
+}
+
+static int sigma_stage(qk_ctx* ctx, int doSRG, double eta, double flow, int nBas, int nC, int nO,
+                       int nR, int nS, const double* e, const double* Om, const double* rho,
+                       double* EcGM, double* Sig, double* Z) {
+  QK_TRY(begin(ctx));
+  const int no = nO - nC, nv = nBas - nO - nR;
+  if (no <= 0 || nv <= 0 || (long long)no * nv != nS) return qk_fail(ctx, QK_ERR_ARG, "bad sizes");
+  const size_t N = nBas, N2S = N * N * nS;
+  double *dR, *sm;
+  QK_TRY(qk_wst(ctx, W_RHO, N2S, &dR));
+  QK_TRY(qk_wst(ctx, W_HOST_A, 4 * N + nS + 16, &sm));
+  double* de = sm;
+  double* dSig = sm + N;
+  double* dZ = sm + 2 * N;
+  double* dOm = sm + 3 * N;
+  double* dGM = dOm + nS;
+  QK_TRY(h2d(ctx, dR, rho, N2S * 8));
+  QK_TRY(h2d(ctx, de, e, N * 8));
+  QK_TRY(h2d(ctx, dOm, Om, nS * 8));
+  QK_TRY(qk_sigma_diag(ctx, doSRG, eta, flow, nBas, nC, nO, nR, nS, de, dOm, dR, dSig, dZ, dGM));
+  QK_TRY(d2h(ctx, Sig, dSig, N * 8));
+  QK_TRY(d2h(ctx, Z, dZ, N * 8));
+  QK_TRY(d2h(ctx, EcGM, dGM, 8));
+  return end(ctx, QK_OK);
+}
+
+int qk_RGW_self_energy_diag(qk_ctx* ctx, double eta, int nBas, int nOrb, int nC, int nO, int nV,
+                            int nR, int nS, const double* e, const double* Om, const double* rho,
+                            double* EcGM, double* Sig, double* Z) {
+  (void)nOrb; (void)nV;
+  return sigma_stage(ctx, 0, eta, 500.0, nBas, nC, nO, nR, nS, e, Om, rho, EcGM, Sig, Z);
+}
+
+int qk_RGW_SRG_self_energy_diag(qk_ctx* ctx, double flow, int nBas, int nOrb, int nC, int nO,
+                                int nV, int nR, int nS, const double* e, const double* Om,
+                                const double* rho, double* EcGM, double* SigC, double* Z) {
+  (void)nBas; (void)nV;
+  // RGW_SRG_self_energy_diag.f90 dimensions its arrays with nOrb
+  return sigma_stage(ctx, 1, 0.0, flow, nOrb, nC, nO, nR, nS, e, Om, rho, EcGM, SigC, Z);
+}
+
+int qk_RGW_QP_graph(qk_ctx* ctx, int doSRG, double eta, double flow, int nBas, int nC, int nO,
+                    int nV, int nR, int nS, const double* eHF, const double* Om, const double* rho,
+                    const double* eGWlin, const double* eOld, double* eGW, double* Z) {
+  QK_TRY(begin(ctx));
+  (void)nV;
+  const int no = nO - nC, nv = nBas - nO - nR;
+  if (no <= 0 || nv <= 0 || (long long)no * nv != nS) return qk_fail(ctx, QK_ERR_ARG, "bad sizes");
+  const size_t N = nBas, N2S = N * N * nS;
+  double *dR, *sm;
+  QK_TRY(qk_wst(ctx, W_RHO, N2S, &dR));
+  QK_TRY(qk_wst(ctx, W_HOST_A, 6 * N + nS + 16, &sm));
+  double* deHF = sm;
+  double* dlin = sm + N;
+  double* dold = sm + 2 * N;
+  double* dGW = sm + 3 * N;
+  double* dZ = sm + 4 * N;
+  double* dOm = sm + 5 * N;
+  QK_TRY(h2d(ctx, dR, rho, N2S * 8));
+  QK_TRY(h2d(ctx, deHF, eHF, N * 8));
+  QK_TRY(h2d(ctx, dlin, eGWlin, N * 8));
+  QK_TRY(h2d(ctx, dold, eOld, N * 8));
+  QK_TRY(h2d(ctx, dZ, Z, N * 8));
+  QK_TRY(h2d(ctx, dGW, eGWlin, N * 8));
+  QK_TRY(h2d(ctx, dOm, Om, nS * 8));
+  QK_TRY(qk_qp_newton(ctx, doSRG, eta, flow, nBas, nC, nO, nR, nS, deHF, dOm, dR, dlin, dold, dGW, dZ));
+  QK_TRY(d2h(ctx, eGW, dGW, N * 8));
+  QK_TRY(d2h(ctx, Z, dZ, N * 8));
+  return end(ctx, QK_OK);
+}
+
+int qk_AOtoMO_ERI_RHF(qk_ctx* ctx, int nBas, int nOrb, const double* c, const double* ERI_AO,
+                      double* ERI_MO) {
+  QK_TRY(begin(ctx));
+  if (nBas <= 0 || nOrb <= 0 || nOrb > nBas) return qk_fail(ctx, QK_ERR_ARG, "bad sizes");
+  const size_t B = nBas, O = nOrb, B4 = B * B * B * B;
+  double *X, *Y, *dc;
+  QK_TRY(qk_wst(ctx, W_ERI, B4, &X));
+  QK_TRY(qk_wst(ctx, W_SLAB, B4, &Y));
+  QK_TRY(qk_wst(ctx, W_HOST_A, B * O, &dc));
+  QK_TRY(h2d(ctx, X, ERI_AO, B4 * 8));
+  QK_TRY(h2d(ctx, dc, c, B * O * 8));
+  // four dgemm('T','N') quarter transforms (AOtoMO_ERI_RHF.f90:26-53)
+  long long R[4] = {(long long)(B * B * B), (long long)(B * B * O), (long long)(B * O * O),
+                    (long long)(O * O * O)};
+  double* src = X;
+  double* dst = Y;
+  for (int s = 0; s < 4; ++s) {
+    QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)R[s], nOrb, nBas, 1.0, src, nBas, 0, dc, nBas, 0, 0.0, dst,
+                    R[s], 0, 1));
+    double* t = src;
+    src = dst;
+    dst = t;
+  }
+  QK_TRY(d2h(ctx, ERI_MO, src, O * O * O * O * 8));
+  return end(ctx, QK_OK);
+}
+
+int qk_DIIS_extrapolation(qk_ctx* ctx, double* rcond, int n_err, int n_e, int n_diis,
+                          double* error, double* e, const double* error_in, double* e_inout) {
+  QK_TRY(begin(ctx));
+  if (n_err <= 0 || n_e <= 0 || n_diis <= 0) return qk_fail(ctx, QK_ERR_ARG, "bad sizes");
+  double* sm;
+  const size_t need = (size_t)n_err * n_diis + (size_t)n_e * n_diis + n_err + n_e + 8;
+  QK_TRY(qk_wst(ctx, W_HOST_A, need, &sm));
+  double* dErr = sm;
+  double* dE = dErr + (size_t)n_err * n_diis;
+  double* dIn = dE + (size_t)n_e * n_diis;
+  double* dIO = dIn + n_err;
+  double* dRc = dIO + n_e;
+  QK_TRY(h2d(ctx, dErr, error, (size_t)n_err * n_diis * 8));
+  QK_TRY(h2d(ctx, dE, e, (size_t)n_e * n_diis * 8));
+  QK_TRY(h2d(ctx, dIn, error_in, n_err * 8));
+  QK_TRY(h2d(ctx, dIO, e_inout, n_e * 8));
+  QK_TRY(qk_diis_dev(ctx, n_err, n_e, n_diis, dErr, dE, dIn, dIO, dRc));
+  QK_TRY(d2h(ctx, error, dErr, (size_t)n_err * n_diis * 8));
+  QK_TRY(d2h(ctx, e, dE, (size_t)n_e * n_diis * 8));
+  QK_TRY(d2h(ctx, e_inout, dIO, n_e * 8));
+  QK_TRY(d2h(ctx, rcond, dRc, 8));
+  return end(ctx, QK_OK);
+}
+
+// ---------------------------------------------------------------------------------------------
+// drivers
+// ---------------------------------------------------------------------------------------------
+int qk_RG0W0_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
+                 int nR, int nS, const double* d_eHF, const double* d_ERI, double* d_eGW,
+                 double* d_SigC, double* d_Z, double* d_Om, double* EcRPA, double* EcGM) {
+  QK_TRY(begin(ctx));
+  if (!prm) return qk_fail(ctx, QK_ERR_ARG, "params required");
+  Dims d;
+  QK_TRY(check_dims(ctx, nBas, nOrb, nC, nO, nV, nR, nS, &d));
+  const int st = g0w0_dev(ctx, prm, d, d_eHF, d_ERI, d_eGW, d_SigC, d_Z, d_Om, EcRPA, EcGM);
+  return end(ctx, st);
+}
+
+int qk_evRGW_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
+                 int nR, int nS, const double* d_eHF, const double* d_ERI, double* d_eGW,
+                 double* d_SigC, double* d_Z, double* EcRPA, double* EcGM, int* nSCF,
+                 double* Conv) {
+  QK_TRY(begin(ctx));
+  if (!prm) return qk_fail(ctx, QK_ERR_ARG, "params required");
+  Dims d;
+  QK_TRY(check_dims(ctx, nBas, nOrb, nC, nO, nV, nR, nS, &d));
+  const int st = evgw_dev(ctx, prm, d, d_eHF, d_ERI, d_eGW, d_SigC, d_Z, EcRPA, EcGM, nSCF, Conv);
+  return end(ctx, st);
+}
+
+int qk_RG0W0(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
+             int nR, int nS, const double* eHF, const double* ERI, double* eGW, double* SigC,
+             double* Z, double* Om, double* EcRPA, double* EcGM) {
+  QK_TRY(begin(ctx));
+  if (!prm) return qk_fail(ctx, QK_ERR_ARG, "params required");
+  Dims d;
+  QK_TRY(check_dims(ctx, nBas, nOrb, nC, nO, nV, nR, nS, &d));
+  const size_t N = nOrb, N4 = N * N * N * N;
+  double *dERI, *io;
+  QK_TRY(qk_wst(ctx, W_ERI, N4, &dERI));
+  QK_TRY(qk_wst(ctx, W_HOST_A, 4 * N + nS + 16, &io));
+  double* de = io;
+  double* dGW = io + N;
+  double* dSig = io + 2 * N;
+  double* dZ = io + 3 * N;
+  double* dOm = io + 4 * N;
+  QK_TRY(h2d(ctx, dERI, ERI, N4 * 8));
+  QK_TRY(h2d(ctx, de, eHF, N * 8));
+  int st = g0w0_dev(ctx, prm, d, de, dERI, dGW, dSig, dZ, dOm, EcRPA, EcGM);
+  if (st != QK_OK) return end(ctx, st);
+  QK_TRY(d2h(ctx, eGW, dGW, N * 8));
+  QK_TRY(d2h(ctx, SigC, dSig, N * 8));
+  QK_TRY(d2h(ctx, Z, dZ, N * 8));
+  QK_TRY(d2h(ctx, Om, dOm, (size_t)nS * 8));
+  return end(ctx, QK_OK);
+}
+
+int qk_evRGW(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
+             int nR, int nS, const double* eHF, const double* ERI, double* eGW, double* SigC,
+             double* Z, double* EcRPA, double* EcGM, int* nSCF, double* Conv) {
+  QK_TRY(begin(ctx));
+  if (!prm) return qk_fail(ctx, QK_ERR_ARG, "params required");
+  Dims d;
+  QK_TRY(check_dims(ctx, nBas, nOrb, nC, nO, nV, nR, nS, &d));
+  const size_t N = nOrb, N4 = N * N * N * N;
+  double *dERI, *io;
+  QK_TRY(qk_wst(ctx, W_ERI, N4, &dERI));
+  QK_TRY(qk_wst(ctx, W_HOST_A, 4 * N + 16, &io));
+  double* de = io;
+  double* dGW = io + N;
+  double* dSig = io + 2 * N;
+  double* dZ = io + 3 * N;
+  QK_TRY(h2d(ctx, dERI, ERI, N4 * 8));
+  QK_TRY(h2d(ctx, de, eHF, N * 8));
+  int st = evgw_dev(ctx, prm, d, de, dERI, dGW, dSig, dZ, EcRPA, EcGM, nSCF, Conv);
+  if (st != QK_OK && st != QK_ERR_NO_CONV) return end(ctx, st);
+  QK_TRY(d2h(ctx, eGW, dGW, N * 8));
+  QK_TRY(d2h(ctx, SigC, dSig, N * 8));
+  QK_TRY(d2h(ctx, Z, dZ, N * 8));
+  return end(ctx, st);
+}
+
+}  // extern "C"

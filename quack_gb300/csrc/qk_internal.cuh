@@ -1,0 +1,189 @@
+// qk_internal.cuh -- shared internals of libqkgw.so (context, workspace, error plumbing,
+// device helpers).  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include "../../include/qkgw.h"
+
+// ------------------------------------------------------------------------------------------
+// device status bits (written by kernels instead of trapping; read back by the host)
+// ------------------------------------------------------------------------------------------
+enum : int {
+  QKD_BARRIER_TIMEOUT = 1,   // a bounded grid/group barrier wait expired
+  QKD_BAD_INDEX = 2,         // an index check failed
+  QKD_NEG_AMB = 4,           // A-B had a negative eigenvalue (reference prints a warning)
+  QKD_NEG_OMEGA = 8,         // Casida produced a negative Omega^2 (reference prints a warning)
+  QKD_QP_NOCONV = 16,        // a Newton QP search hit 64 iterations (reference prints "Cvg Failed!")
+  QKD_MBAR_TIMEOUT = 32      // an mbarrier wait expired in a tensor-core kernel
+};
+
+// stage timers (device time via cudaEvents on the context stream)
+enum {
+  T_BUILD = 0, T_TRIDIAG, T_TRIDIAG_EIGVEC, T_BACKTRANS, T_SLAB, T_RHO, T_SIGMA, T_QP, T_CASIDA2,
+  T_MISC, T_NUM
+};
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+enum {
+  W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
+  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_NUMBUF
+};
+
+struct qk_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[2 * T_NUM + 2] = {};
+  double timings[T_NUM] = {};
+  std::string err;
+  int* d_status = nullptr;      // device status word
+  unsigned* d_bar = nullptr;    // grid-barrier counters (zeroed before each cooperative launch)
+  DevBuf buf[W_NUMBUF];
+  long long launches = 0;
+  int last_dev_status = 0;
+};
+
+// ------------------------------------------------------------------------------------------
+// error helpers
+// ------------------------------------------------------------------------------------------
+int qk_fail(qk_ctx* ctx, int code, const char* fmt, ...);
+int qk_cuda_fail(qk_ctx* ctx, cudaError_t e, const char* what, const char* file, int line);
+
+#define QK_CK(call)                                                                  \
+  do {                                                                               \
+    cudaError_t _e = (call);                                                         \
+    if (_e != cudaSuccess) return qk_cuda_fail(ctx, _e, #call, __FILE__, __LINE__);  \
+  } while (0)
+
+#define QK_LAUNCHED()                                                                \
+  do {                                                                               \
+    ctx->launches++;                                                                 \
+    cudaError_t _e = cudaGetLastError();                                             \
+    if (_e != cudaSuccess) return qk_cuda_fail(ctx, _e, "kernel launch", __FILE__, __LINE__); \
+  } while (0)
+
+#define QK_TRY(expr)                  \
+  do {                                \
+    int _s = (expr);                  \
+    if (_s != QK_OK) return _s;       \
+  } while (0)
+
+// grow-only device workspace slot
+int qk_ws(qk_ctx* ctx, int slot, size_t bytes, void** out);
+template <class T>
+inline int qk_wst(qk_ctx* ctx, int slot, size_t count, T** out) {
+  return qk_ws(ctx, slot, count * sizeof(T), (void**)out);
+}
+// reset and read back the device status word
+int qk_status_reset(qk_ctx* ctx);
+int qk_status_check(qk_ctx* ctx, int fatal_mask);
+
+// stage timing
+void qk_tic(qk_ctx* ctx, int stage);
+void qk_toc(qk_ctx* ctx, int stage);
+void qk_timings_clear(qk_ctx* ctx);
+void qk_timings_collect(qk_ctx* ctx);
+
+// ------------------------------------------------------------------------------------------
+// kernel-level entry points (all enqueue on ctx->stream; device pointers)
+// ------------------------------------------------------------------------------------------
+// DMMA FP64 GEMM, column-major: C = alpha*op(A)*op(B) + beta*C, batched by strides.
+int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, const double* A,
+             long long lda, long long strideA, const double* B, long long ldb, long long strideB,
+             double beta, double* C, long long ldc, long long strideC, int batch);
+
+// dense symmetric eigensolver pieces
+int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, int want_vectors);
+
+// Casida pieces (k_casida.cu)
+int qk_launch_build_AB(qk_ctx* ctx, int which, int ispin, int dRPA, int N, int nC, int nO, int nR,
+                       double lambda, const double* e, const double* ERI, double* out);
+int qk_launch_casida_M(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e,
+                       const double* ERI, double* M, double* sq, double* trA);
+int qk_launch_casida_M_from_AB(qk_ctx* ctx, int nS, const double* A, const double* B, double* M,
+                               double* sq, double* trA);
+int qk_launch_xpy(qk_ctx* ctx, int nS, const double* w, const double* Zt, const double* sq,
+                  double* Om, double* XpY, double* XmY, int want_xmy);
+int qk_launch_sum_sqrt(qk_ctx* ctx, int nS, const double* w, double* out);
+int qk_launch_slab_gather(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* ERI,
+                          double* S);
+
+// self-energy / QP pieces (k_sigma.cu)
+int qk_sigma_diag(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
+                  int nS, const double* e, const double* Om, const double* rho, double* Sig,
+                  double* Z, double* EcGM);
+int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
+                 int nS, const double* eHF, const double* Om, const double* rho,
+                 const double* eGWlin, const double* eOld, double* eGW, double* Z);
+int qk_qp_linear(qk_ctx* ctx, int N, const double* eHF, const double* Z, const double* Sig,
+                 int use_z, double* eGW);
+int qk_diis_dev(qk_ctx* ctx, int n_err, int n_e, int n_diis, double* err_hist, double* e_hist,
+                const double* err_in, double* e_inout, double* rcond_dev);
+int qk_sub(qk_ctx* ctx, int n, const double* a, const double* b, double* out);
+int qk_max_abs_diff(qk_ctx* ctx, int n, const double* a, const double* b, double* out_dev);
+
+// BF16x3 tensor-core GEMM (k_bf16x3.cu): C(m x n, ldc) = A(m x k) * B(n x k)^T, column-major,
+// FP64 in/out, three-way BF16 split, FP32 accumulation in TMEM.
+int qk_gemm_bf16x3_nt(qk_ctx* ctx, int m, int n, int k, const double* A, long long lda,
+                      const double* B, long long ldb, double* C, long long ldc);
+
+// ------------------------------------------------------------------------------------------
+// device helpers
+// ------------------------------------------------------------------------------------------
+#define QK_MAX_SPIN (1u << 25)
+
+__device__ __forceinline__ unsigned qk_ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Monotone-counter barrier over `nblocks` co-resident CTAs (cooperative launch guarantees
+// co-residency).  Bounded: after QK_MAX_SPIN polls it records QKD_BARRIER_TIMEOUT and returns
+// false; callers then leave the kernel.  `epoch` counts barriers passed by this CTA.
+__device__ __forceinline__ bool qk_grid_barrier(unsigned* counter, unsigned nblocks,
+                                                unsigned& epoch, int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    epoch++;
+    unsigned target = epoch * nblocks;
+    __threadfence();
+    atomicAdd(counter, 1u);
+    unsigned spins = 0;
+    while (qk_ld_acquire(counter) < target) {
+      if (++spins > QK_MAX_SPIN) { atomicOr(status, QKD_BARRIER_TIMEOUT); ok = 0; break; }
+      if (spins > 64) __nanosleep(64);
+    }
+    if (ok && (*((volatile int*)status) & QKD_BARRIER_TIMEOUT)) ok = 0;
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+template <class T>
+__device__ __forceinline__ T qk_block_sum(T v, T* red /* >= 32 entries */) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  T s = (T)0;
+  if (wid == 0) {
+    s = lane < nw ? red[lane] : (T)0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) red[0] = s;
+  }
+  __syncthreads();
+  s = red[0];
+  return s;
+}

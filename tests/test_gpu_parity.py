@@ -1,0 +1,295 @@
+"""GPU parity tests: every stage and driver of libqkgw.so (through the C ABI) against the CPU
+oracle on the same seeded inputs, plus the committed golden fixtures.
+
+Tolerances (FP64 plain form): quasiparticle energies and Casida excitation energies within
+1e-8 Ha of the oracle (the bar of the FP64 path); stage outputs that involve no eigensolve are
+compared at 1e-12 relative; eigenvectors are compared up to sign (rows of XpY), since LAPACK
+and the GPU solver may pick either sign.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import qkgw_oracle as O
+from oracle.he631g import GOLDEN, he_system
+from quack_gb300 import api, synth
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+E_TOL = 1e-8
+
+
+def _sys(N, nO, naux, seed):
+    s = synth.small_system(N, nO, naux, seed)
+    return s, synth.eri_phys_numpy(s["L"])
+
+
+def _align_rows(X, R):
+    sg = np.sign(np.sum(X * R, axis=1))
+    sg[sg == 0] = 1.0
+    return X * sg[:, None]
+
+
+# --------------------------------------------------------------------------------------------
+# eigensolver
+# --------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 17, 64, 130, 257, 700])
+def test_dsyev_random(ctx, n):
+    import torch
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n))
+    A = A + A.T
+    w_ref, V_ref = np.linalg.eigh(A)
+    dA = torch.from_numpy(np.asfortranarray(A).ravel(order="F")).cuda()
+    dw = torch.empty(n, dtype=torch.float64, device="cuda")
+    dZ = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    api.dsyev_dev(n, dA.data_ptr(), n, dw.data_ptr(), dZ.data_ptr(), True, ctx=ctx)
+    torch.cuda.synchronize()
+    w = dw.cpu().numpy()
+    Zt = dZ.cpu().numpy().reshape((n, n), order="F")   # rows = eigenvectors
+    nrm = np.abs(w_ref).max()
+    assert np.max(np.abs(w - w_ref)) < 1e-12 * nrm * max(1, np.sqrt(n))
+    res = A @ Zt.T - Zt.T * w[None, :]
+    assert np.max(np.abs(res)) < 1e-11 * nrm
+    assert np.max(np.abs(Zt @ Zt.T - np.eye(n))) < 1e-10
+
+
+def test_dsyev_degenerate_clusters(ctx):
+    """Exactly repeated eigenvalues (block copies) exercise the cluster Gram-Schmidt."""
+    import torch
+    rng = np.random.default_rng(7)
+    k = 40
+    B = rng.standard_normal((k, k))
+    B = B + B.T
+    Q, _ = np.linalg.qr(rng.standard_normal((3 * k, 3 * k)))
+    A = Q @ np.kron(np.eye(3), B) @ Q.T
+    A = 0.5 * (A + A.T)
+    n = 3 * k
+    w_ref = np.linalg.eigvalsh(A)
+    dA = torch.from_numpy(np.asfortranarray(A).ravel(order="F")).cuda()
+    dw = torch.empty(n, dtype=torch.float64, device="cuda")
+    dZ = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    api.dsyev_dev(n, dA.data_ptr(), n, dw.data_ptr(), dZ.data_ptr(), True, ctx=ctx)
+    w = dw.cpu().numpy()
+    Zt = dZ.cpu().numpy().reshape((n, n), order="F")
+    assert np.max(np.abs(w - w_ref)) < 1e-11
+    assert np.max(np.abs(Zt @ Zt.T - np.eye(n))) < 1e-9
+    assert np.max(np.abs(A @ Zt.T - Zt.T * w[None, :])) < 1e-10
+
+
+def test_dsyev_values_only(ctx):
+    import torch
+    rng = np.random.default_rng(3)
+    n = 333
+    A = rng.standard_normal((n, n))
+    A = A @ A.T
+    dA = torch.from_numpy(np.asfortranarray(A).ravel(order="F")).cuda()
+    dw = torch.empty(n, dtype=torch.float64, device="cuda")
+    api.dsyev_dev(n, dA.data_ptr(), n, dw.data_ptr(), 0, False, ctx=ctx)
+    w_ref = np.linalg.eigvalsh(A)
+    assert np.max(np.abs(dw.cpu().numpy() - w_ref)) < 1e-12 * w_ref.max()
+
+
+# --------------------------------------------------------------------------------------------
+# stages
+# --------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("ispin,dRPA", [(1, True), (1, False), (2, True), (2, False)])
+def test_phRLR_A_B(ctx, ispin, dRPA):
+    s, E = _sys(11, 3, 33, 1)
+    N, nO, nC, nR = 11, 3, 0, 1
+    nS = (nO - nC) * (N - nO - nR)
+    A = api.phRLR_A(ispin, dRPA, N, nC, nO, N - nO, nR, nS, 0.7, s["eHF"], E, ctx=ctx)
+    B = api.phRLR_B(ispin, dRPA, N, nC, nO, N - nO, nR, nS, 0.7, E, ctx=ctx)
+    Ar = O.phRLR_A(ispin, dRPA, N, nC, nO, N - nO, nR, nS, 0.7, s["eHF"], E)
+    Br = O.phRLR_B(ispin, dRPA, N, nC, nO, N - nO, nR, nS, 0.7, E)
+    if dRPA:
+        assert np.array_equal(A, Ar) and np.array_equal(B, Br)   # same arithmetic, bit-exact
+    else:
+        assert np.allclose(A, Ar, rtol=1e-14, atol=1e-15)
+        assert np.allclose(B, Br, rtol=1e-14, atol=1e-15)
+
+
+@pytest.mark.parametrize("dRPA", [True, False])
+def test_phRLR(ctx, dRPA):
+    s, E = _sys(14, 4, 42, 2)
+    N, nO = 14, 4
+    nS = nO * (N - nO)
+    Ar = O.phRLR_A(1, dRPA, N, 0, nO, N - nO, 0, nS, 1.0, s["eHF"], E)
+    Br = O.phRLR_B(1, dRPA, N, 0, nO, N - nO, 0, nS, 1.0, E)
+    Ec, Om, XpY, XmY = api.phRLR(False, nS, Ar, Br, ctx=ctx)
+    Ecr, Omr, XpYr, XmYr = O.phRLR(False, nS, Ar, Br)
+    assert abs(Ec - Ecr) < E_TOL
+    assert np.max(np.abs(Om - Omr)) < 1e-10
+    assert np.allclose(_align_rows(XpY, XpYr), XpYr, atol=1e-8)
+    assert np.allclose(_align_rows(XmY, XmYr), XmYr, atol=1e-8)
+
+
+def test_excitation_density(ctx):
+    s, E = _sys(13, 3, 39, 3)
+    N, nO, nC, nR = 13, 3, 1, 0
+    nS = (nO - nC) * (N - nO - nR)
+    X = np.random.default_rng(0).standard_normal((nS, nS))
+    rho = api.RGW_excitation_density(N, nC, nO, nR, nS, E, X, ctx=ctx)
+    ref = O.RGW_excitation_density(N, nC, nO, nR, nS, E, X)
+    assert np.allclose(rho, ref, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("eta,srg", [(0.0, False), (0.1, False), (0.0, True)])
+def test_self_energy_diag(ctx, eta, srg):
+    s, E = _sys(12, 3, 36, 4)
+    N, nO, nC, nR = 12, 3, 0, 1
+    nS = (nO - nC) * (N - nO - nR)
+    A = O.phRLR_A(1, True, N, nC, nO, N - nO, nR, nS, 1.0, s["eHF"], E)
+    B = O.phRLR_B(1, True, N, nC, nO, N - nO, nR, nS, 1.0, E)
+    _, Om, XpY, _ = O.phRLR(False, nS, A, B)
+    rho = O.RGW_excitation_density(N, nC, nO, nR, nS, E, XpY)
+    if srg:
+        gm, Sig, Z = api.RGW_SRG_self_energy_diag(500.0, N, N, nC, nO, N - nO, nR, nS, s["eHF"], Om,
+                                                  rho, ctx=ctx)
+        gmr, Sigr, Zr = O.RGW_SRG_self_energy_diag(500.0, N, N, nC, nO, N - nO, nR, nS, s["eHF"], Om, rho)
+    else:
+        gm, Sig, Z = api.RGW_self_energy_diag(eta, N, N, nC, nO, N - nO, nR, nS, s["eHF"], Om, rho,
+                                              ctx=ctx)
+        gmr, Sigr, Zr = O.RGW_self_energy_diag(eta, N, N, nC, nO, N - nO, nR, nS, s["eHF"], Om, rho)
+    assert np.allclose(Sig, Sigr, rtol=1e-11, atol=1e-13)
+    assert np.allclose(Z, Zr, rtol=1e-11, atol=1e-13)
+    assert abs(gm - gmr) < 1e-11
+
+
+@pytest.mark.parametrize("srg", [False, True])
+def test_qp_graph(ctx, srg):
+    s, E = _sys(12, 3, 36, 5)
+    N, nO, nC, nR = 12, 3, 0, 0
+    nS = nO * (N - nO)
+    A = O.phRLR_A(1, True, N, nC, nO, N - nO, nR, nS, 1.0, s["eHF"], E)
+    B = O.phRLR_B(1, True, N, nC, nO, N - nO, nR, nS, 1.0, E)
+    _, Om, XpY, _ = O.phRLR(False, nS, A, B)
+    rho = O.RGW_excitation_density(N, nC, nO, nR, nS, E, XpY)
+    if srg:
+        _, Sig, Z = O.RGW_SRG_self_energy_diag(500.0, N, N, nC, nO, N - nO, nR, nS, s["eHF"], Om, rho)
+    else:
+        _, Sig, Z = O.RGW_self_energy_diag(0.0, N, N, nC, nO, N - nO, nR, nS, s["eHF"], Om, rho)
+    lin = s["eHF"] + Z * Sig
+    eGW, Zn = api.RGW_QP_graph(srg, 0.0, 500.0, N, nC, nO, N - nO, nR, nS, s["eHF"], Om, rho, lin,
+                               s["eHF"], Z, ctx=ctx)
+    eR, ZR = O.RGW_QP_graph(srg, 0.0, 500.0, N, nC, nO, N - nO, nR, nS, s["eHF"], Om, rho, lin,
+                            s["eHF"], Z)
+    assert np.max(np.abs(eGW - eR)) < 1e-10
+    assert np.max(np.abs(Zn - ZR)) < 1e-9
+
+
+def test_aotomo(ctx):
+    rng = np.random.default_rng(9)
+    nB, nOrb = 9, 7
+    ERI = rng.standard_normal((nB,) * 4)
+    c = rng.standard_normal((nB, nOrb))
+    out = api.AOtoMO_ERI_RHF(nB, nOrb, c, ERI, ctx=ctx)
+    ref = O.AOtoMO_ERI_RHF(nB, nOrb, c, ERI)
+    assert np.allclose(out, ref, rtol=1e-12, atol=1e-11)
+
+
+def test_diis(ctx):
+    rng = np.random.default_rng(4)
+    n, md = 10, 4
+    err = np.zeros((n, md), order="F")
+    ee = np.zeros((n, md), order="F")
+    err_r, ee_r = err.copy(), ee.copy()
+    for nd in range(1, 6):
+        r, e = rng.standard_normal(n), rng.standard_normal(n)
+        k = min(nd, md)
+        rc, out = api.DIIS_extrapolation(n, n, k, err, ee, r, e, ctx=ctx)
+        rcr, err_r, ee_r, outr = O.DIIS_extrapolation(k, err_r, ee_r, r, e)
+        assert np.allclose(out, outr, rtol=1e-10, atol=1e-12)
+        assert np.allclose(err, err_r) and np.allclose(ee, ee_r)
+
+
+# --------------------------------------------------------------------------------------------
+# drivers
+# --------------------------------------------------------------------------------------------
+def test_he_g0w0_featherbench(ctx):
+    he = he_system()
+    r = api.RG0W0(api.GWOptions(), 2, 2, 0, 1, 1, 0, 1, he["ERI_MO"], he["eHF"], ctx=ctx)
+    assert abs(r["EcRPA"] - GOLDEN["G0W0 correlation energy"]) < 1e-9
+    assert abs(r["eGW"][0] - GOLDEN["G0W0 HOMO energy"]) < 1e-9
+    assert abs(r["eGW"][1] - GOLDEN["G0W0 LUMO energy"]) < 1e-9
+
+
+def test_he_evgw_featherbench(ctx):
+    he = he_system()
+    opt = api.GWOptions(maxSCF=256, thresh=1e-5, max_diis=1)
+    r = api.evRGW(opt, 2, 2, 0, 1, 1, 0, 1, he["ERI_MO"], he["eHF"], ctx=ctx)
+    assert abs(r["EcRPA"] - GOLDEN["evGW correlation energy"]) < 1e-9
+    assert abs(r["eGW"][0] - GOLDEN["evGW HOMO energy"]) < 1e-9
+    assert abs(r["eGW"][1] - GOLDEN["evGW LUMO energy"]) < 1e-9
+
+
+@pytest.mark.parametrize("name", ["synth_n24", "synth_n13_frozen"])
+def test_g0w0_fixtures(ctx, name):
+    f = np.load(os.path.join(GOLD, name + ".npz"))
+    N, nO, nC, nR = int(f["N"]), int(f["nO"]), int(f["nC"]), int(f["nR"])
+    E = synth.eri_phys_numpy(f["L"])
+    nS = (nO - nC) * (N - nO - nR)
+    for tag, opt in (("g0w0", api.GWOptions()), ("g0w0lin", api.GWOptions(linearize=True)),
+                     ("g0w0srg", api.GWOptions(reg=True, eta=0.05))):
+        r = api.RG0W0(opt, N, N, nC, nO, N - nO, nR, nS, E, f["eHF"], ctx=ctx)
+        act = slice(nC, N - nR)
+        assert np.max(np.abs(r["eGW"][act] - f[tag + "_eGW"][act])) < E_TOL, tag
+        assert np.max(np.abs(r["SigC"] - f[tag + "_SigC"])) < E_TOL, tag
+        assert np.max(np.abs(r["Z"][act] - f[tag + "_Z"][act])) < 1e-7, tag
+        assert abs(r["EcRPA"] - float(f[tag + "_EcRPA"])) < E_TOL, tag
+        assert abs(r["EcGM"] - float(f[tag + "_EcGM"])) < E_TOL, tag
+        if tag == "g0w0":
+            assert np.max(np.abs(r["Om"] - f["g0w0_Om"])) < E_TOL
+
+
+@pytest.mark.parametrize("name", ["synth_n24", "synth_n13_frozen"])
+def test_evgw_fixtures(ctx, name):
+    f = np.load(os.path.join(GOLD, name + ".npz"))
+    N, nO, nC, nR = int(f["N"]), int(f["nO"]), int(f["nC"]), int(f["nR"])
+    E = synth.eri_phys_numpy(f["L"])
+    nS = (nO - nC) * (N - nO - nR)
+    act = slice(nC, N - nR)
+    for nd in (1, 5):
+        r = api.evRGW(api.GWOptions(maxSCF=64, thresh=1e-5, max_diis=nd), N, N, nC, nO, N - nO, nR,
+                      nS, E, f["eHF"], ctx=ctx)
+        assert r["nSCF"] == int(f["evgw_d%d_nSCF" % nd])
+        assert np.max(np.abs(r["eGW"][act] - f["evgw_d%d_eGW" % nd][act])) < E_TOL
+        assert abs(r["EcRPA"] - float(f["evgw_d%d_EcRPA" % nd])) < E_TOL
+    r = api.evRGW(api.GWOptions(maxSCF=64, thresh=1e-5, max_diis=5, linearize=True), N, N, nC, nO,
+                  N - nO, nR, nS, E, f["eHF"], ctx=ctx)
+    assert r["nSCF"] == int(f["evgwlin_nSCF"])
+    assert np.max(np.abs(r["eGW"][act] - f["evgwlin_eGW"][act])) < E_TOL
+
+
+def test_evgw_maxscf_failure_reported(ctx):
+    """maxSCF exhausted -> QK_ERR_NO_CONV (the reference stops, evRGW.f90:190-198)."""
+    f = np.load(os.path.join(GOLD, "synth_n24.npz"))
+    E = synth.eri_phys_numpy(f["L"])
+    with pytest.raises(api.QkError) as ei:
+        api.evRGW(api.GWOptions(maxSCF=0, thresh=1e-12, max_diis=1), 24, 24, 0, 5, 19, 0, 95, E,
+                  f["eHF"], ctx=ctx)
+    assert ei.value.code == api.QK_ERR_NO_CONV
+
+
+def test_bad_arguments_rejected(ctx):
+    f = np.load(os.path.join(GOLD, "synth_n24.npz"))
+    E = synth.eri_phys_numpy(f["L"])
+    with pytest.raises(api.QkError) as ei:
+        api.RG0W0(api.GWOptions(), 24, 24, 0, 5, 19, 0, 96, E, f["eHF"], ctx=ctx)
+    assert ei.value.code == api.QK_ERR_ARG
+    with pytest.raises(api.QkError) as ei:
+        api.RG0W0(api.GWOptions(TDA_W=True), 24, 24, 0, 5, 19, 0, 95, E, f["eHF"], ctx=ctx)
+    assert ei.value.code == api.QK_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("N,nO,seed", [(40, 5, 21), (57, 7, 22), (96, 12, 23)])
+def test_g0w0_vs_live_oracle(ctx, N, nO, seed):
+    s, E = _sys(N, nO, 3 * N, seed)
+    nS = nO * (N - nO)
+    r = api.RG0W0(api.GWOptions(), N, N, 0, nO, N - nO, 0, nS, E, s["eHF"], ctx=ctx)
+    ref = O.RG0W0(False, 0.0, False, N, N, 0, nO, N - nO, 0, nS, E, s["eHF"])
+    assert np.max(np.abs(r["eGW"] - ref["eGW"])) < E_TOL
+    assert np.max(np.abs(r["Om"] - ref["Om"])) < E_TOL
+    assert abs(r["EcRPA"] - ref["EcRPA"]) < E_TOL
+    assert abs(r["EcGM"] - ref["EcGM"]) < E_TOL

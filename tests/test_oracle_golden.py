@@ -1,0 +1,160 @@
+"""CPU tests: pin the oracle to the reference's golden values and known answers.
+
+He/6-31G values: FeatherBench (reference tests/feather_bench.py:62-91); the reference bench
+compares at relative 1e-7 by default (tests/lunch_bench.py:62-69).  The evGW goldens are
+reproduced with the DIIS extrapolation off (max_diis = 1); with DIIS = 5, as in
+tests/inp/options.RHF, evRGW.f90 as written follows a different trajectory that stops
+2.9e-7 Ha away (still inside its 1e-5 convergence threshold), so the goldens were evidently
+produced without DIIS.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import qkgw_oracle as O
+from oracle.he631g import GOLDEN, he_system
+from quack_gb300 import synth
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def he():
+    return he_system()
+
+
+def test_he_rhf_matches_featherbench(he):
+    assert abs(he["ERHF"] - GOLDEN["RHF energy"]) < 1e-10
+    assert abs(he["eHF"][0] - GOLDEN["RHF HOMO energy"]) < 1e-9
+    assert abs(he["eHF"][1] - GOLDEN["RHF LUMO energy"]) < 1e-9
+
+
+def test_he_g0w0_matches_featherbench(he):
+    r = O.RG0W0(False, 0.0, False, 2, 2, 0, 1, 1, 0, 1, he["ERI_MO"], he["eHF"])
+    assert abs(r["EcRPA"] - GOLDEN["G0W0 correlation energy"]) < 1e-10
+    assert abs(r["eGW"][0] - GOLDEN["G0W0 HOMO energy"]) < 1e-10
+    assert abs(r["eGW"][1] - GOLDEN["G0W0 LUMO energy"]) < 1e-10
+    assert abs(r["EcRPA_HF"] - GOLDEN["phRPA correlation energy"]) < 1e-10
+
+
+def test_he_evgw_matches_featherbench_without_diis(he):
+    r = O.evRGW(256, 1e-5, 1, False, 0.0, False, 2, 2, 0, 1, 1, 0, 1, he["ERI_MO"], he["eHF"])
+    assert abs(r["EcRPA"] - GOLDEN["evGW correlation energy"]) < 1e-10
+    assert abs(r["eGW"][0] - GOLDEN["evGW HOMO energy"]) < 1e-10
+    assert abs(r["eGW"][1] - GOLDEN["evGW LUMO energy"]) < 1e-10
+
+
+def test_he_evgw_with_diis_within_threshold(he):
+    r = O.evRGW(256, 1e-5, 5, False, 0.0, False, 2, 2, 0, 1, 1, 0, 1, he["ERI_MO"], he["eHF"])
+    assert abs(r["eGW"][0] - GOLDEN["evGW HOMO energy"]) < 1e-5
+    assert r["nSCF"] == 3
+
+
+def test_casida_closed_form_ns1(he):
+    """nS = 1: Omega = sqrt(Delta (Delta + 4 (ia|ia)))."""
+    E, e = he["ERI_MO"], he["eHF"]
+    A = O.phRLR_A(1, True, 2, 0, 1, 1, 0, 1, 1.0, e, E)
+    B = O.phRLR_B(1, True, 2, 0, 1, 1, 0, 1, 1.0, E)
+    Ec, Om, XpY, XmY = O.phRLR(False, 1, A, B)
+    d = e[1] - e[0]
+    K = E[1, 0, 0, 1]
+    assert abs(Om[0] - np.sqrt(d * (d + 4 * K))) < 1e-13
+    assert abs(Ec - 0.5 * (Om[0] - A[0, 0])) < 1e-15
+
+
+def test_ecrpa_identity_and_orthogonality():
+    s = synth.small_system(12, 3, 36, 5)
+    E = synth.eri_phys_numpy(s["L"])
+    nS = 3 * 9
+    A = O.phRLR_A(1, True, 12, 0, 3, 9, 0, nS, 1.0, s["eHF"], E)
+    B = O.phRLR_B(1, True, 12, 0, 3, 9, 0, nS, 1.0, E)
+    Ec, Om, XpY, XmY = O.phRLR(False, nS, A, B)
+    assert abs(Ec - 0.5 * (Om.sum() - np.trace(A))) < 1e-12
+    # (X+Y)^T (X-Y) = 1 (Casida normalisation)
+    assert np.allclose(XpY @ XmY.T, np.eye(nS), atol=1e-10)
+    # A+B and A-B positive definite for the synthetic generator
+    assert np.linalg.eigvalsh(A + B).min() > 0 and np.linalg.eigvalsh(A - B).min() > 0
+
+
+def test_eri_symmetry_of_generator():
+    s = synth.small_system(7, 2, 21, 3)
+    E = synth.eri_phys_numpy(s["L"])
+    # <pq|rs> = <qp|sr> = <rq|ps> = <ps|rq> ... 8-fold for real orbitals
+    assert np.allclose(E, E.transpose(1, 0, 3, 2))
+    assert np.allclose(E, E.transpose(2, 1, 0, 3))
+    assert np.allclose(E, E.transpose(0, 3, 2, 1))
+    assert np.allclose(E, E.transpose(2, 3, 0, 1))
+
+
+def test_excitation_density_identity():
+    """rho with XpY = identity equals the ERI slab (pq|jb)."""
+    s = synth.small_system(8, 2, 24, 4)
+    E = synth.eri_phys_numpy(s["L"])
+    nS = 2 * 6
+    rho = O.RGW_excitation_density(8, 0, 2, 0, nS, E, np.eye(nS))
+    for j in range(2):
+        for b in range(6):
+            assert np.allclose(rho[:, :, j * 6 + b], E[:, j, :, 2 + b])
+
+
+def test_sigma_invariant_under_sign_flips():
+    s = synth.small_system(10, 2, 30, 6)
+    E = synth.eri_phys_numpy(s["L"])
+    nS = 16
+    A = O.phRLR_A(1, True, 10, 0, 2, 8, 0, nS, 1.0, s["eHF"], E)
+    B = O.phRLR_B(1, True, 10, 0, 2, 8, 0, nS, 1.0, E)
+    _, Om, XpY, _ = O.phRLR(False, nS, A, B)
+    rng = np.random.default_rng(0)
+    sg = rng.choice([-1.0, 1.0], size=nS)
+    r1 = O.RGW_excitation_density(10, 0, 2, 0, nS, E, XpY)
+    r2 = O.RGW_excitation_density(10, 0, 2, 0, nS, E, sg[:, None] * XpY)
+    s1 = O.RGW_self_energy_diag(0.0, 10, 10, 0, 2, 8, 0, nS, s["eHF"], Om, r1)
+    s2 = O.RGW_self_energy_diag(0.0, 10, 10, 0, 2, 8, 0, nS, s["eHF"], Om, r2)
+    assert np.allclose(s1[1], s2[1], rtol=1e-12, atol=1e-14)
+    assert abs(s1[0] - s2[0]) < 1e-12
+
+
+def test_aotomo_matches_einsum():
+    rng = np.random.default_rng(1)
+    nB, nO_ = 5, 4
+    ERI = rng.standard_normal((nB,) * 4)
+    c = rng.standard_normal((nB, nO_))
+    ref = np.einsum("abcd,ap,bq,cr,ds->pqrs", ERI, c, c, c, c)
+    assert np.allclose(O.AOtoMO_ERI_RHF(nB, nO_, c, ERI), ref)
+
+
+def test_diis_against_closed_form():
+    """Two-vector DIIS: weights minimise |w1 r1 + w2 r2| with w1 + w2 = 1."""
+    n = 4
+    rng = np.random.default_rng(2)
+    r1, r2 = rng.standard_normal(n), rng.standard_normal(n)
+    e1, e2 = rng.standard_normal(n), rng.standard_normal(n)
+    err = np.zeros((n, 3), order="F")
+    ee = np.zeros((n, 3), order="F")
+    _, err, ee, out = O.DIIS_extrapolation(1, err, ee, r1, e1)
+    assert np.allclose(out, e1)
+    rc, err, ee, out = O.DIIS_extrapolation(2, err, ee, r2, e2)
+    d = r2 - r1
+    w2 = -(r1 @ d) / (d @ d)
+    assert np.allclose(out, (1 - w2) * e1 + w2 * e2)
+    assert rc > 1e-13
+
+
+def test_fixtures_reproduce_with_oracle():
+    """The committed fixtures are what the oracle computes now (guards accidental edits)."""
+    for name in ("synth_n24", "synth_n13_frozen"):
+        f = np.load(os.path.join(GOLD, name + ".npz"))
+        N, nO, nC, nR = int(f["N"]), int(f["nO"]), int(f["nC"]), int(f["nR"])
+        E = synth.eri_phys_numpy(f["L"])
+        nS = (nO - nC) * (N - nO - nR)
+        r = O.RG0W0(False, 0.0, False, N, N, nC, nO, N - nO, nR, nS, E, f["eHF"])
+        assert np.allclose(r["eGW"], f["g0w0_eGW"], atol=1e-11)
+        assert abs(r["EcRPA"] - float(f["g0w0_EcRPA"])) < 1e-11
+
+
+def test_generator_is_deterministic():
+    a = synth.small_system(9, 2, 27, 123)
+    b = synth.small_system(9, 2, 27, 123)
+    assert np.array_equal(a["L"], b["L"]) and np.array_equal(a["eHF"], b["eHF"])
+    assert synth.n_occ(20) == 3 and synth.n_occ(24) == 3 and synth.n_occ(28) == 4
