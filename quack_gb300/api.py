@@ -293,3 +293,18 @@ def dsyev_dev(n, d_A, lda, d_w, d_Zt, want_vectors=True, ctx=None):
     c = _ctx(ctx)
     c.check(lib().qk_dsyev_dev(c.handle, n, C.c_void_p(d_A), lda, C.c_void_p(d_w),
                                C.c_void_p(d_Zt), int(bool(want_vectors))))
+
+
+def dgemm_dev(transa, transb, m, n, k, alpha, d_A, lda, d_B, ldb, beta, d_C, ldc, ctx=None):
+    """FP64 (DMMA) GEMM on device buffers, column-major."""
+    c = _ctx(ctx)
+    c.check(lib().qk_dgemm_dev(c.handle, C.c_char(transa.encode()), C.c_char(transb.encode()), m,
+                               n, k, C.c_double(alpha), C.c_void_p(d_A), lda, C.c_void_p(d_B), ldb,
+                               C.c_double(beta), C.c_void_p(d_C), ldc))
+
+
+def gemm_bf16x3_dev(m, n, k, d_A, lda, d_B, ldb, d_C, ldc, ctx=None):
+    """C = A B^T with the BF16x3 split on the tensor cores (FP64 in/out, FP32 accumulate)."""
+    c = _ctx(ctx)
+    c.check(lib().qk_gemm_bf16x3_dev(c.handle, m, n, k, C.c_void_p(d_A), lda, C.c_void_p(d_B), ldb,
+                                     C.c_void_p(d_C), ldc))

@@ -1,8 +1,354 @@
-// k_bf16x3.cu -- placeholder until the tcgen05 kernel lands.
+// k_bf16x3.cu -- split-precision (BF16x3) GEMM on the 5th-generation tensor cores.
+//
+// C(m,n) = sum_k A(m,k) B(n,k) for FP64 A (M x K, column-major) and B (N x K, column-major),
+// FP64 C.  This is the precision tier for the O(N^2 nS^2) excitation-density contraction
+// (GW/RGW_excitation_density.f90:48-50).
+//
+// Each FP64 operand is split into three BF16 parts, x = x0 + x1 + x2 with x0 = bf16(x),
+// x1 = bf16(x - x0), x2 = bf16(x - x0 - x1) (the differences are exact in FP64), and the
+// product keeps the six terms down to 2^-16 relative order:
+//     A0B0 + A0B1 + A1B0 + A0B2 + A1B1 + A2B0,
+// accumulated in FP32 in tensor memory.  Relative error per product is O(2^-24), i.e. FP32-like.
+//
+// Kernel shape (one 128 x 128 output tile per CTA, 128 threads):
+//   warp 0 lane 0 : TMA producer, loads the 3 A parts and 3 B parts of a 64-wide k block into
+//                   one pipeline stage (6 x 16 KB, 128B-swizzled K-major tiles)
+//   warp 1 lane 0 : MMA issuer, 6 products x 4 k-steps of tcgen05.mma.kind::f16 (M=128,N=128,K=16)
+//                   per stage, tcgen05.commit releases the stage / signals the accumulator
+//   warp 2        : allocates / frees 128 TMEM columns
+//   warps 0-3     : epilogue, tcgen05.ld 32x32b -> FP64 stores (each warp owns 32 TMEM lanes)
+// Every mbarrier wait is bounded; on expiry the kernel records QKD_MBAR_TIMEOUT, drains its own
+// copies (bounded) and frees TMEM before returning.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 #include "qk_internal.cuh"
+
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int STAGES = 2;
+constexpr int TILE_BYTES = 128 * BK * 2;           // 16 KB per part tile
+constexpr int STAGE_BYTES = 6 * TILE_BYTES;        // 96 KB
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr uint32_t MBAR_SPIN = 1u << 30;
+constexpr uint32_t TMEM_COLS = 128;
+
+__device__ __forceinline__ uint32_t su32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(su32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// bounded wait: false (and status bit) if the phase does not complete within ~2 s
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
+  if (mbar_test(bar, parity)) return true;
+  const uint64_t t0 = gtimer();
+  for (uint32_t i = 0; i < MBAR_SPIN; ++i) {
+    if (mbar_test(bar, parity)) return true;
+    if ((i & 255) == 255) {
+      if (gtimer() - t0 > 2000000000ull) break;
+      __nanosleep(32);
+    }
+  }
+  atomicOr(status, QKD_MBAR_TIMEOUT);
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x,
+                                            int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          su32(dst)),
+      "l"(map), "r"(su32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ uint64_t sdesc_sw128(const void* tile) {
+  const uint32_t a = su32(tile);
+  uint64_t d = 0;
+  d |= (uint64_t)((a & 0x3FFFF) >> 4);      // start address
+  d |= (uint64_t)1 << 16;                   // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                   // descriptor version (tcgen05)
+  d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          su32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+// instruction descriptor: D=F32, A=B=BF16, both K-major, N=128, M=128
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// the six (A part, B part) pairs, largest terms first
+__device__ __constant__ int kPairA[6] = {0, 0, 1, 0, 1, 2};
+__device__ __constant__ int kPairB[6] = {0, 1, 0, 2, 1, 0};
+
+__global__ void __launch_bounds__(128, 1)
+    k_gemm_bf16x3(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                  int M, int N, int Kpad, int rowsA, int rowsB, double* __restrict__ C,
+                  long long ldc, int n_tiles, int* status) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accum = empty + STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+  int* abort_flag = (int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = blockIdx.x;
+  const int m_tile = tile / n_tiles, n_tile = tile - m_tile * n_tiles;
+  const int m0 = m_tile * BM, n0 = n_tile * BN;
+  const int num_kb = Kpad / BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accum, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     su32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer ----------------
+    int issued = 0;
+    for (int kb = 0; kb < num_kb; ++kb) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (kb / STAGES) & 1;
+      if (!mbar_wait(&empty[s], ph ^ 1, status)) { *(volatile int*)abort_flag = 1; break; }
+      if (*(volatile int*)abort_flag) break;
+      uint8_t* st = smem + s * STAGE_BYTES;
+      mbar_expect_tx(&full[s], STAGE_BYTES);
+      const int k0 = kb * BK;
+      for (int p = 0; p < 3; ++p) {
+        tma_load_2d(st + p * TILE_BYTES, &mapA, &full[s], k0, p * rowsA + m0);
+        tma_load_2d(st + (3 + p) * TILE_BYTES, &mapB, &full[s], k0, p * rowsB + n0);
+      }
+      issued = kb + 1;
+    }
+    // drain: every issued stage must have landed before the CTA may exit
+    for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb)
+      mbar_wait(&full[kb % STAGES], (kb / STAGES) & 1, status);
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer ----------------
+    bool ok = true;
+    for (int kb = 0; kb < num_kb && ok; ++kb) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (kb / STAGES) & 1;
+      if (!mbar_wait(&full[s], ph, status)) { *(volatile int*)abort_flag = 1; ok = false; break; }
+      if (*(volatile int*)abort_flag) { ok = false; break; }
+      tc_fence_after();
+      uint8_t* st = smem + s * STAGE_BYTES;
+#pragma unroll
+      for (int pr = 0; pr < 6; ++pr) {
+        const uint64_t da = sdesc_sw128(st + kPairA[pr] * TILE_BYTES);
+        const uint64_t db = sdesc_sw128(st + (3 + kPairB[pr]) * TILE_BYTES);
+#pragma unroll
+        for (int j = 0; j < BK / 16; ++j)
+          umma_bf16(tmem, da + 2 * j, db + 2 * j, IDESC, (kb | pr | j) != 0);
+      }
+      umma_commit(&empty[s]);
+    }
+    umma_commit(accum);  // fires once all issued MMAs are complete (also on abort)
+  }
+  __syncwarp();
+  // ---------------- epilogue (all 4 warps) ----------------
+  const bool have = mbar_wait(accum, 0, status);
+  tc_fence_after();
+  // tcgen05.ld is warp-collective: take the decision per warp
+  const bool go = __all_sync(0xffffffffu, have && !*(volatile int*)abort_flag);
+  if (go) {
+    const int row = m0 + warp * 32 + lane;
+    const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      uint32_t r[32];
+      tmem_ld32(tbase + c0, r);
+      if (row < M) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = n0 + c0 + j;
+          if (col < N) C[(long long)row + ldc * col] = (double)__uint_as_float(r[j]);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 2)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS)
+                 : "memory");
+  (void)rowsB;
+}
+
+// Split a column-major FP64 matrix X (rows x K, ld) into three BF16 parts stored K-major:
+// P[p*rows_pad*Kpad + r*Kpad + k], zero padded to rows_pad x Kpad.
+__global__ void k_split3(int rows, int K, const double* __restrict__ X, long long ld, int rows_pad,
+                         int Kpad, __nv_bfloat16* __restrict__ P) {
+  __shared__ double t[32][33];
+  const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int i = ty; i < 32; i += 8) {
+    const int r = r0 + tx, k = k0 + i;
+    t[i][tx] = (r < rows && k < K) ? X[(long long)r + ld * k] : 0.0;
+  }
+  __syncthreads();
+  const size_t plane = (size_t)rows_pad * Kpad;
+  for (int i = ty; i < 32; i += 8) {
+    const int r = r0 + i, k = k0 + tx;
+    if (r < rows_pad && k < Kpad) {
+      const double x = t[tx][i];
+      const __nv_bfloat16 x0 = __double2bfloat16(x);
+      const double r1 = x - (double)__bfloat162float(x0);
+      const __nv_bfloat16 x1 = __double2bfloat16(r1);
+      const double r2 = r1 - (double)__bfloat162float(x1);
+      const __nv_bfloat16 x2 = __double2bfloat16(r2);
+      const size_t o = (size_t)r * Kpad + k;
+      P[o] = x0;
+      P[o + plane] = x1;
+      P[o + 2 * plane] = x2;
+    }
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+int make_map(qk_ctx* ctx, CUtensorMap* map, const void* base, int Kpad, long long rows_total) {
+  auto enc = get_encode();
+  if (!enc) return qk_fail(ctx, QK_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  cuuint64_t dims[2] = {(cuuint64_t)Kpad, (cuuint64_t)rows_total};
+  cuuint64_t strides[1] = {(cuuint64_t)Kpad * 2};
+  cuuint32_t box[2] = {BK, 128};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return qk_fail(ctx, QK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return QK_OK;
+}
+
+}  // namespace
+
+int qk_split3(qk_ctx* ctx, int rows, int K, const double* X, long long ld, int rows_pad, int Kpad,
+              void* parts) {
+  dim3 grid((rows_pad + 31) / 32, (Kpad + 31) / 32);
+  if (grid.y > 65535) return qk_fail(ctx, QK_ERR_ARG, "split: K too large");
+  k_split3<<<grid, dim3(32, 8), 0, ctx->stream>>>(rows, K, X, ld, rows_pad, Kpad,
+                                                  (__nv_bfloat16*)parts);
+  QK_LAUNCHED();
+  return QK_OK;
+}
+
+int qk_gemm_bf16x3_parts(qk_ctx* ctx, int m, int n, const void* Ap, int rowsA, const void* Bp,
+                         int rowsB, int Kpad, double* C, long long ldc) {
+  CUtensorMap ma, mb;
+  QK_TRY(make_map(ctx, &ma, Ap, Kpad, 3LL * rowsA));
+  QK_TRY(make_map(ctx, &mb, Bp, Kpad, 3LL * rowsB));
+  static bool attr = false;
+  if (!attr) {
+    QK_CK(cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               SMEM_BYTES));
+    attr = true;
+  }
+  const int m_tiles = rowsA / BM, n_tiles = rowsB / BN;
+  const long long tiles = (long long)m_tiles * n_tiles;
+  if (tiles > 0x7fffffffLL) return qk_fail(ctx, QK_ERR_ARG, "bf16x3: too many tiles");
+  k_gemm_bf16x3<<<(unsigned)tiles, 128, SMEM_BYTES, ctx->stream>>>(ma, mb, m, n, Kpad, rowsA, rowsB,
+                                                                   C, ldc, n_tiles, ctx->d_status);
+  QK_LAUNCHED();
+  return QK_OK;
+}
 
 int qk_gemm_bf16x3_nt(qk_ctx* ctx, int m, int n, int k, const double* A, long long lda,
                       const double* B, long long ldb, double* C, long long ldc) {
-  (void)m; (void)n; (void)k; (void)A; (void)lda; (void)B; (void)ldb; (void)C; (void)ldc;
-  return qk_fail(ctx, QK_ERR_UNSUPPORTED, "BF16x3 tier not built");
+  if (m <= 0 || n <= 0 || k <= 0) return QK_OK;
+  const int rowsA = (m + BM - 1) / BM * BM;
+  const int rowsB = (n + BN - 1) / BN * BN;
+  const int Kpad = (k + BK - 1) / BK * BK;
+  void *Ap = nullptr, *Bp = nullptr;
+  QK_TRY(qk_ws(ctx, W_SPLIT_A, (size_t)3 * rowsA * Kpad * 2, &Ap));
+  QK_TRY(qk_ws(ctx, W_SPLIT_B, (size_t)3 * rowsB * Kpad * 2, &Bp));
+  QK_TRY(qk_split3(ctx, m, k, A, lda, rowsA, Kpad, Ap));
+  QK_TRY(qk_split3(ctx, n, k, B, ldb, rowsB, Kpad, Bp));
+  return qk_gemm_bf16x3_parts(ctx, m, n, Ap, rowsA, Bp, rowsB, Kpad, C, ldc);
 }

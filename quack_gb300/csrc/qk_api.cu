@@ -608,4 +608,21 @@ int qk_evRGW(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, i
   return end(ctx, st);
 }
 
+int qk_dgemm_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, double alpha,
+                 const double* d_A, int lda, const double* d_B, int ldb, double beta, double* d_C,
+                 int ldc) {
+  QK_TRY(begin(ctx));
+  const int st = qk_dgemm(ctx, transa, transb, m, n, k, alpha, d_A, lda, 0, d_B, ldb, 0, beta, d_C,
+                          ldc, 0, 1);
+  return end(ctx, st);
+}
+
+int qk_gemm_bf16x3_dev(qk_ctx* ctx, int m, int n, int k, const double* d_A, int lda,
+                       const double* d_B, int ldb, double* d_C, int ldc) {
+  QK_TRY(begin(ctx));
+  if (lda < m || ldb < n || ldc < m) return qk_fail(ctx, QK_ERR_ARG, "bad leading dimensions");
+  const int st = qk_gemm_bf16x3_nt(ctx, m, n, k, d_A, lda, d_B, ldb, d_C, ldc);
+  return end(ctx, st);
+}
+
 }  // extern "C"
