@@ -142,6 +142,13 @@ int qk_dgemm_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, dou
 int qk_gemm_bf16x3_dev(qk_ctx* ctx, int m, int n, int k, const double* d_A, int lda,
                        const double* d_B, int ldb, double* d_C, int ldc);
 
+/* ---- diagnostics ------------------------------------------------------------------------- */
+/* The cudaStream_t (as void*) on which the context enqueues all of its kernels. */
+void* qk_stream(const qk_ctx* ctx);
+/* Measured FP64 peak of this GPU: back-to-back DMMA (mma.sync.m8n8k4.f64) and DFMA in registers,
+ * TFLOP/s. */
+int qk_probe_fp64_peak(qk_ctx* ctx, double* tflops_dmma, double* tflops_dfma);
+
 #ifdef __cplusplus
 }
 #endif

@@ -308,3 +308,18 @@ def gemm_bf16x3_dev(m, n, k, d_A, lda, d_B, ldb, d_C, ldc, ctx=None):
     c = _ctx(ctx)
     c.check(lib().qk_gemm_bf16x3_dev(c.handle, m, n, k, C.c_void_p(d_A), lda, C.c_void_p(d_B), ldb,
                                      C.c_void_p(d_C), ldc))
+
+
+def stream_handle(ctx=None) -> int:
+    """cudaStream_t of the context (for events on the stream the kernels run on)."""
+    c = _ctx(ctx)
+    lib().qk_stream.restype = C.c_void_p
+    return int(lib().qk_stream(c.handle) or 0)
+
+
+def probe_fp64_peak(ctx=None):
+    """(DMMA TFLOP/s, DFMA TFLOP/s) measured on this GPU."""
+    c = _ctx(ctx)
+    a, b = C.c_double(), C.c_double()
+    c.check(lib().qk_probe_fp64_peak(c.handle, C.byref(a), C.byref(b)))
+    return a.value, b.value

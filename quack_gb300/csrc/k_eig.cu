@@ -145,18 +145,36 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
           const double vi = upd ? vk[i] : 0.0, wi = upd ? wk[i] : 0.0;
           double* col = a.A + i;
           double acc = 0.0;
+          // loads are issued in batches of 8 ahead of the dependent stores so that the compiler
+          // does not serialise them (it cannot prove lda != 0)
+          int cc = cb;
           if (upd) {
-#pragma unroll 4
-            for (int cc = cb; cc < ce; ++cc) {
+            for (; cc + 8 <= ce; cc += 8) {
+              double x[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) x[u] = __ldcg(col + a.lda * (cc + u));
+#pragma unroll
+              for (int u = 0; u < 8; ++u) {
+                const double y = x[u] - vi * wk[cc + u] - wi * vk[cc + u];
+                __stcg(col + a.lda * (cc + u), y);
+                acc += y * vk1[cc + u];
+              }
+            }
+            for (; cc < ce; ++cc) {
               double* ptr = col + a.lda * cc;
-              double x = __ldcg(ptr);
-              x = x - vi * wk[cc] - wi * vk[cc];
-              __stcg(ptr, x);
-              acc += x * vk1[cc];
+              const double y = __ldcg(ptr) - vi * wk[cc] - wi * vk[cc];
+              __stcg(ptr, y);
+              acc += y * vk1[cc];
             }
           } else {
-#pragma unroll 4
-            for (int cc = cb; cc < ce; ++cc) acc += __ldcg(col + a.lda * cc) * vk1[cc];
+            for (; cc + 8 <= ce; cc += 8) {
+              double x[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) x[u] = __ldcg(col + a.lda * (cc + u));
+#pragma unroll
+              for (int u = 0; u < 8; ++u) acc += x[u] * vk1[cc + u];
+            }
+            for (; cc < ce; ++cc) acc += __ldcg(col + a.lda * cc) * vk1[cc];
           }
           if (wantp) atomicAdd(pnext + i, acc);
         }
@@ -230,21 +248,34 @@ __device__ __forceinline__ int sturm_count(int n, const double* __restrict__ d,
   return c;
 }
 
-// one thread per eigenvalue index j: bisection to full precision on the Sturm count
+// k-section on the Sturm count: KSEC consecutive lanes share eigenvalue j and test KSEC interior
+// points of the bracket per step (log2(KSEC+1) bits per step), to full FP64 precision.
+// Sturm counts are monotone in x in IEEE arithmetic, so the points with count <= j form a
+// prefix and the new bracket follows from a popcount of the group's ballot.
+constexpr int KSEC = 8;
 __global__ void k_stebz(int n, const double* __restrict__ d, const double* __restrict__ e2,
                         const double* __restrict__ prep, double* __restrict__ w) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = gt / KSEC, t = gt % KSEC;
+  const bool valid = j < n;
+  const int lane = threadIdx.x & 31;
+  const unsigned gmask = ((1u << KSEC) - 1u) << (lane & ~(KSEC - 1));
   double lo = prep[0], hi = prep[1];
   const double pivmin = prep[2];
-  for (int it = 0; it < 160; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (!(mid > lo && mid < hi)) break;
+  for (int it = 0; it < 96; ++it) {
     if (hi - lo <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + 2.0 * pivmin) break;
-    const int c = sturm_count(n, d, e2, mid, pivmin);
-    if (c <= j) lo = mid; else hi = mid;
+    const double h = (hi - lo) / (KSEC + 1);
+    const double x = lo + h * (t + 1);
+    const int c = valid ? sturm_count(n, d, e2, x, pivmin) : 0;
+    const unsigned le = __ballot_sync(gmask, c <= j) & gmask;
+    const int k = __popc(le);
+    const double nlo = k > 0 ? lo + h * k : lo;
+    const double nhi = k < KSEC ? lo + h * (k + 1) : hi;
+    if (!(nlo < nhi) || (nlo == lo && nhi == hi)) break;
+    lo = nlo;
+    hi = nhi;
   }
-  w[j] = 0.5 * (lo + hi);
+  if (valid && t == 0) w[j] = 0.5 * (lo + hi);
 }
 
 __device__ __forceinline__ double rand_pm1(unsigned long long i, unsigned long long j) {
@@ -415,7 +446,8 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   QK_CK(cudaMemsetAsync(ctx->d_bar, 0, 16 * sizeof(unsigned), ctx->stream));
 
   // ---- 1. tridiagonalisation ----
-  qk_tic(ctx, T_TRIDIAG);
+  const bool tm = ctx->time_eig;
+  if (tm) qk_tic(ctx, T_TRIDIAG);
   {
     const size_t smem_need = 3 * N * sizeof(double);
     const int use_smem = smem_need <= 200 * 1024;
@@ -451,27 +483,26 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
                                       ctx->stream));
     ctx->launches++;
   }
-  qk_toc(ctx, T_TRIDIAG);
+  if (tm) qk_toc(ctx, T_TRIDIAG);
 
   // ---- 2. eigenvalues by bisection ----
-  qk_tic(ctx, T_TRIDIAG_EIGVEC);
+  if (tm) qk_tic(ctx, T_BISECT);
   k_tri_prep<<<1, 1024, 0, ctx->stream>>>(n, d, e, e2, prep);
   QK_LAUNCHED();
-  k_stebz<<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, d, e2, prep, w);
+  k_stebz<<<(n * KSEC + 127) / 128, 128, 0, ctx->stream>>>(n, d, e2, prep, w);
   QK_LAUNCHED();
-  if (!want_vectors) {
-    qk_toc(ctx, T_TRIDIAG_EIGVEC);
-    return QK_OK;
-  }
+  if (tm) qk_toc(ctx, T_BISECT);
+  if (!want_vectors) return QK_OK;
   // ---- 3. eigenvectors of T by inverse iteration ----
   double* Wst = nullptr;
   QK_TRY(qk_wst(ctx, W_EIGWORK, 5 * N * N, &Wst));
+  if (tm) qk_tic(ctx, T_STEIN);
   k_stein<<<(n + 63) / 64, 64, 0, ctx->stream>>>(n, d, e, w, prep, Wst, Zt);
   QK_LAUNCHED();
-  qk_toc(ctx, T_TRIDIAG_EIGVEC);
+  if (tm) qk_toc(ctx, T_STEIN);
 
   // ---- 4. back-transformation Zt <- Zt * Q^T, blocks from last to first ----
-  qk_tic(ctx, T_BACKTRANS);
+  if (tm) qk_tic(ctx, T_BACKTRANS);
   const int nref = n - 2;  // reflectors 0..n-3 can be non-trivial
   if (nref > 0) {
     double *W1 = nullptr, *W2 = nullptr, *G = nullptr, *T = nullptr;
@@ -496,7 +527,7 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
       QK_TRY(qk_dgemm(ctx, 'N', 'T', n, m, nb, -1.0, W2, n, 0, Vb, n, 0, 1.0, Es, n, 0, 1));
     }
   }
-  qk_toc(ctx, T_BACKTRANS);
+  if (tm) qk_toc(ctx, T_BACKTRANS);
   return QK_OK;
 }
 

@@ -26,13 +26,20 @@ __global__ void __launch_bounds__(128) k_dgemm_dmma(int M, int N, int K, double 
                                                      long long sA, const double* __restrict__ B,
                                                      long long ldb, long long sB, double beta,
                                                      double* __restrict__ C, long long ldc,
-                                                     long long sC) {
+                                                     long long sC, int kc) {
   __shared__ double As[2][BK][LDS];
   __shared__ double Bs[2][BK][LDS];
   const long long bz = blockIdx.z;
-  A += bz * sA;
-  B += bz * sB;
-  C += bz * sC;
+  int kbeg = 0, kend = K;
+  if (kc > 0) {  // split-K: slice bz covers [bz*kc, min(K, bz*kc+kc)) and writes its own C slice
+    kbeg = (int)bz * kc;
+    kend = min(K, kbeg + kc);
+    C += bz * sC;
+  } else {
+    A += bz * sA;
+    B += bz * sB;
+    C += bz * sC;
+  }
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
@@ -53,7 +60,7 @@ __global__ void __launch_bounds__(128) k_dgemm_dmma(int M, int N, int K, double 
       if (!TA) { mm = idx & 63; kk = idx >> 6; } else { kk = idx & 15; mm = idx >> 4; }
       const int gm = m0 + mm, gk = k0 + kk;
       double v = 0.0;
-      if (gm < M && gk < K) v = !TA ? A[gm + lda * gk] : A[gk + lda * gm];
+      if (gm < M && gk < kend) v = !TA ? A[gm + lda * gk] : A[gk + lda * gm];
       ra[r] = v;
     }
   };
@@ -74,7 +81,7 @@ __global__ void __launch_bounds__(128) k_dgemm_dmma(int M, int N, int K, double 
       if (!TB) { kk = idx & 15; nn = idx >> 4; } else { nn = idx & 63; kk = idx >> 6; }
       const int gn = n0 + nn, gk = k0 + kk;
       double v = 0.0;
-      if (gn < N && gk < K) v = !TB ? B[gk + ldb * gn] : B[gn + ldb * gk];
+      if (gn < N && gk < kend) v = !TB ? B[gk + ldb * gn] : B[gn + ldb * gk];
       rb[r] = v;
     }
   };
@@ -88,14 +95,14 @@ __global__ void __launch_bounds__(128) k_dgemm_dmma(int M, int N, int K, double 
     }
   };
 
-  ldA(0);
-  ldB(0);
+  ldA(kbeg);
+  ldB(kbeg);
   stA(0);
   stB(0);
   __syncthreads();
   int s = 0;
-  for (int k0 = 0; k0 < K; k0 += BK) {
-    const bool more = (k0 + BK) < K;
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    const bool more = (k0 + BK) < kend;
     if (more) { ldA(k0 + BK); ldB(k0 + BK); }
 #pragma unroll
     for (int kk = 0; kk < BK; kk += 4) {
@@ -134,6 +141,40 @@ __global__ void __launch_bounds__(128) k_dgemm_dmma(int M, int N, int K, double 
   }
 }
 
+// C = alpha * sum_s W[s] + beta * C  (split-K reduction, column-major m x n)
+__global__ void k_splitk_reduce(int m, int n, int S, const double* __restrict__ W, double alpha,
+                                double beta, double* __restrict__ C, long long ldc) {
+  const long long total = (long long)m * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int s = 0; s < S; ++s) acc += W[(long long)s * total + i];
+    const int r = (int)(i % m);
+    const long long c = i / m;
+    double* cp = C + r + ldc * c;
+    double v = alpha * acc;
+    if (beta != 0.0) v += beta * (*cp);
+    *cp = v;
+  }
+}
+
+template <bool TA, bool TB>
+void launch(dim3 grid, cudaStream_t st, int m, int n, int k, double alpha, const double* A,
+            long long lda, long long sA, const double* B, long long ldb, long long sB, double beta,
+            double* C, long long ldc, long long sC, int kc) {
+  k_dgemm_dmma<TA, TB><<<grid, 128, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc,
+                                             sC, kc);
+}
+
+void launch_any(bool TA, bool TB, dim3 grid, cudaStream_t st, int m, int n, int k, double alpha,
+                const double* A, long long lda, long long sA, const double* B, long long ldb,
+                long long sB, double beta, double* C, long long ldc, long long sC, int kc) {
+  if (!TA && !TB) launch<false, false>(grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+  else if (!TA && TB) launch<false, true>(grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+  else if (TA && !TB) launch<true, false>(grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+  else launch<true, true>(grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+}
+
 }  // namespace
 
 int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, const double* A,
@@ -151,18 +192,32 @@ int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, c
   const bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
   dim3 grid((m + BM - 1) / BM, (n + BN - 1) / BN, batch);
   if (grid.y > 65535 || grid.z > 65535) return qk_fail(ctx, QK_ERR_ARG, "qk_dgemm: grid too large");
-  if (!TA && !TB)
-    k_dgemm_dmma<false, false><<<grid, 128, 0, ctx->stream>>>(m, n, k, alpha, A, lda, strideA, B, ldb,
-                                                             strideB, beta, C, ldc, strideC);
-  else if (!TA && TB)
-    k_dgemm_dmma<false, true><<<grid, 128, 0, ctx->stream>>>(m, n, k, alpha, A, lda, strideA, B, ldb,
-                                                            strideB, beta, C, ldc, strideC);
-  else if (TA && !TB)
-    k_dgemm_dmma<true, false><<<grid, 128, 0, ctx->stream>>>(m, n, k, alpha, A, lda, strideA, B, ldb,
-                                                            strideB, beta, C, ldc, strideC);
-  else
-    k_dgemm_dmma<true, true><<<grid, 128, 0, ctx->stream>>>(m, n, k, alpha, A, lda, strideA, B, ldb,
-                                                           strideB, beta, C, ldc, strideC);
+  const long long tiles = (long long)grid.x * grid.y;
+  // too few output tiles to fill the GPU and a long K: split K and reduce
+  if (batch == 1 && tiles * 2 < ctx->num_sms && k >= 4 * BK) {
+    int S = (int)((2LL * ctx->num_sms + tiles - 1) / tiles);
+    const int maxS = k / (2 * BK);
+    if (S > maxS) S = maxS;
+    if (S > 32) S = 32;
+    if (S >= 2) {
+      const int kc = ((k + S - 1) / S + BK - 1) / BK * BK;
+      S = (k + kc - 1) / kc;
+      double* W = nullptr;
+      QK_TRY(qk_wst(ctx, W_SPLITK, (size_t)S * m * n, &W));
+      grid.z = S;
+      launch_any(TA, TB, grid, ctx->stream, m, n, k, 1.0, A, lda, 0, B, ldb, 0, 0.0, W, m,
+                 (long long)m * n, kc);
+      QK_LAUNCHED();
+      long long total = (long long)m * n;
+      int blocks = (int)((total + 255) / 256);
+      if (blocks > 16 * ctx->num_sms) blocks = 16 * ctx->num_sms;
+      k_splitk_reduce<<<blocks, 256, 0, ctx->stream>>>(m, n, S, W, alpha, beta, C, ldc);
+      QK_LAUNCHED();
+      return QK_OK;
+    }
+  }
+  launch_any(TA, TB, grid, ctx->stream, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C,
+             ldc, strideC, 0);
   QK_LAUNCHED();
   return QK_OK;
 }

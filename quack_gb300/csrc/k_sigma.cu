@@ -30,21 +30,30 @@ struct SigArgs {
   const double* wp;    // evaluation energy per p (nullptr -> eq[p])
   const double* Om;
   const double* rho;
-  const int* active;   // per p flag (nullptr -> all active)
-  const int* nact;     // global count of active p (nullptr -> ignore)
+  const int* list;     // compacted list of active p (nullptr -> all p in [nC, N-nR))
+  const int* nact;     // length of list (nullptr -> ignore)
   double* part;        // 3 * nchunks * N : sig, dsig, occ-part
 };
 
 __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial(SigArgs a) {
   extern __shared__ double se[];  // N energies
   __shared__ double ssig[SIG_WARPS][32], sds[SIG_WARPS][32], socc[SIG_WARPS][32];
-  if (a.nact && *a.nact == 0) return;
+  const int nl = a.nact ? *a.nact : 0;
+  if (a.list && (int)blockIdx.x * 32 >= nl) return;  // no active orbital in this tile
   const int N = a.N;
   for (int i = threadIdx.x; i < N; i += blockDim.x) se[i] = a.eq[i];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int p = a.nC + blockIdx.x * 32 + lane;
   const int pend = N - a.nR;
-  const bool pok = p < pend && (a.active == nullptr || a.active[p] != 0);
+  int p;
+  bool pok;
+  if (a.list) {
+    const int idx = blockIdx.x * 32 + lane;
+    pok = idx < nl;
+    p = pok ? a.list[idx] : pend;
+  } else {
+    p = a.nC + blockIdx.x * 32 + lane;
+    pok = p < pend;
+  }
   __syncthreads();
   double sig = 0.0, ds = 0.0, socc_acc = 0.0;
   if (pok) {
@@ -145,31 +154,39 @@ struct QPState {
   int* nit;
   int* active;
   int* nact;
+  int* list;  // compacted active orbitals, ascending
 };
 
-__global__ void k_qp_init(int N, int nC, int nR, const double* __restrict__ eGWlin, QPState s) {
-  __shared__ int cnt;
-  if (threadIdx.x == 0) cnt = 0;
+// rebuild the compacted active list (one block; warp 0 walks the orbitals 32 at a time)
+__device__ void qp_compact(int N, QPState& s) {
   __syncthreads();
+  if (threadIdx.x < 32) {
+    int base = 0;
+    for (int p0 = 0; p0 < N; p0 += 32) {
+      const int p = p0 + threadIdx.x;
+      const bool act = p < N && s.active[p] != 0;
+      const unsigned b = __ballot_sync(0xffffffffu, act);
+      if (act) s.list[base + __popc(b & ((1u << threadIdx.x) - 1u))] = p;
+      base += __popc(b);
+    }
+    if (threadIdx.x == 0) *s.nact = base;
+  }
+}
+
+__global__ void k_qp_init(int N, int nC, int nR, const double* __restrict__ eGWlin, QPState s) {
   for (int p = threadIdx.x; p < N; p += blockDim.x) {
     s.w[p] = eGWlin[p];
     s.df[p] = 0.0;
     s.nit[p] = 0;
-    const int act = (p >= nC && p < N - nR);
-    s.active[p] = act;
-    if (act) atomicAdd(&cnt, 1);
+    s.active[p] = (p >= nC && p < N - nR);
   }
-  __syncthreads();
-  if (threadIdx.x == 0) *s.nact = cnt;
+  qp_compact(N, s);
 }
 
 // one Newton step for every still-active p (RGW_QP_graph.f90:56-76)
 __global__ void k_qp_update(int N, int nchunks, const double* __restrict__ part,
                             const double* __restrict__ eHF, QPState s) {
-  __shared__ int cnt;
   if (*s.nact == 0) return;
-  if (threadIdx.x == 0) cnt = 0;
-  __syncthreads();
   const size_t stride = (size_t)nchunks * N;
   for (int p = threadIdx.x; p < N; p += blockDim.x) {
     if (!s.active[p]) continue;
@@ -185,14 +202,9 @@ __global__ void k_qp_update(int N, int nchunks, const double* __restrict__ part,
     const double df = 1.0 / (1.0 - dsig);
     s.w[p] = w - df * f;
     s.df[p] = df;
-    if (!(fabs(f) > QP_THRESH) || nIt >= QP_MAXIT) {
-      s.active[p] = 0;
-    } else {
-      atomicAdd(&cnt, 1);
-    }
+    if (!(fabs(f) > QP_THRESH) || nIt >= QP_MAXIT) s.active[p] = 0;
   }
-  __syncthreads();
-  if (threadIdx.x == 0) *s.nact = cnt;
+  qp_compact(N, s);
 }
 
 __global__ void k_qp_finish(int N, int nC, int nR, const double* __restrict__ eGWlin, QPState s,
@@ -321,7 +333,7 @@ __global__ void k_diis(int n_err, int n_e, int nd, double* __restrict__ err,
 
 static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                        int nS, const double* eq, const double* wp, const double* Om,
-                       const double* rho, const int* active, const int* nact, double** part_out,
+                       const double* rho, const int* list, const int* nact, double** part_out,
                        int* nchunks_out) {
   const int nact_p = N - nR - nC;
   const int ptiles = (nact_p + 31) / 32;
@@ -338,7 +350,7 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
   a.N = N; a.nC = nC; a.nO = nO; a.nR = nR; a.nS = nS;
   a.nchunks = nchunks; a.mper = mper;
   a.doSRG = doSRG; a.eta = eta; a.flow = flow;
-  a.eq = eq; a.wp = wp; a.Om = Om; a.rho = rho; a.active = active; a.nact = nact; a.part = part;
+  a.eq = eq; a.wp = wp; a.Om = Om; a.rho = rho; a.list = list; a.nact = nact; a.part = part;
   if (ptiles > 0 && nS > 0) {
     k_sigma_partial<<<dim3(ptiles, nchunks), SIG_WARPS * 32, N * sizeof(double), ctx->stream>>>(a);
     QK_LAUNCHED();
@@ -364,20 +376,21 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
                  int nS, const double* eHF, const double* Om, const double* rho,
                  const double* eGWlin, const double* eOld, double* eGW, double* Z) {
   double* st = nullptr;
-  QK_TRY(qk_wst(ctx, W_M2, (size_t)4 * N + 64, &st));
+  QK_TRY(qk_wst(ctx, W_M2, (size_t)5 * N + 64, &st));
   QPState s;
   s.w = st;
   s.df = st + N;
   s.nit = (int*)(st + 2 * N);
   s.active = (int*)(st + 3 * N);
-  s.nact = (int*)(st + 4 * N);
+  s.list = (int*)(st + 4 * N);
+  s.nact = (int*)(st + 5 * N);
   k_qp_init<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, eGWlin, s);
   QK_LAUNCHED();
   int hact = 1;
   for (int it = 0; it < QP_MAXIT; ++it) {
     double* part;
     int nch;
-    QK_TRY(sigma_sweep(ctx, doSRG, eta, flow, N, nC, nO, nR, nS, eOld, s.w, Om, rho, s.active,
+    QK_TRY(sigma_sweep(ctx, doSRG, eta, flow, N, nC, nO, nR, nS, eOld, s.w, Om, rho, s.list,
                        s.nact, &part, &nch));
     k_qp_update<<<1, 1024, 0, ctx->stream>>>(N, nch, part, eHF, s);
     QK_LAUNCHED();

@@ -126,7 +126,10 @@ int casida_dev(qk_ctx* ctx, const Dims& d, const double* e, const double* ERI, d
   QK_TRY(qk_launch_casida_M(ctx, d.N, d.nC, d.nO, d.nR, e, ERI, M, sq, scal + 0));
   qk_toc(ctx, T_BUILD);
   if (want_vectors) QK_TRY(qk_wst(ctx, W_ZT, S2, &Zt));
-  QK_TRY(qk_eig_sym(ctx, d.nS, M, d.nS, w, Zt, want_vectors));
+  ctx->time_eig = want_vectors != 0;
+  const int est = qk_eig_sym(ctx, d.nS, M, d.nS, w, Zt, want_vectors);
+  ctx->time_eig = true;
+  QK_TRY(est);
   if (want_vectors) QK_TRY(qk_launch_xpy(ctx, d.nS, w, Zt, sq, Om, XpY, XmY, XmY != nullptr));
   QK_TRY(qk_launch_sum_sqrt(ctx, d.nS, w, scal + 1));
   k_ecrpa<<<1, 1, 0, ctx->stream>>>(scal + 1, scal + 0, scal + 2);

@@ -4,10 +4,9 @@
 #include <cstring>
 #include "qk_internal.cuh"
 
-static const char* k_timing_names[T_NUM] = {"casida_build", "tridiag",   "tridiag_eigvec",
-                                            "back_transform", "slab",   "rho",
-                                            "sigma",          "qp",     "casida2",
-                                            "misc"};
+static const char* k_timing_names[T_NUM] = {"casida_build", "tridiag", "bisect",  "stein",
+                                            "back_transform", "slab",    "rho",     "sigma",
+                                            "qp",             "casida2", "misc"};
 
 int qk_fail(qk_ctx* ctx, int code, const char* fmt, ...) {
   if (ctx) {

@@ -21,7 +21,7 @@ enum : int {
 
 // stage timers (device time via cudaEvents on the context stream)
 enum {
-  T_BUILD = 0, T_TRIDIAG, T_TRIDIAG_EIGVEC, T_BACKTRANS, T_SLAB, T_RHO, T_SIGMA, T_QP, T_CASIDA2,
+  T_BUILD = 0, T_TRIDIAG, T_BISECT, T_STEIN, T_BACKTRANS, T_SLAB, T_RHO, T_SIGMA, T_QP, T_CASIDA2,
   T_MISC, T_NUM
 };
 
@@ -32,7 +32,7 @@ struct DevBuf {
 
 enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
-  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_NUMBUF
+  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_NUMBUF
 };
 
 struct qk_ctx {
@@ -47,6 +47,7 @@ struct qk_ctx {
   DevBuf buf[W_NUMBUF];
   long long launches = 0;
   int last_dev_status = 0;
+  bool time_eig = true;  // stage timers inside the eigensolver (off for the eigenvalue-only pass)
 };
 
 // ------------------------------------------------------------------------------------------
