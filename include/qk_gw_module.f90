@@ -1,0 +1,141 @@
+! qk_gw_module.f90 -- Fortran bind(C) interfaces to libqkgw.so (include/qkgw.h).
+!
+! Same conventions as QuAcK's src/GPU/cu_quack_module.f90:11-36: integer(c_int) by value,
+! real(c_double) arrays with explicit shape (passed as the first element, Fortran column-major).
+! Every function returns an integer(c_int) status (0 = success).  The context is a type(c_ptr)
+! obtained once from qk_init.
+!
+! Source only: no Fortran compiler is available where this library is built; the interfaces
+! are checked against the C header by hand and the ABI itself is exercised from C/Python.
+module qk_gw_module
+
+  use, intrinsic :: iso_c_binding
+
+  implicit none
+
+  type, bind(C) :: qk_gw_params
+    real(c_double)    :: eta
+    integer(c_int)    :: linearize
+    integer(c_int)    :: doSRG
+    integer(c_int)    :: TDA_W
+    integer(c_int)    :: maxSCF
+    real(c_double)    :: thresh
+    integer(c_int)    :: max_diis
+    integer(c_int)    :: precision
+  end type qk_gw_params
+
+  integer(c_int), parameter :: QK_OK = 0, QK_ERR_NO_CONV = 5
+  integer(c_int), parameter :: QK_PREC_FP64 = 0, QK_PREC_BF16X3 = 1
+
+  interface
+
+    integer(c_int) function qk_init(device, ctx) bind(C, name="qk_init")
+      import c_int, c_ptr
+      integer(c_int), value :: device
+      type(c_ptr)           :: ctx
+    end function qk_init
+
+    integer(c_int) function qk_finalize(ctx) bind(C, name="qk_finalize")
+      import c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function qk_finalize
+
+    ! LR/phRLR_A.f90
+    integer(c_int) function qk_phRLR_A(ctx, ispin, dRPA, nBas, nC, nO, nV, nR, nS, lambda, e, ERI, Aph) &
+        bind(C, name="qk_phRLR_A")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      integer(c_int), value         :: ispin, dRPA, nBas, nC, nO, nV, nR, nS
+      real(c_double), value         :: lambda
+      real(c_double), intent(in)    :: e(nBas), ERI(nBas,nBas,nBas,nBas)
+      real(c_double), intent(out)   :: Aph(nS,nS)
+    end function qk_phRLR_A
+
+    ! LR/phRLR_B.f90
+    integer(c_int) function qk_phRLR_B(ctx, ispin, dRPA, nBas, nC, nO, nV, nR, nS, lambda, ERI, Bph) &
+        bind(C, name="qk_phRLR_B")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      integer(c_int), value         :: ispin, dRPA, nBas, nC, nO, nV, nR, nS
+      real(c_double), value         :: lambda
+      real(c_double), intent(in)    :: ERI(nBas,nBas,nBas,nBas)
+      real(c_double), intent(out)   :: Bph(nS,nS)
+    end function qk_phRLR_B
+
+    ! LR/phRLR.f90 (TDA must be 0)
+    integer(c_int) function qk_phRLR(ctx, TDA, nS, Aph, Bph, EcRPA, Om, XpY, XmY) bind(C, name="qk_phRLR")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      integer(c_int), value         :: TDA, nS
+      real(c_double), intent(in)    :: Aph(nS,nS), Bph(nS,nS)
+      real(c_double), intent(out)   :: EcRPA, Om(nS), XpY(nS,nS), XmY(nS,nS)
+    end function qk_phRLR
+
+    ! GW/RGW_excitation_density.f90
+    integer(c_int) function qk_RGW_excitation_density(ctx, nOrb, nC, nO, nR, nS, ERI, XpY, rho) &
+        bind(C, name="qk_RGW_excitation_density")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      integer(c_int), value         :: nOrb, nC, nO, nR, nS
+      real(c_double), intent(in)    :: ERI(nOrb,nOrb,nOrb,nOrb), XpY(nS,nS)
+      real(c_double), intent(out)   :: rho(nOrb,nOrb,nS)
+    end function qk_RGW_excitation_density
+
+    ! GW/RGW_self_energy_diag.f90
+    integer(c_int) function qk_RGW_self_energy_diag(ctx, eta, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho, &
+        EcGM, Sig, Z) bind(C, name="qk_RGW_self_energy_diag")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      real(c_double), value         :: eta
+      integer(c_int), value         :: nBas, nOrb, nC, nO, nV, nR, nS
+      real(c_double), intent(in)    :: e(nBas), Om(nS), rho(nBas,nBas,nS)
+      real(c_double), intent(out)   :: EcGM, Sig(nBas), Z(nBas)
+    end function qk_RGW_self_energy_diag
+
+    ! GW/RGW_QP_graph.f90 (Z is in/out, as in the reference)
+    integer(c_int) function qk_RGW_QP_graph(ctx, doSRG, eta, flow, nBas, nC, nO, nV, nR, nS, eHF, Om, rho, &
+        eGWlin, eOld, eGW, Z) bind(C, name="qk_RGW_QP_graph")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      integer(c_int), value         :: doSRG, nBas, nC, nO, nV, nR, nS
+      real(c_double), value         :: eta, flow
+      real(c_double), intent(in)    :: eHF(nBas), Om(nS), rho(nBas,nBas,nS), eGWlin(nBas), eOld(nBas)
+      real(c_double), intent(out)   :: eGW(nBas)
+      real(c_double), intent(inout) :: Z(nBas)
+    end function qk_RGW_QP_graph
+
+    ! AOtoMO/AOtoMO_ERI_RHF.f90
+    integer(c_int) function qk_AOtoMO_ERI_RHF(ctx, nBas, nOrb, c, ERI_AO, ERI_MO) bind(C, name="qk_AOtoMO_ERI_RHF")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      integer(c_int), value         :: nBas, nOrb
+      real(c_double), intent(in)    :: c(nBas,nOrb), ERI_AO(nBas,nBas,nBas,nBas)
+      real(c_double), intent(out)   :: ERI_MO(nOrb,nOrb,nOrb,nOrb)
+    end function qk_AOtoMO_ERI_RHF
+
+    ! GW/RG0W0.f90 (driver)
+    integer(c_int) function qk_RG0W0(ctx, prm, nBas, nOrb, nC, nO, nV, nR, nS, eHF, ERI, eGW, SigC, Z, Om, &
+        EcRPA, EcGM) bind(C, name="qk_RG0W0")
+      import c_int, c_ptr, c_double, qk_gw_params
+      type(c_ptr), value            :: ctx
+      type(qk_gw_params), intent(in):: prm
+      integer(c_int), value         :: nBas, nOrb, nC, nO, nV, nR, nS
+      real(c_double), intent(in)    :: eHF(nOrb), ERI(nOrb,nOrb,nOrb,nOrb)
+      real(c_double), intent(out)   :: eGW(nOrb), SigC(nOrb), Z(nOrb), Om(nS), EcRPA, EcGM
+    end function qk_RG0W0
+
+    ! GW/evRGW.f90 (driver; returns QK_ERR_NO_CONV where the reference stops)
+    integer(c_int) function qk_evRGW(ctx, prm, nBas, nOrb, nC, nO, nV, nR, nS, eHF, ERI, eGW, SigC, Z, &
+        EcRPA, EcGM, nSCF, Conv) bind(C, name="qk_evRGW")
+      import c_int, c_ptr, c_double, qk_gw_params
+      type(c_ptr), value            :: ctx
+      type(qk_gw_params), intent(in):: prm
+      integer(c_int), value         :: nBas, nOrb, nC, nO, nV, nR, nS
+      real(c_double), intent(in)    :: eHF(nOrb), ERI(nOrb,nOrb,nOrb,nOrb)
+      real(c_double), intent(out)   :: eGW(nOrb), SigC(nOrb), Z(nOrb), EcRPA, EcGM, Conv
+      integer(c_int), intent(out)   :: nSCF
+    end function qk_evRGW
+
+  end interface
+
+end module qk_gw_module
