@@ -142,6 +142,22 @@ int qk_dgemm_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, dou
 int qk_gemm_bf16x3_dev(qk_ctx* ctx, int m, int n, int k, const double* d_A, int lda,
                        const double* d_B, int ldb, double* d_C, int ldc);
 
+/* ---- allocation-free self-energy (device pointers) -----------------------------------------
+ * No counterpart in the reference.  For hosts that own all device memory themselves (one
+ * preallocated pool, a hard memory budget, or an allocation-free hot loop such as a Fortran-driven
+ * evGW cycle) and therefore cannot let the library call cudaMalloc: computes the same Sig, Z and
+ * EcGM as qk_RGW_self_energy_diag (GW/RGW_self_energy_diag.f90) from caller-owned device buffers
+ * e(nBas), Om(nS), rho(nBas,nBas,nS) into Sig(nBas), Z(nBas), EcGM(1), enqueued on `stream`
+ * (a cudaStream_t, 0 = default stream) and synchronised before returning.  It needs no qk_ctx and
+ * calls no cudaMalloc/cudaFree.  Scratch is a static 3 MiB device array, so nBas <= 1024
+ * (QK_ERR_ARG beyond that).  The first call on each device (made current) resolves the array's
+ * device address; make it before any stream capture.  Calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
+int qk_RGW_self_energy_diag_noalloc_dev(double eta, int nBas, int nOrb, int nC, int nO, int nV,
+                                        int nR, int nS, const double* d_e, const double* d_Om,
+                                        const double* d_rho, double* d_EcGM, double* d_Sig,
+                                        double* d_Z, void* stream);
+
 /* ---- diagnostics ------------------------------------------------------------------------- */
 /* The cudaStream_t (as void*) on which the context enqueues all of its kernels. */
 void* qk_stream(const qk_ctx* ctx);

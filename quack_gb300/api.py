@@ -323,3 +323,15 @@ def probe_fp64_peak(ctx=None):
     a, b = C.c_double(), C.c_double()
     c.check(lib().qk_probe_fp64_peak(c.handle, C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+def RGW_self_energy_diag_noalloc_dev(eta, nBas, nOrb, nC, nO, nV, nR, nS, d_e, d_Om, d_rho,
+                                     d_EcGM, d_Sig, d_Z, stream=0):
+    """Allocation-free self-energy on caller-owned device buffers (integer device addresses).
+    Returns the status code (QK_OK = 0); needs no Context."""
+    L = lib()
+    f = L.qk_RGW_self_energy_diag_noalloc_dev
+    f.restype = C.c_int
+    return f(C.c_double(eta), nBas, nOrb, nC, nO, nV, nR, nS, C.c_void_p(d_e), C.c_void_p(d_Om),
+             C.c_void_p(d_rho), C.c_void_p(d_EcGM), C.c_void_p(d_Sig), C.c_void_p(d_Z),
+             C.c_void_p(stream))
