@@ -67,6 +67,8 @@ const char* qk_timing_name(int i);
 int qk_num_timings(void);
 /* Count of this library's kernel launches since qk_init (diagnostics). */
 long long qk_launch_count(const qk_ctx* ctx);
+/* Newton steps per orbital of the context's last graphical QP solve (64 = not converged). */
+int qk_get_qp_iters(const qk_ctx* ctx, int* iters, int n);
 /* Release cached device workspace. */
 int qk_trim(qk_ctx* ctx);
 
@@ -123,6 +125,19 @@ int qk_evRGW_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int n
                  int nR, int nS, const double* d_eHF, const double* d_ERI, double* d_eGW,
                  double* d_SigC, double* d_Z, double* EcRPA, double* EcGM, int* nSCF,
                  double* Conv);
+
+/* ---- factorised-integral drivers (device pointers) ---------------------------------------
+ * (pq|rs) = sum_P L(p,q,P) L(r,s,P) with L(nOrb,nOrb,naux) column-major (symmetric in p,q).
+ * The slab (pq|jb) and the Casida coupling (ia|jb) are built on the device from L (in the
+ * precision tier of prm->precision); everything else is the RG0W0 / evRGW path above.  No
+ * counterpart in the reference, which reads the full nOrb^4 tensor; these variants avoid it
+ * for large or many systems. */
+int qk_RG0W0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int nOrb, int nC, int nO, int nR,
+                   int naux, const double* d_L, const double* d_eHF, double* d_eGW, double* d_SigC,
+                   double* d_Z, double* d_Om, double* EcRPA, double* EcGM);
+int qk_evRGW_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int nOrb, int nC, int nO, int nR,
+                   int naux, const double* d_L, const double* d_eHF, double* d_eGW, double* d_SigC,
+                   double* d_Z, double* EcRPA, double* EcGM, int* nSCF, double* Conv);
 
 /* ---- dense symmetric eigensolver (device pointers; replaces dsyev('V','U') of
  *      utils/wrap_lapack.f90:99-136 on the GPU).  A (n x n, lda) is destroyed; w ascending;

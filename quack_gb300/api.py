@@ -90,6 +90,12 @@ class Context:
     def launches(self) -> int:
         return int(lib().qk_launch_count(self._h))
 
+    def qp_iters(self, n):
+        """Newton steps per orbital of the last graphical QP solve (64 = not converged)."""
+        buf = (C.c_int * n)()
+        lib().qk_get_qp_iters(self._h, buf, n)
+        return np.array(buf[:], dtype=np.int64)
+
     def close(self):
         if self._h:
             lib().qk_finalize(self._h)
@@ -335,3 +341,37 @@ def RGW_self_energy_diag_noalloc_dev(eta, nBas, nOrb, nC, nO, nV, nR, nS, d_e, d
     return f(C.c_double(eta), nBas, nOrb, nC, nO, nV, nR, nS, C.c_void_p(d_e), C.c_void_p(d_Om),
              C.c_void_p(d_rho), C.c_void_p(d_EcGM), C.c_void_p(d_Sig), C.c_void_p(d_Z),
              C.c_void_p(stream))
+
+
+def RG0W0_L_dev(opts: GWOptions, nOrb, nC, nO, nR, naux, d_L, d_eHF, d_eGW, d_SigC, d_Z, d_Om,
+                ctx=None):
+    """Factorised-integral G0W0 on device buffers.  Returns (EcRPA, EcGM)."""
+    c = _ctx(ctx)
+    Ec, gm = C.c_double(), C.c_double()
+    prm = opts.c()
+    c.check(lib().qk_RG0W0_L_dev(c.handle, C.byref(prm), nOrb, nC, nO, nR, naux, C.c_void_p(d_L),
+                                 C.c_void_p(d_eHF), C.c_void_p(d_eGW), C.c_void_p(d_SigC),
+                                 C.c_void_p(d_Z), C.c_void_p(d_Om), C.byref(Ec), C.byref(gm)))
+    return Ec.value, gm.value
+
+
+def evRGW_L_dev(opts: GWOptions, nOrb, nC, nO, nR, naux, d_L, d_eHF, d_eGW, d_SigC, d_Z,
+                ctx=None, raise_on_fail=True):
+    """Factorised-integral evGW on device buffers.  Returns dict(EcRPA, EcGM, nSCF, Conv, failed)."""
+    c = _ctx(ctx)
+    Ec, gm, conv = C.c_double(), C.c_double(), C.c_double()
+    nscf = C.c_int()
+    prm = opts.c()
+    rc = c.check(lib().qk_evRGW_L_dev(c.handle, C.byref(prm), nOrb, nC, nO, nR, naux,
+                                      C.c_void_p(d_L), C.c_void_p(d_eHF), C.c_void_p(d_eGW),
+                                      C.c_void_p(d_SigC), C.c_void_p(d_Z), C.byref(Ec),
+                                      C.byref(gm), C.byref(nscf), C.byref(conv)),
+                 allow=() if raise_on_fail else (QK_ERR_NO_CONV,))
+    return dict(EcRPA=Ec.value, EcGM=gm.value, nSCF=nscf.value, Conv=conv.value,
+                failed=(rc == QK_ERR_NO_CONV))
+
+
+def L_fortran_flat(L):
+    """Factor L[P,p,q] (numpy) as the flat Fortran-order L(p,q,P) the *_L entry points take."""
+    L = np.asarray(L, dtype=np.float64)
+    return np.ascontiguousarray(L.reshape(L.shape[0], -1)).ravel()

@@ -32,7 +32,9 @@ constexpr int TILE_BYTES = 128 * BK * 2;           // 16 KB per part tile
 constexpr int STAGE_BYTES = 6 * TILE_BYTES;        // 96 KB
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr uint32_t MBAR_SPIN = 1u << 30;
-constexpr uint32_t TMEM_COLS = 128;
+constexpr int CHUNK_KB = 2;                        // k blocks per TMEM accumulation chunk
+constexpr uint32_t TMEM_COLS = 512;                // two chunk accumulators + hi + lo planes
+constexpr int NTHREADS = 320;                      // producer, MMA, 8 epilogue warps
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -134,11 +136,45 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 // the six (A part, B part) pairs, largest terms first
 __device__ __constant__ int kPairA[6] = {0, 0, 1, 0, 1, 2};
 __device__ __constant__ int kPairB[6] = {0, 1, 0, 2, 1, 0};
 
-__global__ void __launch_bounds__(128, 1)
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
+}
+
+// error-free FP32 addition (Knuth's TwoSum): s + e == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
     k_gemm_bf16x3(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                   int M, int N, int Kpad, int rowsA, int rowsB, double* __restrict__ C,
                   long long ldc, int n_tiles, int* status) {
@@ -146,8 +182,9 @@ __global__ void __launch_bounds__(128, 1)
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
   uint64_t* empty = full + STAGES;
-  uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+  uint64_t* acc_full = empty + STAGES;   // [2] chunk finished by the tensor cores
+  uint64_t* acc_empty = acc_full + 2;    // [2] chunk drained by the epilogue warps
+  uint32_t* tmem_slot = (uint32_t*)(acc_empty + 2);
   int* abort_flag = (int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -155,17 +192,21 @@ __global__ void __launch_bounds__(128, 1)
   const int m_tile = tile / n_tiles, n_tile = tile - m_tile * n_tiles;
   const int m0 = m_tile * BM, n0 = n_tile * BN;
   const int num_kb = Kpad / BK;
+  const int nch = (num_kb + CHUNK_KB - 1) / CHUNK_KB;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accum, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 8);  // one arrival per epilogue warp
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 2) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      su32(tmem_slot)),
                  "r"(TMEM_COLS)
@@ -177,73 +218,127 @@ __global__ void __launch_bounds__(128, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0 && lane == 0) {
-    // ---------------- TMA producer ----------------
-    int issued = 0;
-    for (int kb = 0; kb < num_kb; ++kb) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (kb / STAGES) & 1;
-      if (!mbar_wait(&empty[s], ph ^ 1, status)) { *(volatile int*)abort_flag = 1; break; }
-      if (*(volatile int*)abort_flag) break;
-      uint8_t* st = smem + s * STAGE_BYTES;
-      mbar_expect_tx(&full[s], STAGE_BYTES);
-      const int k0 = kb * BK;
-      for (int p = 0; p < 3; ++p) {
-        tma_load_2d(st + p * TILE_BYTES, &mapA, &full[s], k0, p * rowsA + m0);
-        tma_load_2d(st + (3 + p) * TILE_BYTES, &mapB, &full[s], k0, p * rowsB + n0);
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer ----------------
+      int issued = 0;
+      for (int kb = 0; kb < num_kb; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!mbar_wait(&empty[s], ph ^ 1, status)) { *(volatile int*)abort_flag = 1; break; }
+        if (*(volatile int*)abort_flag) break;
+        uint8_t* st = smem + s * STAGE_BYTES;
+        mbar_expect_tx(&full[s], STAGE_BYTES);
+        const int k0 = kb * BK;
+        for (int p = 0; p < 3; ++p) {
+          tma_load_2d(st + p * TILE_BYTES, &mapA, &full[s], k0, p * rowsA + m0);
+          tma_load_2d(st + (3 + p) * TILE_BYTES, &mapB, &full[s], k0, p * rowsB + n0);
+        }
+        issued = kb + 1;
       }
-      issued = kb + 1;
+      // drain: every issued stage must have landed before the CTA may exit
+      for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb)
+        mbar_wait(&full[kb % STAGES], (kb / STAGES) & 1, status);
     }
-    // drain: every issued stage must have landed before the CTA may exit
-    for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb)
-      mbar_wait(&full[kb % STAGES], (kb / STAGES) & 1, status);
-  } else if (warp == 1 && lane == 0) {
-    // ---------------- MMA issuer ----------------
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      bool ok = true;
+      for (int ch = 0; ch < nch && ok; ++ch) {
+        const int buf = ch & 1;
+        if (!mbar_wait(&acc_empty[buf], ((ch >> 1) & 1) ^ 1, status)) {
+          *(volatile int*)abort_flag = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t dacc = tmem + (uint32_t)(buf * BN);
+        const int kb0 = ch * CHUNK_KB;
+        const int kb1 = min(num_kb, kb0 + CHUNK_KB);
+        for (int kb = kb0; kb < kb1; ++kb) {
+          const int s = kb % STAGES;
+          const uint32_t ph = (kb / STAGES) & 1;
+          if (!mbar_wait(&full[s], ph, status)) { *(volatile int*)abort_flag = 1; ok = false; break; }
+          if (*(volatile int*)abort_flag) { ok = false; break; }
+          tc_fence_after();
+          uint8_t* st = smem + s * STAGE_BYTES;
+#pragma unroll
+          for (int pr = 0; pr < 6; ++pr) {
+            const uint64_t da = sdesc_sw128(st + kPairA[pr] * TILE_BYTES);
+            const uint64_t db = sdesc_sw128(st + (3 + kPairB[pr]) * TILE_BYTES);
+#pragma unroll
+            for (int j = 0; j < BK / 16; ++j)
+              umma_bf16(dacc, da + 2 * j, db + 2 * j, IDESC, ((kb - kb0) | pr | j) != 0);
+          }
+          umma_commit(&empty[s]);
+        }
+        umma_commit(&acc_full[buf]);  // chunk complete (also fires on abort)
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---------------- epilogue warps 2..9 ----------------
+    const int q = warp & 3;              // TMEM lane quadrant this warp may access
+    const int half = (warp - 2) >> 2;    // 64-column half of the tile
+    const int row = m0 + q * 32 + lane;
+    const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(half * 64);
+    const uint32_t t_hi = tq + 256, t_lo = tq + 384;
     bool ok = true;
-    for (int kb = 0; kb < num_kb && ok; ++kb) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (kb / STAGES) & 1;
-      if (!mbar_wait(&full[s], ph, status)) { *(volatile int*)abort_flag = 1; ok = false; break; }
-      if (*(volatile int*)abort_flag) { ok = false; break; }
+    for (int ch = 0; ch < nch; ++ch) {
+      const int buf = ch & 1;
+      bool have = mbar_wait(&acc_full[buf], (ch >> 1) & 1, status);
+      have = __all_sync(0xffffffffu, have && !*(volatile int*)abort_flag);
+      if (!have) { ok = false; break; }
       tc_fence_after();
-      uint8_t* st = smem + s * STAGE_BYTES;
-#pragma unroll
-      for (int pr = 0; pr < 6; ++pr) {
-        const uint64_t da = sdesc_sw128(st + kPairA[pr] * TILE_BYTES);
-        const uint64_t db = sdesc_sw128(st + (3 + kPairB[pr]) * TILE_BYTES);
-#pragma unroll
-        for (int j = 0; j < BK / 16; ++j)
-          umma_bf16(tmem, da + 2 * j, db + 2 * j, IDESC, (kb | pr | j) != 0);
-      }
-      umma_commit(&empty[s]);
-    }
-    umma_commit(accum);  // fires once all issued MMAs are complete (also on abort)
-  }
-  __syncwarp();
-  // ---------------- epilogue (all 4 warps) ----------------
-  const bool have = mbar_wait(accum, 0, status);
-  tc_fence_after();
-  // tcgen05.ld is warp-collective: take the decision per warp
-  const bool go = __all_sync(0xffffffffu, have && !*(volatile int*)abort_flag);
-  if (go) {
-    const int row = m0 + warp * 32 + lane;
-    const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
+      const uint32_t t_acc = tq + (uint32_t)(buf * BN);
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-      uint32_t r[32];
-      tmem_ld32(tbase + c0, r);
-      if (row < M) {
+      for (int c = 0; c < 4; ++c) {
+        uint32_t a[16], h[16], l[16];
+        tmem_ld16(t_acc + c * 16, a);
+        if (ch == 0) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int col = n0 + c0 + j;
-          if (col < N) C[(long long)row + ldc * col] = (double)__uint_as_float(r[j]);
+          for (int j = 0; j < 16; ++j) { h[j] = a[j]; l[j] = 0u; }
+        } else {
+          tmem_ld16(t_hi + c * 16, h);
+          tmem_ld16(t_lo + c * 16, l);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            float s, e;
+            two_sum(__uint_as_float(h[j]), __uint_as_float(a[j]), s, e);
+            h[j] = __float_as_uint(s);
+            l[j] = __float_as_uint(__uint_as_float(l[j]) + e);
+          }
+        }
+        tmem_st16(t_hi + c * 16, h);
+        tmem_st16(t_lo + c * 16, l);
+      }
+      tmem_st_wait();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[buf]);
+    }
+    if (ok) {
+      tc_fence_after();
+#pragma unroll 1
+      for (int c = 0; c < 4; ++c) {
+        uint32_t h[16], l[16];
+        tmem_ld16(t_hi + c * 16, h);
+        tmem_ld16(t_lo + c * 16, l);
+        if (row < M) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = n0 + half * 64 + c * 16 + j;
+            if (col < N)
+              C[(long long)row + ldc * col] =
+                  (double)__uint_as_float(h[j]) + (double)__uint_as_float(l[j]);
+          }
         }
       }
     }
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 2)
+  if (warp == 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(TMEM_COLS)
                  : "memory");
@@ -333,7 +428,7 @@ int qk_gemm_bf16x3_parts(qk_ctx* ctx, int m, int n, const void* Ap, int rowsA, c
   const int m_tiles = rowsA / BM, n_tiles = rowsB / BN;
   const long long tiles = (long long)m_tiles * n_tiles;
   if (tiles > 0x7fffffffLL) return qk_fail(ctx, QK_ERR_ARG, "bf16x3: too many tiles");
-  k_gemm_bf16x3<<<(unsigned)tiles, 128, SMEM_BYTES, ctx->stream>>>(ma, mb, m, n, Kpad, rowsA, rowsB,
+  k_gemm_bf16x3<<<(unsigned)tiles, NTHREADS, SMEM_BYTES, ctx->stream>>>(ma, mb, m, n, Kpad, rowsA, rowsB,
                                                                    C, ldc, n_tiles, ctx->d_status);
   QK_LAUNCHED();
   return QK_OK;

@@ -189,7 +189,112 @@ __global__ void k_slab(int N, int nC, int nO, int nR, const double* __restrict__
   }
 }
 
+// Lov(jb, P) = L(j, b, P): occupied-virtual block of the factor, (nS x naux) column-major
+__global__ void k_gather_ov(int N, int nC, int nO, int nR, int naux, const double* __restrict__ L,
+                            double* __restrict__ Lov) {
+  const int no = nO - nC, nv = N - nO - nR;
+  const long long nS = (long long)no * nv;
+  const long long N2 = (long long)N * N;
+  const long long total = nS * naux;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long P = idx / nS, jb = idx - P * nS;
+    const int jp = (int)(jb / nv), bp = (int)(jb - (long long)jp * nv);
+    Lov[idx] = __ldg(L + (jp + nC) + (long long)N * (bp + nO) + N2 * P);
+  }
+}
+
+// diagonal quantities from K = (ia|jb): s_ia = sqrt(fl(A_ii - B_ii)), tr A
+__global__ void k_casida_diag_K(int nS, int nv, int nC, int nO, const double* __restrict__ e,
+                                const double* __restrict__ K, double* __restrict__ sq,
+                                double* __restrict__ trA, int* status) {
+  __shared__ double red[32];
+  double tr = 0.0;
+  for (int ia = threadIdx.x; ia < nS; ia += blockDim.x) {
+    const int ip = ia / nv, ap = ia - ip * nv;
+    const double K2 = 2.0 * K[(long long)ia * nS + ia];
+    const double Aii = (K2 + e[ap + nO]) - e[ip + nC];
+    const double d = Aii - K2;
+    if (d < 0.0) atomicOr(status, QKD_NEG_AMB);
+    sq[ia] = sqrt(d);
+    tr += Aii;
+  }
+  tr = qk_block_sum(tr, red);
+  if (threadIdx.x == 0) *trA = tr;
+}
+
+// M from the lower triangle of K (so that M is exactly symmetric whatever produced K):
+// tiles (bi >= bj) are read once, written to (bi,bj) and transposed to (bj,bi).
+__global__ void __launch_bounds__(TB * 8) k_casida_M_K(int nS, int nv, int nC, int nO,
+                                                        const double* __restrict__ e,
+                                                        const double* __restrict__ K,
+                                                        const double* __restrict__ sq,
+                                                        double* __restrict__ M) {
+  __shared__ double t[TB][TB + 1];
+  // linear lower-triangular tile index -> (bi, bj)
+  const long long lin = blockIdx.x;
+  int bi = (int)((sqrt(8.0 * (double)lin + 1.0) - 1.0) * 0.5);
+  while ((long long)(bi + 1) * (bi + 2) / 2 <= lin) ++bi;
+  while ((long long)bi * (bi + 1) / 2 > lin) --bi;
+  const int bj = (int)(lin - (long long)bi * (bi + 1) / 2);
+  const int r0 = bi * TB, c0 = bj * TB;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int r = ty; r < TB; r += 8) {
+    const int row = r0 + tx, col = c0 + r;
+    double v = 0.0;
+    if (row < nS && col < nS) {
+      // element (row, col) of the lower triangle (row >= col holds for off-diagonal tiles)
+      v = (row >= col) ? K[row + (long long)nS * col] : K[col + (long long)nS * row];
+    }
+    t[r][tx] = v;  // t[col offset][row offset]
+  }
+  __syncthreads();
+  for (int r = ty; r < TB; r += 8) {
+    const int row = r0 + tx, col = c0 + r;
+    if (row < nS && col < nS) {
+      const double K2 = 2.0 * t[r][tx];
+      double A = K2;
+      if (row == col) {
+        const int ip = row / nv, ap = row - ip * nv;
+        A = (A + e[ap + nO]) - e[ip + nC];
+      }
+      M[row + (long long)nS * col] = sq[row] * ((A + K2) * sq[col]);
+    }
+    // transposed element (col, row) for the upper triangle: same K value
+    const int row2 = c0 + tx, col2 = r0 + r;  // row2 < col2 region
+    if (bi != bj && row2 < nS && col2 < nS) {
+      const double K2 = 2.0 * t[tx][r];
+      M[row2 + (long long)nS * col2] = sq[row2] * ((K2 + K2) * sq[col2]);
+    }
+  }
+}
+
 }  // namespace
+
+int qk_launch_gather_ov(qk_ctx* ctx, int N, int nC, int nO, int nR, int naux, const double* L,
+                        double* Lov) {
+  const long long nS = (long long)(nO - nC) * (N - nO - nR);
+  int blocks = (int)((nS * naux + 255) / 256);
+  if (blocks > 32 * ctx->num_sms) blocks = 32 * ctx->num_sms;
+  if (blocks < 1) blocks = 1;
+  k_gather_ov<<<blocks, 256, 0, ctx->stream>>>(N, nC, nO, nR, naux, L, Lov);
+  QK_LAUNCHED();
+  return QK_OK;
+}
+
+int qk_launch_casida_M_K(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e,
+                         const double* K, double* M, double* sq, double* trA) {
+  const int no = nO - nC, nv = N - nO - nR;
+  const int nS = no * nv;
+  if (nS <= 0) return QK_OK;
+  k_casida_diag_K<<<1, 1024, 0, ctx->stream>>>(nS, nv, nC, nO, e, K, sq, trA, ctx->d_status);
+  QK_LAUNCHED();
+  const long long nt = (nS + TB - 1) / TB;
+  const long long tiles = nt * (nt + 1) / 2;
+  k_casida_M_K<<<(unsigned)tiles, dim3(TB, 8), 0, ctx->stream>>>(nS, nv, nC, nO, e, K, sq, M);
+  QK_LAUNCHED();
+  return QK_OK;
+}
 
 int qk_launch_build_AB(qk_ctx* ctx, int which, int ispin, int dRPA, int N, int nC, int nO, int nR,
                        double lambda, const double* e, const double* ERI, double* out) {

@@ -20,7 +20,7 @@
 
 namespace {
 
-constexpr int TRI_THREADS = 512;
+constexpr int TRI_THREADS = 1024;
 constexpr int TRI_SMAX = 64;        // max column segments per row chunk
 constexpr int BT_NB = 64;           // reflectors per compact-WY block
 constexpr double CLUSTER_REL = 1e-7;  // eigenvalues closer than this * ||T||_1 share a cluster
@@ -235,15 +235,37 @@ __global__ void k_tri_prep(int n, const double* __restrict__ d, const double* __
   (void)red;
 }
 
+// Number of eigenvalues of T below x: sign changes of the leading principal minors
+// p_0 = 1, p_1 = d_0 - x, p_{i+1} = (d_i - x) p_i - e_{i-1}^2 p_{i-1} (Sturm sequence of the
+// characteristic polynomials).  Division-free: 3 FP64 operations per step.  A zero minor takes
+// the sign opposite to its predecessor (the convention that a zero pivot counts as negative), and
+// every 4 steps the pair (p_i, p_{i-1}) is rescaled by an exact power of two when it drifts
+// towards overflow or underflow (signs and ratios are unchanged by the scaling).
 __device__ __forceinline__ int sturm_count(int n, const double* __restrict__ d,
                                            const double* __restrict__ e2, double x, double pivmin) {
-  double q = d[0] - x;
-  if (fabs(q) <= pivmin) q = -pivmin;
-  int c = q < 0.0;
+  (void)pivmin;
+  double p0 = 1.0, p1 = __ldg(d) - x;
+  int neg = p1 < 0.0 || p1 == 0.0;
+  int c = neg;
   for (int i = 1; i < n; ++i) {
-    q = (d[i] - x) - __ldg(e2 + i - 1) / q;
-    if (fabs(q) <= pivmin) q = -pivmin;
-    c += q < 0.0;
+    const double p2 = (__ldg(d + i) - x) * p1 - __ldg(e2 + i - 1) * p0;
+    const int n2 = (p2 != 0.0) ? (p2 < 0.0) : !neg;
+    c += (n2 != neg);
+    neg = n2;
+    p0 = p1;
+    p1 = p2;
+    if ((i & 3) == 0) {
+      const int ex1 = (__double2hiint(p1) >> 20) & 0x7ff;
+      const int ex0 = (__double2hiint(p0) >> 20) & 0x7ff;
+      const int ex = ex1 > ex0 ? ex1 : ex0;
+      if (ex > 1023 + 400) {
+        p0 *= 0x1p-400;
+        p1 *= 0x1p-400;
+      } else if (ex < 1023 - 400) {
+        p0 *= 0x1p+400;
+        p1 *= 0x1p+400;
+      }
+    }
   }
   return c;
 }
@@ -457,10 +479,12 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
     int per_sm = 0;
     QK_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sytrd, TRI_THREADS, smem));
     if (per_sm < 1) return qk_fail(ctx, QK_ERR_CUDA, "k_sytrd cannot be resident");
-    if (per_sm > 2) per_sm = 2;
+    // one CTA per SM: the O(n) vector work of each column is repeated by every CTA, so fewer,
+    // wider CTAs waste less FP64 issue
+    per_sm = 1;
     int grid = per_sm * ctx->num_sms;
     // small problems do not need the whole GPU
-    const int want = (int)((N * N) / (32 * 64)) + 1;
+    const int want = (int)((N * N) / (32 * 128)) + 1;
     if (grid > want) grid = want < 1 ? 1 : want;
     double* gvec = nullptr;
     if (!use_smem) QK_TRY(qk_wst(ctx, W_VEC, (size_t)grid * 3 * N, &gvec));

@@ -17,6 +17,19 @@
 
 namespace {
 
+// 1/x in FP64 by Newton-Raphson refinement of an FP32 reciprocal seed: each step
+// r <- r (2 - x r) squares the relative error (2^-23 -> 2^-46 -> below 2^-53), ending within a
+// few ulps of the correctly rounded quotient.  Outside the FP32 normal range it falls back to
+// the IEEE division.
+__device__ __forceinline__ double rcp_nr(double x) {
+  const double ax = fabs(x);
+  if (!(ax > 1e-30 && ax < 1e30)) return 1.0 / x;
+  double r = (double)__frcp_rn((float)x);
+  r = r * fma(-x, r, 2.0);
+  r = r * fma(-x, r, 2.0);
+  return r;
+}
+
 constexpr int SIG_WARPS = 8;
 constexpr int QP_MAXIT = 64;        // RGW_QP_graph.f90:38
 constexpr double QP_THRESH = 1e-6;  // RGW_QP_graph.f90:39
@@ -73,12 +86,12 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial(SigArgs a) {
         const double eps = w - se[q] + om;
         if (!a.doSRG) {
           const double e2 = eps * eps;
-          const double rr = 1.0 / (e2 + eta2);
+          const double rr = rcp_nr(e2 + eta2);
           so += num * eps * rr;
           ds -= num * (e2 - eta2) * rr * rr;
         } else {
           const double reg = 1.0 - exp(-2.0 * a.flow * eps * eps);
-          const double ie = 1.0 / eps;
+          const double ie = rcp_nr(eps);
           so += num * reg * ie;
           ds -= num * reg * ie * ie;
         }
@@ -91,12 +104,12 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial(SigArgs a) {
         const double eps = w - se[q] - om;
         if (!a.doSRG) {
           const double e2 = eps * eps;
-          const double rr = 1.0 / (e2 + eta2);
+          const double rr = rcp_nr(e2 + eta2);
           sig += num * eps * rr;
           ds -= num * (e2 - eta2) * rr * rr;
         } else {
           const double reg = 1.0 - exp(-2.0 * a.flow * eps * eps);
-          const double ie = 1.0 / eps;
+          const double ie = rcp_nr(eps);
           sig += num * reg * ie;
           ds -= num * reg * ie * ie;
         }
@@ -402,6 +415,11 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
   }
   k_qp_finish<<<(N + 255) / 256, 256, 0, ctx->stream>>>(N, nC, nR, eGWlin, s, eGW, Z, ctx->d_status);
   QK_LAUNCHED();
+  // per-orbital Newton step counts for diagnostics (qk_get_qp_stats)
+  ctx->qp_iters.resize(N);
+  QK_CK(cudaMemcpyAsync(ctx->qp_iters.data(), s.nit, N * sizeof(int), cudaMemcpyDeviceToHost,
+                        ctx->stream));
+  QK_CK(cudaStreamSynchronize(ctx->stream));
   return QK_OK;
 }
 

@@ -116,14 +116,17 @@ int rho_gemm(qk_ctx* ctx, int prec, int N, int nS, const double* S, const double
 // Outputs: Om (nS), XpY (nS*nS), optional XmY, sumOm/trA (device scalars) for EcRPA.
 int casida_dev(qk_ctx* ctx, const Dims& d, const double* e, const double* ERI, double* Om,
                double* XpY, double* XmY, double* scal /* [0]=trA [1]=sumOm [2]=EcRPA */,
-               int want_vectors) {
+               int want_vectors, const double* K = nullptr) {
   const size_t S2 = (size_t)d.nS * d.nS;
   double *M = nullptr, *Zt = nullptr, *sq = nullptr;
   QK_TRY(qk_wst(ctx, W_M, S2, &M));
   QK_TRY(qk_wst(ctx, W_E, 2 * (size_t)d.nS + 64, &sq));
   double* w = sq + d.nS;
   qk_tic(ctx, T_BUILD);
-  QK_TRY(qk_launch_casida_M(ctx, d.N, d.nC, d.nO, d.nR, e, ERI, M, sq, scal + 0));
+  if (K)
+    QK_TRY(qk_launch_casida_M_K(ctx, d.N, d.nC, d.nO, d.nR, e, K, M, sq, scal + 0));
+  else
+    QK_TRY(qk_launch_casida_M(ctx, d.N, d.nC, d.nO, d.nR, e, ERI, M, sq, scal + 0));
   qk_toc(ctx, T_BUILD);
   if (want_vectors) QK_TRY(qk_wst(ctx, W_ZT, S2, &Zt));
   ctx->time_eig = want_vectors != 0;
@@ -256,6 +259,142 @@ int evgw_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   if (hnSCF) *hnSCF = nSCF;
   if (hConv) *hConv = Conv;
   if (nSCF == prm->maxSCF + 1)  // evRGW.f90:190-198
+    return qk_fail(ctx, QK_ERR_NO_CONV, "evGW convergence failed after %d cycles (Conv=%g)", nSCF, Conv);
+  return QK_OK;
+}
+
+// contractions of the factorised integrals (the "ERI transform" of the factorised path):
+//   Lov(jb,P) = L(j,b,P);  K = Lov Lov^T = (ia|jb);  slab = Lmat Lov^T = (pq|jb)
+int factor_prep(qk_ctx* ctx, int prec, const Dims& d, int naux, const double* L, double** K_out,
+                double** slab_out) {
+  const int N = d.N, nS = d.nS;
+  const long long N2 = (long long)N * N;
+  double *Lov, *K, *slab;
+  QK_TRY(qk_wst(ctx, W_VEC2, (size_t)nS * naux, &Lov));
+  QK_TRY(qk_wst(ctx, W_KMAT, (size_t)nS * nS, &K));
+  QK_TRY(qk_wst(ctx, W_SLAB, (size_t)N2 * nS, &slab));
+  qk_tic(ctx, T_SLAB);
+  QK_TRY(qk_launch_gather_ov(ctx, N, d.nC, d.nO, d.nR, naux, L, Lov));
+  if (prec == QK_PREC_BF16X3) {
+    QK_TRY(qk_gemm_bf16x3_nt(ctx, nS, nS, naux, Lov, nS, Lov, nS, K, nS));
+    QK_TRY(qk_gemm_bf16x3_nt(ctx, (int)N2, nS, naux, L, N2, Lov, nS, slab, N2));
+  } else {
+    QK_TRY(qk_dgemm(ctx, 'N', 'T', nS, nS, naux, 1.0, Lov, nS, 0, Lov, nS, 0, 0.0, K, nS, 0, 1));
+    QK_TRY(qk_dgemm(ctx, 'N', 'T', (int)N2, nS, naux, 1.0, L, N2, 0, Lov, nS, 0, 0.0, slab, N2, 0,
+                    1));
+  }
+  qk_toc(ctx, T_SLAB);
+  *K_out = K;
+  *slab_out = slab;
+  return QK_OK;
+}
+
+int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, const double* L,
+               const double* eHF, double* eGW, double* SigC, double* Z, double* Om,
+               double* hEcRPA, double* hEcGM) {
+  if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
+  const double flow = 500.0;
+  const int N = d.N, nS = d.nS;
+  const size_t S2 = (size_t)nS * nS, N2S = (size_t)N * N * nS;
+  double *XpY, *rho, *small, *K, *slab;
+  qk_timings_clear(ctx);
+  QK_TRY(factor_prep(ctx, prm->precision, d, naux, L, &K, &slab));
+  QK_TRY(qk_wst(ctx, W_XPY, S2, &XpY));
+  QK_TRY(qk_wst(ctx, W_RHO, N2S, &rho));
+  QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)2 * N + 16, &small));
+  double* scal = small;
+  double* eGWlin = small + 16;
+  QK_TRY(casida_dev(ctx, d, eHF, nullptr, Om, XpY, nullptr, scal, 1, K));
+  qk_tic(ctx, T_RHO);
+  QK_TRY(rho_gemm(ctx, prm->precision, N, nS, slab, XpY, rho));
+  qk_toc(ctx, T_RHO);
+  qk_tic(ctx, T_SIGMA);
+  QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho, SigC,
+                       Z, scal + 8));
+  QK_TRY(qk_qp_linear(ctx, N, eHF, Z, SigC, 1, eGWlin));
+  qk_toc(ctx, T_SIGMA);
+  qk_tic(ctx, T_QP);
+  if (prm->linearize) {
+    QK_CK(cudaMemcpyAsync(eGW, eGWlin, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
+    QK_TRY(qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho,
+                        eGWlin, eHF, eGW, Z));
+  }
+  qk_toc(ctx, T_QP);
+  qk_tic(ctx, T_CASIDA2);
+  QK_TRY(casida_dev(ctx, d, eGW, nullptr, nullptr, nullptr, nullptr, scal + 3, 0, K));
+  qk_toc(ctx, T_CASIDA2);
+  double h[16];
+  QK_TRY(d2h(ctx, h, scal, 16 * sizeof(double)));
+  QK_CK(cudaStreamSynchronize(ctx->stream));
+  qk_timings_collect(ctx);
+  if (hEcRPA) *hEcRPA = h[5];
+  if (hEcGM) *hEcGM = h[8];
+  return QK_OK;
+}
+
+int evgw_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, const double* L,
+               const double* eHF, double* eGW, double* SigC, double* Z, double* hEcRPA,
+               double* hEcGM, int* hnSCF, double* hConv) {
+  if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
+  const double flow = 500.0;
+  const int N = d.N, nS = d.nS;
+  const size_t S2 = (size_t)nS * nS, N2S = (size_t)N * N * nS;
+  const int maxd = prm->max_diis > 1 ? prm->max_diis : 1;
+  double *XpY, *rho, *small, *K, *slab;
+  qk_timings_clear(ctx);
+  QK_TRY(factor_prep(ctx, prm->precision, d, naux, L, &K, &slab));
+  QK_TRY(qk_wst(ctx, W_XPY, S2, &XpY));
+  QK_TRY(qk_wst(ctx, W_RHO, N2S, &rho));
+  QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)(6 + 2 * maxd) * N + nS + 64, &small));
+  double* scal = small;
+  double* eOld = small + 64;
+  double* errv = eOld + N;
+  double* Om = errv + N;
+  double* err_hist = Om + nS;
+  double* e_hist = err_hist + (size_t)N * maxd;
+  QK_CK(cudaMemsetAsync(err_hist, 0, sizeof(double) * 2 * (size_t)N * maxd, ctx->stream));
+  QK_CK(cudaMemcpyAsync(eGW, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  QK_CK(cudaMemcpyAsync(eOld, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  int nSCF = 0, n_diis = 0;
+  double Conv = 1.0;
+  while (Conv > prm->thresh && nSCF <= prm->maxSCF) {
+    QK_TRY(casida_dev(ctx, d, eGW, nullptr, Om, XpY, nullptr, scal, 1, K));
+    qk_tic(ctx, T_RHO);
+    QK_TRY(rho_gemm(ctx, prm->precision, N, nS, slab, XpY, rho));
+    qk_toc(ctx, T_RHO);
+    qk_tic(ctx, T_SIGMA);
+    QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eGW, Om, rho,
+                         SigC, Z, scal + 8));
+    qk_toc(ctx, T_SIGMA);
+    qk_tic(ctx, T_QP);
+    if (prm->linearize) {
+      QK_TRY(qk_qp_linear(ctx, N, eHF, Z, SigC, 0, eGW));
+    } else {
+      QK_TRY(qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho,
+                          eOld, eOld, eGW, Z));
+    }
+    qk_toc(ctx, T_QP);
+    QK_TRY(qk_max_abs_diff(ctx, N, eGW, eOld, scal + 9));
+    if (prm->max_diis > 1) {
+      n_diis = n_diis + 1 < prm->max_diis ? n_diis + 1 : prm->max_diis;
+      QK_TRY(qk_sub(ctx, N, eGW, eOld, errv));
+      QK_TRY(qk_diis_dev(ctx, N, N, n_diis, err_hist, e_hist, errv, eGW, scal + 10));
+    }
+    QK_CK(cudaMemcpyAsync(eOld, eGW, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    QK_TRY(d2h(ctx, &Conv, scal + 9, sizeof(double)));
+    QK_CK(cudaStreamSynchronize(ctx->stream));
+    nSCF++;
+  }
+  double h[16];
+  QK_TRY(d2h(ctx, h, scal, 16 * sizeof(double)));
+  QK_CK(cudaStreamSynchronize(ctx->stream));
+  qk_timings_collect(ctx);
+  if (hEcRPA) *hEcRPA = h[2];
+  if (hEcGM) *hEcGM = h[8];
+  if (hnSCF) *hnSCF = nSCF;
+  if (hConv) *hConv = Conv;
+  if (nSCF == prm->maxSCF + 1)
     return qk_fail(ctx, QK_ERR_NO_CONV, "evGW convergence failed after %d cycles (Conv=%g)", nSCF, Conv);
   return QK_OK;
 }
@@ -625,6 +764,31 @@ int qk_gemm_bf16x3_dev(qk_ctx* ctx, int m, int n, int k, const double* d_A, int 
   QK_TRY(begin(ctx));
   if (lda < m || ldb < n || ldc < m) return qk_fail(ctx, QK_ERR_ARG, "bad leading dimensions");
   const int st = qk_gemm_bf16x3_nt(ctx, m, n, k, d_A, lda, d_B, ldb, d_C, ldc);
+  return end(ctx, st);
+}
+
+int qk_RG0W0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int nOrb, int nC, int nO, int nR,
+                   int naux, const double* d_L, const double* d_eHF, double* d_eGW, double* d_SigC,
+                   double* d_Z, double* d_Om, double* EcRPA, double* EcGM) {
+  QK_TRY(begin(ctx));
+  if (!prm || naux <= 0) return qk_fail(ctx, QK_ERR_ARG, "params/naux required");
+  Dims d;
+  const int nS = (nO - nC) * (nOrb - nO - nR);
+  QK_TRY(check_dims(ctx, nOrb, nOrb, nC, nO, nOrb - nO, nR, nS, &d));
+  const int st = g0w0_L_dev(ctx, prm, d, naux, d_L, d_eHF, d_eGW, d_SigC, d_Z, d_Om, EcRPA, EcGM);
+  return end(ctx, st);
+}
+
+int qk_evRGW_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int nOrb, int nC, int nO, int nR,
+                   int naux, const double* d_L, const double* d_eHF, double* d_eGW, double* d_SigC,
+                   double* d_Z, double* EcRPA, double* EcGM, int* nSCF, double* Conv) {
+  QK_TRY(begin(ctx));
+  if (!prm || naux <= 0) return qk_fail(ctx, QK_ERR_ARG, "params/naux required");
+  Dims d;
+  const int nS = (nO - nC) * (nOrb - nO - nR);
+  QK_TRY(check_dims(ctx, nOrb, nOrb, nC, nO, nOrb - nO, nR, nS, &d));
+  const int st = evgw_L_dev(ctx, prm, d, naux, d_L, d_eHF, d_eGW, d_SigC, d_Z, EcRPA, EcGM, nSCF,
+                            Conv);
   return end(ctx, st);
 }
 

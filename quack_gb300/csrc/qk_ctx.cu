@@ -154,4 +154,11 @@ const char* qk_timing_name(int i) { return (i >= 0 && i < T_NUM) ? k_timing_name
 int qk_num_timings(void) { return T_NUM; }
 long long qk_launch_count(const qk_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+int qk_get_qp_iters(const qk_ctx* ctx, int* iters, int n) {
+  if (!ctx || !iters) return QK_ERR_ARG;
+  const int m = (int)ctx->qp_iters.size();
+  for (int i = 0; i < n; ++i) iters[i] = i < m ? ctx->qp_iters[i] : 0;
+  return QK_OK;
+}
+
 }  // extern "C"

@@ -32,7 +32,7 @@ struct DevBuf {
 
 enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
-  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_NUMBUF
+  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_NUMBUF
 };
 
 struct qk_ctx {
@@ -48,6 +48,7 @@ struct qk_ctx {
   long long launches = 0;
   int last_dev_status = 0;
   bool time_eig = true;  // stage timers inside the eigensolver (off for the eigenvalue-only pass)
+  std::vector<int> qp_iters;  // Newton steps per orbital of the last QP solve
 };
 
 // ------------------------------------------------------------------------------------------
@@ -112,6 +113,10 @@ int qk_launch_casida_M_from_AB(qk_ctx* ctx, int nS, const double* A, const doubl
 int qk_launch_xpy(qk_ctx* ctx, int nS, const double* w, const double* Zt, const double* sq,
                   double* Om, double* XpY, double* XmY, int want_xmy);
 int qk_launch_sum_sqrt(qk_ctx* ctx, int nS, const double* w, double* out);
+int qk_launch_gather_ov(qk_ctx* ctx, int N, int nC, int nO, int nR, int naux, const double* L,
+                        double* Lov);
+int qk_launch_casida_M_K(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e,
+                         const double* K, double* M, double* sq, double* trA);
 int qk_launch_slab_gather(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* ERI,
                           double* S);
 

@@ -338,3 +338,61 @@ def test_g0w0_linearized_vs_live_oracle(ctx, N, nO, seed):
     assert np.max(np.abs(r["Z"] - ref["Z"])) < 1e-7
     if np.isfinite(ref["EcRPA"]):
         assert abs(r["EcRPA"] - ref["EcRPA"]) < E_TOL
+
+
+# --------------------------------------------------------------------------------------------
+# factorised-integral drivers (slab and Casida coupling built on the device from L)
+# --------------------------------------------------------------------------------------------
+def _dev(x):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+@pytest.mark.parametrize("N,nO,seed,lin", [(24, 5, 11, False), (40, 5, 21, True), (33, 4, 25, False)])
+def test_g0w0_L_path_vs_oracle(ctx, N, nO, seed, lin):
+    import torch
+    s = synth.small_system(N, nO, 3 * N, seed)
+    E = synth.eri_phys_numpy(s["L"])
+    nS = nO * (N - nO)
+    ref = O.RG0W0(lin, 0.0, False, N, N, 0, nO, N - nO, 0, nS, E, s["eHF"])
+    dL = _dev(api.L_fortran_flat(s["L"]))
+    de = _dev(s["eHF"])
+    out = [torch.empty(N, dtype=torch.float64, device="cuda") for _ in range(3)]
+    dOm = torch.empty(nS, dtype=torch.float64, device="cuda")
+    Ec, gm = api.RG0W0_L_dev(api.GWOptions(linearize=lin), N, 0, nO, 0, 3 * N, dL.data_ptr(),
+                             de.data_ptr(), out[0].data_ptr(), out[1].data_ptr(),
+                             out[2].data_ptr(), dOm.data_ptr(), ctx=ctx)
+    eGW = out[0].cpu().numpy()
+    scale = np.maximum(1.0, np.abs(ref["SigC"]))
+    assert np.max(np.abs(dOm.cpu().numpy() - ref["Om"])) < E_TOL
+    assert np.max(np.abs(out[1].cpu().numpy() - ref["SigC"]) / scale) < E_TOL
+    if lin:
+        assert np.max(np.abs(eGW - ref["eGW"]) / scale) < E_TOL
+    else:
+        stable = np.asarray(ref["qp_iters"]) <= 4
+        assert np.max(np.abs(eGW[stable] - ref["eGW"][stable]) / scale[stable]) < E_TOL
+    if np.isfinite(ref["EcRPA"]):
+        assert abs(Ec - ref["EcRPA"]) < E_TOL * max(1.0, abs(ref["EcRPA"]))
+
+
+def test_evgw_L_path_vs_fixture(ctx):
+    import torch
+    f = np.load(os.path.join(GOLD, "synth_n24.npz"))
+    N, nO = int(f["N"]), int(f["nO"])
+    dL = _dev(api.L_fortran_flat(f["L"]))
+    de = _dev(f["eHF"])
+    out = [torch.empty(N, dtype=torch.float64, device="cuda") for _ in range(3)]
+    r = api.evRGW_L_dev(api.GWOptions(maxSCF=64, thresh=1e-5, max_diis=5), N, 0, nO, 0, 3 * N,
+                        dL.data_ptr(), de.data_ptr(), out[0].data_ptr(), out[1].data_ptr(),
+                        out[2].data_ptr(), ctx=ctx)
+    assert r["nSCF"] == int(f["evgw_d5_nSCF"])
+    assert np.max(np.abs(out[0].cpu().numpy() - f["evgw_d5_eGW"])) < E_TOL
+    assert abs(r["EcRPA"] - float(f["evgw_d5_EcRPA"])) < E_TOL
+
+
+def test_qp_iteration_counts_match_oracle(ctx):
+    f = np.load(os.path.join(GOLD, "synth_n24.npz"))
+    N, nO = int(f["N"]), int(f["nO"])
+    E = synth.eri_phys_numpy(f["L"])
+    api.RG0W0(api.GWOptions(), N, N, 0, nO, N - nO, 0, nO * (N - nO), E, f["eHF"], ctx=ctx)
+    assert np.array_equal(ctx.qp_iters(N), f["g0w0_qp_iters"])
