@@ -290,6 +290,8 @@ def run_ours(args):
         "qp_error_mixed_vs_fp64": qp_err,
         "fp64_peak_tflops": {"dmma": dmma_peak, "dfma": dfma_peak},
     }
+    if not args.no_batch:
+        res["batched_evgw"] = run_batched(args, ctx)
     if rank == 0 and not args.no_cpu:
         res["cpu_baseline"] = cpu_baseline(args, s)
     if rank == 0:
@@ -298,6 +300,44 @@ def run_ours(args):
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def run_batched(args, ctx):
+    """Batched evGW on a subset of the 256-system configuration (seed 1, N ~ U{24..160},
+    nO = floor(N/8 + 1/2), naux = 3N, at most 5 cycles at 1e-5 Ha, DIIS 5, Newton QP), all
+    systems in one qk_gw_batch_L_dev call over several streams; plain FP64 vs BF16x3."""
+    import numpy as np
+    import torch
+    from quack_gb300 import api, synth
+
+    systems = synth.batch_systems(256, 24, 160, seed=1)[: args.batch_systems]
+    desc, Lf, Ef = api.pack_systems(systems)
+    dL = torch.from_numpy(Lf).cuda()
+    dE = torch.from_numpy(Ef).cuda()
+    out = {"systems": len(systems), "N": [s["N"] for s in systems],
+           "config": "evGW maxSCF=4 (<=5 cycles) thresh 1e-5 DIIS 5 Newton QP; 256-system "
+                     "generator seed 1, first %d systems" % len(systems)}
+    res = {}
+    for tier, name in ((api.QK_PREC_BF16X3, "mixed"), (api.QK_PREC_FP64, "plain_fp64")):
+        opts = api.GWOptions(maxSCF=4, thresh=1e-5, max_diis=5, precision=tier)
+        dG = torch.zeros_like(dE)
+        api.gw_batch_L_dev(opts, 1, desc, dL.data_ptr(), dE.data_ptr(), dG.data_ptr(),
+                           n_workers=args.batch_workers, ctx=ctx)   # warm-up (workspaces)
+        torch.cuda.synchronize()
+        t0 = time.time()
+        r = api.gw_batch_L_dev(opts, 1, desc, dL.data_ptr(), dE.data_ptr(), dG.data_ptr(),
+                               n_workers=args.batch_workers, ctx=ctx)
+        torch.cuda.synchronize()
+        dt = time.time() - t0
+        res[name] = dG.cpu().numpy()
+        out[name] = {"value": len(systems) / dt, "unit": "systems/s", "seconds": dt,
+                     "cycles": int(r["nSCF"].sum()), "not_converged": int((r["status"] == 5).sum()),
+                     "errors": int(((r["status"] != 0) & (r["status"] != 5)).sum())}
+    d = np.abs(res["mixed"] - res["plain_fp64"])
+    out["speedup_mixed_vs_plain"] = out["mixed"]["value"] / out["plain_fp64"]["value"]
+    out["qp_max_abs_diff_Ha"] = float(d.max())
+    out["qp_median_abs_diff_Ha"] = float(np.median(d))
+    return out
 
 
 # --------------------------------------------------------------------------------------------
@@ -413,6 +453,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--reference-budget-s", type=float, default=150.0)
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-systems", type=int, default=32)
+    ap.add_argument("--batch-workers", type=int, default=8)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -139,6 +139,23 @@ int qk_evRGW_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int nOrb, int nC, int n
                    int naux, const double* d_L, const double* d_eHF, double* d_eGW, double* d_SigC,
                    double* d_Z, double* EcRPA, double* EcGM, int* nSCF, double* Conv);
 
+/* ---- batched drivers (device pointers) ------------------------------------------------------
+ * Many independent systems of uneven size in one call (no counterpart in the reference, which
+ * runs one molecule per process).  Per system i, desc[i] gives its sizes and the element offsets
+ * of its factor L(nOrb,nOrb,naux) in d_L and of its energies in d_eHF / d_eGW.  method 0 = G0W0,
+ * 1 = evGW.  The systems are spread over n_workers CUDA streams (one host thread each), largest
+ * first.  Per-system results: status[i] (QK_OK, QK_ERR_NO_CONV, ...), EcRPA[i], nSCF[i] (host
+ * arrays); a failing system does not stop the others.  Returns the worst status other than
+ * QK_ERR_NO_CONV. */
+typedef struct qk_sys_desc {
+  int nOrb, nC, nO, nR, naux;
+  long long offset_L;
+  long long offset_e;
+} qk_sys_desc;
+int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int method, int nsys,
+                      const qk_sys_desc* desc, const double* d_L, const double* d_eHF,
+                      double* d_eGW, double* EcRPA, int* status, int* nSCF, int n_workers);
+
 /* ---- dense symmetric eigensolver (device pointers; replaces dsyev('V','U') of
  *      utils/wrap_lapack.f90:99-136 on the GPU).  A (n x n, lda) is destroyed; w ascending;
  *      if want_vectors, Zt receives the eigenvectors as ROWS: Zt[j + n*i] = component i of

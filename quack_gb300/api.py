@@ -62,6 +62,11 @@ def _f(a):
     return np.asfortranarray(np.asarray(a, dtype=np.float64))
 
 
+class qk_sys_desc(C.Structure):
+    _fields_ = [("nOrb", C.c_int), ("nC", C.c_int), ("nO", C.c_int), ("nR", C.c_int),
+                ("naux", C.c_int), ("offset_L", C.c_longlong), ("offset_e", C.c_longlong)]
+
+
 class Context:
     """A qk_ctx: one CUDA stream plus cached device workspace on one GPU."""
 
@@ -375,3 +380,34 @@ def L_fortran_flat(L):
     """Factor L[P,p,q] (numpy) as the flat Fortran-order L(p,q,P) the *_L entry points take."""
     L = np.asarray(L, dtype=np.float64)
     return np.ascontiguousarray(L.reshape(L.shape[0], -1)).ravel()
+
+
+def pack_systems(systems):
+    """Pack synthetic systems (dicts with L[P,p,q], eHF, nO) for the batched driver.
+    Returns (desc array, flat L, flat eHF)."""
+    nsys = len(systems)
+    desc = (qk_sys_desc * nsys)()
+    offL = offE = 0
+    Ls, Es = [], []
+    for i, s in enumerate(systems):
+        naux, N, _ = s["L"].shape
+        desc[i] = qk_sys_desc(N, 0, int(s["nO"]), 0, naux, offL, offE)
+        Ls.append(L_fortran_flat(s["L"]))
+        Es.append(np.asarray(s["eHF"], dtype=np.float64))
+        offL += naux * N * N
+        offE += N
+    return desc, np.concatenate(Ls), np.concatenate(Es)
+
+
+def gw_batch_L_dev(opts: GWOptions, method, desc, d_L, d_eHF, d_eGW, n_workers=8, ctx=None):
+    """Batched G0W0 (method 0) / evGW (method 1) over packed device arrays.
+    Returns dict(status, EcRPA, nSCF, rc) with per-system host arrays."""
+    c = _ctx(ctx)
+    n = len(desc)
+    st = (C.c_int * n)()
+    ns = (C.c_int * n)()
+    ec = (C.c_double * n)()
+    prm = opts.c()
+    rc = lib().qk_gw_batch_L_dev(c.handle, C.byref(prm), int(method), n, desc, C.c_void_p(d_L),
+                                 C.c_void_p(d_eHF), C.c_void_p(d_eGW), ec, st, ns, int(n_workers))
+    return dict(status=np.array(st[:]), EcRPA=np.array(ec[:]), nSCF=np.array(ns[:]), rc=rc)

@@ -22,6 +22,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
+#include <mutex>
 #include "qk_internal.cuh"
 
 namespace {
@@ -419,12 +420,13 @@ int qk_gemm_bf16x3_parts(qk_ctx* ctx, int m, int n, const void* Ap, int rowsA, c
   CUtensorMap ma, mb;
   QK_TRY(make_map(ctx, &ma, Ap, Kpad, 3LL * rowsA));
   QK_TRY(make_map(ctx, &mb, Bp, Kpad, 3LL * rowsB));
-  static bool attr = false;
-  if (!attr) {
-    QK_CK(cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               SMEM_BYTES));
-    attr = true;
-  }
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
+    attr_err = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    SMEM_BYTES);
+  });
+  QK_CK(attr_err);
   const int m_tiles = rowsA / BM, n_tiles = rowsB / BN;
   const long long tiles = (long long)m_tiles * n_tiles;
   if (tiles > 0x7fffffffLL) return qk_fail(ctx, QK_ERR_ARG, "bf16x3: too many tiles");

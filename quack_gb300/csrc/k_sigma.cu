@@ -17,14 +17,15 @@
 
 namespace {
 
-// 1/x in FP64 by Newton-Raphson refinement of an FP32 reciprocal seed: each step
-// r <- r (2 - x r) squares the relative error (2^-23 -> 2^-46 -> below 2^-53), ending within a
-// few ulps of the correctly rounded quotient.  Outside the FP32 normal range it falls back to
-// the IEEE division.
+// 1/x in FP64: the hardware's approximate FP64 reciprocal (rcp.approx.ftz.f64) refined by two
+// Newton-Raphson steps r <- r (2 - x r), each of which squares the relative error, ending within
+// a few ulps of the correctly rounded quotient.  Inputs outside [1e-300, 1e300] in magnitude
+// (where the approximation flushes) fall back to the IEEE division.
 __device__ __forceinline__ double rcp_nr(double x) {
   const double ax = fabs(x);
-  if (!(ax > 1e-30 && ax < 1e30)) return 1.0 / x;
-  double r = (double)__frcp_rn((float)x);
+  if (!(ax > 1e-300 && ax < 1e300)) return 1.0 / x;
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
   r = r * fma(-x, r, 2.0);
   r = r * fma(-x, r, 2.0);
   return r;
@@ -79,7 +80,29 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial(SigArgs a) {
       const double om = __ldg(a.Om + m);
       const double* r = a.rho + p + N2 * m;
       double so = 0.0;
-      // occupied part: eps = w - e_i + Om_m
+      // eta = 0 takes the fast path; otherwise occupied part: eps = w - e_i + Om_m
+      if (!a.doSRG && a.eta == 0.0) {
+        // eta = 0: num*eps/(eps^2) = num/eps and num*eps^2/(eps^2)^2 = num/eps^2
+        double s1 = 0.0, s2 = 0.0, d1 = 0.0;
+        for (int q = a.nC; q < a.nO; ++q) {
+          const double x = __ldg(r + N1 * q);
+          const double ir = rcp_nr(w - se[q] + om);
+          const double t = (x * x) * ir;
+          s1 += t;
+          d1 = fma(t, ir, d1);
+        }
+        for (int q = a.nO; q < pend; ++q) {
+          const double x = __ldg(r + N1 * q);
+          const double ir = rcp_nr(w - se[q] - om);
+          const double t = (x * x) * ir;
+          s2 += t;
+          d1 = fma(t, ir, d1);
+        }
+        socc_acc += 2.0 * s1;
+        sig += 2.0 * s2;
+        ds -= 2.0 * d1;
+        continue;
+      }
       for (int q = a.nC; q < a.nO; ++q) {
         const double x = __ldg(r + N1 * q);
         const double num = 2.0 * x * x;

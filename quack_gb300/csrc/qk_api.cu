@@ -399,6 +399,28 @@ int evgw_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   return QK_OK;
 }
 
+}  // namespace
+
+int qk_g0w0_L(qk_ctx* ctx, const qk_gw_params* prm, int N, int nC, int nO, int nR, int naux,
+              const double* L, const double* eHF, double* eGW, double* SigC, double* Z, double* Om,
+              double* EcRPA, double* EcGM) {
+  Dims d;
+  const int nS = (nO - nC) * (N - nO - nR);
+  QK_TRY(check_dims(ctx, N, N, nC, nO, N - nO, nR, nS, &d));
+  return g0w0_L_dev(ctx, prm, d, naux, L, eHF, eGW, SigC, Z, Om, EcRPA, EcGM);
+}
+
+int qk_evgw_L(qk_ctx* ctx, const qk_gw_params* prm, int N, int nC, int nO, int nR, int naux,
+              const double* L, const double* eHF, double* eGW, double* SigC, double* Z,
+              double* EcRPA, double* EcGM, int* nSCF, double* Conv) {
+  Dims d;
+  const int nS = (nO - nC) * (N - nO - nR);
+  QK_TRY(check_dims(ctx, N, N, nC, nO, N - nO, nR, nS, &d));
+  return evgw_L_dev(ctx, prm, d, naux, L, eHF, eGW, SigC, Z, EcRPA, EcGM, nSCF, Conv);
+}
+
+namespace {
+
 int begin(qk_ctx* ctx) {
   if (!ctx) return QK_ERR_ARG;
   cudaError_t e = cudaSetDevice(ctx->device);

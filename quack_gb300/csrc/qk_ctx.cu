@@ -118,6 +118,8 @@ int qk_init(int device, qk_ctx** out) {
 
 int qk_finalize(qk_ctx* ctx) {
   if (!ctx) return QK_OK;
+  for (auto* w : ctx->workers) qk_finalize(w);
+  ctx->workers.clear();
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto& b : ctx->buf)

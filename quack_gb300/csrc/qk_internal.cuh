@@ -32,7 +32,7 @@ struct DevBuf {
 
 enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
-  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_NUMBUF
+  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_NUMBUF
 };
 
 struct qk_ctx {
@@ -49,7 +49,17 @@ struct qk_ctx {
   int last_dev_status = 0;
   bool time_eig = true;  // stage timers inside the eigensolver (off for the eigenvalue-only pass)
   std::vector<int> qp_iters;  // Newton steps per orbital of the last QP solve
+  std::vector<qk_ctx*> workers;  // per-stream sub-contexts of the batched driver
 };
+
+// Factorised-integral drivers on one context (qk_api.cu), reused by the batched driver.
+int qk_g0w0_L(qk_ctx* ctx, const qk_gw_params* prm, int N, int nC, int nO, int nR, int naux,
+              const double* L, const double* eHF, double* eGW, double* SigC, double* Z, double* Om,
+              double* EcRPA, double* EcGM);
+int qk_evgw_L(qk_ctx* ctx, const qk_gw_params* prm, int N, int nC, int nO, int nR, int naux,
+              const double* L, const double* eHF, double* eGW, double* SigC, double* Z,
+              double* EcRPA, double* EcGM, int* nSCF, double* Conv);
+
 
 // ------------------------------------------------------------------------------------------
 // error helpers

@@ -396,3 +396,57 @@ def test_qp_iteration_counts_match_oracle(ctx):
     E = synth.eri_phys_numpy(f["L"])
     api.RG0W0(api.GWOptions(), N, N, 0, nO, N - nO, 0, nO * (N - nO), E, f["eHF"], ctx=ctx)
     assert np.array_equal(ctx.qp_iters(N), f["g0w0_qp_iters"])
+
+
+# --------------------------------------------------------------------------------------------
+# batched driver: uneven systems on several streams, each checked against the oracle
+# --------------------------------------------------------------------------------------------
+def _batch_systems():
+    rng = np.random.default_rng(99)
+    out = []
+    for N in (13, 40, 24, 31, 18, 36, 27):
+        nO = synth.n_occ(N)
+        out.append(synth.gen_system(N, nO, 3 * N, rng))
+    return out
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_batched_driver_vs_oracle(ctx, method):
+    import torch
+    systems = _batch_systems()
+    desc, Lf, Ef = api.pack_systems(systems)
+    dL, dE = _dev(Lf), _dev(Ef)
+    dG = torch.zeros_like(dE)
+    opt = api.GWOptions(linearize=(method == 0), maxSCF=64, thresh=1e-5, max_diis=5)
+    r = api.gw_batch_L_dev(opt, method, desc, dL.data_ptr(), dE.data_ptr(), dG.data_ptr(),
+                           n_workers=3, ctx=ctx)
+    assert r["rc"] == api.QK_OK
+    eG = dG.cpu().numpy()
+    for i, s in enumerate(systems):
+        N, nO = s["N"], s["nO"]
+        nS = nO * (N - nO)
+        E = synth.eri_phys_numpy(s["L"])
+        if method == 0:
+            ref = O.RG0W0(True, 0.0, False, N, N, 0, nO, N - nO, 0, nS, E, s["eHF"])
+        else:
+            ref = O.evRGW(64, 1e-5, 5, False, 0.0, False, N, N, 0, nO, N - nO, 0, nS, E, s["eHF"],
+                          raise_on_fail=False)
+        got = eG[desc[i].offset_e:desc[i].offset_e + N]
+        assert r["status"][i] == (api.QK_ERR_NO_CONV if ref.get("failed") else api.QK_OK)
+        scale = np.maximum(1.0, np.abs(ref["SigC"]))
+        assert np.max(np.abs(got - ref["eGW"]) / scale) < 1e-7, i
+        if method == 1:
+            assert r["nSCF"][i] == ref["nSCF"]
+
+
+def test_batched_driver_isolates_bad_system(ctx):
+    import torch
+    systems = _batch_systems()[:3]
+    desc, Lf, Ef = api.pack_systems(systems)
+    desc[1].nO = desc[1].nOrb  # no virtual orbitals: invalid
+    dL, dE = _dev(Lf), _dev(Ef)
+    dG = torch.zeros_like(dE)
+    r = api.gw_batch_L_dev(api.GWOptions(linearize=True), 0, desc, dL.data_ptr(), dE.data_ptr(),
+                           dG.data_ptr(), n_workers=2, ctx=ctx)
+    assert r["status"][1] == api.QK_ERR_ARG
+    assert r["status"][0] == api.QK_OK and r["status"][2] == api.QK_OK
