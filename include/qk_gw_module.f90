@@ -22,6 +22,7 @@ module qk_gw_module
     real(c_double)    :: thresh
     integer(c_int)    :: max_diis
     integer(c_int)    :: precision
+    integer(c_int)    :: qp_guess
   end type qk_gw_params
 
   integer(c_int), parameter :: QK_OK = 0, QK_ERR_NO_CONV = 5

@@ -55,6 +55,9 @@ typedef struct qk_gw_params {
   double thresh;     /* thresh_GW (evGW) */
   int max_diis;      /* max_diis_GW (evGW) */
   int precision;     /* QK_PREC_* */
+  int qp_guess;      /* 0: Newton from the reference start (eGWlin); 1: Newton from the learned
+                        guess of the context's model (qk_set_qp_model), restarted from the
+                        reference start for orbitals that do not converge within 8 steps */
 } qk_gw_params;
 
 /* ---- context ------------------------------------------------------------------------------ */
@@ -69,6 +72,8 @@ int qk_num_timings(void);
 long long qk_launch_count(const qk_ctx* ctx);
 /* Newton steps per orbital of the context's last graphical QP solve (64 = not converged). */
 int qk_get_qp_iters(const qk_ctx* ctx, int* iters, int n);
+/* Sigma evaluations (orbital x Newton step, all phases) of the last graphical QP solve. */
+long long qk_qp_evals(const qk_ctx* ctx);
 /* Release cached device workspace. */
 int qk_trim(qk_ctx* ctx);
 
@@ -138,6 +143,33 @@ int qk_RG0W0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int nOrb, int nC, int n
 int qk_evRGW_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int nOrb, int nC, int nO, int nR,
                    int naux, const double* d_L, const double* d_eHF, double* d_eGW, double* d_SigC,
                    double* d_Z, double* EcRPA, double* EcGM, int* nSCF, double* Conv);
+
+/* ---- learned quasiparticle guess ----------------------------------------------------------
+ * No counterpart in the reference.  A 16 -> 64 -> 64 -> 1 SiLU perceptron predicts the QP shift
+ * eGW_p - eHF_p from 16 per-orbital features of the linearised G0W0 stage; it is trained on the
+ * GPU (FP32, Adam) by this library's own kernels and evaluated in BF16.  Parameters are one flat
+ * float vector of QK_MLP_NPARAM entries: W1 (64x16, row-major), b1, W2 (64x64), b2, W3 (1x64), b3.
+ * Inputs/targets of train/grad/predict are already normalised; qk_mlp_set_scaling records the
+ * normalisation the drivers apply to raw features and predicted shifts. */
+#define QK_MLP_NIN 16
+#define QK_MLP_NH 64
+#define QK_MLP_NPARAM (QK_MLP_NH * QK_MLP_NIN + QK_MLP_NH + QK_MLP_NH * QK_MLP_NH + QK_MLP_NH + QK_MLP_NH + 1)
+typedef struct qk_mlp qk_mlp;
+int qk_mlp_create(qk_ctx* ctx, unsigned long long seed, qk_mlp** mlp);
+int qk_mlp_free(qk_mlp* mlp);
+int qk_mlp_params(qk_ctx* ctx, qk_mlp* mlp, float* host_params, int set);
+int qk_mlp_set_scaling(qk_mlp* mlp, const float* xmean, const float* xstd, float ymean, float ystd);
+int qk_mlp_grad_dev(qk_ctx* ctx, qk_mlp* mlp, int n, const float* d_X, const float* d_T,
+                    float* d_grad, float* loss);
+int qk_mlp_train_dev(qk_ctx* ctx, qk_mlp* mlp, int n, const float* d_X, const float* d_T,
+                     int epochs, int batch, float lr, float* final_loss);
+int qk_mlp_predict_dev(qk_ctx* ctx, qk_mlp* mlp, int n, const float* d_X, float* d_Y, int bf16);
+/* Attach a model to the context (used when prm->qp_guess = 1); NULL detaches. */
+int qk_set_qp_model(qk_ctx* ctx, qk_mlp* mlp);
+/* Capture the 16 raw features per orbital of each subsequent G0W0 driver call (on/off) and read
+ * the last captured set (N x 16, row-major, host). */
+int qk_set_feature_capture(qk_ctx* ctx, int on);
+int qk_get_features(const qk_ctx* ctx, float* host, int n);
 
 /* ---- batched drivers (device pointers) ------------------------------------------------------
  * Many independent systems of uneven size in one call (no counterpart in the reference, which

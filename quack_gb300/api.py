@@ -35,7 +35,7 @@ class QkError(RuntimeError):
 class qk_gw_params(C.Structure):
     _fields_ = [("eta", C.c_double), ("linearize", C.c_int), ("doSRG", C.c_int),
                 ("TDA_W", C.c_int), ("maxSCF", C.c_int), ("thresh", C.c_double),
-                ("max_diis", C.c_int), ("precision", C.c_int)]
+                ("max_diis", C.c_int), ("precision", C.c_int), ("qp_guess", C.c_int)]
 
 
 def lib():
@@ -94,6 +94,23 @@ class Context:
 
     def launches(self) -> int:
         return int(lib().qk_launch_count(self._h))
+
+    def qp_evals(self) -> int:
+        """Sigma evaluations (orbital x Newton step) of the last graphical QP solve."""
+        lib().qk_qp_evals.restype = C.c_longlong
+        return int(lib().qk_qp_evals(self._h))
+
+    def set_feature_capture(self, on=True):
+        self.check(lib().qk_set_feature_capture(self._h, int(bool(on))))
+
+    def features(self, N):
+        """Raw per-orbital features (N x 16) captured by the last G0W0 driver call."""
+        buf = (C.c_float * (N * 16))()
+        lib().qk_get_features(self._h, buf, N * 16)
+        return np.array(buf[:], dtype=np.float32).reshape(N, 16)
+
+    def set_qp_model(self, model):
+        self.check(lib().qk_set_qp_model(self._h, model.handle if model is not None else None))
 
     def qp_iters(self, n):
         """Newton steps per orbital of the last graphical QP solve (64 = not converged)."""
@@ -249,10 +266,12 @@ class GWOptions:
     TDA_W: bool = False
     reg: bool = False
     precision: int = QK_PREC_FP64
+    qp_guess: bool = False
 
     def c(self):
         return qk_gw_params(self.eta, int(self.linearize), int(self.reg), int(self.TDA_W),
-                            self.maxSCF, self.thresh, self.max_diis, self.precision)
+                            self.maxSCF, self.thresh, self.max_diis, self.precision,
+                            int(self.qp_guess))
 
 
 def RG0W0(opts: GWOptions, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eHF, ctx=None):

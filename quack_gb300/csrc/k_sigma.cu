@@ -190,7 +190,9 @@ struct QPState {
   int* nit;
   int* active;
   int* nact;
-  int* list;  // compacted active orbitals, ascending
+  int* list;   // compacted active orbitals, ascending
+  int* conv;   // 1 if the last evaluation met |f| <= thresh
+  int* evals;  // Sigma evaluations per orbital, all phases
 };
 
 // rebuild the compacted active list (one block; warp 0 walks the orbitals 32 at a time)
@@ -209,19 +211,34 @@ __device__ void qp_compact(int N, QPState& s) {
   }
 }
 
-__global__ void k_qp_init(int N, int nC, int nR, const double* __restrict__ eGWlin, QPState s) {
+__global__ void k_qp_init(int N, int nC, int nR, const double* __restrict__ w0, QPState s) {
   for (int p = threadIdx.x; p < N; p += blockDim.x) {
-    s.w[p] = eGWlin[p];
+    s.w[p] = w0[p];
     s.df[p] = 0.0;
     s.nit[p] = 0;
+    s.conv[p] = 0;
+    s.evals[p] = 0;
     s.active[p] = (p >= nC && p < N - nR);
+  }
+  qp_compact(N, s);
+}
+
+// orbitals whose guess-started search did not converge restart from the reference start
+__global__ void k_qp_restart(int N, int nC, int nR, const double* __restrict__ eGWlin, QPState s) {
+  for (int p = threadIdx.x; p < N; p += blockDim.x) {
+    const bool act = (p >= nC && p < N - nR) && !s.conv[p];
+    if (act) {
+      s.w[p] = eGWlin[p];
+      s.nit[p] = 0;
+    }
+    s.active[p] = act;
   }
   qp_compact(N, s);
 }
 
 // one Newton step for every still-active p (RGW_QP_graph.f90:56-76)
 __global__ void k_qp_update(int N, int nchunks, const double* __restrict__ part,
-                            const double* __restrict__ eHF, QPState s) {
+                            const double* __restrict__ eHF, QPState s, int maxit) {
   if (*s.nact == 0) return;
   const size_t stride = (size_t)nchunks * N;
   for (int p = threadIdx.x; p < N; p += blockDim.x) {
@@ -233,12 +250,17 @@ __global__ void k_qp_update(int N, int nchunks, const double* __restrict__ part,
     }
     const int nIt = s.nit[p] + 1;
     s.nit[p] = nIt;
+    s.evals[p] += 1;
     const double w = s.w[p];
     const double f = w - eHF[p] - sig;
     const double df = 1.0 / (1.0 - dsig);
     s.w[p] = w - df * f;
     s.df[p] = df;
-    if (!(fabs(f) > QP_THRESH) || nIt >= QP_MAXIT) s.active[p] = 0;
+    const bool ok = !(fabs(f) > QP_THRESH);
+    if (ok || nIt >= maxit) {
+      s.active[p] = 0;
+      s.conv[p] = ok;
+    }
   }
   qp_compact(N, s);
 }
@@ -410,39 +432,167 @@ int qk_sigma_diag(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC
 
 int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                  int nS, const double* eHF, const double* Om, const double* rho,
-                 const double* eGWlin, const double* eOld, double* eGW, double* Z) {
+                 const double* eGWlin, const double* eOld, double* eGW, double* Z,
+                 const double* w_guess, int guess_maxit) {
   double* st = nullptr;
-  QK_TRY(qk_wst(ctx, W_M2, (size_t)5 * N + 64, &st));
+  QK_TRY(qk_wst(ctx, W_M2, (size_t)8 * N + 64, &st));
   QPState s;
   s.w = st;
   s.df = st + N;
   s.nit = (int*)(st + 2 * N);
   s.active = (int*)(st + 3 * N);
   s.list = (int*)(st + 4 * N);
-  s.nact = (int*)(st + 5 * N);
-  k_qp_init<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, eGWlin, s);
+  s.conv = (int*)(st + 5 * N);
+  s.evals = (int*)(st + 6 * N);
+  s.nact = (int*)(st + 7 * N);
+  // phase 1 (learned guess only): at most guess_maxit steps from the guess; phase 2: the
+  // reference search (RGW_QP_graph.f90:50-92) from eGWlin for every orbital not yet converged
+  k_qp_init<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, w_guess ? w_guess : eGWlin, s);
   QK_LAUNCHED();
-  int hact = 1;
-  for (int it = 0; it < QP_MAXIT; ++it) {
-    double* part;
-    int nch;
-    QK_TRY(sigma_sweep(ctx, doSRG, eta, flow, N, nC, nO, nR, nS, eOld, s.w, Om, rho, s.list,
-                       s.nact, &part, &nch));
-    k_qp_update<<<1, 1024, 0, ctx->stream>>>(N, nch, part, eHF, s);
-    QK_LAUNCHED();
-    if ((it & 3) == 3) {  // poll the active count every 4 steps
-      QK_CK(cudaMemcpyAsync(&hact, s.nact, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-      QK_CK(cudaStreamSynchronize(ctx->stream));
-      if (hact == 0) break;
+  for (int phase = w_guess ? 1 : 2; phase <= 2; ++phase) {
+    const int maxit = phase == 1 ? guess_maxit : QP_MAXIT;
+    if (phase == 2 && w_guess) {
+      k_qp_restart<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, eGWlin, s);
+      QK_LAUNCHED();
+    }
+    int hact = 1;
+    for (int it = 0; it < maxit; ++it) {
+      double* part;
+      int nch;
+      QK_TRY(sigma_sweep(ctx, doSRG, eta, flow, N, nC, nO, nR, nS, eOld, s.w, Om, rho, s.list,
+                         s.nact, &part, &nch));
+      k_qp_update<<<1, 1024, 0, ctx->stream>>>(N, nch, part, eHF, s, maxit);
+      QK_LAUNCHED();
+      if ((it & 3) == 3) {  // poll the active count every 4 steps
+        QK_CK(cudaMemcpyAsync(&hact, s.nact, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        QK_CK(cudaStreamSynchronize(ctx->stream));
+        if (hact == 0) break;
+      }
     }
   }
   k_qp_finish<<<(N + 255) / 256, 256, 0, ctx->stream>>>(N, nC, nR, eGWlin, s, eGW, Z, ctx->d_status);
   QK_LAUNCHED();
-  // per-orbital Newton step counts for diagnostics (qk_get_qp_stats)
+  // per-orbital Newton step counts and Sigma evaluations for diagnostics (qk_get_qp_iters)
   ctx->qp_iters.resize(N);
+  std::vector<int> ev(N);
   QK_CK(cudaMemcpyAsync(ctx->qp_iters.data(), s.nit, N * sizeof(int), cudaMemcpyDeviceToHost,
                         ctx->stream));
+  QK_CK(cudaMemcpyAsync(ev.data(), s.evals, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   QK_CK(cudaStreamSynchronize(ctx->stream));
+  long long tot = 0;
+  for (int v : ev) tot += v;
+  ctx->qp_evals = tot;
+  return QK_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// per-orbital features of the linearised stage for the learned guess
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+constexpr int NMOM = 6;  // occupied/virtual pole weight, first and second moments
+
+__global__ void __launch_bounds__(SIG_WARPS * 32)
+    k_feature_partial(int N, int nC, int nO, int nR, int nS, int nchunks, int mper,
+                      const double* __restrict__ e, const double* __restrict__ Om,
+                      const double* __restrict__ rho, double* __restrict__ part) {
+  extern __shared__ double se[];
+  __shared__ double acc[NMOM][SIG_WARPS][32];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) se[i] = e[i];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p = nC + blockIdx.x * 32 + lane;
+  const int pend = N - nR;
+  __syncthreads();
+  double m[NMOM] = {0, 0, 0, 0, 0, 0};
+  if (p < pend) {
+    const long long N1 = N, N2 = N1 * N1;
+    const int m0 = blockIdx.y * mper, m1 = min(nS, m0 + mper);
+    for (int mm = m0 + warp; mm < m1; mm += SIG_WARPS) {
+      const double om = Om[mm];
+      const double* r = rho + p + N2 * mm;
+      for (int q = nC; q < nO; ++q) {
+        const double x = r[N1 * q], w = x * x, pole = se[q] - om;
+        m[0] += w; m[1] += w * pole; m[2] += w * pole * pole;
+      }
+      for (int q = nO; q < pend; ++q) {
+        const double x = r[N1 * q], w = x * x, pole = se[q] + om;
+        m[3] += w; m[4] += w * pole; m[5] += w * pole * pole;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NMOM; ++k) acc[k][warp][lane] = m[k];
+  __syncthreads();
+  if (warp == 0 && p < pend) {
+    const size_t stride = (size_t)nchunks * N;
+#pragma unroll
+    for (int k = 0; k < NMOM; ++k) {
+      double t = 0.0;
+      for (int w = 0; w < SIG_WARPS; ++w) t += acc[k][w][lane];
+      part[(size_t)k * stride + (size_t)blockIdx.y * N + p] = t;
+    }
+  }
+}
+
+__global__ void k_feature_final(int N, int nC, int nO, int nR, int nchunks,
+                                const double* __restrict__ part, const double* __restrict__ e,
+                                const double* __restrict__ Om, const double* __restrict__ Sig,
+                                const double* __restrict__ Z, float* __restrict__ F) {
+  const size_t stride = (size_t)nchunks * N;
+  const double eh = e[nO - 1], el = e[nO];
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+    double m[NMOM] = {0, 0, 0, 0, 0, 0};
+    if (p >= nC && p < N - nR)
+      for (int c = 0; c < nchunks; ++c)
+        for (int k = 0; k < NMOM; ++k) m[k] += part[(size_t)k * stride + (size_t)c * N + p];
+    const double ep = e[p];
+    const double co = m[0] > 0 ? m[1] / m[0] : ep, cv = m[3] > 0 ? m[4] / m[3] : ep;
+    const double so = m[0] > 0 ? sqrt(fmax(0.0, m[2] / m[0] - co * co)) : 0.0;
+    const double sv = m[3] > 0 ? sqrt(fmax(0.0, m[5] / m[3] - cv * cv)) : 0.0;
+    float* f = F + (size_t)p * QK_MLP_NIN;
+    f[0] = (float)ep;
+    f[1] = p < nO ? 1.f : 0.f;
+    f[2] = (float)(ep - eh);
+    f[3] = (float)(ep - el);
+    f[4] = (float)Sig[p];
+    f[5] = (float)Z[p];
+    f[6] = (float)(Z[p] * Sig[p]);
+    f[7] = (float)(1.0 - 1.0 / Z[p]);
+    f[8] = (float)m[0];
+    f[9] = (float)m[3];
+    f[10] = (float)(co - ep);
+    f[11] = (float)(cv - ep);
+    f[12] = (float)so;
+    f[13] = (float)sv;
+    f[14] = (float)Om[0];
+    f[15] = (float)log((double)N);
+  }
+}
+
+}  // namespace
+
+int qk_features(qk_ctx* ctx, int N, int nC, int nO, int nR, int nS, const double* e,
+                const double* Om, const double* rho, const double* Sig, const double* Z,
+                float* F) {
+  const int nact = N - nR - nC;
+  const int ptiles = (nact + 31) / 32;
+  int nchunks = (4 * ctx->num_sms + ptiles - 1) / (ptiles > 0 ? ptiles : 1);
+  const int maxch = (nS + SIG_WARPS - 1) / SIG_WARPS;
+  if (nchunks > maxch) nchunks = maxch;
+  if (nchunks < 1) nchunks = 1;
+  const int mper = (nS + nchunks - 1) / nchunks;
+  nchunks = (nS + mper - 1) / mper;
+  double* part = nullptr;
+  QK_TRY(qk_wst(ctx, W_MISC, (size_t)NMOM * nchunks * N + 64, &part));
+  QK_CK(cudaMemsetAsync(part, 0, sizeof(double) * NMOM * (size_t)nchunks * N, ctx->stream));
+  if (ptiles > 0) {
+    k_feature_partial<<<dim3(ptiles, nchunks), SIG_WARPS * 32, N * sizeof(double), ctx->stream>>>(
+        N, nC, nO, nR, nS, nchunks, mper, e, Om, rho, part);
+    QK_LAUNCHED();
+  }
+  k_feature_final<<<(N + 127) / 128, 128, 0, ctx->stream>>>(N, nC, nO, nR, nchunks, part, e, Om,
+                                                           Sig, Z, F);
+  QK_LAUNCHED();
   return QK_OK;
 }
 

@@ -140,6 +140,37 @@ int casida_dev(qk_ctx* ctx, const Dims& d, const double* e, const double* ERI, d
   return QK_OK;
 }
 
+// Newton QP of RG0W0 (reference start eGWlin) or, with prm->qp_guess, from the learned guess;
+// captures the per-orbital features when requested.
+int g0w0_qp(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, double flow, const double* eHF,
+            const double* Om, const double* rho, const double* SigC, double* Z,
+            const double* eGWlin, double* eGW) {
+  const int N = d.N, nS = d.nS;
+  float* F = nullptr;
+  const bool need_f = ctx->capture_features || prm->qp_guess;
+  if (need_f) {
+    QK_TRY(qk_wst(ctx, W_FEAT, (size_t)N * QK_MLP_NIN + 16, &F));
+    QK_TRY(qk_features(ctx, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho, SigC, Z, F));
+    if (ctx->capture_features) {
+      ctx->features.resize((size_t)N * QK_MLP_NIN);
+      QK_CK(cudaMemcpyAsync(ctx->features.data(), F, sizeof(float) * N * QK_MLP_NIN,
+                            cudaMemcpyDeviceToHost, ctx->stream));
+      QK_CK(cudaStreamSynchronize(ctx->stream));
+    }
+  }
+  double* w0 = nullptr;
+  if (prm->qp_guess && !prm->linearize) {
+    QK_TRY(qk_wst(ctx, W_GUESS, (size_t)N + 16, &w0));
+    QK_TRY(qk_guess_from_model(ctx, N, F, eHF, w0));
+  }
+  if (prm->linearize) {
+    QK_CK(cudaMemcpyAsync(eGW, eGWlin, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    return QK_OK;
+  }
+  return qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho,
+                      eGWlin, eHF, eGW, Z, w0, 8);
+}
+
 int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* eHF,
              const double* ERI, double* eGW, double* SigC, double* Z, double* Om, double* hEcRPA,
              double* hEcGM) {
@@ -173,12 +204,7 @@ int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   QK_TRY(qk_qp_linear(ctx, N, eHF, Z, SigC, 1, eGWlin));
   qk_toc(ctx, T_SIGMA);
   qk_tic(ctx, T_QP);
-  if (prm->linearize) {
-    QK_CK(cudaMemcpyAsync(eGW, eGWlin, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  } else {
-    QK_TRY(qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho,
-                        eGWlin, eHF, eGW, Z));
-  }
+  QK_TRY(g0w0_qp(ctx, prm, d, flow, eHF, Om, rho, SigC, Z, eGWlin, eGW));
   qk_toc(ctx, T_QP);
   // second Casida at eGW for EcRPA (RG0W0.f90:222-225): eigenvalues only
   qk_tic(ctx, T_CASIDA2);
@@ -314,12 +340,7 @@ int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   QK_TRY(qk_qp_linear(ctx, N, eHF, Z, SigC, 1, eGWlin));
   qk_toc(ctx, T_SIGMA);
   qk_tic(ctx, T_QP);
-  if (prm->linearize) {
-    QK_CK(cudaMemcpyAsync(eGW, eGWlin, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  } else {
-    QK_TRY(qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho,
-                        eGWlin, eHF, eGW, Z));
-  }
+  QK_TRY(g0w0_qp(ctx, prm, d, flow, eHF, Om, rho, SigC, Z, eGWlin, eGW));
   qk_toc(ctx, T_QP);
   qk_tic(ctx, T_CASIDA2);
   QK_TRY(casida_dev(ctx, d, eGW, nullptr, nullptr, nullptr, nullptr, scal + 3, 0, K));

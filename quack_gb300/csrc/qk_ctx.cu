@@ -156,6 +156,8 @@ const char* qk_timing_name(int i) { return (i >= 0 && i < T_NUM) ? k_timing_name
 int qk_num_timings(void) { return T_NUM; }
 long long qk_launch_count(const qk_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+long long qk_qp_evals(const qk_ctx* ctx) { return ctx ? ctx->qp_evals : 0; }
+
 int qk_get_qp_iters(const qk_ctx* ctx, int* iters, int n) {
   if (!ctx || !iters) return QK_ERR_ARG;
   const int m = (int)ctx->qp_iters.size();

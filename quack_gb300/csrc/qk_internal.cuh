@@ -32,7 +32,7 @@ struct DevBuf {
 
 enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
-  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_NUMBUF
+  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_NUMBUF
 };
 
 struct qk_ctx {
@@ -50,6 +50,10 @@ struct qk_ctx {
   bool time_eig = true;  // stage timers inside the eigensolver (off for the eigenvalue-only pass)
   std::vector<int> qp_iters;  // Newton steps per orbital of the last QP solve
   std::vector<qk_ctx*> workers;  // per-stream sub-contexts of the batched driver
+  qk_mlp* mlp = nullptr;         // learned QP guess model (not owned)
+  bool capture_features = false;
+  std::vector<float> features;   // last captured N x 16 raw features
+  long long qp_evals = 0;        // orbital-evaluations of Sigma in the last Newton solve
 };
 
 // Factorised-integral drivers on one context (qk_api.cu), reused by the batched driver.
@@ -136,7 +140,14 @@ int qk_sigma_diag(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC
                   double* Z, double* EcGM);
 int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                  int nS, const double* eHF, const double* Om, const double* rho,
-                 const double* eGWlin, const double* eOld, double* eGW, double* Z);
+                 const double* eGWlin, const double* eOld, double* eGW, double* Z,
+                 const double* w_guess = nullptr, int guess_maxit = 8);
+// per-orbital features of the linearised stage (N x 16 floats, row-major, raw)
+int qk_features(qk_ctx* ctx, int N, int nC, int nO, int nR, int nS, const double* e,
+                const double* Om, const double* rho, const double* Sig, const double* Z,
+                float* F);
+// learned guess w0 = e + shift(features) with the attached model
+int qk_guess_from_model(qk_ctx* ctx, int N, const float* F, const double* e, double* w0);
 int qk_qp_linear(qk_ctx* ctx, int N, const double* eHF, const double* Z, const double* Sig,
                  int use_z, double* eGW);
 int qk_diis_dev(qk_ctx* ctx, int n_err, int n_e, int n_diis, double* err_hist, double* e_hist,

@@ -1,0 +1,70 @@
+"""GPU tests of the learned QP guess: the perceptron's forward/backward/Adam kernels against the
+NumPy oracle, BF16 inference against FP32, and the guess-seeded Newton search returning the
+reference roots."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as M
+from quack_gb300 import api, learned, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _t(x):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).cuda()
+
+
+def test_mlp_gradient_matches_oracle(ctx):
+    import torch
+    m = learned.QPModel(ctx, seed=7)
+    rng = np.random.default_rng(1)
+    p = (rng.standard_normal(M.NPARAM) * 0.3).astype(np.float32)
+    m.set_params(p)
+    X = rng.standard_normal((300, 16)).astype(np.float32)
+    T = rng.standard_normal(300).astype(np.float32)
+    dX, dT = _t(X), _t(T)
+    dG = torch.zeros(M.NPARAM, dtype=torch.float32, device="cuda")
+    loss = m.grad_dev(300, dX.data_ptr(), dT.data_ptr(), dG.data_ptr())
+    ref_loss, ref_g = M.loss_and_grad(p.astype(np.float64), X.astype(np.float64), T.astype(np.float64))
+    g = dG.cpu().numpy()
+    assert abs(loss - ref_loss) < 1e-4 * max(1.0, ref_loss)
+    scale = np.abs(ref_g).max()
+    assert np.max(np.abs(g - ref_g)) < 2e-4 * scale
+
+
+def test_mlp_training_and_bf16_inference(ctx):
+    import torch
+    m = learned.QPModel(ctx, seed=3)
+    rng = np.random.default_rng(2)
+    X = rng.standard_normal((4096, 16)).astype(np.float32)
+    T = (np.sin(X[:, 0]) + 0.5 * X[:, 1] * X[:, 2] - 0.3 * X[:, 3]).astype(np.float32)
+    dX, dT = _t(X), _t(T)
+    Y0 = torch.zeros(4096, dtype=torch.float32, device="cuda")
+    m.predict_dev(4096, dX.data_ptr(), Y0.data_ptr(), bf16=False)
+    loss0 = float(np.mean((Y0.cpu().numpy() - T) ** 2))
+    loss = m.train_dev(4096, dX.data_ptr(), dT.data_ptr(), epochs=60, batch=256, lr=3e-3)
+    assert loss < 0.1 * loss0
+    # forward kernel against the oracle with the trained parameters
+    Y = torch.zeros(4096, dtype=torch.float32, device="cuda")
+    m.predict_dev(4096, dX.data_ptr(), Y.data_ptr(), bf16=False)
+    Yref, _ = M.forward(m.get_params().astype(np.float64), X.astype(np.float64))
+    assert np.max(np.abs(Y.cpu().numpy() - Yref)) < 1e-3 * max(1.0, np.abs(Yref).max())
+    # BF16 inference stays close to FP32
+    Yb = torch.zeros(4096, dtype=torch.float32, device="cuda")
+    m.predict_dev(4096, dX.data_ptr(), Yb.data_ptr(), bf16=True)
+    assert np.sqrt(np.mean((Yb.cpu().numpy() - Yref) ** 2)) < 0.05 * np.std(Yref)
+
+
+def test_learned_guess_keeps_reference_roots(ctx):
+    rng = np.random.default_rng(11)
+    train_sys = [synth.gen_system(N, synth.n_occ(N), 3 * N, rng) for N in (24, 28, 32, 36, 30, 26)]
+    test_sys = [synth.gen_system(N, synth.n_occ(N), 3 * N, rng) for N in (25, 34)]
+    X, T = learned.collect(ctx, train_sys)
+    assert len(T) > 50
+    m = learned.QPModel(ctx, seed=5)
+    learned.train(m, X, T, epochs=150, batch=128, lr=3e-3)
+    rows = learned.evaluate(ctx, m, test_sys)
+    for r in rows:
+        # every orbital converged by the reference search is found again (same root) or restarted
+        assert r["n_same"] == r["n_conv"], r
