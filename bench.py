@@ -292,6 +292,8 @@ def run_ours(args):
     }
     if not args.no_batch:
         res["batched_evgw"] = run_batched(args, ctx)
+    if not args.no_learned:
+        res["learned_guess"] = run_learned(args, ctx)
     if rank == 0 and not args.no_cpu:
         res["cpu_baseline"] = cpu_baseline(args, s)
     if rank == 0:
@@ -338,6 +340,40 @@ def run_batched(args, ctx):
     out["qp_max_abs_diff_Ha"] = float(d.max())
     out["qp_median_abs_diff_Ha"] = float(np.median(d))
     return out
+
+
+def run_learned(args, ctx):
+    """Learned QP guess on systems drawn like the 4096-system configuration (seed 3,
+    N ~ U{24..200}, reduced here to N <= 80 and an 80/20 split of args.learned_systems systems):
+    train on the plain FP64 G0W0 roots of 80%, then compare the Newton search from the reference
+    start with the guess-seeded search on the held-out 20%."""
+    import numpy as np
+    from quack_gb300 import learned, synth
+
+    n = args.learned_systems
+    systems = synth.batch_systems(n, 24, 80, seed=3)
+    ntr = int(0.8 * n)
+    t0 = time.time()
+    X, T = learned.collect(ctx, systems[:ntr])
+    t1 = time.time()
+    model = learned.QPModel(ctx, seed=3)
+    mse = learned.train(model, X, T, epochs=200, batch=256, lr=2e-3)
+    t2 = time.time()
+    rows = learned.evaluate(ctx, model, systems[ntr:])
+    ev_ref = sum(r["evals_ref"] for r in rows)
+    ev_g = sum(r["evals_guess"] for r in rows)
+    n_conv = sum(r["n_conv"] for r in rows)
+    n_same = sum(r["n_same"] for r in rows)
+    return {"train_systems": ntr, "test_systems": n - ntr, "train_orbitals": int(len(T)),
+            "collect_s": t1 - t0, "train_s": t2 - t1, "train_mse_normalised": mse,
+            "newton_sigma_evals_reference": ev_ref, "newton_sigma_evals_guess": ev_g,
+            "eval_ratio": ev_g / max(1, ev_ref),
+            "qp_ms_reference": sum(r["qp_ms_ref"] for r in rows),
+            "qp_ms_guess": sum(r["qp_ms_guess"] for r in rows),
+            "systems_per_s_reference": len(rows) / sum(r["wall_ref"] for r in rows),
+            "systems_per_s_guess": len(rows) / sum(r["wall_guess"] for r in rows),
+            "converged_orbitals": n_conv, "same_root": n_same,
+            "max_abs_diff_converged_Ha": max(r["max_diff_conv"] for r in rows)}
 
 
 # --------------------------------------------------------------------------------------------
@@ -456,6 +492,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-systems", type=int, default=32)
     ap.add_argument("--batch-workers", type=int, default=8)
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--learned-systems", type=int, default=120)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

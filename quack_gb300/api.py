@@ -429,4 +429,6 @@ def gw_batch_L_dev(opts: GWOptions, method, desc, d_L, d_eHF, d_eGW, n_workers=8
     prm = opts.c()
     rc = lib().qk_gw_batch_L_dev(c.handle, C.byref(prm), int(method), n, desc, C.c_void_p(d_L),
                                  C.c_void_p(d_eHF), C.c_void_p(d_eGW), ec, st, ns, int(n_workers))
-    return dict(status=np.array(st[:]), EcRPA=np.array(ec[:]), nSCF=np.array(ns[:]), rc=rc)
+    err = lib().qk_last_error_string(c.handle).decode() if rc != QK_OK else ""
+    return dict(status=np.array(st[:]), EcRPA=np.array(ec[:]), nSCF=np.array(ns[:]), rc=rc,
+                error=err)

@@ -16,11 +16,13 @@
 // degenerate subspaces, which every downstream GW quantity is invariant to.
 #include <cmath>
 #include <cfloat>
+#include <mutex>
 #include "qk_internal.cuh"
 
 namespace {
 
 constexpr int TRI_THREADS = 1024;
+constexpr int TRI_SMEM_MAX = 200 * 1024;  // vectors kept in shared memory up to n = 8533
 constexpr int TRI_SMAX = 64;        // max column segments per row chunk
 constexpr int BT_NB = 64;           // reflectors per compact-WY block
 constexpr double CLUSTER_REL = 1e-7;  // eigenvalues closer than this * ||T||_1 share a cluster
@@ -472,10 +474,17 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   if (tm) qk_tic(ctx, T_TRIDIAG);
   {
     const size_t smem_need = 3 * N * sizeof(double);
-    const int use_smem = smem_need <= 200 * 1024;
+    const int use_smem = smem_need <= (size_t)TRI_SMEM_MAX;
     const size_t smem = use_smem ? smem_need : 0;
-    QK_CK(cudaFuncSetAttribute(k_sytrd, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(use_smem ? smem : 0)));
+    // the attribute is global to the kernel: set it once, at its maximum, so that concurrent
+    // callers on other streams/threads never see a smaller limit than their launch needs
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+      attr_err = cudaFuncSetAttribute(k_sytrd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      TRI_SMEM_MAX);
+    });
+    QK_CK(attr_err);
     int per_sm = 0;
     QK_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sytrd, TRI_THREADS, smem));
     if (per_sm < 1) return qk_fail(ctx, QK_ERR_CUDA, "k_sytrd cannot be resident");

@@ -223,10 +223,16 @@ __global__ void k_qp_init(int N, int nC, int nR, const double* __restrict__ w0, 
   qp_compact(N, s);
 }
 
-// orbitals whose guess-started search did not converge restart from the reference start
-__global__ void k_qp_restart(int N, int nC, int nR, const double* __restrict__ eGWlin, QPState s) {
+// Orbitals whose guess-started search did not converge, or converged outside the trust region
+// |w - eGWlin| <= |eGWlin - eHF| + 0.02 Ha around the reference start, restart from the
+// reference start (the root must stay the one the linearised solution points at).
+__global__ void k_qp_restart(int N, int nC, int nR, const double* __restrict__ eGWlin,
+                             const double* __restrict__ eHF, QPState s) {
   for (int p = threadIdx.x; p < N; p += blockDim.x) {
-    const bool act = (p >= nC && p < N - nR) && !s.conv[p];
+    const double trust = fabs(eGWlin[p] - eHF[p]) + 0.02;
+    const double wnew = s.w[p];
+    const bool keep = s.conv[p] && fabs(wnew - eGWlin[p]) <= trust;
+    const bool act = (p >= nC && p < N - nR) && !keep;
     if (act) {
       s.w[p] = eGWlin[p];
       s.nit[p] = 0;
@@ -452,7 +458,7 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
   for (int phase = w_guess ? 1 : 2; phase <= 2; ++phase) {
     const int maxit = phase == 1 ? guess_maxit : QP_MAXIT;
     if (phase == 2 && w_guess) {
-      k_qp_restart<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, eGWlin, s);
+      k_qp_restart<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, eGWlin, eHF, s);
       QK_LAUNCHED();
     }
     int hact = 1;

@@ -444,6 +444,7 @@ namespace {
 
 int begin(qk_ctx* ctx) {
   if (!ctx) return QK_ERR_ARG;
+  (void)cudaGetLastError();  // drop a non-sticky error left in this host thread by an earlier call
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return qk_cuda_fail(ctx, e, "cudaSetDevice", __FILE__, __LINE__);
   ctx->err.clear();

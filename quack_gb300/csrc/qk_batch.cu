@@ -8,6 +8,8 @@
 // A failing or non-converged system is recorded in its status word and does not stop the batch.
 #include <algorithm>
 #include <atomic>
+#include <mutex>
+#include <string>
 #include <thread>
 #include <vector>
 #include "qk_internal.cuh"
@@ -51,6 +53,8 @@ extern "C" int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int metho
   }
   std::sort(order.begin(), order.end(), [](const Item& a, const Item& b) { return a.cost > b.cost; });
   std::atomic<int> next(0);
+  std::mutex err_mu;
+  std::string first_err;
   auto run = [&](int wi) {
     qk_ctx* w = ctx->workers[wi];
     cudaSetDevice(w->device);
@@ -66,6 +70,7 @@ extern "C" int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int metho
       int ns = 0;
       if (st == QK_OK) {
         w->err.clear();
+        (void)cudaGetLastError();
         st = qk_status_reset(w);
         if (st == QK_OK) {
           const double* L = d_L + s.offset_L;
@@ -82,6 +87,10 @@ extern "C" int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int metho
           const int s2 = qk_status_check(w, QKD_BARRIER_TIMEOUT | QKD_BAD_INDEX | QKD_MBAR_TIMEOUT);
           if (s2 != QK_OK) st = s2;
         }
+      }
+      if (st != QK_OK && st != QK_ERR_NO_CONV) {
+        std::lock_guard<std::mutex> lk(err_mu);
+        if (first_err.empty()) first_err = "system " + std::to_string(i) + ": " + w->err;
       }
       if (status) status[i] = st;
       if (EcRPA) EcRPA[i] = ec;
@@ -100,5 +109,6 @@ extern "C" int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int metho
   if (status)
     for (int i = 0; i < nsys; ++i)
       if (status[i] != QK_OK && status[i] != QK_ERR_NO_CONV) worst = status[i];
+  if (worst != QK_OK) ctx->err = first_err;
   return worst;
 }

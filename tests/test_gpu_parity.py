@@ -420,7 +420,7 @@ def test_batched_driver_vs_oracle(ctx, method):
     opt = api.GWOptions(linearize=(method == 0), maxSCF=64, thresh=1e-5, max_diis=5)
     r = api.gw_batch_L_dev(opt, method, desc, dL.data_ptr(), dE.data_ptr(), dG.data_ptr(),
                            n_workers=3, ctx=ctx)
-    assert r["rc"] == api.QK_OK
+    assert r["rc"] == api.QK_OK, (r["error"], r["status"])
     eG = dG.cpu().numpy()
     for i, s in enumerate(systems):
         N, nO = s["N"], s["nO"]
