@@ -76,6 +76,12 @@ int qk_get_qp_iters(const qk_ctx* ctx, int* iters, int n);
 long long qk_qp_evals(const qk_ctx* ctx);
 /* Release cached device workspace. */
 int qk_trim(qk_ctx* ctx);
+/* evGW execution mode of this context: 0 (default) enqueues every cycle from the host and reads
+ * the convergence measure back after each one; 1 runs the first cycle that way and replays all
+ * further cycles from one CUDA graph whose device-side loop (a conditional WHILE node) stops at
+ * convergence or maxSCF, with the Newton search unrolled to its 64-step bound (finished orbitals
+ * drop out on the device).  Results are the same; mode 1 removes the per-cycle host round trips. */
+int qk_set_graph_mode(qk_ctx* ctx, int on);
 
 /* ---- stage-level drop-ins (host pointers) ------------------------------------------------- */
 /* LR/phRLR_A.f90:1-138 */

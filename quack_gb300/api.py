@@ -100,6 +100,10 @@ class Context:
         lib().qk_qp_evals.restype = C.c_longlong
         return int(lib().qk_qp_evals(self._h))
 
+    def set_graph_mode(self, on=True):
+        """evGW cycles 2.. replayed from one CUDA graph with a device-side WHILE loop."""
+        self.check(lib().qk_set_graph_mode(self._h, int(bool(on))))
+
     def set_feature_capture(self, on=True):
         self.check(lib().qk_set_feature_capture(self._h, int(bool(on))))
 

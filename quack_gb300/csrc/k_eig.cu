@@ -511,9 +511,18 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
     ta.bar = ctx->d_bar;
     ta.status = ctx->d_status;
     ta.use_smem = use_smem;
-    void* args[] = {&ta};
-    QK_CK(cudaLaunchCooperativeKernel((void*)k_sytrd, dim3(grid), dim3(TRI_THREADS), args, smem,
-                                      ctx->stream));
+    // cooperative launch (all CTAs co-resident for the grid barrier); also valid under capture
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(TRI_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    QK_CK(cudaLaunchKernelEx(&cfg, k_sytrd, ta));
     ctx->launches++;
   }
   if (tm) qk_toc(ctx, T_TRIDIAG);

@@ -310,9 +310,11 @@ __global__ void k_max_abs_diff(int n, const double* __restrict__ a, const double
 // partial pivoting; rcond is the exact reciprocal 1-norm condition number from the explicit
 // inverse (dsysvx reports an estimate of the same quantity).
 constexpr int DIIS_MAX = 32;
-__global__ void k_diis(int n_err, int n_e, int nd, double* __restrict__ err,
+__global__ void k_diis(int n_err, int n_e, int nd_host, double* __restrict__ err,
                        double* __restrict__ e, const double* __restrict__ err_in,
-                       double* __restrict__ e_inout, double* __restrict__ rcond_out) {
+                       double* __restrict__ e_inout, double* __restrict__ rcond_out,
+                       const int* __restrict__ nd_dev) {
+  const int nd = nd_dev ? *nd_dev : nd_host;
   __shared__ double A[DIIS_MAX + 1][DIIS_MAX + 1];
   __shared__ double wv[DIIS_MAX + 1];
   __shared__ double red[32];
@@ -408,8 +410,8 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
   const int mper = (nS + nchunks - 1) / nchunks;
   nchunks = (nS + mper - 1) / mper;
   double* part = nullptr;
+  // every (chunk, p) entry the consumers read is written by the sweep: no clearing needed
   QK_TRY(qk_wst(ctx, W_MISC, (size_t)3 * nchunks * N + 64, &part));
-  QK_CK(cudaMemsetAsync(part, 0, sizeof(double) * 3 * (size_t)nchunks * N, ctx->stream));
   SigArgs a;
   a.N = N; a.nC = nC; a.nO = nO; a.nR = nR; a.nS = nS;
   a.nchunks = nchunks; a.mper = mper;
@@ -469,7 +471,7 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
                          s.nact, &part, &nch));
       k_qp_update<<<1, 1024, 0, ctx->stream>>>(N, nch, part, eHF, s, maxit);
       QK_LAUNCHED();
-      if ((it & 3) == 3) {  // poll the active count every 4 steps
+      if (!ctx->capturing && (it & 3) == 3) {  // poll the active count every 4 steps
         QK_CK(cudaMemcpyAsync(&hact, s.nact, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         QK_CK(cudaStreamSynchronize(ctx->stream));
         if (hact == 0) break;
@@ -478,6 +480,7 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
   }
   k_qp_finish<<<(N + 255) / 256, 256, 0, ctx->stream>>>(N, nC, nR, eGWlin, s, eGW, Z, ctx->d_status);
   QK_LAUNCHED();
+  if (ctx->capturing) return QK_OK;  // no host readback inside a graph
   // per-orbital Newton step counts and Sigma evaluations for diagnostics (qk_get_qp_iters)
   ctx->qp_iters.resize(N);
   std::vector<int> ev(N);
@@ -610,9 +613,10 @@ int qk_qp_linear(qk_ctx* ctx, int N, const double* eHF, const double* Z, const d
 }
 
 int qk_diis_dev(qk_ctx* ctx, int n_err, int n_e, int n_diis, double* err_hist, double* e_hist,
-                const double* err_in, double* e_inout, double* rcond_dev) {
+                const double* err_in, double* e_inout, double* rcond_dev, const int* n_diis_dev) {
   if (n_diis < 1 || n_diis > DIIS_MAX) return qk_fail(ctx, QK_ERR_ARG, "n_diis out of range (1..%d)", DIIS_MAX);
-  k_diis<<<1, 256, 0, ctx->stream>>>(n_err, n_e, n_diis, err_hist, e_hist, err_in, e_inout, rcond_dev);
+  k_diis<<<1, 256, 0, ctx->stream>>>(n_err, n_e, n_diis, err_hist, e_hist, err_in, e_inout, rcond_dev,
+                                     n_diis_dev);
   QK_LAUNCHED();
   return QK_OK;
 }

@@ -219,6 +219,144 @@ int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   return QK_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// evGW cycle (evRGW.f90:119-180) without host synchronisation, so that it can be enqueued
+// eagerly or captured once into a CUDA graph and replayed by a device-side WHILE loop.
+// dstate (device ints): [0] nSCF, [1] n_diis, [2] continue flag.  scal[9] = Conv.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_diis_count(int* st, int max_diis) {
+  st[1] = st[1] + 1 < max_diis ? st[1] + 1 : max_diis;
+}
+
+__global__ void k_cycle_end(int* st, const double* conv, double thresh, int maxSCF,
+                            cudaGraphConditionalHandle h, int use_handle) {
+  st[0] += 1;
+  const int cont = (*conv > thresh) && (st[0] <= maxSCF);  // evRGW.f90:119
+  st[2] = cont;
+  if (use_handle) cudaGraphSetConditional(h, cont ? 1u : 0u);
+}
+
+struct EvBufs {
+  const double* ERI;   // full-ERI path (or nullptr)
+  const double* K;     // factorised path (or nullptr)
+  const double* slab;
+  const double* eHF;
+  double *eGW, *eOld, *SigC, *Z, *Om, *XpY, *rho, *scal, *errv, *err_hist, *e_hist;
+  int* dstate;
+};
+
+int evgw_cycle(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const EvBufs& b,
+               cudaGraphConditionalHandle h, int use_handle) {
+  const double flow = 500.0;
+  const int N = d.N, nS = d.nS;
+  QK_TRY(casida_dev(ctx, d, b.eGW, b.ERI, b.Om, b.XpY, nullptr, b.scal, 1, b.K));
+  qk_tic(ctx, T_RHO);
+  QK_TRY(rho_gemm(ctx, prm->precision, N, nS, b.slab, b.XpY, b.rho));
+  qk_toc(ctx, T_RHO);
+  qk_tic(ctx, T_SIGMA);
+  QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, b.eGW, b.Om,
+                       b.rho, b.SigC, b.Z, b.scal + 8));
+  qk_toc(ctx, T_SIGMA);
+  qk_tic(ctx, T_QP);
+  if (prm->linearize) {
+    QK_TRY(qk_qp_linear(ctx, N, b.eHF, b.Z, b.SigC, 0, b.eGW));  // evRGW.f90:147
+  } else {
+    QK_TRY(qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, b.eHF, b.Om,
+                        b.rho, b.eOld, b.eOld, b.eGW, b.Z));  // evRGW.f90:154
+  }
+  qk_toc(ctx, T_QP);
+  QK_TRY(qk_max_abs_diff(ctx, N, b.eGW, b.eOld, b.scal + 9));  // evRGW.f90:160
+  if (prm->max_diis > 1) {  // evRGW.f90:166-171
+    k_diis_count<<<1, 1, 0, ctx->stream>>>(b.dstate, prm->max_diis);
+    QK_LAUNCHED();
+    QK_TRY(qk_sub(ctx, N, b.eGW, b.eOld, b.errv));
+    QK_TRY(qk_diis_dev(ctx, N, N, prm->max_diis, b.err_hist, b.e_hist, b.errv, b.eGW, b.scal + 10,
+                       b.dstate + 1));
+  }
+  QK_CK(cudaMemcpyAsync(b.eOld, b.eGW, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  k_cycle_end<<<1, 1, 0, ctx->stream>>>(b.dstate, b.scal + 9, prm->thresh, prm->maxSCF, h, use_handle);
+  QK_LAUNCHED();
+  return QK_OK;
+}
+
+// Build (or reuse) a graph whose WHILE node replays evgw_cycle until the device flag drops.
+int evgw_graph_run(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const EvBufs& b) {
+  std::vector<long long> key = {(long long)d.N, d.nC, d.nO, d.nR, prm->precision, prm->linearize,
+                                prm->doSRG, prm->max_diis, prm->maxSCF,
+                                (long long)(prm->thresh * 1e15), (long long)(prm->eta * 1e15),
+                                (long long)b.ERI, (long long)b.K, (long long)b.slab,
+                                (long long)b.eHF, (long long)b.eGW, (long long)b.dstate};
+  if (!ctx->evgw_exec || ctx->evgw_key != key) {
+    if (ctx->evgw_exec) {
+      cudaGraphExecDestroy(ctx->evgw_exec);
+      ctx->evgw_exec = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    QK_CK(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle h;
+    QK_CK(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    QK_CK(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    QK_CK(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeRelaxed));
+    ctx->capturing = true;
+    const int st = evgw_cycle(ctx, prm, d, b, h, 1);
+    ctx->capturing = false;
+    cudaGraph_t captured = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(ctx->stream, &captured);
+    if (st != QK_OK) {
+      cudaGraphDestroy(graph);
+      return st;
+    }
+    QK_CK(ec);
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    QK_CK(ei);
+    ctx->evgw_exec = exec;
+    ctx->evgw_key = key;
+  }
+  QK_CK(cudaGraphLaunch(ctx->evgw_exec, ctx->stream));
+  return QK_OK;
+}
+
+// cycles of evGW: the first eagerly (it sizes every workspace), the rest either eagerly or from
+// the graph; returns nSCF and Conv read back from the device
+int evgw_loop(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const EvBufs& b, int* hnSCF,
+              double* hConv) {
+  QK_CK(cudaMemsetAsync(b.dstate, 0, 4 * sizeof(int), ctx->stream));
+  cudaGraphConditionalHandle none = 0;
+  int hst[4] = {0, 0, 1, 0};
+  double conv = 1.0;
+  QK_TRY(evgw_cycle(ctx, prm, d, b, none, 0));
+  QK_CK(cudaMemcpyAsync(hst, b.dstate, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QK_CK(cudaMemcpyAsync(&conv, b.scal + 9, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QK_CK(cudaStreamSynchronize(ctx->stream));
+  if (hst[2]) {
+    if (ctx->graph_mode) {
+      QK_TRY(evgw_graph_run(ctx, prm, d, b));
+    } else {
+      while (hst[2]) {
+        QK_TRY(evgw_cycle(ctx, prm, d, b, none, 0));
+        QK_CK(cudaMemcpyAsync(hst, b.dstate, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        QK_CK(cudaStreamSynchronize(ctx->stream));
+      }
+    }
+    QK_CK(cudaMemcpyAsync(hst, b.dstate, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    QK_CK(cudaMemcpyAsync(&conv, b.scal + 9, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QK_CK(cudaStreamSynchronize(ctx->stream));
+  }
+  *hnSCF = hst[0];
+  *hConv = conv;
+  return QK_OK;
+}
+
 int evgw_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* eHF,
              const double* ERI, double* eGW, double* SigC, double* Z, double* hEcRPA,
              double* hEcGM, int* hnSCF, double* hConv) {
@@ -231,13 +369,14 @@ int evgw_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   QK_TRY(qk_wst(ctx, W_XPY, S2, &XpY));
   QK_TRY(qk_wst(ctx, W_SLAB, N2S, &slab));
   QK_TRY(qk_wst(ctx, W_RHO, N2S, &rho));
-  QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)(6 + 2 * maxd) * N + nS + 64, &small));
+  QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)(6 + 2 * maxd) * N + nS + 64 + 8, &small));
   double* scal = small;            // [0]=trA [1]=sumOm [2]=EcRPA [8]=EcGM [9]=Conv [10]=rcond
   double* eOld = small + 64;
   double* errv = eOld + N;
   double* Om = errv + N;
   double* err_hist = Om + nS;
   double* e_hist = err_hist + (size_t)N * maxd;
+  int* dstate = (int*)(e_hist + (size_t)N * maxd);
   QK_CK(cudaMemsetAsync(err_hist, 0, sizeof(double) * 2 * (size_t)N * maxd, ctx->stream));
   QK_CK(cudaMemcpyAsync(eGW, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   QK_CK(cudaMemcpyAsync(eOld, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -246,36 +385,11 @@ int evgw_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   qk_tic(ctx, T_SLAB);
   QK_TRY(qk_launch_slab_gather(ctx, N, d.nC, d.nO, d.nR, ERI, slab));
   qk_toc(ctx, T_SLAB);
-  int nSCF = 0, n_diis = 0;
+  EvBufs bb{ERI, nullptr, slab, eHF, eGW, eOld, SigC, Z, Om, XpY, rho, scal, errv,
+            err_hist, e_hist, dstate};
+  int nSCF = 0;
   double Conv = 1.0;
-  while (Conv > prm->thresh && nSCF <= prm->maxSCF) {  // evRGW.f90:119
-    QK_TRY(casida_dev(ctx, d, eGW, ERI, Om, XpY, nullptr, scal, 1));
-    qk_tic(ctx, T_RHO);
-    QK_TRY(rho_gemm(ctx, prm->precision, N, nS, slab, XpY, rho));
-    qk_toc(ctx, T_RHO);
-    qk_tic(ctx, T_SIGMA);
-    QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eGW, Om, rho,
-                         SigC, Z, scal + 8));
-    qk_toc(ctx, T_SIGMA);
-    qk_tic(ctx, T_QP);
-    if (prm->linearize) {
-      QK_TRY(qk_qp_linear(ctx, N, eHF, Z, SigC, 0, eGW));  // evRGW.f90:147
-    } else {
-      QK_TRY(qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho,
-                          eOld, eOld, eGW, Z));  // evRGW.f90:154
-    }
-    qk_toc(ctx, T_QP);
-    QK_TRY(qk_max_abs_diff(ctx, N, eGW, eOld, scal + 9));
-    if (prm->max_diis > 1) {  // evRGW.f90:166-171
-      n_diis = n_diis + 1 < prm->max_diis ? n_diis + 1 : prm->max_diis;
-      QK_TRY(qk_sub(ctx, N, eGW, eOld, errv));
-      QK_TRY(qk_diis_dev(ctx, N, N, n_diis, err_hist, e_hist, errv, eGW, scal + 10));
-    }
-    QK_CK(cudaMemcpyAsync(eOld, eGW, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-    QK_TRY(d2h(ctx, &Conv, scal + 9, sizeof(double)));
-    QK_CK(cudaStreamSynchronize(ctx->stream));
-    nSCF++;
-  }
+  QK_TRY(evgw_loop(ctx, prm, d, bb, &nSCF, &Conv));
   double h[16];
   QK_TRY(d2h(ctx, h, scal, 16 * sizeof(double)));
   QK_CK(cudaStreamSynchronize(ctx->stream));
@@ -367,46 +481,22 @@ int evgw_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   QK_TRY(factor_prep(ctx, prm->precision, d, naux, L, &K, &slab));
   QK_TRY(qk_wst(ctx, W_XPY, S2, &XpY));
   QK_TRY(qk_wst(ctx, W_RHO, N2S, &rho));
-  QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)(6 + 2 * maxd) * N + nS + 64, &small));
+  QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)(6 + 2 * maxd) * N + nS + 64 + 8, &small));
   double* scal = small;
   double* eOld = small + 64;
   double* errv = eOld + N;
   double* Om = errv + N;
   double* err_hist = Om + nS;
   double* e_hist = err_hist + (size_t)N * maxd;
+  int* dstate = (int*)(e_hist + (size_t)N * maxd);
   QK_CK(cudaMemsetAsync(err_hist, 0, sizeof(double) * 2 * (size_t)N * maxd, ctx->stream));
   QK_CK(cudaMemcpyAsync(eGW, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   QK_CK(cudaMemcpyAsync(eOld, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  int nSCF = 0, n_diis = 0;
+  EvBufs bb{nullptr, K, slab, eHF, eGW, eOld, SigC, Z, Om, XpY, rho, scal, errv,
+            err_hist, e_hist, dstate};
+  int nSCF = 0;
   double Conv = 1.0;
-  while (Conv > prm->thresh && nSCF <= prm->maxSCF) {
-    QK_TRY(casida_dev(ctx, d, eGW, nullptr, Om, XpY, nullptr, scal, 1, K));
-    qk_tic(ctx, T_RHO);
-    QK_TRY(rho_gemm(ctx, prm->precision, N, nS, slab, XpY, rho));
-    qk_toc(ctx, T_RHO);
-    qk_tic(ctx, T_SIGMA);
-    QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eGW, Om, rho,
-                         SigC, Z, scal + 8));
-    qk_toc(ctx, T_SIGMA);
-    qk_tic(ctx, T_QP);
-    if (prm->linearize) {
-      QK_TRY(qk_qp_linear(ctx, N, eHF, Z, SigC, 0, eGW));
-    } else {
-      QK_TRY(qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho,
-                          eOld, eOld, eGW, Z));
-    }
-    qk_toc(ctx, T_QP);
-    QK_TRY(qk_max_abs_diff(ctx, N, eGW, eOld, scal + 9));
-    if (prm->max_diis > 1) {
-      n_diis = n_diis + 1 < prm->max_diis ? n_diis + 1 : prm->max_diis;
-      QK_TRY(qk_sub(ctx, N, eGW, eOld, errv));
-      QK_TRY(qk_diis_dev(ctx, N, N, n_diis, err_hist, e_hist, errv, eGW, scal + 10));
-    }
-    QK_CK(cudaMemcpyAsync(eOld, eGW, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-    QK_TRY(d2h(ctx, &Conv, scal + 9, sizeof(double)));
-    QK_CK(cudaStreamSynchronize(ctx->stream));
-    nSCF++;
-  }
+  QK_TRY(evgw_loop(ctx, prm, d, bb, &nSCF, &Conv));
   double h[16];
   QK_TRY(d2h(ctx, h, scal, 16 * sizeof(double)));
   QK_CK(cudaStreamSynchronize(ctx->stream));

@@ -63,8 +63,11 @@ int qk_status_check(qk_ctx* ctx, int fatal_mask) {
   return QK_OK;
 }
 
-void qk_tic(qk_ctx* ctx, int stage) { cudaEventRecord(ctx->ev[2 * stage], ctx->stream); }
+void qk_tic(qk_ctx* ctx, int stage) {
+  if (ctx->timing && !ctx->capturing) cudaEventRecord(ctx->ev[2 * stage], ctx->stream);
+}
 void qk_toc(qk_ctx* ctx, int stage) {
+  if (!ctx->timing || ctx->capturing) return;
   cudaEventRecord(ctx->ev[2 * stage + 1], ctx->stream);
   ctx->timings[stage] = -1.0;  // mark pending
 }
@@ -120,6 +123,7 @@ int qk_finalize(qk_ctx* ctx) {
   if (!ctx) return QK_OK;
   for (auto* w : ctx->workers) qk_finalize(w);
   ctx->workers.clear();
+  if (ctx->evgw_exec) cudaGraphExecDestroy(ctx->evgw_exec);
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto& b : ctx->buf)
@@ -157,6 +161,12 @@ int qk_num_timings(void) { return T_NUM; }
 long long qk_launch_count(const qk_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 long long qk_qp_evals(const qk_ctx* ctx) { return ctx ? ctx->qp_evals : 0; }
+
+int qk_set_graph_mode(qk_ctx* ctx, int on) {
+  if (!ctx) return QK_ERR_ARG;
+  ctx->graph_mode = on != 0;
+  return QK_OK;
+}
 
 int qk_get_qp_iters(const qk_ctx* ctx, int* iters, int n) {
   if (!ctx || !iters) return QK_ERR_ARG;

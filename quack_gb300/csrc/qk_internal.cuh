@@ -54,6 +54,11 @@ struct qk_ctx {
   bool capture_features = false;
   std::vector<float> features;   // last captured N x 16 raw features
   long long qp_evals = 0;        // orbital-evaluations of Sigma in the last Newton solve
+  bool timing = true;            // stage events (off while a graph is being captured)
+  bool graph_mode = false;       // evGW cycles 2.. replayed from a CUDA graph
+  bool capturing = false;        // inside stream capture: no host synchronisation allowed
+  cudaGraphExec_t evgw_exec = nullptr;
+  std::vector<long long> evgw_key;  // shape/pointer key of the cached evGW graph
 };
 
 // Factorised-integral drivers on one context (qk_api.cu), reused by the batched driver.
@@ -151,7 +156,8 @@ int qk_guess_from_model(qk_ctx* ctx, int N, const float* F, const double* e, dou
 int qk_qp_linear(qk_ctx* ctx, int N, const double* eHF, const double* Z, const double* Sig,
                  int use_z, double* eGW);
 int qk_diis_dev(qk_ctx* ctx, int n_err, int n_e, int n_diis, double* err_hist, double* e_hist,
-                const double* err_in, double* e_inout, double* rcond_dev);
+                const double* err_in, double* e_inout, double* rcond_dev,
+                const int* n_diis_dev = nullptr);
 int qk_sub(qk_ctx* ctx, int n, const double* a, const double* b, double* out);
 int qk_max_abs_diff(qk_ctx* ctx, int n, const double* a, const double* b, double* out_dev);
 

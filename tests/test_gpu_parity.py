@@ -450,3 +450,31 @@ def test_batched_driver_isolates_bad_system(ctx):
                            dG.data_ptr(), n_workers=2, ctx=ctx)
     assert r["status"][1] == api.QK_ERR_ARG
     assert r["status"][0] == api.QK_OK and r["status"][2] == api.QK_OK
+
+
+# --------------------------------------------------------------------------------------------
+# evGW cycles replayed from a CUDA graph (device-side WHILE loop) == eager cycles
+# --------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("lin,nd", [(False, 5), (True, 5), (False, 1)])
+def test_evgw_graph_mode_matches_fixture(ctx, lin, nd):
+    import torch
+    f = np.load(os.path.join(GOLD, "synth_n24.npz"))
+    N, nO = int(f["N"]), int(f["nO"])
+    E = synth.eri_phys_numpy(f["L"])
+    opt = api.GWOptions(maxSCF=64, thresh=1e-5, max_diis=nd, linearize=lin)
+    key = "evgwlin" if lin else "evgw_d%d" % nd
+    ctx.set_graph_mode(True)
+    try:
+        for _ in range(2):  # second call reuses the cached graph
+            r = api.evRGW(opt, N, N, 0, nO, N - nO, 0, nO * (N - nO), E, f["eHF"], ctx=ctx)
+            assert r["nSCF"] == int(f[key + "_nSCF"])
+            assert np.max(np.abs(r["eGW"] - f[key + "_eGW"])) < E_TOL
+        dL = _dev(api.L_fortran_flat(f["L"]))
+        de = _dev(f["eHF"])
+        out = [torch.empty(N, dtype=torch.float64, device="cuda") for _ in range(3)]
+        r = api.evRGW_L_dev(opt, N, 0, nO, 0, 3 * N, dL.data_ptr(), de.data_ptr(),
+                            out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), ctx=ctx)
+        assert r["nSCF"] == int(f[key + "_nSCF"])
+        assert np.max(np.abs(out[0].cpu().numpy() - f[key + "_eGW"])) < E_TOL
+    finally:
+        ctx.set_graph_mode(False)
