@@ -228,6 +228,20 @@ int qk_RGW_self_energy_diag_noalloc_dev(double eta, int nBas, int nOrb, int nC, 
                                         const double* d_rho, double* d_EcGM, double* d_Sig,
                                         double* d_Z, void* stream);
 
+/* ---- autotuner ------------------------------------------------------------------------------
+ * No counterpart in the reference.  Runtime launch parameters of this library's kernels, tuned
+ * per size bucket floor(log2(size)): "bf16x3_chunk" (k blocks per TMEM chunk of the BF16x3 GEMM,
+ * size = K), "splitk_mult" (split-K target CTAs per SM of the DMMA GEMM, size = K),
+ * "sigma_chunks" (m chunks of the pole sweeps per SM, size = nS), "sytrd_grid" (quarters of the
+ * SMs in the cooperative tridiagonalisation, size = n).  qk_autotune times all candidates on
+ * problems of the given sizes (allocates temporary buffers) and keeps the fastest; the table
+ * can be saved to / loaded from a JSON file. */
+int qk_autotune(qk_ctx* ctx, int nOrb, int nS, int flags);
+int qk_tune_set(qk_ctx* ctx, const char* name, long long size, int value);
+int qk_tune_query(const qk_ctx* ctx, const char* name, long long size);
+int qk_tune_save(const qk_ctx* ctx, const char* path);
+int qk_tune_load(qk_ctx* ctx, const char* path);
+
 /* ---- diagnostics ------------------------------------------------------------------------- */
 /* The cudaStream_t (as void*) on which the context enqueues all of its kernels. */
 void* qk_stream(const qk_ctx* ctx);

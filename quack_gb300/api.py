@@ -100,6 +100,24 @@ class Context:
         lib().qk_qp_evals.restype = C.c_longlong
         return int(lib().qk_qp_evals(self._h))
 
+    def autotune(self, nOrb, nS):
+        """Time the tunable launch parameters on problems of these sizes; keep the fastest."""
+        self.check(lib().qk_autotune(self._h, nOrb, nS, 0))
+
+    def tune_query(self, name, size):
+        lib().qk_tune_query.argtypes = [C.c_void_p, C.c_char_p, C.c_longlong]
+        return int(lib().qk_tune_query(self._h, name.encode(), size))
+
+    def tune_set(self, name, size, value):
+        lib().qk_tune_set.argtypes = [C.c_void_p, C.c_char_p, C.c_longlong, C.c_int]
+        self.check(lib().qk_tune_set(self._h, name.encode(), size, value))
+
+    def tune_save(self, path):
+        self.check(lib().qk_tune_save(self._h, str(path).encode()))
+
+    def tune_load(self, path):
+        self.check(lib().qk_tune_load(self._h, str(path).encode()))
+
     def set_graph_mode(self, on=True):
         """evGW cycles 2.. replayed from one CUDA graph with a device-side WHILE loop."""
         self.check(lib().qk_set_graph_mode(self._h, int(bool(on))))

@@ -33,7 +33,7 @@ constexpr int TILE_BYTES = 128 * BK * 2;           // 16 KB per part tile
 constexpr int STAGE_BYTES = 6 * TILE_BYTES;        // 96 KB
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr uint32_t MBAR_SPIN = 1u << 30;
-constexpr int CHUNK_KB = 2;                        // k blocks per TMEM accumulation chunk
+// k blocks per TMEM accumulation chunk: a template parameter (1, 2 or 4) chosen by the autotuner
 constexpr uint32_t TMEM_COLS = 512;                // two chunk accumulators + hi + lo planes
 constexpr int NTHREADS = 320;                      // producer, MMA, 8 epilogue warps
 
@@ -175,6 +175,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bp)) + (b - bp);
 }
 
+template <int CHUNK_KB>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_gemm_bf16x3(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                   int M, int N, int Kpad, int rowsA, int rowsB, double* __restrict__ C,
@@ -423,15 +424,29 @@ int qk_gemm_bf16x3_parts(qk_ctx* ctx, int m, int n, const void* Ap, int rowsA, c
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
-    attr_err = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    attr_err = cudaFuncSetAttribute(k_gemm_bf16x3<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     SMEM_BYTES);
+    if (attr_err == cudaSuccess)
+      attr_err = cudaFuncSetAttribute(k_gemm_bf16x3<2>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (attr_err == cudaSuccess)
+      attr_err = cudaFuncSetAttribute(k_gemm_bf16x3<4>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
   });
   QK_CK(attr_err);
   const int m_tiles = rowsA / BM, n_tiles = rowsB / BN;
   const long long tiles = (long long)m_tiles * n_tiles;
   if (tiles > 0x7fffffffLL) return qk_fail(ctx, QK_ERR_ARG, "bf16x3: too many tiles");
-  k_gemm_bf16x3<<<(unsigned)tiles, NTHREADS, SMEM_BYTES, ctx->stream>>>(ma, mb, m, n, Kpad, rowsA, rowsB,
-                                                                   C, ldc, n_tiles, ctx->d_status);
+  const int chunk = qk_tune_get(ctx, TUNE_BF16X3_CHUNK, Kpad, 2);
+  if (chunk == 1)
+    k_gemm_bf16x3<1><<<(unsigned)tiles, NTHREADS, SMEM_BYTES, ctx->stream>>>(
+        ma, mb, m, n, Kpad, rowsA, rowsB, C, ldc, n_tiles, ctx->d_status);
+  else if (chunk == 4)
+    k_gemm_bf16x3<4><<<(unsigned)tiles, NTHREADS, SMEM_BYTES, ctx->stream>>>(
+        ma, mb, m, n, Kpad, rowsA, rowsB, C, ldc, n_tiles, ctx->d_status);
+  else
+    k_gemm_bf16x3<2><<<(unsigned)tiles, NTHREADS, SMEM_BYTES, ctx->stream>>>(
+        ma, mb, m, n, Kpad, rowsA, rowsB, C, ldc, n_tiles, ctx->d_status);
   QK_LAUNCHED();
   return QK_OK;
 }

@@ -491,7 +491,10 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
     // one CTA per SM: the O(n) vector work of each column is repeated by every CTA, so fewer,
     // wider CTAs waste less FP64 issue
     per_sm = 1;
-    int grid = per_sm * ctx->num_sms;
+    // CTAs of the cooperative grid: 4/4 of the SMs by default, or the tuned fraction
+    const int gq = qk_tune_get(ctx, TUNE_SYTRD_GRID, n, 4);
+    int grid = per_sm * ctx->num_sms * gq / 4;
+    if (grid < 1) grid = 1;
     // small problems do not need the whole GPU
     const int want = (int)((N * N) / (32 * 128)) + 1;
     if (grid > want) grid = want < 1 ? 1 : want;

@@ -403,7 +403,8 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
                        int* nchunks_out) {
   const int nact_p = N - nR - nC;
   const int ptiles = (nact_p + 31) / 32;
-  int nchunks = (4 * ctx->num_sms + ptiles - 1) / (ptiles > 0 ? ptiles : 1);
+  const int cm = qk_tune_get(ctx, TUNE_SIGMA_CHUNKS, (long long)nS, 4);
+  int nchunks = (cm * ctx->num_sms + ptiles - 1) / (ptiles > 0 ? ptiles : 1);
   const int maxch = (nS + SIG_WARPS - 1) / SIG_WARPS;
   if (nchunks > maxch) nchunks = maxch;
   if (nchunks < 1) nchunks = 1;

@@ -25,6 +25,10 @@ enum {
   T_MISC, T_NUM
 };
 
+// runtime-tunable launch parameters (chosen by qk_autotune, looked up by size bucket)
+enum { TUNE_BF16X3_CHUNK = 0, TUNE_SPLITK_MULT, TUNE_SIGMA_CHUNKS, TUNE_SYTRD_GRID, TUNE_NUM };
+constexpr int TUNE_BUCKETS = 40;
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -32,7 +36,7 @@ struct DevBuf {
 
 enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
-  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_NUMBUF
+  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_NUMBUF
 };
 
 struct qk_ctx {
@@ -57,6 +61,7 @@ struct qk_ctx {
   bool timing = true;            // stage events (off while a graph is being captured)
   bool graph_mode = false;       // evGW cycles 2.. replayed from a CUDA graph
   bool capturing = false;        // inside stream capture: no host synchronisation allowed
+  int tune[TUNE_NUM][TUNE_BUCKETS] = {};  // 0 = not tuned (defaults apply)
   cudaGraphExec_t evgw_exec = nullptr;
   std::vector<long long> evgw_key;  // shape/pointer key of the cached evGW graph
 };
@@ -94,6 +99,9 @@ int qk_cuda_fail(qk_ctx* ctx, cudaError_t e, const char* what, const char* file,
     int _s = (expr);                  \
     if (_s != QK_OK) return _s;       \
   } while (0)
+
+// tuned value of a parameter for a problem size (bucket = floor(log2(size))), or dflt
+int qk_tune_get(const qk_ctx* ctx, int param, long long size, int dflt);
 
 // grow-only device workspace slot
 int qk_ws(qk_ctx* ctx, int slot, size_t bytes, void** out);

@@ -478,3 +478,27 @@ def test_evgw_graph_mode_matches_fixture(ctx, lin, nd):
         assert np.max(np.abs(out[0].cpu().numpy() - f[key + "_eGW"])) < E_TOL
     finally:
         ctx.set_graph_mode(False)
+
+
+# --------------------------------------------------------------------------------------------
+# autotuner: picks from its candidate sets, persists as JSON, and does not change results
+# --------------------------------------------------------------------------------------------
+def test_autotuner_roundtrip_and_parity(ctx, tmp_path):
+    f = np.load(os.path.join(GOLD, "synth_n24.npz"))
+    N, nO = int(f["N"]), int(f["nO"])
+    nS = nO * (N - nO)
+    E = synth.eri_phys_numpy(f["L"])
+    ctx.autotune(N, nS)
+    assert ctx.tune_query("bf16x3_chunk", (nS + 63) // 64 * 64) in (1, 2, 4)
+    assert ctx.tune_query("splitk_mult", nS) in (1, 2, 4)
+    assert ctx.tune_query("sytrd_grid", nS) in (2, 3, 4)
+    path = tmp_path / "tune.json"
+    ctx.tune_save(path)
+    c2 = api.Context(0)
+    c2.tune_load(path)
+    for name, size in (("bf16x3_chunk", (nS + 63) // 64 * 64), ("splitk_mult", nS),
+                       ("sytrd_grid", nS)):
+        assert c2.tune_query(name, size) == ctx.tune_query(name, size)
+    c2.close()
+    r = api.RG0W0(api.GWOptions(), N, N, 0, nO, N - nO, 0, nS, E, f["eHF"], ctx=ctx)
+    assert np.max(np.abs(r["eGW"] - f["g0w0_eGW"])) < E_TOL
