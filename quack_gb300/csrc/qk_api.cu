@@ -112,6 +112,39 @@ int rho_gemm(qk_ctx* ctx, int prec, int N, int nS, const double* S, const double
   return qk_dgemm(ctx, 'N', 'T', (int)N2, nS, nS, 1.0, S, N2, 0, XpY, nS, 0, 0.0, rho, N2, 0, 1);
 }
 
+// contractions of the factorised integrals:
+//   Lov(jb,P) = L(j,b,P);  K = Lov Lov^T = (ia|jb)  (always FP64: the Casida matrix stays exact)
+int factor_prep(qk_ctx* ctx, const Dims& d, int naux, const double* L, double** K_out,
+                double** Lov_out) {
+  const int N = d.N, nS = d.nS;
+  double *Lov, *K;
+  QK_TRY(qk_wst(ctx, W_VEC2, (size_t)nS * naux, &Lov));
+  QK_TRY(qk_wst(ctx, W_KMAT, (size_t)nS * nS, &K));
+  qk_tic(ctx, T_SLAB);
+  QK_TRY(qk_launch_gather_ov(ctx, N, d.nC, d.nO, d.nR, naux, L, Lov));
+  QK_TRY(qk_dgemm(ctx, 'N', 'T', nS, nS, naux, 1.0, Lov, nS, 0, Lov, nS, 0, 0.0, K, nS, 0, 1));
+  qk_toc(ctx, T_SLAB);
+  *K_out = K;
+  *Lov_out = Lov;
+  return QK_OK;
+}
+
+// Excitation densities through the factor (RGW_excitation_density.f90:48-50 re-associated):
+//   rho(pq,m) = sum_jb (pq|jb) XpY(m,jb) = sum_P L(pq,P) T(m,P),  T = XpY Lov  (nS x naux, FP64)
+// 2 N^2 nS naux + 2 nS^2 naux flops instead of 2 N^2 nS naux (slab) + 2 N^2 nS^2; the long
+// contraction is the precision-tier one, with the short k = naux.
+int rho_factored(qk_ctx* ctx, int prec, const Dims& d, int naux, const double* L,
+                 const double* Lov, const double* XpY, double* rho) {
+  const int N = d.N, nS = d.nS;
+  const long long N2 = (long long)N * N;
+  double* T = nullptr;
+  QK_TRY(qk_wst(ctx, W_TMAT, (size_t)nS * naux, &T));
+  QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, naux, nS, 1.0, XpY, nS, 0, Lov, nS, 0, 0.0, T, nS, 0, 1));
+  if (prec == QK_PREC_BF16X3)
+    return qk_gemm_bf16x3_nt(ctx, (int)N2, nS, naux, L, N2, T, nS, rho, N2);
+  return qk_dgemm(ctx, 'N', 'T', (int)N2, nS, naux, 1.0, L, N2, 0, T, nS, 0, 0.0, rho, N2, 0, 1);
+}
+
 // Casida with eigenvectors for the dRPA singlet screening at energies e.
 // Outputs: Om (nS), XpY (nS*nS), optional XmY, sumOm/trA (device scalars) for EcRPA.
 int casida_dev(qk_ctx* ctx, const Dims& d, const double* e, const double* ERI, double* Om,
@@ -239,10 +272,13 @@ __global__ void k_cycle_end(int* st, const double* conv, double thresh, int maxS
 struct EvBufs {
   const double* ERI;   // full-ERI path (or nullptr)
   const double* K;     // factorised path (or nullptr)
-  const double* slab;
+  const double* slab;  // full-ERI path: (pq|jb)
   const double* eHF;
   double *eGW, *eOld, *SigC, *Z, *Om, *XpY, *rho, *scal, *errv, *err_hist, *e_hist;
   int* dstate;
+  const double* L = nullptr;    // factorised path: L(pq,P) and Lov(jb,P)
+  const double* Lov = nullptr;
+  int naux = 0;
 };
 
 int evgw_cycle(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const EvBufs& b,
@@ -251,7 +287,10 @@ int evgw_cycle(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const EvBufs
   const int N = d.N, nS = d.nS;
   QK_TRY(casida_dev(ctx, d, b.eGW, b.ERI, b.Om, b.XpY, nullptr, b.scal, 1, b.K));
   qk_tic(ctx, T_RHO);
-  QK_TRY(rho_gemm(ctx, prm->precision, N, nS, b.slab, b.XpY, b.rho));
+  if (b.L)
+    QK_TRY(rho_factored(ctx, prm->precision, d, b.naux, b.L, b.Lov, b.XpY, b.rho));
+  else
+    QK_TRY(rho_gemm(ctx, prm->precision, N, nS, b.slab, b.XpY, b.rho));
   qk_toc(ctx, T_RHO);
   qk_tic(ctx, T_SIGMA);
   QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, b.eGW, b.Om,
@@ -285,7 +324,8 @@ int evgw_graph_run(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const Ev
                                 prm->doSRG, prm->max_diis, prm->maxSCF,
                                 (long long)(prm->thresh * 1e15), (long long)(prm->eta * 1e15),
                                 (long long)b.ERI, (long long)b.K, (long long)b.slab,
-                                (long long)b.eHF, (long long)b.eGW, (long long)b.dstate};
+                                (long long)b.eHF, (long long)b.eGW, (long long)b.dstate,
+                                (long long)b.L, (long long)b.naux};
   if (!ctx->evgw_exec || ctx->evgw_key != key) {
     if (ctx->evgw_exec) {
       cudaGraphExecDestroy(ctx->evgw_exec);
@@ -403,32 +443,6 @@ int evgw_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   return QK_OK;
 }
 
-// contractions of the factorised integrals (the "ERI transform" of the factorised path):
-//   Lov(jb,P) = L(j,b,P);  K = Lov Lov^T = (ia|jb);  slab = Lmat Lov^T = (pq|jb)
-int factor_prep(qk_ctx* ctx, int prec, const Dims& d, int naux, const double* L, double** K_out,
-                double** slab_out) {
-  const int N = d.N, nS = d.nS;
-  const long long N2 = (long long)N * N;
-  double *Lov, *K, *slab;
-  QK_TRY(qk_wst(ctx, W_VEC2, (size_t)nS * naux, &Lov));
-  QK_TRY(qk_wst(ctx, W_KMAT, (size_t)nS * nS, &K));
-  QK_TRY(qk_wst(ctx, W_SLAB, (size_t)N2 * nS, &slab));
-  qk_tic(ctx, T_SLAB);
-  QK_TRY(qk_launch_gather_ov(ctx, N, d.nC, d.nO, d.nR, naux, L, Lov));
-  if (prec == QK_PREC_BF16X3) {
-    QK_TRY(qk_gemm_bf16x3_nt(ctx, nS, nS, naux, Lov, nS, Lov, nS, K, nS));
-    QK_TRY(qk_gemm_bf16x3_nt(ctx, (int)N2, nS, naux, L, N2, Lov, nS, slab, N2));
-  } else {
-    QK_TRY(qk_dgemm(ctx, 'N', 'T', nS, nS, naux, 1.0, Lov, nS, 0, Lov, nS, 0, 0.0, K, nS, 0, 1));
-    QK_TRY(qk_dgemm(ctx, 'N', 'T', (int)N2, nS, naux, 1.0, L, N2, 0, Lov, nS, 0, 0.0, slab, N2, 0,
-                    1));
-  }
-  qk_toc(ctx, T_SLAB);
-  *K_out = K;
-  *slab_out = slab;
-  return QK_OK;
-}
-
 int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, const double* L,
                const double* eHF, double* eGW, double* SigC, double* Z, double* Om,
                double* hEcRPA, double* hEcGM) {
@@ -436,9 +450,9 @@ int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   const double flow = 500.0;
   const int N = d.N, nS = d.nS;
   const size_t S2 = (size_t)nS * nS, N2S = (size_t)N * N * nS;
-  double *XpY, *rho, *small, *K, *slab;
+  double *XpY, *rho, *small, *K, *Lov;
   qk_timings_clear(ctx);
-  QK_TRY(factor_prep(ctx, prm->precision, d, naux, L, &K, &slab));
+  QK_TRY(factor_prep(ctx, d, naux, L, &K, &Lov));
   QK_TRY(qk_wst(ctx, W_XPY, S2, &XpY));
   QK_TRY(qk_wst(ctx, W_RHO, N2S, &rho));
   QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)2 * N + 16, &small));
@@ -446,7 +460,7 @@ int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   double* eGWlin = small + 16;
   QK_TRY(casida_dev(ctx, d, eHF, nullptr, Om, XpY, nullptr, scal, 1, K));
   qk_tic(ctx, T_RHO);
-  QK_TRY(rho_gemm(ctx, prm->precision, N, nS, slab, XpY, rho));
+  QK_TRY(rho_factored(ctx, prm->precision, d, naux, L, Lov, XpY, rho));
   qk_toc(ctx, T_RHO);
   qk_tic(ctx, T_SIGMA);
   QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho, SigC,
@@ -476,9 +490,9 @@ int evgw_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   const int N = d.N, nS = d.nS;
   const size_t S2 = (size_t)nS * nS, N2S = (size_t)N * N * nS;
   const int maxd = prm->max_diis > 1 ? prm->max_diis : 1;
-  double *XpY, *rho, *small, *K, *slab;
+  double *XpY, *rho, *small, *K, *Lov;
   qk_timings_clear(ctx);
-  QK_TRY(factor_prep(ctx, prm->precision, d, naux, L, &K, &slab));
+  QK_TRY(factor_prep(ctx, d, naux, L, &K, &Lov));
   QK_TRY(qk_wst(ctx, W_XPY, S2, &XpY));
   QK_TRY(qk_wst(ctx, W_RHO, N2S, &rho));
   QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)(6 + 2 * maxd) * N + nS + 64 + 8, &small));
@@ -492,8 +506,11 @@ int evgw_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   QK_CK(cudaMemsetAsync(err_hist, 0, sizeof(double) * 2 * (size_t)N * maxd, ctx->stream));
   QK_CK(cudaMemcpyAsync(eGW, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   QK_CK(cudaMemcpyAsync(eOld, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  EvBufs bb{nullptr, K, slab, eHF, eGW, eOld, SigC, Z, Om, XpY, rho, scal, errv,
+  EvBufs bb{nullptr, K, nullptr, eHF, eGW, eOld, SigC, Z, Om, XpY, rho, scal, errv,
             err_hist, e_hist, dstate};
+  bb.L = L;
+  bb.Lov = Lov;
+  bb.naux = naux;
   int nSCF = 0;
   double Conv = 1.0;
   QK_TRY(evgw_loop(ctx, prm, d, bb, &nSCF, &Conv));
