@@ -154,7 +154,7 @@ __global__ void k_xpy(int nS, const double* __restrict__ w, const double* __rest
     const double om = sqrt(fabs(w[m]));
     const double z = Zt[idx];
     const double s = sq[ia];
-    XpY[idx] = (z * s) * (1.0 / sqrt(om));
+    if (XpY) XpY[idx] = (z * s) * (1.0 / sqrt(om));
     if (XmY) XmY[idx] = (z * (1.0 / s)) * sqrt(om);
     if (ia == 0) {
       Om[m] = om;
@@ -269,7 +269,45 @@ __global__ void __launch_bounds__(TB * 8) k_casida_M_K(int nS, int nv, int nC, i
   }
 }
 
+// Y(r,c) = f(d_r) X(r,c), f: 0 -> d, 1 -> 1/sqrt(|d|) ; rows x cols, column-major
+__global__ void k_rowscale2(int rows, int cols, const double* __restrict__ d, int mode,
+                            const double* __restrict__ X, long long ldx, double* __restrict__ Y,
+                            long long ldy) {
+  const long long total = (long long)rows * cols;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i % rows);
+    const long long c = i / rows;
+    const double f = mode == 0 ? d[r] : 1.0 / sqrt(sqrt(fabs(d[r])));
+    Y[r + ldy * c] = f * X[r + ldx * c];
+  }
+}
+
+__global__ void k_omega(int nS, const double* __restrict__ w, double* __restrict__ Om, int* status) {
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nS; m += gridDim.x * blockDim.x) {
+    Om[m] = sqrt(fabs(w[m]));  // phRLR.f90:76
+    if (w[m] < 0.0) atomicOr(status, QKD_NEG_OMEGA);
+  }
+}
+
 }  // namespace
+
+int qk_launch_omega(qk_ctx* ctx, int nS, const double* w, double* Om) {
+  k_omega<<<(nS + 255) / 256, 256, 0, ctx->stream>>>(nS, w, Om, ctx->d_status);
+  QK_LAUNCHED();
+  return QK_OK;
+}
+
+int qk_launch_rowscale(qk_ctx* ctx, int rows, int cols, const double* d, int mode,
+                       const double* X, long long ldx, double* Y, long long ldy) {
+  const long long total = (long long)rows * cols;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 32 * ctx->num_sms) blocks = 32 * ctx->num_sms;
+  if (blocks < 1) blocks = 1;
+  k_rowscale2<<<blocks, 256, 0, ctx->stream>>>(rows, cols, d, mode, X, ldx, Y, ldy);
+  QK_LAUNCHED();
+  return QK_OK;
+}
 
 int qk_launch_gather_ov(qk_ctx* ctx, int N, int nC, int nO, int nR, int naux, const double* L,
                         double* Lov) {

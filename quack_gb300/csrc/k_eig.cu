@@ -452,7 +452,8 @@ __global__ void k_larft(int nb, const double* __restrict__ G, const double* __re
 }  // namespace
 
 // ------------------------------------------------------------------------------------------
-int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, int want_vectors) {
+int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, int want_vectors,
+               int backtransform) {
   if (n <= 0) return QK_OK;
   const size_t N = (size_t)n;
   // workspace: V (n*n), small vectors (d, e, tau, e2, pbuf(3n), prep(8))
@@ -546,6 +547,7 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   QK_LAUNCHED();
   if (tm) qk_toc(ctx, T_STEIN);
 
+  if (!backtransform) return QK_OK;  // caller applies Q^T itself (qk_eig_apply_qt)
   // ---- 4. back-transformation Zt <- Zt * Q^T, blocks from last to first ----
   if (tm) qk_tic(ctx, T_BACKTRANS);
   const int nref = n - 2;  // reflectors 0..n-3 can be non-trivial
@@ -576,11 +578,45 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   return QK_OK;
 }
 
+// X (n x ncols, ldx) <- Q^T X with the reflectors of the last qk_eig_sym call on this context
+// (Q = H_0 H_1 ... H_{n-3}); compact-WY blocks applied first to last:
+//   X <- X - V (T^T (V^T X)) on rows kb+1..n-1.
+int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols) {
+  const int nref = n - 2;
+  if (nref <= 0 || ncols <= 0) return QK_OK;
+  const size_t N = (size_t)n;
+  double *V = nullptr, *tri = nullptr, *bt = nullptr;
+  QK_TRY(qk_wst(ctx, W_V, N * N, &V));
+  QK_TRY(qk_wst(ctx, W_TRI, 8 * N + 64, &tri));
+  double* tau = tri + 2 * N;
+  QK_TRY(qk_wst(ctx, W_PART, 2 * (size_t)ncols * BT_NB + 2 * BT_NB * BT_NB + 2 * N * BT_NB, &bt));
+  double* W1 = bt;
+  double* W2 = bt + (size_t)ncols * BT_NB;
+  double* G = W2 + (size_t)ncols * BT_NB;
+  double* T = G + BT_NB * BT_NB;
+  const int nblk = (nref + BT_NB - 1) / BT_NB;
+  for (int b = 0; b < nblk; ++b) {
+    const int kb = b * BT_NB;
+    const int nb = (nref - kb) < BT_NB ? (nref - kb) : BT_NB;
+    const int m = n - kb - 1;
+    const double* Vb = V + (kb + 1) + N * kb;
+    double* Xs = X + (kb + 1);
+    QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, nb, m, 1.0, Vb, n, 0, Vb, n, 0, 0.0, G, nb, 0, 1));
+    k_larft<<<1, 64, 0, ctx->stream>>>(nb, G, tau + kb, T);
+    QK_LAUNCHED();
+    // W1 = V^T X (nb x ncols), W2 = T^T W1, X -= V W2
+    QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, ncols, m, 1.0, Vb, n, 0, Xs, ldx, 0, 0.0, W1, nb, 0, 1));
+    QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, ncols, nb, 1.0, T, nb, 0, W1, nb, 0, 0.0, W2, nb, 0, 1));
+    QK_TRY(qk_dgemm(ctx, 'N', 'N', m, ncols, nb, -1.0, Vb, n, 0, W2, nb, 0, 1.0, Xs, ldx, 0, 1));
+  }
+  return QK_OK;
+}
+
 extern "C" int qk_dsyev_dev(qk_ctx* ctx, int n, double* d_A, int lda, double* d_w, double* d_Zt,
                             int want_vectors) {
   if (!ctx || n < 0 || lda < n) return QK_ERR_ARG;
   cudaSetDevice(ctx->device);
   QK_TRY(qk_status_reset(ctx));
-  QK_TRY(qk_eig_sym(ctx, n, d_A, lda, d_w, d_Zt, want_vectors));
+  QK_TRY(qk_eig_sym(ctx, n, d_A, lda, d_w, d_Zt, want_vectors, 1));
   return qk_status_check(ctx, QKD_BARRIER_TIMEOUT | QKD_BAD_INDEX);
 }

@@ -130,16 +130,43 @@ int factor_prep(qk_ctx* ctx, const Dims& d, int naux, const double* L, double** 
 }
 
 // Excitation densities through the factor (RGW_excitation_density.f90:48-50 re-associated):
-//   rho(pq,m) = sum_jb (pq|jb) XpY(m,jb) = sum_P L(pq,P) T(m,P),  T = XpY Lov  (nS x naux, FP64)
-// 2 N^2 nS naux + 2 nS^2 naux flops instead of 2 N^2 nS naux (slab) + 2 N^2 nS^2; the long
-// contraction is the precision-tier one, with the short k = naux.
-int rho_factored(qk_ctx* ctx, int prec, const Dims& d, int naux, const double* L,
-                 const double* Lov, const double* XpY, double* rho) {
+//   rho(pq,m) = sum_jb (pq|jb) XpY(m,jb) = sum_P L(pq,P) T(m,P),   T = XpY Lov  (nS x naux)
+// and, with XpY = D_Om^-1/2 Z_M^T D_s and Z_M = Q Z_T (Householder Q, tridiagonal vectors Z_T):
+//   T = D_Om^-1/2 Z_T^T (Q^T (D_s Lov)),
+// so the eigenvectors of M are never back-transformed: Q^T is applied to the nS x naux factor
+// (2 nS^2 naux flops instead of 2 nS^3) -- all in FP64, the same numbers in another order.
+int casida_factored(qk_ctx* ctx, const Dims& d, const double* e, const double* K, const double* Lov,
+                    int naux, double* Om, double* T, double* scal) {
+  const int nS = d.nS;
+  const size_t S2 = (size_t)nS * nS;
+  double *M = nullptr, *Zt = nullptr, *sq = nullptr, *X = nullptr;
+  QK_TRY(qk_wst(ctx, W_M, S2, &M));
+  QK_TRY(qk_wst(ctx, W_E, 2 * (size_t)nS + 64, &sq));
+  QK_TRY(qk_wst(ctx, W_ZT, S2, &Zt));
+  QK_TRY(qk_wst(ctx, W_TMAT2, (size_t)nS * naux, &X));
+  double* w = sq + nS;
+  qk_tic(ctx, T_BUILD);
+  QK_TRY(qk_launch_casida_M_K(ctx, d.N, d.nC, d.nO, d.nR, e, K, M, sq, scal + 0));
+  qk_toc(ctx, T_BUILD);
+  QK_TRY(qk_eig_sym(ctx, nS, M, nS, w, Zt, 1, 0));
+  QK_TRY(qk_launch_omega(ctx, nS, w, Om));
+  qk_tic(ctx, T_BACKTRANS);
+  QK_TRY(qk_launch_rowscale(ctx, nS, naux, sq, 0, Lov, nS, X, nS));           // D_s Lov
+  QK_TRY(qk_eig_apply_qt(ctx, nS, X, nS, naux));                             // Q^T (.)
+  QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, naux, nS, 1.0, Zt, nS, 0, X, nS, 0, 0.0, T, nS, 0, 1));
+  QK_TRY(qk_launch_rowscale(ctx, nS, naux, w, 1, T, nS, T, nS));             // D_Om^-1/2
+  qk_toc(ctx, T_BACKTRANS);
+  QK_TRY(qk_launch_sum_sqrt(ctx, nS, w, scal + 1));
+  k_ecrpa<<<1, 1, 0, ctx->stream>>>(scal + 1, scal + 0, scal + 2);
+  QK_LAUNCHED();
+  return QK_OK;
+}
+
+// rho(pq,m) = sum_P L(pq,P) T(m,P) in the precision tier
+int rho_from_T(qk_ctx* ctx, int prec, const Dims& d, int naux, const double* L, const double* T,
+               double* rho) {
   const int N = d.N, nS = d.nS;
   const long long N2 = (long long)N * N;
-  double* T = nullptr;
-  QK_TRY(qk_wst(ctx, W_TMAT, (size_t)nS * naux, &T));
-  QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, naux, nS, 1.0, XpY, nS, 0, Lov, nS, 0, 0.0, T, nS, 0, 1));
   if (prec == QK_PREC_BF16X3)
     return qk_gemm_bf16x3_nt(ctx, (int)N2, nS, naux, L, N2, T, nS, rho, N2);
   return qk_dgemm(ctx, 'N', 'T', (int)N2, nS, naux, 1.0, L, N2, 0, T, nS, 0, 0.0, rho, N2, 0, 1);
@@ -285,13 +312,19 @@ int evgw_cycle(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const EvBufs
                cudaGraphConditionalHandle h, int use_handle) {
   const double flow = 500.0;
   const int N = d.N, nS = d.nS;
-  QK_TRY(casida_dev(ctx, d, b.eGW, b.ERI, b.Om, b.XpY, nullptr, b.scal, 1, b.K));
-  qk_tic(ctx, T_RHO);
-  if (b.L)
-    QK_TRY(rho_factored(ctx, prm->precision, d, b.naux, b.L, b.Lov, b.XpY, b.rho));
-  else
+  if (b.L) {
+    double* T = nullptr;
+    QK_TRY(qk_wst(ctx, W_TMAT, (size_t)nS * b.naux, &T));
+    QK_TRY(casida_factored(ctx, d, b.eGW, b.K, b.Lov, b.naux, b.Om, T, b.scal));
+    qk_tic(ctx, T_RHO);
+    QK_TRY(rho_from_T(ctx, prm->precision, d, b.naux, b.L, T, b.rho));
+    qk_toc(ctx, T_RHO);
+  } else {
+    QK_TRY(casida_dev(ctx, d, b.eGW, b.ERI, b.Om, b.XpY, nullptr, b.scal, 1, b.K));
+    qk_tic(ctx, T_RHO);
     QK_TRY(rho_gemm(ctx, prm->precision, N, nS, b.slab, b.XpY, b.rho));
-  qk_toc(ctx, T_RHO);
+    qk_toc(ctx, T_RHO);
+  }
   qk_tic(ctx, T_SIGMA);
   QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, b.eGW, b.Om,
                        b.rho, b.SigC, b.Z, b.scal + 8));
@@ -449,18 +482,19 @@ int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
   const double flow = 500.0;
   const int N = d.N, nS = d.nS;
-  const size_t S2 = (size_t)nS * nS, N2S = (size_t)N * N * nS;
-  double *XpY, *rho, *small, *K, *Lov;
+  const size_t N2S = (size_t)N * N * nS;
+  double *rho, *small, *K, *Lov;
   qk_timings_clear(ctx);
   QK_TRY(factor_prep(ctx, d, naux, L, &K, &Lov));
-  QK_TRY(qk_wst(ctx, W_XPY, S2, &XpY));
   QK_TRY(qk_wst(ctx, W_RHO, N2S, &rho));
   QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)2 * N + 16, &small));
   double* scal = small;
   double* eGWlin = small + 16;
-  QK_TRY(casida_dev(ctx, d, eHF, nullptr, Om, XpY, nullptr, scal, 1, K));
+  double* T = nullptr;
+  QK_TRY(qk_wst(ctx, W_TMAT, (size_t)nS * naux, &T));
+  QK_TRY(casida_factored(ctx, d, eHF, K, Lov, naux, Om, T, scal));
   qk_tic(ctx, T_RHO);
-  QK_TRY(rho_factored(ctx, prm->precision, d, naux, L, Lov, XpY, rho));
+  QK_TRY(rho_from_T(ctx, prm->precision, d, naux, L, T, rho));
   qk_toc(ctx, T_RHO);
   qk_tic(ctx, T_SIGMA);
   QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho, SigC,
@@ -488,12 +522,11 @@ int evgw_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
   const double flow = 500.0;
   const int N = d.N, nS = d.nS;
-  const size_t S2 = (size_t)nS * nS, N2S = (size_t)N * N * nS;
+  const size_t N2S = (size_t)N * N * nS;
   const int maxd = prm->max_diis > 1 ? prm->max_diis : 1;
-  double *XpY, *rho, *small, *K, *Lov;
+  double *rho, *small, *K, *Lov;
   qk_timings_clear(ctx);
   QK_TRY(factor_prep(ctx, d, naux, L, &K, &Lov));
-  QK_TRY(qk_wst(ctx, W_XPY, S2, &XpY));
   QK_TRY(qk_wst(ctx, W_RHO, N2S, &rho));
   QK_TRY(qk_wst(ctx, W_HOST_B, (size_t)(6 + 2 * maxd) * N + nS + 64 + 8, &small));
   double* scal = small;
@@ -506,7 +539,7 @@ int evgw_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   QK_CK(cudaMemsetAsync(err_hist, 0, sizeof(double) * 2 * (size_t)N * maxd, ctx->stream));
   QK_CK(cudaMemcpyAsync(eGW, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   QK_CK(cudaMemcpyAsync(eOld, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  EvBufs bb{nullptr, K, nullptr, eHF, eGW, eOld, SigC, Z, Om, XpY, rho, scal, errv,
+  EvBufs bb{nullptr, K, nullptr, eHF, eGW, eOld, SigC, Z, Om, nullptr, rho, scal, errv,
             err_hist, e_hist, dstate};
   bb.L = L;
   bb.Lov = Lov;

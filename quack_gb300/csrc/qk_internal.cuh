@@ -36,7 +36,7 @@ struct DevBuf {
 
 enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
-  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_NUMBUF
+  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_TMAT2, W_NUMBUF
 };
 
 struct qk_ctx {
@@ -128,7 +128,9 @@ int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, c
              double beta, double* C, long long ldc, long long strideC, int batch);
 
 // dense symmetric eigensolver pieces
-int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, int want_vectors);
+int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, int want_vectors,
+               int backtransform = 1);
+int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols);
 
 // Casida pieces (k_casida.cu)
 int qk_launch_build_AB(qk_ctx* ctx, int which, int ispin, int dRPA, int N, int nC, int nO, int nR,
@@ -140,6 +142,9 @@ int qk_launch_casida_M_from_AB(qk_ctx* ctx, int nS, const double* A, const doubl
 int qk_launch_xpy(qk_ctx* ctx, int nS, const double* w, const double* Zt, const double* sq,
                   double* Om, double* XpY, double* XmY, int want_xmy);
 int qk_launch_sum_sqrt(qk_ctx* ctx, int nS, const double* w, double* out);
+int qk_launch_omega(qk_ctx* ctx, int nS, const double* w, double* Om);
+int qk_launch_rowscale(qk_ctx* ctx, int rows, int cols, const double* d, int mode,
+                       const double* X, long long ldx, double* Y, long long ldy);
 int qk_launch_gather_ov(qk_ctx* ctx, int N, int nC, int nO, int nR, int naux, const double* L,
                         double* Lov);
 int qk_launch_casida_M_K(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e,
