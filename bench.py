@@ -42,6 +42,29 @@ def load_peaks():
         return 6800.0, 1900.0, "fallback"
 
 
+def load_traffic():
+    """DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the stages'
+    dominant kernels, from the ncu summaries in profiles/ (lines 'traffic <stage> <bytes>')."""
+    out = {}
+    pdir = os.path.join(ROOT, "profiles")
+    try:
+        names = sorted(os.listdir(pdir))
+    except OSError:
+        return out
+    for fn in names:
+        if not fn.endswith(".md"):
+            continue
+        with open(os.path.join(pdir, fn)) as f:
+            for ln in f:
+                t = ln.strip().strip("`").split()
+                if len(t) == 3 and t[0] == "traffic":
+                    try:
+                        out[t[1]] = int(float(t[2]))
+                    except ValueError:
+                        pass
+    return out
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -262,12 +285,7 @@ def run_ours(args):
         stages.append({"kernel": name, "ms": t, "bound": bound, "achieved": ach, "peak": peak,
                        "unit": unit, "frac": ach / peak, "peak_source": pk, "work": desc})
     stages.sort(key=lambda d: -d["ms"])
-    traffic = {}
-    try:
-        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
-            traffic = json.load(f)
-    except Exception:
-        pass
+    traffic = load_traffic()
     top = dict(stages[0]) if stages else None
     if top is not None:
         top["traffic"] = traffic.get(top["kernel"])
@@ -283,7 +301,7 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f64 (BF16x3 tcgen05 contractions)", "data": "synthetic",
         "config": dict(WORKLOAD, tier="bf16x3", parallelism="replicas" if ws > 1 else "single"),
         "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": top,
-        "roofline_tensor_kernel": rho_stage, "stages": stages,
+        "roofline_tensor_kernel": rho_stage, "stages": stages, "stage_ms": st_mix,
         "plain_fp64": {"value": plain, "unit": "systems/s", "ms_per_step": ms_fp / Kp,
                        "steps": Kp, "stages": st_fp},
         "speedup_mixed_vs_plain": value / plain,

@@ -39,10 +39,15 @@ enum {
   QK_ERR_NO_DEVICE = 8     /* no CUDA device / library not built for this GPU */
 };
 
-/* precision tiers for the O(N^2 nS^2) contractions (excitation density, ERI slabs) */
+/* precision tiers */
 enum {
   QK_PREC_FP64 = 0,        /* FP64 throughout (plain form) */
-  QK_PREC_BF16X3 = 1       /* BF16x3 split products on tcgen05, FP32 accumulation */
+  QK_PREC_BF16X3 = 1       /* mixed: the excitation-density contraction as BF16x3 split products
+                              on tcgen05 (FP32 accumulation, compensated); with eta = 0 and no SRG
+                              the pole sums of Sigma/dSigma (linearised stage and Newton) take the
+                              terms with |w - e +- Om| >= 0.1 Ha in FP32 and the near-pole terms in
+                              FP64.  The Casida build and eigensolve, the Newton update and DIIS
+                              stay FP64. */
 };
 
 /* Options of the GW line of QuAcK's input/options (QuAcK/read_options.f90:242-267). */
@@ -82,6 +87,10 @@ int qk_trim(qk_ctx* ctx);
  * convergence or maxSCF, with the Newton search unrolled to its 64-step bound (finished orbitals
  * drop out on the device).  Results are the same; mode 1 removes the per-cycle host round trips. */
 int qk_set_graph_mode(qk_ctx* ctx, int on);
+/* Tier of the stage-level drop-ins below (qk_RGW_excitation_density, qk_RGW_self_energy_diag,
+ * qk_RGW_QP_graph), which have the Fortran argument lists and so no precision argument:
+ * QK_PREC_FP64 (default) or QK_PREC_BF16X3. */
+int qk_set_stage_precision(qk_ctx* ctx, int precision);
 
 /* ---- stage-level drop-ins (host pointers) ------------------------------------------------- */
 /* LR/phRLR_A.f90:1-138 */
@@ -151,8 +160,10 @@ int qk_evRGW_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int nOrb, int nC, int n
                    double* d_Z, double* EcRPA, double* EcGM, int* nSCF, double* Conv);
 
 /* ---- learned quasiparticle guess ----------------------------------------------------------
- * No counterpart in the reference.  A 16 -> 64 -> 64 -> 1 SiLU perceptron predicts the QP shift
- * eGW_p - eHF_p from 16 per-orbital features of the linearised G0W0 stage; it is trained on the
+ * No counterpart in the reference.  A 16 -> 64 -> 64 -> 1 SiLU perceptron predicts the nonlinear
+ * part eGW_p - eGWlin_p of the QP shift from 16 per-orbital features of the linearised G0W0 stage
+ * (energies, Sigma, Z, and one pole sweep at eGWlin: the Newton and Halley steps from there and
+ * the nearest pole); the Newton search then starts at eGWlin_p + prediction.  It is trained on the
  * GPU (FP32, Adam) by this library's own kernels and evaluated in BF16.  Parameters are one flat
  * float vector of QK_MLP_NPARAM entries: W1 (64x16, row-major), b1, W2 (64x64), b2, W3 (1x64), b3.
  * Inputs/targets of train/grad/predict are already normalised; qk_mlp_set_scaling records the
@@ -195,7 +206,9 @@ int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int method, int nsys
                       double* d_eGW, double* EcRPA, int* status, int* nSCF, int n_workers);
 
 /* ---- dense symmetric eigensolver (device pointers; replaces dsyev('V','U') of
- *      utils/wrap_lapack.f90:99-136 on the GPU).  A (n x n, lda) is destroyed; w ascending;
+ *      utils/wrap_lapack.f90:99-136 on the GPU).  A (n x n, lda) is symmetric and only its
+ *      lower triangle is referenced (dsyev('V','U') reads the upper one: the same numbers for
+ *      a symmetric matrix); A is destroyed; w ascending;
  *      if want_vectors, Zt receives the eigenvectors as ROWS: Zt[j + n*i] = component i of
  *      eigenvector j. ------------------------------------------------------------------------ */
 int qk_dsyev_dev(qk_ctx* ctx, int n, double* d_A, int lda, double* d_w, double* d_Zt,

@@ -122,6 +122,10 @@ class Context:
         """evGW cycles 2.. replayed from one CUDA graph with a device-side WHILE loop."""
         self.check(lib().qk_set_graph_mode(self._h, int(bool(on))))
 
+    def set_stage_precision(self, precision):
+        """Tier of the stage-level drop-ins (excitation density, self-energy, QP graph)."""
+        self.check(lib().qk_set_stage_precision(self._h, int(precision)))
+
     def set_feature_capture(self, on=True):
         self.check(lib().qk_set_feature_capture(self._h, int(bool(on))))
 

@@ -4,7 +4,8 @@
 // Pipeline (all on the GPU, no vendor solver):
 //   1. k_sytrd: Householder tridiagonalisation (lower variant) in ONE persistent cooperative
 //      kernel.  Each iteration fuses the rank-2 update of step k with the symmetric mat-vec of
-//      step k+1, so the trailing matrix is streamed once per column (read+write); every CTA
+//      step k+1 on the lower triangle only, so the trailing triangle is streamed once per column
+//      (read+write) and every element costs 4 FMAs (LAPACK's 4/3 n^3 flops); every CTA
 //      recomputes the O(n) vector work redundantly (bitwise identical in all CTAs), leaving
 //      one bounded grid barrier per column.
 //   2. k_stebz: Sturm-count bisection, one thread per eigenvalue, full FP64 precision.
@@ -22,10 +23,37 @@
 namespace {
 
 constexpr int TRI_THREADS = 1024;
-constexpr int TRI_SMEM_MAX = 200 * 1024;  // vectors kept in shared memory up to n = 8533
-constexpr int TRI_SMAX = 64;        // max column segments per row chunk
+constexpr int TRI_SMEM_MAX = 227 * 1024 - 1024;  // tiles + (when they fit) the three vectors
+constexpr int TRI_TC = 16;          // columns per lower-triangle tile of the fused pass
+constexpr int TRI_TLD = 33;         // padded leading dimension of a warp's shared tile
+constexpr int TRI_TILE_BYTES = (TRI_THREADS / 32) * TRI_TC * TRI_TLD * 8;
 constexpr int BT_NB = 64;           // reflectors per compact-WY block
 constexpr double CLUSTER_REL = 1e-7;  // eigenvalues closer than this * ||T||_1 share a cluster
+
+// Sum over the CTA with few FP64 operations (the FP64 pipe is the scarce resource here): the
+// per-thread partials go to shared memory and warp 0 adds them with four independent chains per
+// lane, then one butterfly.  scratch holds blockDim.x doubles.  Result returned to every thread.
+__device__ __forceinline__ double tri_block_sum(double v, double* scratch, double* out) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  scratch[tid] = v;
+  __syncthreads();
+  if (tid < 32) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int i = tid;
+    for (; i + 96 < nt; i += 128) {
+      a0 += scratch[i];
+      a1 += scratch[i + 32];
+      a2 += scratch[i + 64];
+      a3 += scratch[i + 96];
+    }
+    for (; i < nt; i += 32) a0 += scratch[i];
+    double t = (a0 + a1) + (a2 + a3);
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (tid == 0) *out = t;
+  }
+  __syncthreads();
+  return *out;
+}
 
 struct TriArgs {
   double* A;
@@ -47,11 +75,12 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
   extern __shared__ double sm[];
   __shared__ double red[32];
   const int n = a.n;
+  double* ytile = sm;  // one TRI_TC x TRI_TLD tile per warp
   double *vk, *wk, *vk1;
   if (a.use_smem) {
-    vk = sm;
-    wk = sm + n;
-    vk1 = sm + 2 * n;
+    vk = sm + TRI_TILE_BYTES / 8;
+    wk = vk + n;
+    vk1 = vk + 2 * n;
   } else {
     double* base = a.gvec + (size_t)blockIdx.x * 3 * n;
     vk = base;
@@ -80,7 +109,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
         wk[i] = pi;
         dot += pi * vk[i];
       }
-      dot = qk_block_sum(dot, red);
+      dot = tri_block_sum(dot, ytile, red);
       const double c = 0.5 * tau_k * tau_k * dot;
       for (int i = k + 1 + tid; i < n; i += nt) wk[i] = tau_k * wk[i] - c * vk[i];
       __syncthreads();
@@ -100,7 +129,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       if (j <= n - 2) {
         double ss = 0.0;
         for (int i = j + 2 + tid; i < n; i += nt) ss += vk1[i] * vk1[i];
-        const double sigma = qk_block_sum(ss, red);
+        const double sigma = tri_block_sum(ss, ytile, red);
         const double alpha = vk1[j + 1];
         double beta, scal;
         if (sigma == 0.0) {
@@ -124,62 +153,88 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       if (blockIdx.x == 0 && tid == 0) a.d[j] = dj;
     }
     __syncthreads();
-    // ---- big pass: rank-2 update of step k fused with p_{k+1} = A' v_{k+1} ----
+    // ---- big pass: rank-2 update of step k fused with p_{k+1} = A' v_{k+1}, lower triangle ----
+    // The trailing lower triangle is cut into tiles of 32 rows x TRI_TC columns (row block bi
+    // holds tiles t = 0..2bi+1; tiles are numbered row block after row block).  Each warp takes a
+    // contiguous range of tiles.  Lane = row i: it updates A(i,c) for c <= i, accumulates the row
+    // part of p_i, and parks the strictly lower y(i,c) in its warp's shared tile; the lanes then
+    // read the tile by columns for the transposed part of p_c.  Every element costs the two FMAs
+    // of the update and one FMA for each of its two appearances in the symmetric mat-vec.
     const int r0 = k + 2;
     const int mm = n - r0;
     if (mm > 0) {
-      const int nchunks = (mm + 31) >> 5;
-      int S = totwarps / nchunks;
-      S = S < 1 ? 1 : (S > TRI_SMAX ? TRI_SMAX : S);
-      const int smax2 = (mm + 7) / 8;
-      if (S > smax2) S = smax2;
-      const int L = (mm + S - 1) / S;
       double* pnext = a.pbuf + (size_t)((k + 1) % 3) * n;
       const bool upd = (k >= 0);
       const bool wantp = (j <= n - 2);
-      const int items = nchunks * S;
-      for (int item = gwarp; item < items; item += totwarps) {
-        const int c = item / S, sgi = item - c * S;
-        const int i = r0 + c * 32 + lane;
-        const int cb = r0 + sgi * L;
-        const int ce = min(n, cb + L);
-        if (i < n && cb < ce) {
-          const double vi = upd ? vk[i] : 0.0, wi = upd ? wk[i] : 0.0;
-          double* col = a.A + i;
-          double acc = 0.0;
-          // loads are issued in batches of 8 ahead of the dependent stores so that the compiler
-          // does not serialise them (it cannot prove lda != 0)
-          int cc = cb;
-          if (upd) {
-            for (; cc + 8 <= ce; cc += 8) {
-              double x[8];
-#pragma unroll
-              for (int u = 0; u < 8; ++u) x[u] = __ldcg(col + a.lda * (cc + u));
-#pragma unroll
-              for (int u = 0; u < 8; ++u) {
-                const double y = x[u] - vi * wk[cc + u] - wi * vk[cc + u];
-                __stcg(col + a.lda * (cc + u), y);
-                acc += y * vk1[cc + u];
-              }
-            }
-            for (; cc < ce; ++cc) {
-              double* ptr = col + a.lda * cc;
-              const double y = __ldcg(ptr) - vi * wk[cc] - wi * vk[cc];
-              __stcg(ptr, y);
-              acc += y * vk1[cc];
-            }
-          } else {
-            for (; cc + 8 <= ce; cc += 8) {
-              double x[8];
-#pragma unroll
-              for (int u = 0; u < 8; ++u) x[u] = __ldcg(col + a.lda * (cc + u));
-#pragma unroll
-              for (int u = 0; u < 8; ++u) acc += x[u] * vk1[cc + u];
-            }
-            for (; cc < ce; ++cc) acc += __ldcg(col + a.lda * cc) * vk1[cc];
+      const int nb = (mm + 31) >> 5;
+      const int items = nb * (nb + 1);  // < 2^31 for every n this kernel can hold
+      const int per = (items + totwarps - 1) / totwarps;
+      const int it0 = gwarp * per;
+      const int it1 = it0 + per < items ? it0 + per : items;
+      double* tile = ytile + (size_t)warp * (TRI_TC * TRI_TLD);
+      if (it0 < it1) {
+        int bi = (int)((sqrtf(4.0f * (float)it0 + 1.0f) - 1.0f) * 0.5f);
+        while (bi > 0 && bi * (bi + 1) > it0) --bi;
+        while ((bi + 1) * (bi + 2) <= it0) ++bi;
+        int off = bi * (bi + 1);
+        int cur = -1;
+        int i = 0;
+        bool rowok = false;
+        double vi = 0.0, wi = 0.0, rowacc = 0.0;
+        for (int it = it0; it < it1; ++it) {
+          while (it >= off + 2 * bi + 2) {
+            off += 2 * bi + 2;
+            ++bi;
           }
-          if (wantp) atomicAdd(pnext + i, acc);
+          if (bi != cur) {
+            if (cur >= 0 && wantp && rowok) atomicAdd(pnext + i, rowacc);
+            cur = bi;
+            i = r0 + 32 * bi + lane;
+            rowok = i < n;
+            vi = (upd && rowok) ? vk[i] : 0.0;
+            wi = (upd && rowok) ? wk[i] : 0.0;
+            rowacc = 0.0;
+          }
+          const int c0 = r0 + TRI_TC * (it - off);
+          double* col = a.A + i;
+#pragma unroll 1
+          for (int h = 0; h < TRI_TC; h += 8) {
+            // loads first, in a batch, ahead of the dependent stores
+            double x[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int c = c0 + h + u;
+              x[u] = (rowok && c <= i) ? __ldcg(col + a.lda * c) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int c = c0 + h + u;
+              const bool ok = rowok && c <= i;
+              double y = 0.0;
+              if (ok) {
+                y = upd ? x[u] - vi * wk[c] - wi * vk[c] : x[u];
+                __stcg(col + a.lda * c, y);
+                rowacc += y * vk1[c];
+              }
+              tile[(h + u) * TRI_TLD + lane] = (ok && c < i) ? y : 0.0;
+            }
+          }
+          __syncwarp();
+          if (wantp) {
+            // transposed part: lanes 0-15 sum rows 0-15 and lanes 16-31 rows 16-31 of column u
+            const int u = lane & (TRI_TC - 1), hh = lane >> 4;
+            const int rb = r0 + 32 * bi + 16 * hh;
+            const double* tp = tile + u * TRI_TLD + 16 * hh;
+            double cs = 0.0;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) cs += tp[r] * (rb + r < n ? vk1[rb + r] : 0.0);
+            cs += __shfl_xor_sync(0xffffffffu, cs, 16);
+            const int c = c0 + u;
+            if (hh == 0 && c < n && c <= r0 + 32 * bi + 31) atomicAdd(pnext + c, cs);
+          }
+          __syncwarp();
         }
+        if (wantp && rowok) atomicAdd(pnext + i, rowacc);
       }
     }
     if (!qk_grid_barrier(a.bar, gridDim.x, epoch, a.status)) return;
@@ -474,9 +529,9 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   const bool tm = ctx->time_eig;
   if (tm) qk_tic(ctx, T_TRIDIAG);
   {
-    const size_t smem_need = 3 * N * sizeof(double);
+    const size_t smem_need = TRI_TILE_BYTES + 3 * N * sizeof(double);
     const int use_smem = smem_need <= (size_t)TRI_SMEM_MAX;
-    const size_t smem = use_smem ? smem_need : 0;
+    const size_t smem = use_smem ? smem_need : (size_t)TRI_TILE_BYTES;
     // the attribute is global to the kernel: set it once, at its maximum, so that concurrent
     // callers on other streams/threads never see a smaller limit than their launch needs
     static std::once_flag once;

@@ -185,11 +185,21 @@ __global__ void k_normalise(int n, const float* __restrict__ F, const float* __r
 }
 
 // w0 = e + (y * ystd + ymean)
+// The network predicts the nonlinear correction y = eGW - eGWlin.  The Halley step h of the QP
+// equation from eGWlin (FP64, from the feature sweep) is exact to far below the network's
+// resolution where the search is regular; where the two agree to QK_GUESS_AGREE the search starts
+// at eGWlin + h, elsewhere it starts at the reference start and follows the reference trajectory.
+constexpr double QK_GUESS_AGREE = 3e-3;  // Ha
 __global__ void k_guess(int n, const float* __restrict__ Y, float ymean, float ystd,
-                        const double* __restrict__ e, double* __restrict__ w0) {
+                        const double* __restrict__ base, const double* __restrict__ hal,
+                        double* __restrict__ w0, int* __restrict__ fromref) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  w0[i] = e[i] + (double)(Y[i] * ystd + ymean);
+  const double y = (double)(Y[i] * ystd + ymean);
+  const double h = hal[i];
+  const bool agree = (h == h) && fabs(y - h) <= QK_GUESS_AGREE;
+  w0[i] = agree ? base[i] + h : base[i];
+  fromref[i] = agree ? 0 : 1;
 }
 
 }  // namespace
@@ -218,7 +228,8 @@ static int mlp_work(qk_ctx* ctx, qk_mlp* m, int B) {
   return QK_OK;
 }
 
-int qk_guess_from_model(qk_ctx* ctx, int N, const float* F, const double* e, double* w0) {
+int qk_guess_from_model(qk_ctx* ctx, int N, const float* F, const double* base, const double* hal,
+                        double* w0, int* fromref) {
   qk_mlp* m = ctx->mlp;
   if (!m) return qk_fail(ctx, QK_ERR_ARG, "qp_guess requested but no model attached");
   float* buf = nullptr;
@@ -232,7 +243,8 @@ int qk_guess_from_model(qk_ctx* ctx, int N, const float* F, const double* e, dou
   QK_LAUNCHED();
   k_mlp_infer_bf16<<<(N + 127) / 128, 128, 0, ctx->stream>>>(N, X, m->P, Y);
   QK_LAUNCHED();
-  k_guess<<<(N + 127) / 128, 128, 0, ctx->stream>>>(N, Y, m->ymean, m->ystd, e, w0);
+  k_guess<<<(N + 127) / 128, 128, 0, ctx->stream>>>(N, Y, m->ymean, m->ystd, base, hal, w0,
+                                                   fromref);
   QK_LAUNCHED();
   return QK_OK;
 }

@@ -159,6 +159,156 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial(SigArgs a) {
   }
 }
 
+// Mixed-tier sweep (eta = 0, no SRG).  Same CTA layout and outputs as k_sigma_partial (lanes =
+// orbitals p, CTAs over (p tile, m chunk)), but the 8 warps split the q index and each warp runs
+// over the whole m chunk, so that the per-(p,q) setup is done once: c = w - e_q in FP64 and its
+// float pair (c_hi, c_lo), and the window [lo, hi) of the m with |w - e_q +- Om_m| < tau (Om
+// ascending: two bisections).  Outside the window, eps = (c_hi +- Om_hi) + (c_lo +- Om_lo) is
+// accurate to a few FP32 ulps and the term R/eps with R = 2 rho^2 (FP32) runs on the FP32 pipe;
+// the per-(p,q) FP32 partials are added into float-float (TwoSum) accumulators.  Inside the
+// window the term is evaluated exactly as in k_sigma_partial (FP64).  All lanes step through the
+// same m (the window only masks the reciprocal), so the R loads stay coalesced.
+__device__ __forceinline__ float rcp32(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// first m in [lo, hi) with OmF[m].x >= v (OmF ascending)
+__device__ __forceinline__ int om_lower_bound(const float2* __restrict__ O, int lo, int hi, float v) {
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(&O[mid].x) < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// (hi, lo) += x, error-free (Knuth's TwoSum) up to the final rounding of lo
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float x) {
+  const float t = hi + x;
+  const float z = t - hi;
+  lo += (hi - (t - z)) + (x - z);
+  hi = t;
+}
+
+struct SigFF {
+  const float* R;
+  const float2* OmF;
+  const int* bad;
+  float tau;
+};
+
+__global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial_ff(SigArgs a, SigFF f) {
+  extern __shared__ double se[];
+  __shared__ double ssig[SIG_WARPS][32], sds[SIG_WARPS][32], socc[SIG_WARPS][32];
+  const int nl = a.nact ? *a.nact : 0;
+  if (a.list && (int)blockIdx.x * 32 >= nl) return;
+  const int N = a.N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) se[i] = a.eq[i];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int pend = N - a.nR;
+  int p;
+  bool pok;
+  if (a.list) {
+    const int idx = blockIdx.x * 32 + lane;
+    pok = idx < nl;
+    p = pok ? a.list[idx] : pend;
+  } else {
+    p = a.nC + blockIdx.x * 32 + lane;
+    pok = p < pend;
+  }
+  __syncthreads();
+  double sig = 0.0, ds = 0.0, so = 0.0;
+  if (pok) {
+    const double w = a.wp ? a.wp[p] : se[p];
+    const long long N1 = N, N2 = N1 * N1;
+    const int m0 = blockIdx.y * a.mper;
+    const int m1 = min(a.nS, m0 + a.mper);
+    const bool bad = *f.bad != 0;
+    const float* Rp = f.R + p;
+    const double* rp = a.rho + p;
+    float so_h = 0.f, so_l = 0.f, sv_h = 0.f, sv_l = 0.f, d_h = 0.f, d_l = 0.f;
+    double Sn_o = 0.0, Sn_v = 0.0, Dn = 0.0;  // near-pole (FP64) parts
+    for (int q = a.nC + warp; q < pend; q += SIG_WARPS) {
+      const bool occ = q < a.nO;
+      const double c = w - se[q];
+      const float chi = (float)c;
+      const float clo = (float)(c - (double)chi);
+      const float sg = occ ? 1.f : -1.f;
+      int lo = m0, hi = m1;
+      if (!bad) {
+        const float ctr = -sg * chi;  // the pole sits at Om = -c (occupied) or Om = c (virtual)
+        lo = om_lower_bound(f.OmF, m0, m1, ctr - f.tau);
+        hi = om_lower_bound(f.OmF, lo, m1, ctr + f.tau);
+      }
+      const float* Rq = Rp + N1 * q;
+      float s = 0.f, d = 0.f;
+#pragma unroll 4
+      for (int m = m0; m < m1; ++m) {
+        const float2 o = __ldg(f.OmF + m);
+        const float e = fmaf(sg, o.x, chi) + fmaf(sg, o.y, clo);
+        float r = rcp32(e);
+        r = (m >= lo && m < hi) ? 0.f : r;
+        const float t = __ldg(Rq + N2 * m) * r;
+        s += t;
+        d = fmaf(t, r, d);
+      }
+      if (occ) ff_add(so_h, so_l, s);
+      else ff_add(sv_h, sv_l, s);
+      ff_add(d_h, d_l, d);
+      // the window, in FP64 (RGW_Re_SigC.f90:30-50 / RGW_Re_dSigC.f90:30-50 with eta = 0)
+      for (int m = lo; m < hi; ++m) {
+        const double om = __ldg(a.Om + m);
+        const double x = __ldg(rp + N1 * q + N2 * m);
+        const double ir = rcp_nr(occ ? (w - se[q] + om) : (w - se[q] - om));
+        const double t = (2.0 * (x * x)) * ir;
+        if (occ) Sn_o += t;
+        else Sn_v += t;
+        Dn = fma(t, ir, Dn);
+      }
+    }
+    so = ((double)so_h + (double)so_l) + Sn_o;
+    sig = ((double)sv_h + (double)sv_l) + Sn_v + so;
+    ds = -(((double)d_h + (double)d_l) + Dn);
+  }
+  ssig[warp][lane] = sig;
+  sds[warp][lane] = ds;
+  socc[warp][lane] = so;
+  __syncthreads();
+  if (warp == 0 && p < pend) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int w = 0; w < SIG_WARPS; ++w) {
+      s0 += ssig[w][lane];
+      s1 += sds[w][lane];
+      s2 += socc[w][lane];
+    }
+    const size_t o = (size_t)blockIdx.y * N + p;
+    const size_t stride = (size_t)a.nchunks * N;
+    a.part[o] = s0;
+    a.part[o + stride] = s1;
+    a.part[o + 2 * stride] = s2;
+  }
+}
+
+// R = 2 rho^2 in FP32; Om split into float pairs; flag Om that is not ascending (or NaN)
+__global__ void k_sigma_ff_prep(long long n, const double* __restrict__ rho, float* __restrict__ R,
+                                int nS, const double* __restrict__ Om, float2* __restrict__ OmF,
+                                int* __restrict__ bad) {
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long nth = (long long)gridDim.x * blockDim.x;
+  for (long long i = tid; i < n; i += nth) {
+    const double x = rho[i];
+    R[i] = (float)(2.0 * (x * x));
+  }
+  for (long long m = tid; m < nS; m += nth) {
+    const double om = Om[m];
+    const float hi = (float)om;
+    OmF[m] = make_float2(hi, (float)(om - (double)hi));
+    if (!(om >= 0.0) || (m + 1 < nS && !(Om[m + 1] >= om))) atomicOr(bad, 1);
+  }
+}
+
 // diag mode: Sig, Z = 1/(1 - dSig), EcGM
 __global__ void k_sigma_final(int N, int nC, int nO, int nR, int nchunks,
                               const double* __restrict__ part, double* __restrict__ Sig,
@@ -193,6 +343,7 @@ struct QPState {
   int* list;   // compacted active orbitals, ascending
   int* conv;   // 1 if the last evaluation met |f| <= thresh
   int* evals;  // Sigma evaluations per orbital, all phases
+  const int* fromref;  // learned-guess mode: 1 where the search started at the reference start
 };
 
 // rebuild the compacted active list (one block; warp 0 walks the orbitals 32 at a time)
@@ -225,10 +376,15 @@ __global__ void k_qp_init(int N, int nC, int nR, const double* __restrict__ w0, 
 
 // Orbitals whose guess-started search did not converge, or converged outside the trust region
 // |w - eGWlin| <= |eGWlin - eHF| + 0.02 Ha around the reference start, restart from the
-// reference start (the root must stay the one the linearised solution points at).
+// reference start (the root must stay the one the linearised solution points at).  Orbitals that
+// started at the reference start are already on the reference trajectory and just continue.
 __global__ void k_qp_restart(int N, int nC, int nR, const double* __restrict__ eGWlin,
                              const double* __restrict__ eHF, QPState s) {
   for (int p = threadIdx.x; p < N; p += blockDim.x) {
+    if (s.fromref && s.fromref[p]) {
+      s.active[p] = (p >= nC && p < N - nR) && !s.conv[p] && s.nit[p] < QP_MAXIT;
+      continue;
+    }
     const double trust = fabs(eGWlin[p] - eHF[p]) + 0.02;
     const double wnew = s.w[p];
     const bool keep = s.conv[p] && fabs(wnew - eGWlin[p]) <= trust;
@@ -400,7 +556,7 @@ __global__ void k_diis(int n_err, int n_e, int nd_host, double* __restrict__ err
 static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                        int nS, const double* eq, const double* wp, const double* Om,
                        const double* rho, const int* list, const int* nact, double** part_out,
-                       int* nchunks_out) {
+                       int* nchunks_out, const qk_sigma_ff* ff = nullptr) {
   const int nact_p = N - nR - nC;
   const int ptiles = (nact_p + 31) / 32;
   const int cm = qk_tune_get(ctx, TUNE_SIGMA_CHUNKS, (long long)nS, 4);
@@ -419,7 +575,13 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
   a.doSRG = doSRG; a.eta = eta; a.flow = flow;
   a.eq = eq; a.wp = wp; a.Om = Om; a.rho = rho; a.list = list; a.nact = nact; a.part = part;
   if (ptiles > 0 && nS > 0) {
-    k_sigma_partial<<<dim3(ptiles, nchunks), SIG_WARPS * 32, N * sizeof(double), ctx->stream>>>(a);
+    if (ff && !doSRG && eta == 0.0) {
+      SigFF f{ff->R, ff->OmF, ff->bad, ff->tau};
+      k_sigma_partial_ff<<<dim3(ptiles, nchunks), SIG_WARPS * 32, N * sizeof(double), ctx->stream>>>(
+          a, f);
+    } else {
+      k_sigma_partial<<<dim3(ptiles, nchunks), SIG_WARPS * 32, N * sizeof(double), ctx->stream>>>(a);
+    }
     QK_LAUNCHED();
   }
   *part_out = part;
@@ -427,13 +589,35 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
   return QK_OK;
 }
 
+int qk_sigma_ff_prep(qk_ctx* ctx, int N, int nS, const double* rho, const double* Om,
+                     qk_sigma_ff* ff) {
+  const long long n = (long long)N * N * nS;
+  float *R = nullptr, *of = nullptr;
+  QK_TRY(qk_wst(ctx, W_RHO32, (size_t)n + 32, &R));
+  QK_TRY(qk_wst(ctx, W_OMF, 2 * (size_t)nS + 16, &of));
+  float2* OmF = (float2*)of;
+  int* bad = (int*)(of + 2 * (size_t)nS);
+  QK_CK(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+  long long blocks = (n + 255) / 256;
+  const long long cap = 16LL * ctx->num_sms;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  k_sigma_ff_prep<<<(int)blocks, 256, 0, ctx->stream>>>(n, rho, R, nS, Om, OmF, bad);
+  QK_LAUNCHED();
+  ff->R = R;
+  ff->OmF = OmF;
+  ff->bad = bad;
+  ff->tau = 0.1f;
+  return QK_OK;
+}
+
 int qk_sigma_diag(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                   int nS, const double* e, const double* Om, const double* rho, double* Sig,
-                  double* Z, double* EcGM) {
+                  double* Z, double* EcGM, const qk_sigma_ff* ff) {
   double* part;
   int nch;
   QK_TRY(sigma_sweep(ctx, doSRG, eta, flow, N, nC, nO, nR, nS, e, nullptr, Om, rho, nullptr,
-                     nullptr, &part, &nch));
+                     nullptr, &part, &nch, ff));
   k_sigma_final<<<1, 1024, 0, ctx->stream>>>(N, nC, nO, nR, nch, part, Sig, Z, EcGM);
   QK_LAUNCHED();
   return QK_OK;
@@ -442,7 +626,8 @@ int qk_sigma_diag(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC
 int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                  int nS, const double* eHF, const double* Om, const double* rho,
                  const double* eGWlin, const double* eOld, double* eGW, double* Z,
-                 const double* w_guess, int guess_maxit) {
+                 const double* w_guess, int guess_maxit, const qk_sigma_ff* ff,
+                 const int* guess_fromref) {
   double* st = nullptr;
   QK_TRY(qk_wst(ctx, W_M2, (size_t)8 * N + 64, &st));
   QPState s;
@@ -454,6 +639,7 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
   s.conv = (int*)(st + 5 * N);
   s.evals = (int*)(st + 6 * N);
   s.nact = (int*)(st + 7 * N);
+  s.fromref = w_guess ? guess_fromref : nullptr;
   // phase 1 (learned guess only): at most guess_maxit steps from the guess; phase 2: the
   // reference search (RGW_QP_graph.f90:50-92) from eGWlin for every orbital not yet converged
   k_qp_init<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, w_guess ? w_guess : eGWlin, s);
@@ -469,7 +655,7 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
       double* part;
       int nch;
       QK_TRY(sigma_sweep(ctx, doSRG, eta, flow, N, nC, nO, nR, nS, eOld, s.w, Om, rho, s.list,
-                         s.nact, &part, &nch));
+                         s.nact, &part, &nch, ff));
       k_qp_update<<<1, 1024, 0, ctx->stream>>>(N, nch, part, eHF, s, maxit);
       QK_LAUNCHED();
       if (!ctx->capturing && (it & 3) == 3) {  // poll the active count every 4 steps
@@ -500,65 +686,106 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
 // ---------------------------------------------------------------------------------------------
 namespace {
 
-constexpr int NMOM = 6;  // occupied/virtual pole weight, first and second moments
+// Per orbital p the feature sweep evaluates the pole sums at the linearised root w = eGWlin_p:
+// S0 = sum R/eps, S1 = sum R/eps^2, S2 = sum R/eps^3 (R = 2 rho^2, eps = w - e_q +- Om_m, eta = 0)
+// and the nearest pole (min |eps| with its R): one sweep gives the Newton and Halley steps of the
+// QP equation f(w) = w - eHF - Sigma(w) from the reference start.
+constexpr int NACC = 5;  // S0, S1, S2, min |eps|, R at the minimum
 
 __global__ void __launch_bounds__(SIG_WARPS * 32)
     k_feature_partial(int N, int nC, int nO, int nR, int nS, int nchunks, int mper,
-                      const double* __restrict__ e, const double* __restrict__ Om,
-                      const double* __restrict__ rho, double* __restrict__ part) {
+                      const double* __restrict__ e, const double* __restrict__ wlin,
+                      const double* __restrict__ Om, const double* __restrict__ rho,
+                      double* __restrict__ part) {
   extern __shared__ double se[];
-  __shared__ double acc[NMOM][SIG_WARPS][32];
+  __shared__ double acc[NACC][SIG_WARPS][32];
   for (int i = threadIdx.x; i < N; i += blockDim.x) se[i] = e[i];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p = nC + blockIdx.x * 32 + lane;
   const int pend = N - nR;
   __syncthreads();
-  double m[NMOM] = {0, 0, 0, 0, 0, 0};
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, emin = INFINITY, rmin = 0.0;
   if (p < pend) {
+    const double w = wlin[p];
     const long long N1 = N, N2 = N1 * N1;
     const int m0 = blockIdx.y * mper, m1 = min(nS, m0 + mper);
     for (int mm = m0 + warp; mm < m1; mm += SIG_WARPS) {
       const double om = Om[mm];
       const double* r = rho + p + N2 * mm;
-      for (int q = nC; q < nO; ++q) {
-        const double x = r[N1 * q], w = x * x, pole = se[q] - om;
-        m[0] += w; m[1] += w * pole; m[2] += w * pole * pole;
-      }
-      for (int q = nO; q < pend; ++q) {
-        const double x = r[N1 * q], w = x * x, pole = se[q] + om;
-        m[3] += w; m[4] += w * pole; m[5] += w * pole * pole;
+      for (int q = nC; q < pend; ++q) {
+        const double x = r[N1 * q];
+        const double R = 2.0 * (x * x);
+        const double eps = q < nO ? (w - se[q] + om) : (w - se[q] - om);
+        const double ie = rcp_nr(eps);
+        const double t = R * ie;
+        s0 += t;
+        s1 = fma(t, ie, s1);
+        s2 = fma(t * ie, ie, s2);
+        if (fabs(eps) < emin) {
+          emin = fabs(eps);
+          rmin = R;
+        }
       }
     }
   }
-#pragma unroll
-  for (int k = 0; k < NMOM; ++k) acc[k][warp][lane] = m[k];
+  acc[0][warp][lane] = s0;
+  acc[1][warp][lane] = s1;
+  acc[2][warp][lane] = s2;
+  acc[3][warp][lane] = emin;
+  acc[4][warp][lane] = rmin;
   __syncthreads();
   if (warp == 0 && p < pend) {
     const size_t stride = (size_t)nchunks * N;
-#pragma unroll
-    for (int k = 0; k < NMOM; ++k) {
-      double t = 0.0;
-      for (int w = 0; w < SIG_WARPS; ++w) t += acc[k][w][lane];
-      part[(size_t)k * stride + (size_t)blockIdx.y * N + p] = t;
+    double t0 = 0.0, t1 = 0.0, t2 = 0.0, em = INFINITY, rm = 0.0;
+    for (int w = 0; w < SIG_WARPS; ++w) {
+      t0 += acc[0][w][lane];
+      t1 += acc[1][w][lane];
+      t2 += acc[2][w][lane];
+      if (acc[3][w][lane] < em) {
+        em = acc[3][w][lane];
+        rm = acc[4][w][lane];
+      }
     }
+    const size_t o = (size_t)blockIdx.y * N + p;
+    part[o] = t0;
+    part[o + stride] = t1;
+    part[o + 2 * stride] = t2;
+    part[o + 3 * stride] = em;
+    part[o + 4 * stride] = rm;
   }
+}
+
+__device__ __forceinline__ float clampf(double x, double lim) {
+  return (float)(x != x ? 0.0 : fmax(-lim, fmin(lim, x)));
 }
 
 __global__ void k_feature_final(int N, int nC, int nO, int nR, int nchunks,
                                 const double* __restrict__ part, const double* __restrict__ e,
-                                const double* __restrict__ Om, const double* __restrict__ Sig,
-                                const double* __restrict__ Z, float* __restrict__ F) {
+                                const double* __restrict__ wlin, const double* __restrict__ Om,
+                                const double* __restrict__ Sig, const double* __restrict__ Z,
+                                float* __restrict__ F, double* __restrict__ hal) {
   const size_t stride = (size_t)nchunks * N;
   const double eh = e[nO - 1], el = e[nO];
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
-    double m[NMOM] = {0, 0, 0, 0, 0, 0};
+    double S0 = 0.0, S1 = 0.0, S2 = 0.0, em = INFINITY, rm = 0.0;
     if (p >= nC && p < N - nR)
-      for (int c = 0; c < nchunks; ++c)
-        for (int k = 0; k < NMOM; ++k) m[k] += part[(size_t)k * stride + (size_t)c * N + p];
+      for (int c = 0; c < nchunks; ++c) {
+        const size_t o = (size_t)c * N + p;
+        S0 += part[o];
+        S1 += part[o + stride];
+        S2 += part[o + 2 * stride];
+        if (part[o + 3 * stride] < em) {
+          em = part[o + 3 * stride];
+          rm = part[o + 4 * stride];
+        }
+      }
     const double ep = e[p];
-    const double co = m[0] > 0 ? m[1] / m[0] : ep, cv = m[3] > 0 ? m[4] / m[3] : ep;
-    const double so = m[0] > 0 ? sqrt(fmax(0.0, m[2] / m[0] - co * co)) : 0.0;
-    const double sv = m[3] > 0 ? sqrt(fmax(0.0, m[5] / m[3] - cv * cv)) : 0.0;
+    const double w = wlin[p];
+    // f(w) = w - eHF - Sigma(w), f' = 1 - Sigma' = 1 + S1, f'' = -Sigma'' = -2 S2
+    const double f0 = w - ep - S0, f1 = 1.0 + S1, f2 = -2.0 * S2;
+    const double dn = -f0 / f1;
+    const double dh = -2.0 * f0 * f1 / (2.0 * f1 * f1 - f0 * f2);
+    if (hal) hal[p] = (dh == dh && fabs(dh) <= 1.0) ? dh : NAN;
     float* f = F + (size_t)p * QK_MLP_NIN;
     f[0] = (float)ep;
     f[1] = p < nO ? 1.f : 0.f;
@@ -566,14 +793,14 @@ __global__ void k_feature_final(int N, int nC, int nO, int nR, int nchunks,
     f[3] = (float)(ep - el);
     f[4] = (float)Sig[p];
     f[5] = (float)Z[p];
-    f[6] = (float)(Z[p] * Sig[p]);
+    f[6] = (float)(Z[p] * Sig[p]);  // eGWlin - eHF
     f[7] = (float)(1.0 - 1.0 / Z[p]);
-    f[8] = (float)m[0];
-    f[9] = (float)m[3];
-    f[10] = (float)(co - ep);
-    f[11] = (float)(cv - ep);
-    f[12] = (float)so;
-    f[13] = (float)sv;
+    f[8] = clampf(dn, 1.0);          // Newton step from eGWlin
+    f[9] = clampf(dh, 1.0);          // Halley step from eGWlin
+    f[10] = clampf(f0, 1.0);
+    f[11] = clampf(S1, 20.0);
+    f[12] = (float)log10(em + 1e-12);
+    f[13] = clampf(log10(rm / (em + 1e-300) + 1e-12), 12.0);
     f[14] = (float)Om[0];
     f[15] = (float)log((double)N);
   }
@@ -582,8 +809,8 @@ __global__ void k_feature_final(int N, int nC, int nO, int nR, int nchunks,
 }  // namespace
 
 int qk_features(qk_ctx* ctx, int N, int nC, int nO, int nR, int nS, const double* e,
-                const double* Om, const double* rho, const double* Sig, const double* Z,
-                float* F) {
+                const double* wlin, const double* Om, const double* rho, const double* Sig,
+                const double* Z, float* F, double* hal) {
   const int nact = N - nR - nC;
   const int ptiles = (nact + 31) / 32;
   int nchunks = (4 * ctx->num_sms + ptiles - 1) / (ptiles > 0 ? ptiles : 1);
@@ -593,15 +820,15 @@ int qk_features(qk_ctx* ctx, int N, int nC, int nO, int nR, int nS, const double
   const int mper = (nS + nchunks - 1) / nchunks;
   nchunks = (nS + mper - 1) / mper;
   double* part = nullptr;
-  QK_TRY(qk_wst(ctx, W_MISC, (size_t)NMOM * nchunks * N + 64, &part));
-  QK_CK(cudaMemsetAsync(part, 0, sizeof(double) * NMOM * (size_t)nchunks * N, ctx->stream));
+  QK_TRY(qk_wst(ctx, W_MISC, (size_t)NACC * nchunks * N + 64, &part));
+  QK_CK(cudaMemsetAsync(part, 0, sizeof(double) * NACC * (size_t)nchunks * N, ctx->stream));
   if (ptiles > 0) {
     k_feature_partial<<<dim3(ptiles, nchunks), SIG_WARPS * 32, N * sizeof(double), ctx->stream>>>(
-        N, nC, nO, nR, nS, nchunks, mper, e, Om, rho, part);
+        N, nC, nO, nR, nS, nchunks, mper, e, wlin, Om, rho, part);
     QK_LAUNCHED();
   }
-  k_feature_final<<<(N + 127) / 128, 128, 0, ctx->stream>>>(N, nC, nO, nR, nchunks, part, e, Om,
-                                                           Sig, Z, F);
+  k_feature_final<<<(N + 127) / 128, 128, 0, ctx->stream>>>(N, nC, nO, nR, nchunks, part, e, wlin,
+                                                           Om, Sig, Z, F, hal);
   QK_LAUNCHED();
   return QK_OK;
 }

@@ -200,17 +200,30 @@ int casida_dev(qk_ctx* ctx, const Dims& d, const double* e, const double* ERI, d
   return QK_OK;
 }
 
+// The mixed tier evaluates the pole sums with FP32 far-pole terms (eta = 0 and no SRG only;
+// otherwise, and in the FP64 tier, every term is FP64).
+int sigma_tier(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* rho,
+               const double* Om, qk_sigma_ff* ff, const qk_sigma_ff** use) {
+  *use = nullptr;
+  if (prm->precision != QK_PREC_BF16X3 || prm->eta != 0.0 || prm->doSRG) return QK_OK;
+  QK_TRY(qk_sigma_ff_prep(ctx, d.N, d.nS, rho, Om, ff));
+  *use = ff;
+  return QK_OK;
+}
+
 // Newton QP of RG0W0 (reference start eGWlin) or, with prm->qp_guess, from the learned guess;
 // captures the per-orbital features when requested.
 int g0w0_qp(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, double flow, const double* eHF,
             const double* Om, const double* rho, const double* SigC, double* Z,
-            const double* eGWlin, double* eGW) {
+            const double* eGWlin, double* eGW, const qk_sigma_ff* ff) {
   const int N = d.N, nS = d.nS;
   float* F = nullptr;
+  double* gbuf = nullptr;  // [0, N): start; [N, 2N): Halley step; then N ints: fromref
   const bool need_f = ctx->capture_features || prm->qp_guess;
   if (need_f) {
     QK_TRY(qk_wst(ctx, W_FEAT, (size_t)N * QK_MLP_NIN + 16, &F));
-    QK_TRY(qk_features(ctx, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho, SigC, Z, F));
+    QK_TRY(qk_wst(ctx, W_GUESS, (size_t)3 * N + 16, &gbuf));
+    QK_TRY(qk_features(ctx, N, d.nC, d.nO, d.nR, nS, eHF, eGWlin, Om, rho, SigC, Z, F, gbuf + N));
     if (ctx->capture_features) {
       ctx->features.resize((size_t)N * QK_MLP_NIN);
       QK_CK(cudaMemcpyAsync(ctx->features.data(), F, sizeof(float) * N * QK_MLP_NIN,
@@ -219,16 +232,18 @@ int g0w0_qp(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, double flow, co
     }
   }
   double* w0 = nullptr;
+  int* fromref = nullptr;
   if (prm->qp_guess && !prm->linearize) {
-    QK_TRY(qk_wst(ctx, W_GUESS, (size_t)N + 16, &w0));
-    QK_TRY(qk_guess_from_model(ctx, N, F, eHF, w0));
+    w0 = gbuf;
+    fromref = (int*)(gbuf + 2 * N);
+    QK_TRY(qk_guess_from_model(ctx, N, F, eGWlin, gbuf + N, w0, fromref));
   }
   if (prm->linearize) {
     QK_CK(cudaMemcpyAsync(eGW, eGWlin, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
     return QK_OK;
   }
   return qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho,
-                      eGWlin, eHF, eGW, Z, w0, 8);
+                      eGWlin, eHF, eGW, Z, w0, 8, ff, fromref);
 }
 
 int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* eHF,
@@ -259,12 +274,15 @@ int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   qk_toc(ctx, T_RHO);
   // self-energy
   qk_tic(ctx, T_SIGMA);
+  qk_sigma_ff ff;
+  const qk_sigma_ff* ffp = nullptr;
+  QK_TRY(sigma_tier(ctx, prm, d, rho, Om, &ff, &ffp));
   QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho, SigC,
-                       Z, EcGM_d));
+                       Z, EcGM_d, ffp));
   QK_TRY(qk_qp_linear(ctx, N, eHF, Z, SigC, 1, eGWlin));
   qk_toc(ctx, T_SIGMA);
   qk_tic(ctx, T_QP);
-  QK_TRY(g0w0_qp(ctx, prm, d, flow, eHF, Om, rho, SigC, Z, eGWlin, eGW));
+  QK_TRY(g0w0_qp(ctx, prm, d, flow, eHF, Om, rho, SigC, Z, eGWlin, eGW, ffp));
   qk_toc(ctx, T_QP);
   // second Casida at eGW for EcRPA (RG0W0.f90:222-225): eigenvalues only
   qk_tic(ctx, T_CASIDA2);
@@ -326,15 +344,18 @@ int evgw_cycle(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const EvBufs
     qk_toc(ctx, T_RHO);
   }
   qk_tic(ctx, T_SIGMA);
+  qk_sigma_ff ff;
+  const qk_sigma_ff* ffp = nullptr;
+  QK_TRY(sigma_tier(ctx, prm, d, b.rho, b.Om, &ff, &ffp));
   QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, b.eGW, b.Om,
-                       b.rho, b.SigC, b.Z, b.scal + 8));
+                       b.rho, b.SigC, b.Z, b.scal + 8, ffp));
   qk_toc(ctx, T_SIGMA);
   qk_tic(ctx, T_QP);
   if (prm->linearize) {
     QK_TRY(qk_qp_linear(ctx, N, b.eHF, b.Z, b.SigC, 0, b.eGW));  // evRGW.f90:147
   } else {
     QK_TRY(qk_qp_newton(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, b.eHF, b.Om,
-                        b.rho, b.eOld, b.eOld, b.eGW, b.Z));  // evRGW.f90:154
+                        b.rho, b.eOld, b.eOld, b.eGW, b.Z, nullptr, 8, ffp));  // evRGW.f90:154
   }
   qk_toc(ctx, T_QP);
   QK_TRY(qk_max_abs_diff(ctx, N, b.eGW, b.eOld, b.scal + 9));  // evRGW.f90:160
@@ -497,12 +518,15 @@ int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   QK_TRY(rho_from_T(ctx, prm->precision, d, naux, L, T, rho));
   qk_toc(ctx, T_RHO);
   qk_tic(ctx, T_SIGMA);
+  qk_sigma_ff ff;
+  const qk_sigma_ff* ffp = nullptr;
+  QK_TRY(sigma_tier(ctx, prm, d, rho, Om, &ff, &ffp));
   QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, eHF, Om, rho, SigC,
-                       Z, scal + 8));
+                       Z, scal + 8, ffp));
   QK_TRY(qk_qp_linear(ctx, N, eHF, Z, SigC, 1, eGWlin));
   qk_toc(ctx, T_SIGMA);
   qk_tic(ctx, T_QP);
-  QK_TRY(g0w0_qp(ctx, prm, d, flow, eHF, Om, rho, SigC, Z, eGWlin, eGW));
+  QK_TRY(g0w0_qp(ctx, prm, d, flow, eHF, Om, rho, SigC, Z, eGWlin, eGW, ffp));
   qk_toc(ctx, T_QP);
   qk_tic(ctx, T_CASIDA2);
   QK_TRY(casida_dev(ctx, d, eGW, nullptr, nullptr, nullptr, nullptr, scal + 3, 0, K));
@@ -730,7 +754,7 @@ int qk_RGW_excitation_density(qk_ctx* ctx, int nOrb, int nC, int nO, int nR, int
   QK_TRY(h2d(ctx, dERI, ERI, N4 * 8));
   QK_TRY(h2d(ctx, dX, XpY, S2 * 8));
   QK_TRY(qk_launch_slab_gather(ctx, nOrb, nC, nO, nR, dERI, dS));
-  QK_TRY(rho_gemm(ctx, QK_PREC_FP64, nOrb, nS, dS, dX, dR));
+  QK_TRY(rho_gemm(ctx, ctx->stage_precision, nOrb, nS, dS, dX, dR));
   QK_TRY(d2h(ctx, rho, dR, N2S * 8));
   return end(ctx, QK_OK);
 }
@@ -753,11 +777,24 @@ static int sigma_stage(qk_ctx* ctx, int doSRG, double eta, double flow, int nBas
   QK_TRY(h2d(ctx, dR, rho, N2S * 8));
   QK_TRY(h2d(ctx, de, e, N * 8));
   QK_TRY(h2d(ctx, dOm, Om, nS * 8));
-  QK_TRY(qk_sigma_diag(ctx, doSRG, eta, flow, nBas, nC, nO, nR, nS, de, dOm, dR, dSig, dZ, dGM));
+  qk_sigma_ff ff;
+  const qk_sigma_ff* ffp = nullptr;
+  if (ctx->stage_precision == QK_PREC_BF16X3 && eta == 0.0 && !doSRG) {
+    QK_TRY(qk_sigma_ff_prep(ctx, nBas, nS, dR, dOm, &ff));
+    ffp = &ff;
+  }
+  QK_TRY(qk_sigma_diag(ctx, doSRG, eta, flow, nBas, nC, nO, nR, nS, de, dOm, dR, dSig, dZ, dGM,
+                       ffp));
   QK_TRY(d2h(ctx, Sig, dSig, N * 8));
   QK_TRY(d2h(ctx, Z, dZ, N * 8));
   QK_TRY(d2h(ctx, EcGM, dGM, 8));
   return end(ctx, QK_OK);
+}
+
+int qk_set_stage_precision(qk_ctx* ctx, int precision) {
+  if (!ctx || (precision != QK_PREC_FP64 && precision != QK_PREC_BF16X3)) return QK_ERR_ARG;
+  ctx->stage_precision = precision;
+  return QK_OK;
 }
 
 int qk_RGW_self_energy_diag(qk_ctx* ctx, double eta, int nBas, int nOrb, int nC, int nO, int nV,
@@ -799,7 +836,14 @@ int qk_RGW_QP_graph(qk_ctx* ctx, int doSRG, double eta, double flow, int nBas, i
   QK_TRY(h2d(ctx, dZ, Z, N * 8));
   QK_TRY(h2d(ctx, dGW, eGWlin, N * 8));
   QK_TRY(h2d(ctx, dOm, Om, nS * 8));
-  QK_TRY(qk_qp_newton(ctx, doSRG, eta, flow, nBas, nC, nO, nR, nS, deHF, dOm, dR, dlin, dold, dGW, dZ));
+  qk_sigma_ff ff;
+  const qk_sigma_ff* ffp = nullptr;
+  if (ctx->stage_precision == QK_PREC_BF16X3 && eta == 0.0 && !doSRG) {
+    QK_TRY(qk_sigma_ff_prep(ctx, nBas, nS, dR, dOm, &ff));
+    ffp = &ff;
+  }
+  QK_TRY(qk_qp_newton(ctx, doSRG, eta, flow, nBas, nC, nO, nR, nS, deHF, dOm, dR, dlin, dold, dGW, dZ,
+                      nullptr, 8, ffp));
   QK_TRY(d2h(ctx, eGW, dGW, N * 8));
   QK_TRY(d2h(ctx, Z, dZ, N * 8));
   return end(ctx, QK_OK);

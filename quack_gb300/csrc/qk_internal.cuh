@@ -36,7 +36,7 @@ struct DevBuf {
 
 enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
-  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_TMAT2, W_NUMBUF
+  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_TMAT2, W_RHO32, W_OMF, W_NUMBUF
 };
 
 struct qk_ctx {
@@ -50,6 +50,7 @@ struct qk_ctx {
   unsigned* d_bar = nullptr;    // grid-barrier counters (zeroed before each cooperative launch)
   DevBuf buf[W_NUMBUF];
   long long launches = 0;
+  int stage_precision = QK_PREC_FP64;  // tier of the stage-level drop-ins (qk_set_stage_precision)
   int last_dev_status = 0;
   bool time_eig = true;  // stage timers inside the eigensolver (off for the eigenvalue-only pass)
   std::vector<int> qp_iters;  // Newton steps per orbital of the last QP solve
@@ -153,19 +154,35 @@ int qk_launch_slab_gather(qk_ctx* ctx, int N, int nC, int nO, int nR, const doub
                           double* S);
 
 // self-energy / QP pieces (k_sigma.cu)
+// Mixed-tier pole sums (eta = 0, no SRG): terms with |eps| >= tau in FP32 from R = 2 rho^2
+// (FP32) and Om as (hi, lo) float pairs, the terms within tau of a pole in FP64 from rho.
+struct qk_sigma_ff {
+  const float* R = nullptr;
+  const float2* OmF = nullptr;
+  const int* bad = nullptr;  // set when Om is not ascending (every term then goes to FP64)
+  float tau = 0.1f;
+};
+int qk_sigma_ff_prep(qk_ctx* ctx, int N, int nS, const double* rho, const double* Om,
+                     qk_sigma_ff* ff);
 int qk_sigma_diag(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                   int nS, const double* e, const double* Om, const double* rho, double* Sig,
-                  double* Z, double* EcGM);
+                  double* Z, double* EcGM, const qk_sigma_ff* ff = nullptr);
 int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                  int nS, const double* eHF, const double* Om, const double* rho,
                  const double* eGWlin, const double* eOld, double* eGW, double* Z,
-                 const double* w_guess = nullptr, int guess_maxit = 8);
+                 const double* w_guess = nullptr, int guess_maxit = 8,
+                 const qk_sigma_ff* ff = nullptr, const int* guess_fromref = nullptr);
 // per-orbital features of the linearised stage (N x 16 floats, row-major, raw)
+// features of the linearised stage (F: N x QK_MLP_NIN); hal (optional): the FP64 Halley step
+// of the QP equation from eGWlin (NaN where it is not usable)
 int qk_features(qk_ctx* ctx, int N, int nC, int nO, int nR, int nS, const double* e,
-                const double* Om, const double* rho, const double* Sig, const double* Z,
-                float* F);
+                const double* wlin, const double* Om, const double* rho, const double* Sig,
+                const double* Z, float* F, double* hal = nullptr);
 // learned guess w0 = e + shift(features) with the attached model
-int qk_guess_from_model(qk_ctx* ctx, int N, const float* F, const double* e, double* w0);
+// Newton start per orbital from the attached model: eGWlin + Halley step where the network's
+// predicted shift agrees with it, else the reference start (fromref = 1)
+int qk_guess_from_model(qk_ctx* ctx, int N, const float* F, const double* base, const double* hal,
+                        double* w0, int* fromref);
 int qk_qp_linear(qk_ctx* ctx, int N, const double* eHF, const double* Z, const double* Sig,
                  int use_z, double* eGW);
 int qk_diis_dev(qk_ctx* ctx, int n_err, int n_e, int n_diis, double* err_hist, double* e_hist,

@@ -2,11 +2,14 @@
 
 The model (16 -> 64 -> 64 -> 1 SiLU) and its forward/backward/Adam kernels live in libqkgw.so
 (k_mlp.cu).  Features are the 16 per-orbital quantities of the linearised G0W0 stage that the
-driver captures (orbital energy and its distance to the frontier orbitals, Sigma_c(e_p), Z_p,
-the linearised shift, dSigma/dw, the occupied/virtual pole weights of rho^2 with their centroids
-and spreads, the lowest screening energy and log N).  The target is the converged QP shift
-eGW_p - eHF_p of the plain FP64 Newton search.  Trained weights are saved as a flat float32
-binary plus a JSON file with the normalisation.
+driver captures: orbital energy and its distance to the frontier orbitals, Sigma_c(e_p), Z_p,
+the linearised shift Z*Sigma (= eGWlin - eHF), dSigma/dw, then from one pole sweep at eGWlin the
+Newton and Halley steps of the QP equation, its residual and slope there, the distance to the
+nearest pole and that pole's strength, and finally the lowest screening energy and log N.  The
+target is the nonlinear part of the converged QP shift, eGW_p - eGWlin_p, of the plain FP64
+Newton search on the orbitals whose search from eGWlin is regular (few steps, small correction);
+the guess is eGWlin_p plus the prediction.  Trained weights are saved as a flat float32 binary
+plus a JSON file with the normalisation.
 """
 from __future__ import annotations
 
@@ -122,14 +125,19 @@ def run_g0w0_L(ctx, system, opts, capture=False):
     return res
 
 
-def collect(ctx, systems, maxit_ok=63):
-    """Features and converged QP-shift targets from plain FP64 Newton G0W0 runs."""
+def collect(ctx, systems, maxit_ok=16, max_corr=0.25):
+    """Features and targets eGW - eGWlin from plain FP64 Newton G0W0 runs.  Feature 6 is the
+    linearised shift Z*Sigma = eGWlin - eHF.  Orbitals whose search wandered (more than maxit_ok
+    steps) or jumped far from the linearised root carry no learnable signal and are left out."""
     X, T = [], []
     for s in systems:
         r = run_g0w0_L(ctx, s, api.GWOptions(), capture=True)
-        ok = (r["iters"] <= maxit_ok) & np.isfinite(r["eGW"]) & np.all(np.isfinite(r["features"]), 1)
-        X.append(r["features"][ok])
-        T.append((r["eGW"] - s["eHF"])[ok])
+        F = r["features"]
+        corr = r["eGW"] - s["eHF"] - F[:, 6].astype(np.float64)
+        ok = ((r["iters"] <= maxit_ok) & np.isfinite(r["eGW"]) & np.all(np.isfinite(F), 1)
+              & (np.abs(corr) <= max_corr))
+        X.append(F[ok])
+        T.append(corr[ok])
     return np.concatenate(X).astype(np.float32), np.concatenate(T).astype(np.float32)
 
 

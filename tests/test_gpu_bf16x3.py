@@ -61,3 +61,92 @@ def test_mixed_g0w0_within_1mev(ctx, N, nO, seed):
     err = np.max(np.abs(r["eGW"] - ref["eGW"]))
     assert err < MEV, err
     assert np.max(np.abs(r["Om"] - ref["Om"])) < 1e-8     # the Casida stays FP64
+
+
+def _stage_inputs(N, nO, seed):
+    s = synth.small_system(N, nO, 3 * N, seed)
+    E = synth.eri_phys_numpy(s["L"])
+    nS = nO * (N - nO)
+    A = O.phRLR_A(1, True, N, 0, nO, N - nO, 0, nS, 1.0, s["eHF"], E)
+    B = O.phRLR_B(1, True, N, 0, nO, N - nO, 0, nS, 1.0, E)
+    _, Om, XpY, _ = O.phRLR(False, nS, A, B)
+    rho = O.RGW_excitation_density(N, 0, nO, 0, nS, E, XpY)
+    return s, nS, Om, rho
+
+
+class _StagePrecision:
+    def __init__(self, ctx, prec):
+        self.ctx, self.prec = ctx, prec
+
+    def __enter__(self):
+        self.ctx.set_stage_precision(self.prec)
+
+    def __exit__(self, *exc):
+        self.ctx.set_stage_precision(api.QK_PREC_FP64)
+
+
+@pytest.mark.parametrize("N,nO,seed", [(40, 5, 21), (64, 8, 24)])
+def test_mixed_pole_sums_vs_fp64(ctx, N, nO, seed):
+    """FP32 far-pole / FP64 near-pole evaluation of Sigma, Z and EcGM with the exact FP64 rho:
+    the only error left is the FP32 rounding of the far terms (a few 1e-7 relative per term)."""
+    s, nS, Om, rho = _stage_inputs(N, nO, seed)
+    gmr, Sigr, Zr = O.RGW_self_energy_diag(0.0, N, N, 0, nO, N - nO, 0, nS, s["eHF"], Om, rho)
+    with _StagePrecision(ctx, api.QK_PREC_BF16X3):
+        gm, Sig, Z = api.RGW_self_energy_diag(0.0, N, N, 0, nO, N - nO, 0, nS, s["eHF"], Om, rho,
+                                              ctx=ctx)
+    assert np.max(np.abs(Sig - Sigr) / np.maximum(1.0, np.abs(Sigr))) < 1e-7
+    assert np.max(np.abs(Z - Zr) / np.maximum(1.0, np.abs(Zr))) < 1e-6
+    assert abs(gm - gmr) < 1e-7 * max(1.0, abs(gmr))
+
+
+def test_mixed_pole_sums_unsorted_screening_goes_fp64(ctx):
+    """Om out of order (here: permuted together with rho's m index, which leaves Sigma unchanged)
+    cannot be windowed; every term then takes the FP64 branch and the FP64 bar holds."""
+    N, nO = 24, 3
+    s, nS, Om, rho = _stage_inputs(N, nO, 31)
+    perm = np.random.default_rng(3).permutation(nS)
+    gmr, Sigr, Zr = O.RGW_self_energy_diag(0.0, N, N, 0, nO, N - nO, 0, nS, s["eHF"], Om, rho)
+    with _StagePrecision(ctx, api.QK_PREC_BF16X3):
+        gm, Sig, Z = api.RGW_self_energy_diag(0.0, N, N, 0, nO, N - nO, 0, nS, s["eHF"], Om[perm],
+                                              np.ascontiguousarray(rho[:, :, perm]), ctx=ctx)
+    assert np.allclose(Sig, Sigr, rtol=1e-11, atol=1e-13)
+    assert np.allclose(Z, Zr, rtol=1e-11, atol=1e-13)
+    assert abs(gm - gmr) < 1e-11 * max(1.0, abs(gmr))
+
+
+def test_mixed_qp_graph_vs_fp64(ctx):
+    """Newton with the mixed pole sums: on orbitals whose FP64 search is regular (at most 6
+    steps) the root agrees with the FP64 oracle far inside 1 meV; every other orbital ends on a
+    root of the FP64 QP equation or on the linearised fallback."""
+    N, nO = 40, 5
+    s, nS, Om, rho = _stage_inputs(N, nO, 21)
+    _, Sig, Z = O.RGW_self_energy_diag(0.0, N, N, 0, nO, N - nO, 0, nS, s["eHF"], Om, rho)
+    lin = s["eHF"] + Z * Sig
+    eR, _, iters = O.RGW_QP_graph(False, 0.0, 500.0, N, 0, nO, N - nO, 0, nS, s["eHF"], Om, rho,
+                                  lin, s["eHF"], Z, return_iters=True)
+    with _StagePrecision(ctx, api.QK_PREC_BF16X3):
+        eGW, _ = api.RGW_QP_graph(False, 0.0, 500.0, N, 0, nO, N - nO, 0, nS, s["eHF"], Om, rho, lin,
+                                  s["eHF"], Z, ctx=ctx)
+    regular = np.asarray(iters) <= 6
+    assert regular.sum() >= N // 2
+    assert np.max(np.abs(eGW[regular] - eR[regular])) < 1e-7
+    for p in np.where(~regular)[0]:
+        w = eGW[p]
+        f = w - s["eHF"][p] - O.RGW_Re_SigC(p, w, 0.0, N, 0, nO, N - nO, 0, nS, s["eHF"], Om, rho)
+        assert abs(f) < 1e-5 or abs(w - lin[p]) < 1e-12, (p, f)
+
+
+@pytest.mark.parametrize("N,nO,seed", [(40, 5, 21)])
+def test_mixed_g0w0_newton_regular_orbitals(ctx, N, nO, seed):
+    """Mixed driver (BF16x3 rho + mixed pole sums) with the Newton QP: regular orbitals within
+    1 meV of the FP64 oracle."""
+    s = synth.small_system(N, nO, 3 * N, seed)
+    E = synth.eri_phys_numpy(s["L"])
+    nS = nO * (N - nO)
+    ref = O.RG0W0(False, 0.0, False, N, N, 0, nO, N - nO, 0, nS, E, s["eHF"])
+    r = api.RG0W0(api.GWOptions(precision=api.QK_PREC_BF16X3), N, N, 0, nO, N - nO, 0, nS, E,
+                  s["eHF"], ctx=ctx)
+    regular = np.asarray(ref["qp_iters"]) <= 6
+    assert regular.sum() >= N // 2
+    assert np.max(np.abs(r["eGW"][regular] - ref["eGW"][regular])) < MEV
+    assert abs(r["EcGM"] - ref["EcGM"]) < 1e-5 * max(1.0, abs(ref["EcGM"]))

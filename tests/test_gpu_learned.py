@@ -67,6 +67,25 @@ def test_learned_guess_keeps_reference_roots(ctx):
     rows = learned.evaluate(ctx, m, test_sys)
     n_conv = sum(r["n_conv"] for r in rows)
     n_same = sum(r["n_same"] for r in rows)
-    # the guess path reproduces the reference root for (nearly) every converged orbital; with
-    # eta = 0 poles are dense, so a different start can in rare cases land on another root
+    # the guess path reproduces the reference root for (nearly) every converged orbital: orbitals
+    # the gate sends to the reference start follow the reference trajectory exactly; a Halley
+    # start can in rare cases land on another root (eta = 0: the poles are dense)
     assert n_same >= 0.95 * n_conv, rows
+
+
+def test_learned_guess_saves_newton_evaluations(ctx):
+    """What the trained network gains: Newton Sigma evaluations with the guess vs the reference
+    search from eGWlin on held-out systems (same generator family, N = 24..60)."""
+    systems = synth.batch_systems(60, 24, 60, seed=7)
+    X, T = learned.collect(ctx, systems[:48])
+    m = learned.QPModel(ctx, seed=2)
+    learned.train(m, X, T, epochs=200, batch=256, lr=2e-3)
+    rows = learned.evaluate(ctx, m, systems[48:])
+    ev_ref = sum(r["evals_ref"] for r in rows)
+    ev_g = sum(r["evals_guess"] for r in rows)
+    n_conv = sum(r["n_conv"] for r in rows)
+    n_same = sum(r["n_same"] for r in rows)
+    print("newton evals: reference %d, learned guess %d (%.1f%% fewer); same root %d/%d"
+          % (ev_ref, ev_g, 100.0 * (1.0 - ev_g / ev_ref), n_same, n_conv))
+    assert ev_g < ev_ref
+    assert n_same >= 0.95 * n_conv
