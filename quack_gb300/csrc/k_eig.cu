@@ -74,6 +74,7 @@ struct TriArgs {
 __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
   extern __shared__ double sm[];
   __shared__ double red[32];
+  __shared__ double s_pj, s_dj, s_alpha;
   const int n = a.n;
   double* ytile = sm;  // one TRI_TC x TRI_TLD tile per warp
   double *vk, *wk, *vk1;
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
   unsigned epoch = 0;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
-  const int gwarp = blockIdx.x * nwarps + warp, totwarps = gridDim.x * nwarps;
+  const int totwarps = gridDim.x * nwarps;
   const int gthread = blockIdx.x * nt + tid, totthreads = gridDim.x * nt;
   double tau_k = 0.0;
 
@@ -100,37 +101,50 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       double* pz = a.pbuf + (size_t)((k + 2) % 3) * n;
       for (int i = gthread; i < n; i += totthreads) __stcg(pz + i, 0.0);
     }
-    // ---- small phase (redundant in every CTA) ----
-    if (k >= 0) {
-      const double* p = a.pbuf + (size_t)(k % 3) * n;
-      double dot = 0.0;
-      for (int i = k + 1 + tid; i < n; i += nt) {
-        const double pi = __ldcg(p + i);
-        wk[i] = pi;
-        dot += pi * vk[i];
-      }
-      dot = tri_block_sum(dot, ytile, red);
-      const double c = 0.5 * tau_k * tau_k * dot;
-      for (int i = k + 1 + tid; i < n; i += nt) wk[i] = tau_k * wk[i] - c * vk[i];
-      __syncthreads();
-    }
+    // ---- small phase (redundant in every CTA): w_k, then v_{k+1} from column j = k+1 ----
+    // FP64 is the scarce resource (one warp instruction per 64 cycles per SM sub-partition), so
+    // the passes are fused: p_k and the raw column j are loaded together, one pass forms w_k,
+    // the updated column and its norm, one pass scales the reflector.
     const int j = k + 1;
     double tau1 = 0.0;
-    if (j <= n - 1) {
-      double wj = 0.0, vj = 0.0;
-      if (k >= 0) { wj = wk[j]; vj = vk[j]; }
+    {
+      const double* p = a.pbuf + (size_t)((k + 3) % 3) * n;
+      double dot = 0.0;
       for (int i = j + tid; i < n; i += nt) {
-        double x = __ldcg(a.A + i + a.lda * j);
-        if (k >= 0) x = x - vk[i] * wj - wk[i] * vj;
-        vk1[i] = x;
+        vk1[i] = __ldcg(a.A + i + a.lda * j);
+        if (k >= 0) {
+          const double pi = __ldcg(p + i);
+          wk[i] = pi;
+          if (i == j) s_pj = pi;
+          dot = fma(pi, vk[i], dot);
+        }
       }
-      __syncthreads();
-      const double dj = vk1[j];
+      double c = 0.0, wj = 0.0, vj = 0.0;
+      if (k >= 0) {
+        dot = tri_block_sum(dot, ytile, red);  // (its barriers publish vk1, wk, s_pj)
+        c = 0.5 * tau_k * tau_k * dot;
+        vj = vk[j];
+        wj = tau_k * s_pj - c * vj;
+      } else {
+        __syncthreads();
+      }
+      double ss = 0.0;
+      for (int i = j + tid; i < n; i += nt) {
+        double x = vk1[i];
+        if (k >= 0) {
+          const double w = tau_k * wk[i] - c * vk[i];
+          wk[i] = w;
+          x = x - vk[i] * wj - w * vj;
+          vk1[i] = x;
+        }
+        if (i == j) s_dj = x;
+        else if (i == j + 1) s_alpha = x;
+        else ss = fma(x, x, ss);
+      }
+      const double sigma = tri_block_sum(ss, ytile, red);  // (publishes s_dj, s_alpha, vk1)
+      const double dj = s_dj;
       if (j <= n - 2) {
-        double ss = 0.0;
-        for (int i = j + 2 + tid; i < n; i += nt) ss += vk1[i] * vk1[i];
-        const double sigma = tri_block_sum(ss, ytile, red);
-        const double alpha = vk1[j + 1];
+        const double alpha = s_alpha;
         double beta, scal;
         if (sigma == 0.0) {
           tau1 = 0.0;
@@ -141,18 +155,17 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
           tau1 = (beta - alpha) / beta;
           scal = 1.0 / (alpha - beta);
         }
-        for (int i = j + 2 + tid; i < n; i += nt) vk1[i] *= scal;
-        __syncthreads();
-        if (tid == 0) vk1[j + 1] = 1.0;
+        for (int i = j + 1 + tid; i < n; i += nt) vk1[i] = (i == j + 1) ? 1.0 : vk1[i] * scal;
         __syncthreads();
         if (blockIdx.x == 0) {
           if (tid == 0) { a.e[j] = beta; a.tau[j] = tau1; }
           for (int i = j + 1 + tid; i < n; i += nt) a.V[i + a.ldv * j] = vk1[i];
         }
+      } else {
+        __syncthreads();
       }
       if (blockIdx.x == 0 && tid == 0) a.d[j] = dj;
     }
-    __syncthreads();
     // ---- big pass: rank-2 update of step k fused with p_{k+1} = A' v_{k+1}, lower triangle ----
     // The trailing lower triangle is cut into tiles of 32 rows x TRI_TC columns (row block bi
     // holds tiles t = 0..2bi+1; tiles are numbered row block after row block).  Each warp takes a
@@ -169,7 +182,8 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       const int nb = (mm + 31) >> 5;
       const int items = nb * (nb + 1);  // < 2^31 for every n this kernel can hold
       const int per = (items + totwarps - 1) / totwarps;
-      const int it0 = gwarp * per;
+      // warps numbered across CTAs first, so that a short tile list still spreads over all SMs
+      const int it0 = (warp * (int)gridDim.x + (int)blockIdx.x) * per;
       const int it1 = it0 + per < items ? it0 + per : items;
       double* tile = ytile + (size_t)warp * (TRI_TC * TRI_TLD);
       if (it0 < it1) {

@@ -455,7 +455,6 @@ int evgw_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
              const double* ERI, double* eGW, double* SigC, double* Z, double* hEcRPA,
              double* hEcGM, int* hnSCF, double* hConv) {
   if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
-  const double flow = 500.0;
   const int N = d.N, nS = d.nS;
   const size_t S2 = (size_t)nS * nS, N2S = (size_t)N * N * nS;
   const int maxd = prm->max_diis > 1 ? prm->max_diis : 1;
@@ -544,7 +543,6 @@ int evgw_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
                const double* eHF, double* eGW, double* SigC, double* Z, double* hEcRPA,
                double* hEcGM, int* hnSCF, double* hConv) {
   if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
-  const double flow = 500.0;
   const int N = d.N, nS = d.nS;
   const size_t N2S = (size_t)N * N * nS;
   const int maxd = prm->max_diis > 1 ? prm->max_diis : 1;
