@@ -32,8 +32,11 @@ constexpr double CLUSTER_REL = 1e-7;  // eigenvalues closer than this * ||T||_1 
 
 // Sum over the CTA with few FP64 operations (the FP64 pipe is the scarce resource here): the
 // per-thread partials go to shared memory and warp 0 adds them with four independent chains per
-// lane, then one butterfly.  scratch holds blockDim.x doubles.  Result returned to every thread.
-__device__ __forceinline__ double tri_block_sum(double v, double* scratch, double* out) {
+// lane, then one butterfly.  Thread 0 then runs fin(total) -- the scalar follow-up work, done
+// once instead of by every warp -- before the closing barrier publishes its results.
+// scratch holds blockDim.x doubles.
+template <class Fin>
+__device__ __forceinline__ void tri_block_sum(double v, double* scratch, Fin fin) {
   const int tid = threadIdx.x, nt = blockDim.x;
   scratch[tid] = v;
   __syncthreads();
@@ -49,10 +52,9 @@ __device__ __forceinline__ double tri_block_sum(double v, double* scratch, doubl
     for (; i < nt; i += 32) a0 += scratch[i];
     double t = (a0 + a1) + (a2 + a3);
     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (tid == 0) *out = t;
+    if (tid == 0) fin(t);
   }
   __syncthreads();
-  return *out;
 }
 
 struct TriArgs {
@@ -73,8 +75,7 @@ struct TriArgs {
 
 __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
   extern __shared__ double sm[];
-  __shared__ double red[32];
-  __shared__ double s_pj, s_dj, s_alpha;
+  __shared__ double s_pj, s_dj, s_alpha, s_sc[6];
   const int n = a.n;
   double* ytile = sm;  // one TRI_TC x TRI_TLD tile per warp
   double *vk, *wk, *vk1;
@@ -119,15 +120,20 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
           dot = fma(pi, vk[i], dot);
         }
       }
-      double c = 0.0, wj = 0.0, vj = 0.0;
       if (k >= 0) {
-        dot = tri_block_sum(dot, ytile, red);  // (its barriers publish vk1, wk, s_pj)
-        c = 0.5 * tau_k * tau_k * dot;
-        vj = vk[j];
-        wj = tau_k * s_pj - c * vj;
+        // (the barriers publish vk1, wk and s_pj as well)
+        tri_block_sum(dot, ytile, [&](double t) {
+          const double cc = 0.5 * tau_k * tau_k * t;
+          const double v = vk[j];
+          s_sc[0] = cc;
+          s_sc[1] = v;
+          s_sc[2] = tau_k * s_pj - cc * v;
+        });
       } else {
+        if (tid == 0) s_sc[0] = s_sc[1] = s_sc[2] = 0.0;
         __syncthreads();
       }
+      const double c = s_sc[0], vj = s_sc[1], wj = s_sc[2];
       double ss = 0.0;
       for (int i = j + tid; i < n; i += nt) {
         double x = vk1[i];
@@ -141,28 +147,33 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
         else if (i == j + 1) s_alpha = x;
         else ss = fma(x, x, ss);
       }
-      const double sigma = tri_block_sum(ss, ytile, red);  // (publishes s_dj, s_alpha, vk1)
-      const double dj = s_dj;
-      if (j <= n - 2) {
-        const double alpha = s_alpha;
-        double beta, scal;
-        if (sigma == 0.0) {
-          tau1 = 0.0;
-          beta = alpha;
-          scal = 1.0;
-        } else {
-          beta = -copysign(sqrt(alpha * alpha + sigma), alpha);
-          tau1 = (beta - alpha) / beta;
-          scal = 1.0 / (alpha - beta);
+      // Householder reflector of the updated column (dlarfg), computed once by thread 0
+      tri_block_sum(ss, ytile, [&](double sigma) {
+        double beta = 0.0, t1 = 0.0, scal = 1.0;
+        if (j <= n - 2) {
+          const double alpha = s_alpha;
+          if (sigma == 0.0) {
+            beta = alpha;
+          } else {
+            beta = -copysign(sqrt(alpha * alpha + sigma), alpha);
+            t1 = (beta - alpha) / beta;
+            scal = 1.0 / (alpha - beta);
+          }
         }
+        s_sc[3] = beta;
+        s_sc[4] = t1;
+        s_sc[5] = scal;
+      });
+      const double dj = s_dj;
+      tau1 = s_sc[4];
+      if (j <= n - 2) {
+        const double beta = s_sc[3], scal = s_sc[5];
         for (int i = j + 1 + tid; i < n; i += nt) vk1[i] = (i == j + 1) ? 1.0 : vk1[i] * scal;
         __syncthreads();
         if (blockIdx.x == 0) {
           if (tid == 0) { a.e[j] = beta; a.tau[j] = tau1; }
           for (int i = j + 1 + tid; i < n; i += nt) a.V[i + a.ldv * j] = vk1[i];
         }
-      } else {
-        __syncthreads();
       }
       if (blockIdx.x == 0 && tid == 0) a.d[j] = dj;
     }
