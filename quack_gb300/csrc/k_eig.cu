@@ -319,19 +319,24 @@ __global__ void k_tri_prep(int n, const double* __restrict__ d, const double* __
 
 // Number of eigenvalues of T below x: sign changes of the leading principal minors
 // p_0 = 1, p_1 = d_0 - x, p_{i+1} = (d_i - x) p_i - e_{i-1}^2 p_{i-1} (Sturm sequence of the
-// characteristic polynomials).  Division-free: 3 FP64 operations per step.  A zero minor takes
-// the sign opposite to its predecessor (the convention that a zero pivot counts as negative), and
-// every 4 steps the pair (p_i, p_{i-1}) is rescaled by an exact power of two when it drifts
-// towards overflow or underflow (signs and ratios are unchanged by the scaling).
+// characteristic polynomials).  Division-free, and the sign and zero tests read the bits, so a
+// step costs 3 FP64 operations.  A zero minor takes the sign opposite to its predecessor (the
+// convention that a zero pivot counts as negative), and every 4 steps the pair (p_i, p_{i-1}) is
+// rescaled by an exact power of two when it drifts towards overflow or underflow (signs and
+// ratios are unchanged by the scaling).
+__device__ __forceinline__ int sign_bit(double v, int prev_neg) {
+  const int hi = __double2hiint(v), lo = __double2loint(v);
+  return (((hi & 0x7fffffff) | lo) == 0) ? !prev_neg : (hi < 0);
+}
+
 __device__ __forceinline__ int sturm_count(int n, const double* __restrict__ d,
-                                           const double* __restrict__ e2, double x, double pivmin) {
-  (void)pivmin;
+                                           const double* __restrict__ e2, double x) {
   double p0 = 1.0, p1 = __ldg(d) - x;
-  int neg = p1 < 0.0 || p1 == 0.0;
+  int neg = sign_bit(p1, 0);
   int c = neg;
   for (int i = 1; i < n; ++i) {
-    const double p2 = (__ldg(d + i) - x) * p1 - __ldg(e2 + i - 1) * p0;
-    const int n2 = (p2 != 0.0) ? (p2 < 0.0) : !neg;
+    const double p2 = fma(__ldg(d + i) - x, p1, -(__ldg(e2 + i - 1) * p0));
+    const int n2 = sign_bit(p2, neg);
     c += (n2 != neg);
     neg = n2;
     p0 = p1;
@@ -352,34 +357,51 @@ __device__ __forceinline__ int sturm_count(int n, const double* __restrict__ d,
   return c;
 }
 
-// k-section on the Sturm count: KSEC consecutive lanes share eigenvalue j and test KSEC interior
-// points of the bracket per step (log2(KSEC+1) bits per step), to full FP64 precision.
-// Sturm counts are monotone in x in IEEE arithmetic, so the points with count <= j form a
-// prefix and the new bracket follows from a popcount of the group's ballot.
-constexpr int KSEC = 8;
-__global__ void k_stebz(int n, const double* __restrict__ d, const double* __restrict__ e2,
-                        const double* __restrict__ prep, double* __restrict__ w) {
+// k-section on the Sturm count: K consecutive lanes share eigenvalue j and test K interior points
+// of the bracket per step (log2(K+1) bits per step), to full FP64 precision.  Sturm counts are
+// monotone in x in IEEE arithmetic, so the points with count <= j form a prefix and the new
+// bracket follows from a popcount of the group's ballot.  K trades extra sweeps for parallelism:
+// the FP64 pipe of an SM sub-partition issues one warp instruction per 64 cycles, so the launch
+// picks the largest K whose warps still fit one per sub-partition.
+template <int K>
+__global__ void __launch_bounds__(128) k_stebz(int n, const double* __restrict__ d,
+                                               const double* __restrict__ e2,
+                                               const double* __restrict__ prep,
+                                               double* __restrict__ w) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = gt / KSEC, t = gt % KSEC;
+  const int j = gt / K, t = gt % K;
   const bool valid = j < n;
   const int lane = threadIdx.x & 31;
-  const unsigned gmask = ((1u << KSEC) - 1u) << (lane & ~(KSEC - 1));
+  const unsigned gmask = (K == 32 ? 0xffffffffu : ((1u << K) - 1u)) << (lane & ~(K - 1));
   double lo = prep[0], hi = prep[1];
   const double pivmin = prep[2];
-  for (int it = 0; it < 96; ++it) {
+  for (int it = 0; it < 128; ++it) {
     if (hi - lo <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + 2.0 * pivmin) break;
-    const double h = (hi - lo) / (KSEC + 1);
+    const double h = (hi - lo) / (K + 1);
     const double x = lo + h * (t + 1);
-    const int c = valid ? sturm_count(n, d, e2, x, pivmin) : 0;
+    const int c = valid ? sturm_count(n, d, e2, x) : 0;
     const unsigned le = __ballot_sync(gmask, c <= j) & gmask;
     const int k = __popc(le);
     const double nlo = k > 0 ? lo + h * k : lo;
-    const double nhi = k < KSEC ? lo + h * (k + 1) : hi;
+    const double nhi = k < K ? lo + h * (k + 1) : hi;
     if (!(nlo < nhi) || (nlo == lo && nhi == hi)) break;
     lo = nlo;
     hi = nhi;
   }
   if (valid && t == 0) w[j] = 0.5 * (lo + hi);
+}
+
+void launch_stebz(qk_ctx* ctx, int n, const double* d, const double* e2, const double* prep,
+                  double* w) {
+  const long long slots = 4LL * 32 * ctx->num_sms;  // one warp per SM sub-partition
+  const int K = slots >= 8LL * n ? 8 : slots >= 4LL * n ? 4 : slots >= 2LL * n ? 2 : 1;
+  const int blocks = (int)((K * (long long)n + 127) / 128);
+  switch (K) {
+    case 8: k_stebz<8><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, w); break;
+    case 4: k_stebz<4><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, w); break;
+    case 2: k_stebz<2><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, w); break;
+    default: k_stebz<1><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, w); break;
+  }
 }
 
 __device__ __forceinline__ double rand_pm1(unsigned long long i, unsigned long long j) {
@@ -388,6 +410,13 @@ __device__ __forceinline__ double rand_pm1(unsigned long long i, unsigned long l
   z ^= z >> 27; z *= 0x94D049BB133111EBull;
   z ^= z >> 31;
   return ((double)(z >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;
+}
+
+// reciprocal of a U pivot, tiny pivots perturbed to +-tiny first (stored once, so that the three
+// back substitutions multiply instead of divide on their dependency chain)
+__device__ __forceinline__ double pivot_rcp(double u, double tiny) {
+  if (fabs(u) < tiny) u = (u < 0.0) ? -tiny : tiny;
+  return qk_rcp(u);
 }
 
 // Inverse iteration.  Thread j leads the cluster that starts at eigenvalue j (clusters are
@@ -429,14 +458,16 @@ __global__ void k_stein(int n, const double* __restrict__ d, const double* __res
       const double ak1 = d[k + 1] - x;
       const double bk1 = (k + 1 < n - 1) ? e[k + 1] : 0.0;
       if (fabs(ck) <= fabs(r0)) {
-        const double m = (r0 != 0.0) ? ck / r0 : 0.0;
-        at(U0, k) = r0; at(U1, k) = r1; at(U2, k) = r2; at(ML, k) = m; at(SW, k) = 0.0;
+        const double m = (r0 != 0.0) ? ck * qk_rcp(r0) : 0.0;
+        at(U0, k) = pivot_rcp(r0, tiny); at(U1, k) = r1; at(U2, k) = r2; at(ML, k) = m;
+        at(SW, k) = 0.0;
         r0 = ak1 - m * r1;
         r1 = bk1 - m * r2;
         r2 = 0.0;
       } else {
-        const double m = r0 / ck;
-        at(U0, k) = ck; at(U1, k) = ak1; at(U2, k) = bk1; at(ML, k) = m; at(SW, k) = 1.0;
+        const double m = r0 * qk_rcp(ck);
+        at(U0, k) = pivot_rcp(ck, tiny); at(U1, k) = ak1; at(U2, k) = bk1; at(ML, k) = m;
+        at(SW, k) = 1.0;
         const double n0 = r1 - m * ak1;
         const double n1 = r2 - m * bk1;
         r0 = n0;
@@ -444,7 +475,7 @@ __global__ void k_stein(int n, const double* __restrict__ d, const double* __res
         r2 = 0.0;
       }
     }
-    at(U0, n - 1) = r0; at(U1, n - 1) = 0.0; at(U2, n - 1) = 0.0;
+    at(U0, n - 1) = pivot_rcp(r0, tiny); at(U1, n - 1) = 0.0; at(U2, n - 1) = 0.0;
     // ---- start vector ----
     for (int i = 0; i < n; ++i) Zt[(size_t)jj + N * i] = rand_pm1(i, jj);
     for (int it = 0; it < 3; ++it) {
@@ -471,9 +502,7 @@ __global__ void k_stein(int n, const double* __restrict__ d, const double* __res
       // back substitution with U (tiny pivots perturbed)
       double y1 = 0.0, y2 = 0.0;
       for (int k = n - 1; k >= 0; --k) {
-        double u = at(U0, k);
-        if (fabs(u) < tiny) u = (u < 0.0) ? -tiny : tiny;
-        const double yv = (Zt[(size_t)jj + N * k] - at(U1, k) * y1 - at(U2, k) * y2) / u;
+        const double yv = (Zt[(size_t)jj + N * k] - at(U1, k) * y1 - at(U2, k) * y2) * at(U0, k);
         Zt[(size_t)jj + N * k] = yv;
         y2 = y1;
         y1 = yv;
@@ -615,7 +644,7 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   if (tm) qk_tic(ctx, T_BISECT);
   k_tri_prep<<<1, 1024, 0, ctx->stream>>>(n, d, e, e2, prep);
   QK_LAUNCHED();
-  k_stebz<<<(n * KSEC + 127) / 128, 128, 0, ctx->stream>>>(n, d, e2, prep, w);
+  launch_stebz(ctx, n, d, e2, prep, w);
   QK_LAUNCHED();
   if (tm) qk_toc(ctx, T_BISECT);
   if (!want_vectors) return QK_OK;

@@ -233,6 +233,19 @@ __device__ __forceinline__ bool qk_grid_barrier(unsigned* counter, unsigned nblo
   return s_ok != 0;
 }
 
+// 1/x in FP64: the hardware's approximate FP64 reciprocal (rcp.approx.ftz.f64) refined by two
+// Newton-Raphson steps r <- r (2 - x r), each of which squares the relative error; magnitudes
+// outside [1e-300, 1e300] (where the approximation flushes) take the IEEE division.
+__device__ __forceinline__ double qk_rcp(double x) {
+  const double ax = fabs(x);
+  if (!(ax > 1e-300 && ax < 1e300)) return 1.0 / x;
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  r = r * fma(-x, r, 2.0);
+  r = r * fma(-x, r, 2.0);
+  return r;
+}
+
 template <class T>
 __device__ __forceinline__ T qk_block_sum(T v, T* red /* >= 32 entries */) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
