@@ -325,18 +325,24 @@ def run_ours(args):
 def run_batched(args, ctx):
     """Batched evGW on a subset of the 256-system configuration (seed 1, N ~ U{24..160},
     nO = floor(N/8 + 1/2), naux = 3N, at most 5 cycles at 1e-5 Ha, DIIS 5, Newton QP), all
-    systems in one qk_gw_batch_L_dev call over several streams; plain FP64 vs BF16x3."""
+    systems in one qk_gw_batch_L_dev call over several streams; plain FP64 vs BF16x3.  Under
+    torchrun the systems are spread over the ranks by cost (quack_gb300.shard, no data-path
+    collective) and the time is the slowest rank's."""
     import numpy as np
     import torch
-    from quack_gb300 import api, synth
+    from quack_gb300 import api, shard, synth
 
-    systems = synth.batch_systems(256, 24, 160, seed=1)[: args.batch_systems]
+    ws, rank, _ = dist_env()
+    allsys = synth.batch_systems(256, 24, 160, seed=1)[: args.batch_systems]
+    mine = shard.partition([shard.cost(s["N"], s["nO"]) for s in allsys], ws)[rank]
+    systems = [allsys[i] for i in mine]
     desc, Lf, Ef = api.pack_systems(systems)
     dL = torch.from_numpy(Lf).cuda()
     dE = torch.from_numpy(Ef).cuda()
-    out = {"systems": len(systems), "N": [s["N"] for s in systems],
+    out = {"systems": len(allsys), "N": [s["N"] for s in allsys],
            "config": "evGW maxSCF=4 (<=5 cycles) thresh 1e-5 DIIS 5 Newton QP; 256-system "
-                     "generator seed 1, first %d systems" % len(systems)}
+                     "generator seed 1, first %d systems" % len(allsys),
+           "sharding": "systems spread over %d rank(s) by nS^3 cost" % ws}
     res = {}
     for tier, name in ((api.QK_PREC_BF16X3, "mixed"), (api.QK_PREC_FP64, "plain_fp64")):
         opts = api.GWOptions(maxSCF=4, thresh=1e-5, max_diis=5, precision=tier)
@@ -344,15 +350,24 @@ def run_batched(args, ctx):
         api.gw_batch_L_dev(opts, 1, desc, dL.data_ptr(), dE.data_ptr(), dG.data_ptr(),
                            n_workers=args.batch_workers, ctx=ctx)   # warm-up (workspaces)
         torch.cuda.synchronize()
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
         t0 = time.time()
         r = api.gw_batch_L_dev(opts, 1, desc, dL.data_ptr(), dE.data_ptr(), dG.data_ptr(),
                                n_workers=args.batch_workers, ctx=ctx)
         torch.cuda.synchronize()
         dt = time.time() - t0
+        if ws > 1:
+            import torch.distributed as dist
+            t = torch.tensor([dt], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
         res[name] = dG.cpu().numpy()
-        out[name] = {"value": len(systems) / dt, "unit": "systems/s", "seconds": dt,
-                     "cycles": int(r["nSCF"].sum()), "not_converged": int((r["status"] == 5).sum()),
-                     "errors": int(((r["status"] != 0) & (r["status"] != 5)).sum())}
+        out[name] = {"value": len(allsys) / dt, "unit": "systems/s", "seconds": dt,
+                     "cycles_rank0": int(r["nSCF"].sum()),
+                     "not_converged_rank0": int((r["status"] == 5).sum()),
+                     "errors_rank0": int(((r["status"] != 0) & (r["status"] != 5)).sum())}
     d = np.abs(res["mixed"] - res["plain_fp64"])
     out["speedup_mixed_vs_plain"] = out["mixed"]["value"] / out["plain_fp64"]["value"]
     out["qp_max_abs_diff_Ha"] = float(d.max())
