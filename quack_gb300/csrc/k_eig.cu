@@ -27,7 +27,7 @@ constexpr int TRI_SMEM_MAX = 227 * 1024 - 1024;  // tiles + (when they fit) the 
 constexpr int TRI_TC = 16;          // columns per lower-triangle tile of the fused pass
 constexpr int TRI_TLD = 33;         // padded leading dimension of a warp's shared tile
 constexpr int TRI_TILE_BYTES = (TRI_THREADS / 32) * TRI_TC * TRI_TLD * 8;
-constexpr int BT_NB = 64;           // reflectors per compact-WY block
+constexpr int BT_NB = 128;          // reflectors per compact-WY block
 constexpr double CLUSTER_REL = 1e-7;  // eigenvalues closer than this * ||T||_1 share a cluster
 
 // Sum over the CTA with few FP64 operations (the FP64 pipe is the scarce resource here): the
@@ -532,30 +532,80 @@ __global__ void k_stein(int n, const double* __restrict__ d, const double* __res
   }
 }
 
-// Forward compact-WY T factor (upper triangular) for nb reflectors from G = V^T V.
-__global__ void k_larft(int nb, const double* __restrict__ G, const double* __restrict__ tau,
-                        double* __restrict__ T) {
-  // single block, nb <= 64 threads used
-  __shared__ double sT[BT_NB][BT_NB + 1];
-  __shared__ double z[BT_NB];
-  const int t = threadIdx.x;
-  for (int idx = t; idx < BT_NB * (BT_NB + 1); idx += blockDim.x) (&sT[0][0])[idx] = 0.0;
+// Forward compact-WY T factors (upper triangular, dlarft 'F','C') of every reflector block,
+// one CTA per block: T_ii = tau_i, T(0:i, i) = -tau_i T(0:i, 0:i) G(0:i, i) with G = V_b^T V_b.
+// G and T are BT_NB x BT_NB per block (leading dimension BT_NB); the last block may hold fewer
+// than BT_NB reflectors (the rest of its T is zero).
+constexpr int LARFT_SMEM = (BT_NB * (BT_NB + 1) + BT_NB) * 8;
+__global__ void __launch_bounds__(BT_NB) k_larft_all(int nref, const double* __restrict__ G,
+                                                     const double* __restrict__ tau,
+                                                     double* __restrict__ T) {
+  extern __shared__ double lsm[];
+  double* sT = lsm;                       // [BT_NB][BT_NB + 1]
+  double* z = lsm + BT_NB * (BT_NB + 1);  // [BT_NB]
+  const int b = blockIdx.x, t = threadIdx.x;
+  const int kb = b * BT_NB;
+  const int nb = (nref - kb) < BT_NB ? (nref - kb) : BT_NB;
+  const double* Gb = G + (size_t)b * BT_NB * BT_NB;
+  const double* tb = tau + kb;
+  for (int idx = t; idx < BT_NB * (BT_NB + 1); idx += blockDim.x) sT[idx] = 0.0;
   __syncthreads();
   for (int i = 0; i < nb; ++i) {
-    if (t < i) z[t] = G[t + nb * i];
+    if (t < i) z[t] = Gb[t + BT_NB * i];
     __syncthreads();
     if (t < i) {
-      double s = 0.0;
-      for (int c = t; c < i; ++c) s += sT[t][c] * z[c];
-      sT[t][i] = -tau[i] * s;
+      double s0 = 0.0, s1 = 0.0;
+      int c = t;
+      for (; c + 1 < i; c += 2) {
+        s0 = fma(sT[t * (BT_NB + 1) + c], z[c], s0);
+        s1 = fma(sT[t * (BT_NB + 1) + c + 1], z[c + 1], s1);
+      }
+      if (c < i) s0 = fma(sT[t * (BT_NB + 1) + c], z[c], s0);
+      sT[t * (BT_NB + 1) + i] = -tb[i] * (s0 + s1);
     }
-    if (t == 0) sT[i][i] = tau[i];
+    if (t == 0) sT[i * (BT_NB + 1) + i] = tb[i];
     __syncthreads();
   }
-  for (int idx = t; idx < nb * nb; idx += blockDim.x) {
-    const int r = idx % nb, c = idx / nb;
-    T[idx] = sT[r][c];
+  double* Tb = T + (size_t)b * BT_NB * BT_NB;
+  for (int idx = t; idx < BT_NB * BT_NB; idx += blockDim.x) {
+    const int r = idx % BT_NB, c = idx / BT_NB;
+    Tb[idx] = sT[r * (BT_NB + 1) + c];
   }
+}
+
+// T factors of all reflector blocks of the last tridiagonalisation on this context:
+// G_b = V_b^T V_b for the full blocks in one batched GEMM (V is zero above its unit diagonal,
+// so all n rows can be used), the last partial block on its own, then k_larft_all.
+int eig_tfactors(qk_ctx* ctx, int n, const double* V, const double* tau, const double** T_out) {
+  const int nref = n - 2;
+  const int nblk = (nref + BT_NB - 1) / BT_NB;
+  const size_t B2 = (size_t)BT_NB * BT_NB;
+  double* buf = nullptr;
+  QK_TRY(qk_wst(ctx, W_TFAC, 2 * B2 * nblk + 16, &buf));
+  double* G = buf;
+  double* T = buf + B2 * nblk;
+  const int full = nref / BT_NB;
+  const long long bstride = (long long)n * BT_NB;
+  if (full > 0)
+    QK_TRY(qk_dgemm(ctx, 'T', 'N', BT_NB, BT_NB, n, 1.0, V, n, bstride, V, n, bstride, 0.0, G,
+                    BT_NB, (long long)B2, full));
+  if (full < nblk) {
+    const int kb = full * BT_NB, nb = nref - kb;
+    const double* Vb = V + (size_t)n * kb;
+    QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, nb, n, 1.0, Vb, n, 0, Vb, n, 0, 0.0, G + B2 * full, BT_NB,
+                    0, 1));
+  }
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
+    attr_err = cudaFuncSetAttribute(k_larft_all, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    LARFT_SMEM);
+  });
+  QK_CK(attr_err);
+  k_larft_all<<<nblk, BT_NB, LARFT_SMEM, ctx->stream>>>(nref, G, tau, T);
+  QK_LAUNCHED();
+  *T_out = T;
+  return QK_OK;
 }
 
 }  // namespace
@@ -661,25 +711,22 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   if (tm) qk_tic(ctx, T_BACKTRANS);
   const int nref = n - 2;  // reflectors 0..n-3 can be non-trivial
   if (nref > 0) {
-    double *W1 = nullptr, *W2 = nullptr, *G = nullptr, *T = nullptr;
+    const double* Tall = nullptr;
+    QK_TRY(eig_tfactors(ctx, n, V, tau, &Tall));
     double* bt = nullptr;
-    QK_TRY(qk_wst(ctx, W_PART, 2 * N * BT_NB + 2 * BT_NB * BT_NB, &bt));
-    W1 = bt;
-    W2 = bt + N * BT_NB;
-    G = bt + 2 * N * BT_NB;
-    T = G + BT_NB * BT_NB;
+    QK_TRY(qk_wst(ctx, W_PART, 2 * N * BT_NB, &bt));
+    double* W1 = bt;
+    double* W2 = bt + N * BT_NB;
     const int nblk = (nref + BT_NB - 1) / BT_NB;
     for (int b = nblk - 1; b >= 0; --b) {
       const int kb = b * BT_NB;
       const int nb = (nref - kb) < BT_NB ? (nref - kb) : BT_NB;
       const int m = n - kb - 1;
       const double* Vb = V + (kb + 1) + N * kb;
+      const double* Tb = Tall + (size_t)b * BT_NB * BT_NB;
       double* Es = Zt + N * (kb + 1);
-      QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, nb, m, 1.0, Vb, n, 0, Vb, n, 0, 0.0, G, nb, 0, 1));
-      k_larft<<<1, 64, 0, ctx->stream>>>(nb, G, tau + kb, T);
-      QK_LAUNCHED();
       QK_TRY(qk_dgemm(ctx, 'N', 'N', n, nb, m, 1.0, Es, n, 0, Vb, n, 0, 0.0, W1, n, 0, 1));
-      QK_TRY(qk_dgemm(ctx, 'N', 'T', n, nb, nb, 1.0, W1, n, 0, T, nb, 0, 0.0, W2, n, 0, 1));
+      QK_TRY(qk_dgemm(ctx, 'N', 'T', n, nb, nb, 1.0, W1, n, 0, Tb, BT_NB, 0, 0.0, W2, n, 0, 1));
       QK_TRY(qk_dgemm(ctx, 'N', 'T', n, m, nb, -1.0, W2, n, 0, Vb, n, 0, 1.0, Es, n, 0, 1));
     }
   }
@@ -698,24 +745,22 @@ int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols) {
   QK_TRY(qk_wst(ctx, W_V, N * N, &V));
   QK_TRY(qk_wst(ctx, W_TRI, 8 * N + 64, &tri));
   double* tau = tri + 2 * N;
-  QK_TRY(qk_wst(ctx, W_PART, 2 * (size_t)ncols * BT_NB + 2 * BT_NB * BT_NB + 2 * N * BT_NB, &bt));
+  const double* Tall = nullptr;
+  QK_TRY(eig_tfactors(ctx, n, V, tau, &Tall));
+  QK_TRY(qk_wst(ctx, W_PART, 2 * (size_t)ncols * BT_NB, &bt));
   double* W1 = bt;
   double* W2 = bt + (size_t)ncols * BT_NB;
-  double* G = W2 + (size_t)ncols * BT_NB;
-  double* T = G + BT_NB * BT_NB;
   const int nblk = (nref + BT_NB - 1) / BT_NB;
   for (int b = 0; b < nblk; ++b) {
     const int kb = b * BT_NB;
     const int nb = (nref - kb) < BT_NB ? (nref - kb) : BT_NB;
     const int m = n - kb - 1;
     const double* Vb = V + (kb + 1) + N * kb;
+    const double* Tb = Tall + (size_t)b * BT_NB * BT_NB;
     double* Xs = X + (kb + 1);
-    QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, nb, m, 1.0, Vb, n, 0, Vb, n, 0, 0.0, G, nb, 0, 1));
-    k_larft<<<1, 64, 0, ctx->stream>>>(nb, G, tau + kb, T);
-    QK_LAUNCHED();
     // W1 = V^T X (nb x ncols), W2 = T^T W1, X -= V W2
     QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, ncols, m, 1.0, Vb, n, 0, Xs, ldx, 0, 0.0, W1, nb, 0, 1));
-    QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, ncols, nb, 1.0, T, nb, 0, W1, nb, 0, 0.0, W2, nb, 0, 1));
+    QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, ncols, nb, 1.0, Tb, BT_NB, 0, W1, nb, 0, 0.0, W2, nb, 0, 1));
     QK_TRY(qk_dgemm(ctx, 'N', 'N', m, ncols, nb, -1.0, Vb, n, 0, W2, nb, 0, 1.0, Xs, ldx, 0, 1));
   }
   return QK_OK;
