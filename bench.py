@@ -286,11 +286,20 @@ def run_ours(args):
                        "unit": unit, "frac": ach / peak, "peak_source": pk, "work": desc})
     stages.sort(key=lambda d: -d["ms"])
     traffic = load_traffic()
-    top = dict(stages[0]) if stages else None
+    # the dominant single kernel: k_sytrd (one launch per Casida, two per G0W0 step; the
+    # back-transform stage is split over many GEMM launches)
+    top = next((dict(d) for d in stages if d["kernel"] == "tridiag"),
+               dict(stages[0]) if stages else None)
     if top is not None:
-        top["traffic"] = traffic.get(top["kernel"])
+        if top["kernel"] == "tridiag":
+            top["kernel"] = "k_sytrd (tridiagonalisation, one launch)"
+            top["launches_per_step"] = 2
+            top["traffic"] = traffic.get("k_sytrd")
+        else:
+            top["traffic"] = traffic.get(top["kernel"])
         if top["bound"] == "fp64":
-            top["note"] = "FP64-issue-bound stage; peak = measured FP64 rate of this GPU"
+            top["note"] = ("FP64-issue-bound kernel; achieved = LAPACK flop count / CUDA-event time "
+                           "of the launch; peak = measured FP64 rate of this GPU")
     rho_stage = next((d for d in stages if d["kernel"] == "rho"), None)
 
     value = ws * K / (ms_mix * 1e-3)
@@ -511,6 +520,64 @@ def run_reference(args):
     print(json.dumps(res))
 
 
+def run_profile_case(args):
+    """One small, self-contained case of a single kernel family, for ncu captures (prints one
+    JSON line of CUDA-event times; not a bench result).
+      tridiag   : eigenvalues of a random symmetric n x n matrix (k_sytrd + k_stebz)
+      g0w0_L    : the N=200 G0W0 from its factor L (no N^4 tensor on the device), mixed tier
+      g0w0_mixed: the bench's G0W0 step, mixed tier only (launch list of one step)"""
+    import numpy as np
+    import torch
+    from quack_gb300 import api, synth
+
+    ctx = api.Context(0)
+    out = {"case": args.profile_case}
+    if args.profile_case == "tridiag":
+        n = args.case_n
+        A = np.random.default_rng(n).standard_normal((n, n))
+        A = A + A.T
+        dA0 = torch.from_numpy(np.asfortranarray(A).ravel(order="F")).cuda()
+        dw = torch.empty(n, dtype=torch.float64, device="cuda")
+        ts = []
+        for _ in range(args.case_reps):
+            dA = dA0.clone()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            api.dsyev_dev(n, dA.data_ptr(), n, dw.data_ptr(), 0, False, ctx=ctx)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        out.update(n=n, ms=ts)
+    else:
+        N, nO, naux, seed = WORKLOAD["N"], WORKLOAD["nO"], WORKLOAD["naux"], WORKLOAD["seed"]
+        nS = nO * (N - nO)
+        s = synth.gen_system(N, nO, naux, np.random.default_rng(seed))
+        de = torch.from_numpy(s["eHF"]).cuda()
+        b = [torch.empty(N, dtype=torch.float64, device="cuda") for _ in range(3)]
+        dOm = torch.empty(nS, dtype=torch.float64, device="cuda")
+        opts = api.GWOptions(precision=api.QK_PREC_BF16X3)
+        if args.profile_case == "g0w0_L":
+            dL = torch.from_numpy(api.L_fortran_flat(s["L"])).cuda()
+            run = lambda: api.RG0W0_L_dev(opts, N, 0, nO, 0, naux, dL.data_ptr(), de.data_ptr(),
+                                          b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr(),
+                                          dOm.data_ptr(), ctx=ctx)
+        else:
+            dE = synth.eri_fortran_flat_torch(s["L"], device="cuda")
+            run = lambda: api.RG0W0_dev(opts, N, 0, nO, 0, dE.data_ptr(), de.data_ptr(),
+                                        b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr(),
+                                        dOm.data_ptr(), ctx=ctx)
+        stages = []
+        for _ in range(args.case_reps):
+            torch.cuda.synchronize()
+            run()
+            torch.cuda.synchronize()
+            stages.append(ctx.timings())
+        out.update(stages=stages, qp_evals=ctx.qp_evals())
+    print(json.dumps(out))
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -527,8 +594,14 @@ def main():
     ap.add_argument("--batch-workers", type=int, default=8)
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-systems", type=int, default=120)
+    ap.add_argument("--profile-case", choices=["tridiag", "g0w0_L", "g0w0_mixed"], default=None,
+                    help="run one small kernel case for an ncu capture instead of the bench")
+    ap.add_argument("--case-n", type=int, default=3600)
+    ap.add_argument("--case-reps", type=int, default=1)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_case:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -29,6 +29,7 @@ constexpr int TRI_TLD = 33;         // padded leading dimension of a warp's shar
 constexpr int TRI_TILE_BYTES = (TRI_THREADS / 32) * TRI_TC * TRI_TLD * 8;
 constexpr int BT_NB = 128;          // reflectors per compact-WY block
 constexpr double CLUSTER_REL = 1e-7;  // eigenvalues closer than this * ||T||_1 share a cluster
+constexpr int SB = 8;                 // inverse iteration: steps per batch of prefetched loads
 
 // Sum over the CTA with few FP64 operations (the FP64 pipe is the scarce resource here): the
 // per-thread partials go to shared memory and warp 0 adds them with four independent chains per
@@ -75,7 +76,7 @@ struct TriArgs {
 
 __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
   extern __shared__ double sm[];
-  __shared__ double s_pj, s_dj, s_alpha, s_sc[6];
+  __shared__ double s_pj, s_dj, s_alpha, s_sc[7];
   const int n = a.n;
   double* ytile = sm;  // one TRI_TC x TRI_TLD tile per warp
   double *vk, *wk, *vk1;
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
   const int totwarps = gridDim.x * nwarps;
   const int gthread = blockIdx.x * nt + tid, totthreads = gridDim.x * nt;
-  double tau_k = 0.0;
+  double tau_k = 0.0, scal_k = 1.0;
 
   for (int k = -1; k <= n - 2; ++k) {
     // ---- zero the p accumulator used two iterations ahead (triple buffering) ----
@@ -104,10 +105,13 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
     }
     // ---- small phase (redundant in every CTA): w_k, then v_{k+1} from column j = k+1 ----
     // FP64 is the scarce resource (one warp instruction per 64 cycles per SM sub-partition), so
-    // the passes are fused: p_k and the raw column j are loaded together, one pass forms w_k,
-    // the updated column and its norm, one pass scales the reflector.
+    // the passes are fused: p_k and the raw column j are loaded together and one pass forms w_k,
+    // the updated column and its norm.  The reflector is kept unscaled, u = v / scal with
+    // u_{j+1} = 1/scal: the scale factor goes into the scalars of the next step instead of a
+    // pass over the vector (the big pass computes p~ = A' u, so p = scal p~, and with
+    // w' = scal w the update A - v w^T - w v^T = A - u w'^T - w' u^T keeps its form).
     const int j = k + 1;
-    double tau1 = 0.0;
+    double tau1 = 0.0, scal1 = 1.0;
     {
       const double* p = a.pbuf + (size_t)((k + 3) % 3) * n;
       double dot = 0.0;
@@ -123,24 +127,28 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       if (k >= 0) {
         // (the barriers publish vk1, wk and s_pj as well)
         tri_block_sum(dot, ytile, [&](double t) {
-          const double cc = 0.5 * tau_k * tau_k * t;
-          const double v = vk[j];
-          s_sc[0] = cc;
-          s_sc[1] = v;
-          s_sc[2] = tau_k * s_pj - cc * v;
+          // true dot p.v = scal^2 p~.u;  c = tau^2 dot / 2;  w' = scal^2 (tau p~ - c u)
+          const double s2 = scal_k * scal_k;
+          const double cc = 0.5 * tau_k * tau_k * (s2 * t);
+          const double a1 = tau_k * s2, a2 = cc * s2;
+          const double u = vk[j];
+          s_sc[0] = a1;
+          s_sc[1] = a2;
+          s_sc[2] = u;
+          s_sc[6] = a1 * s_pj - a2 * u;
         });
       } else {
-        if (tid == 0) s_sc[0] = s_sc[1] = s_sc[2] = 0.0;
+        if (tid == 0) s_sc[0] = s_sc[1] = s_sc[2] = s_sc[6] = 0.0;
         __syncthreads();
       }
-      const double c = s_sc[0], vj = s_sc[1], wj = s_sc[2];
+      const double a1 = s_sc[0], a2 = s_sc[1], uj = s_sc[2], wj = s_sc[6];
       double ss = 0.0;
       for (int i = j + tid; i < n; i += nt) {
         double x = vk1[i];
         if (k >= 0) {
-          const double w = tau_k * wk[i] - c * vk[i];
+          const double w = a1 * wk[i] - a2 * vk[i];
           wk[i] = w;
-          x = x - vk[i] * wj - w * vj;
+          x = x - vk[i] * wj - w * uj;
           vk1[i] = x;
         }
         if (i == j) s_dj = x;
@@ -149,7 +157,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       }
       // Householder reflector of the updated column (dlarfg), computed once by thread 0
       tri_block_sum(ss, ytile, [&](double sigma) {
-        double beta = 0.0, t1 = 0.0, scal = 1.0;
+        double beta = 0.0, t1 = 0.0, scal = 1.0, inv = 1.0;
         if (j <= n - 2) {
           const double alpha = s_alpha;
           if (sigma == 0.0) {
@@ -157,8 +165,10 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
           } else {
             beta = -copysign(sqrt(alpha * alpha + sigma), alpha);
             t1 = (beta - alpha) / beta;
-            scal = 1.0 / (alpha - beta);
+            inv = alpha - beta;
+            scal = 1.0 / inv;
           }
+          vk1[j + 1] = inv;  // u_{j+1} = 1/scal, so that scal * u_{j+1} = 1
         }
         s_sc[3] = beta;
         s_sc[4] = t1;
@@ -166,14 +176,11 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       });
       const double dj = s_dj;
       tau1 = s_sc[4];
-      if (j <= n - 2) {
-        const double beta = s_sc[3], scal = s_sc[5];
-        for (int i = j + 1 + tid; i < n; i += nt) vk1[i] = (i == j + 1) ? 1.0 : vk1[i] * scal;
-        __syncthreads();
-        if (blockIdx.x == 0) {
-          if (tid == 0) { a.e[j] = beta; a.tau[j] = tau1; }
-          for (int i = j + 1 + tid; i < n; i += nt) a.V[i + a.ldv * j] = vk1[i];
-        }
+      scal1 = s_sc[5];
+      if (j <= n - 2 && blockIdx.x == 0) {
+        if (tid == 0) { a.e[j] = s_sc[3]; a.tau[j] = tau1; }
+        for (int i = j + 1 + tid; i < n; i += nt)
+          a.V[i + a.ldv * j] = (i == j + 1) ? 1.0 : vk1[i] * scal1;
       }
       if (blockIdx.x == 0 && tid == 0) a.d[j] = dj;
     }
@@ -268,6 +275,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
     vk = vk1;
     vk1 = t;
     tau_k = tau1;
+    scal_k = scal1;
   }
 }
 
@@ -483,9 +491,34 @@ __global__ void k_stein(int n, const double* __restrict__ d, const double* __res
       double mx = 0.0;
       for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(Zt[(size_t)jj + N * i]));
       const double sc = mx > 0.0 ? 1.0 / mx : 1.0;
-      // forward: apply P and L^{-1}
+      // forward: apply P and L^{-1}.  The loads of a batch of SB steps are issued before its
+      // stores (they read entries the batch has not written yet), so the memory latency is paid
+      // once per batch instead of once per step of the dependency chain.
       double yk = Zt[jj] * sc;
-      for (int k = 0; k < n - 1; ++k) {
+      int k = 0;
+      for (; k + SB <= n - 1; k += SB) {
+        double zv[SB], mv[SB], sv[SB];
+#pragma unroll
+        for (int u = 0; u < SB; ++u) {
+          zv[u] = Zt[(size_t)jj + N * (k + 1 + u)];
+          mv[u] = at(ML, k + u);
+          sv[u] = at(SW, k + u);
+        }
+#pragma unroll
+        for (int u = 0; u < SB; ++u) {
+          double yk1 = zv[u] * sc;
+          if (sv[u] != 0.0) {
+            const double t = yk;
+            yk = yk1;
+            yk1 = t - mv[u] * yk;
+          } else {
+            yk1 = yk1 - mv[u] * yk;
+          }
+          Zt[(size_t)jj + N * (k + u)] = yk;
+          yk = yk1;
+        }
+      }
+      for (; k < n - 1; ++k) {
         double yk1 = Zt[(size_t)jj + N * (k + 1)] * sc;
         const double m = at(ML, k);
         if (at(SW, k) != 0.0) {
@@ -499,9 +532,27 @@ __global__ void k_stein(int n, const double* __restrict__ d, const double* __res
         yk = yk1;
       }
       Zt[(size_t)jj + N * (n - 1)] = yk;
-      // back substitution with U (tiny pivots perturbed)
+      // back substitution with U (pivots stored as reciprocals), batched the same way
       double y1 = 0.0, y2 = 0.0;
-      for (int k = n - 1; k >= 0; --k) {
+      k = n - 1;
+      for (; k - SB + 1 >= 0; k -= SB) {
+        double zv[SB], a0[SB], a1[SB], a2[SB];
+#pragma unroll
+        for (int u = 0; u < SB; ++u) {
+          zv[u] = Zt[(size_t)jj + N * (k - u)];
+          a0[u] = at(U0, k - u);
+          a1[u] = at(U1, k - u);
+          a2[u] = at(U2, k - u);
+        }
+#pragma unroll
+        for (int u = 0; u < SB; ++u) {
+          const double yv = (zv[u] - a1[u] * y1 - a2[u] * y2) * a0[u];
+          Zt[(size_t)jj + N * (k - u)] = yv;
+          y2 = y1;
+          y1 = yv;
+        }
+      }
+      for (; k >= 0; --k) {
         const double yv = (Zt[(size_t)jj + N * k] - at(U1, k) * y1 - at(U2, k) * y2) * at(U0, k);
         Zt[(size_t)jj + N * k] = yv;
         y2 = y1;

@@ -1,4 +1,4 @@
-// k_gemm64.cu -- FP64 GEMM on the FP64 tensor path (DMMA, mma.sync.m8n8k4.f64).
+// k_gemm64.cu -- FP64 GEMM: the FP64 tensor path (DMMA, mma.sync.m8n8k4.f64) and a DFMA path.
 //
 // Column-major C = alpha*op(A)*op(B) + beta*C, strided batch.  Used for the AO->MO quarter
 // transforms (AOtoMO/AOtoMO_ERI_RHF.f90:26-53), the FP64 excitation density
@@ -141,6 +141,126 @@ __global__ void __launch_bounds__(128) k_dgemm_dmma(int M, int N, int K, double 
   }
 }
 
+// The same GEMM on the FP64 FMA path (DFMA).  On GB300 DFMA and DMMA share one FP64 datapath
+// and DFMA issues slightly faster (1.2 vs 1.05 TFLOP/s measured), so a plain register-tiled
+// kernel can beat the tensor path: 256 threads, each a 4x4 block of C (rows tx + 16 i, columns
+// ty + 16 j) with 16 independent FMA chains, 8 shared loads per 16 DFMA.
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) k_dgemm_simt(int M, int N, int K, double alpha,
+                                                     const double* __restrict__ A, long long lda,
+                                                     long long sA, const double* __restrict__ B,
+                                                     long long ldb, long long sB, double beta,
+                                                     double* __restrict__ C, long long ldc,
+                                                     long long sC, int kc) {
+  __shared__ double As[2][BK][BM];
+  __shared__ double Bs[2][BK][BN];
+  const long long bz = blockIdx.z;
+  int kbeg = 0, kend = K;
+  if (kc > 0) {
+    kbeg = (int)bz * kc;
+    kend = min(K, kbeg + kc);
+    C += bz * sC;
+  } else {
+    A += bz * sA;
+    B += bz * sB;
+    C += bz * sC;
+  }
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+
+  double ra[4], rb[4];
+  auto ldA = [&](int k0) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = tid + r * 256;
+      int mm, kk;
+      if (!TA) { mm = idx & 63; kk = idx >> 6; } else { kk = idx & 15; mm = idx >> 4; }
+      const int gm = m0 + mm, gk = k0 + kk;
+      double v = 0.0;
+      if (gm < M && gk < kend) v = !TA ? A[gm + lda * gk] : A[gk + lda * gm];
+      ra[r] = v;
+    }
+  };
+  auto stA = [&](int st) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = tid + r * 256;
+      int mm, kk;
+      if (!TA) { mm = idx & 63; kk = idx >> 6; } else { kk = idx & 15; mm = idx >> 4; }
+      As[st][kk][mm] = ra[r];
+    }
+  };
+  auto ldB = [&](int k0) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = tid + r * 256;
+      int nn, kk;
+      if (!TB) { kk = idx & 15; nn = idx >> 4; } else { nn = idx & 63; kk = idx >> 6; }
+      const int gn = n0 + nn, gk = k0 + kk;
+      double v = 0.0;
+      if (gn < N && gk < kend) v = !TB ? B[gk + ldb * gn] : B[gn + ldb * gk];
+      rb[r] = v;
+    }
+  };
+  auto stB = [&](int st) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = tid + r * 256;
+      int nn, kk;
+      if (!TB) { kk = idx & 15; nn = idx >> 4; } else { nn = idx & 63; kk = idx >> 6; }
+      Bs[st][kk][nn] = rb[r];
+    }
+  };
+
+  ldA(kbeg);
+  ldB(kbeg);
+  stA(0);
+  stB(0);
+  __syncthreads();
+  int st = 0;
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    const bool more = (k0 + BK) < kend;
+    if (more) { ldA(k0 + BK); ldB(k0 + BK); }
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double af[4], bf[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) af[i] = As[st][kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bf[j] = Bs[st][kk][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(af[i], bf[j], acc[i][j]);
+    }
+    if (more) { stA(st ^ 1); stB(st ^ 1); }
+    __syncthreads();
+    st ^= 1;
+  }
+
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + tx + 16 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gn = n0 + ty + 16 * j;
+      if (gn < N) {
+        double* c = C + gm + ldc * (long long)gn;
+        double v = alpha * acc[i][j];
+        if (beta != 0.0) v += beta * (*c);
+        *c = v;
+      }
+    }
+  }
+}
+
 // C = alpha * sum_s W[s] + beta * C  (split-K reduction, column-major m x n)
 __global__ void k_splitk_reduce(int m, int n, int S, const double* __restrict__ W, double alpha,
                                 double beta, double* __restrict__ C, long long ldc) {
@@ -159,20 +279,25 @@ __global__ void k_splitk_reduce(int m, int n, int S, const double* __restrict__ 
 }
 
 template <bool TA, bool TB>
-void launch(dim3 grid, cudaStream_t st, int m, int n, int k, double alpha, const double* A,
-            long long lda, long long sA, const double* B, long long ldb, long long sB, double beta,
-            double* C, long long ldc, long long sC, int kc) {
-  k_dgemm_dmma<TA, TB><<<grid, 128, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc,
-                                             sC, kc);
+void launch(bool simt, dim3 grid, cudaStream_t st, int m, int n, int k, double alpha,
+            const double* A, long long lda, long long sA, const double* B, long long ldb,
+            long long sB, double beta, double* C, long long ldc, long long sC, int kc) {
+  if (simt)
+    k_dgemm_simt<TA, TB><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C,
+                                               ldc, sC, kc);
+  else
+    k_dgemm_dmma<TA, TB><<<grid, 128, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C,
+                                               ldc, sC, kc);
 }
 
-void launch_any(bool TA, bool TB, dim3 grid, cudaStream_t st, int m, int n, int k, double alpha,
-                const double* A, long long lda, long long sA, const double* B, long long ldb,
-                long long sB, double beta, double* C, long long ldc, long long sC, int kc) {
-  if (!TA && !TB) launch<false, false>(grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
-  else if (!TA && TB) launch<false, true>(grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
-  else if (TA && !TB) launch<true, false>(grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
-  else launch<true, true>(grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+void launch_any(bool simt, bool TA, bool TB, dim3 grid, cudaStream_t st, int m, int n, int k,
+                double alpha, const double* A, long long lda, long long sA, const double* B,
+                long long ldb, long long sB, double beta, double* C, long long ldc, long long sC,
+                int kc) {
+  if (!TA && !TB) launch<false, false>(simt, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+  else if (!TA && TB) launch<false, true>(simt, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+  else if (TA && !TB) launch<true, false>(simt, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+  else launch<true, true>(simt, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
 }
 
 }  // namespace
@@ -190,6 +315,8 @@ int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, c
     return QK_OK;
   }
   const bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
+  // FP64 path: 1 = DFMA (default), 2 = DMMA tensor path; tunable per size of the product
+  const bool simt = qk_tune_get(ctx, TUNE_DGEMM_PATH, (long long)m * n, 1) != 2;
   dim3 grid((m + BM - 1) / BM, (n + BN - 1) / BN, batch);
   if (grid.y > 65535 || grid.z > 65535) return qk_fail(ctx, QK_ERR_ARG, "qk_dgemm: grid too large");
   const long long tiles = (long long)grid.x * grid.y;
@@ -207,7 +334,7 @@ int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, c
       double* W = nullptr;
       QK_TRY(qk_wst(ctx, W_SPLITK, (size_t)S * m * n, &W));
       grid.z = S;
-      launch_any(TA, TB, grid, ctx->stream, m, n, k, 1.0, A, lda, 0, B, ldb, 0, 0.0, W, m,
+      launch_any(simt, TA, TB, grid, ctx->stream, m, n, k, 1.0, A, lda, 0, B, ldb, 0, 0.0, W, m,
                  (long long)m * n, kc);
       QK_LAUNCHED();
       long long total = (long long)m * n;
@@ -218,8 +345,8 @@ int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, c
       return QK_OK;
     }
   }
-  launch_any(TA, TB, grid, ctx->stream, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C,
-             ldc, strideC, 0);
+  launch_any(simt, TA, TB, grid, ctx->stream, m, n, k, alpha, A, lda, strideA, B, ldb, strideB,
+             beta, C, ldc, strideC, 0);
   QK_LAUNCHED();
   return QK_OK;
 }

@@ -174,11 +174,12 @@ __device__ __forceinline__ float rcp32(float x) {
   return r;
 }
 
-// first m in [lo, hi) with OmF[m].x >= v (OmF ascending)
-__device__ __forceinline__ int om_lower_bound(const float2* __restrict__ O, int lo, int hi, float v) {
+// first m in [lo, hi) with Om_hi(m) >= v, Om_hi(m) = O[m - mb].x (ascending)
+__device__ __forceinline__ int om_lower_bound(const float2* __restrict__ O, int mb, int lo, int hi,
+                                              float v) {
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
-    if (__ldg(&O[mid].x) < v) lo = mid + 1;
+    if (O[mid - mb].x < v) lo = mid + 1;
     else hi = mid;
   }
   return lo;
@@ -192,20 +193,41 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float x) {
   hi = t;
 }
 
+constexpr int FF_B = 12;  // terms per batch of independent loads
+
 struct SigFF {
   const float* R;
   const float2* OmF;
   const int* bad;
   float tau;
+  int om_smem;  // stage the chunk's Om pairs in shared memory
 };
 
 __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial_ff(SigArgs a, SigFF f) {
+  // dynamic shared memory: e (N doubles) | e as float pairs (N) | Om pairs of this m chunk
   extern __shared__ double se[];
   __shared__ double ssig[SIG_WARPS][32], sds[SIG_WARPS][32], socc[SIG_WARPS][32];
   const int nl = a.nact ? *a.nact : 0;
   if (a.list && (int)blockIdx.x * 32 >= nl) return;
   const int N = a.N;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) se[i] = a.eq[i];
+  float2* eF = (float2*)(se + N);
+  const int m0 = blockIdx.y * a.mper;
+  const int m1 = min(a.nS, m0 + a.mper);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double e = a.eq[i];
+    const float h = (float)e;
+    se[i] = e;
+    eF[i] = make_float2(h, (float)(e - (double)h));
+  }
+  // Om pairs of the chunk: omp[m - mb] for m0 <= m < m1 (shared copy when it fits)
+  const float2* omp = f.OmF;
+  int mb = 0;
+  if (f.om_smem) {
+    float2* oms = eF + N;
+    for (int i = threadIdx.x; i < m1 - m0; i += blockDim.x) oms[i] = f.OmF[m0 + i];
+    omp = oms;
+    mb = m0;
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int pend = N - a.nR;
   int p;
@@ -222,9 +244,9 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial_ff(SigArgs a, 
   double sig = 0.0, ds = 0.0, so = 0.0;
   if (pok) {
     const double w = a.wp ? a.wp[p] : se[p];
+    const float w_hi = (float)w;
+    const float w_lo = (float)(w - (double)w_hi);
     const long long N1 = N, N2 = N1 * N1;
-    const int m0 = blockIdx.y * a.mper;
-    const int m1 = min(a.nS, m0 + a.mper);
     const bool bad = *f.bad != 0;
     const float* Rp = f.R + p;
     const double* rp = a.rho + p;
@@ -232,25 +254,46 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial_ff(SigArgs a, 
     double Sn_o = 0.0, Sn_v = 0.0, Dn = 0.0;  // near-pole (FP64) parts
     for (int q = a.nC + warp; q < pend; q += SIG_WARPS) {
       const bool occ = q < a.nO;
-      const double c = w - se[q];
-      const float chi = (float)c;
-      const float clo = (float)(c - (double)chi);
+      // c = w - e_q as a float pair, FP32 only: TwoSum of the high parts plus the low parts
+      const float2 eq = eF[q];
+      const float chi = w_hi - eq.x;
+      const float bb = chi - w_hi;
+      const float clo = ((w_hi - (chi - bb)) + (-eq.x - bb)) + (w_lo - eq.y);
       const float sg = occ ? 1.f : -1.f;
       int lo = m0, hi = m1;
       if (!bad) {
         const float ctr = -sg * chi;  // the pole sits at Om = -c (occupied) or Om = c (virtual)
-        lo = om_lower_bound(f.OmF, m0, m1, ctr - f.tau);
-        hi = om_lower_bound(f.OmF, lo, m1, ctr + f.tau);
+        lo = om_lower_bound(omp, mb, m0, m1, ctr - f.tau);
+        hi = om_lower_bound(omp, mb, lo, m1, ctr + f.tau);
       }
-      const float* Rq = Rp + N1 * q;
+      const float* Rq = Rp + N1 * q + N2 * m0;
       float s = 0.f, d = 0.f;
-#pragma unroll 4
-      for (int m = m0; m < m1; ++m) {
-        const float2 o = __ldg(f.OmF + m);
+      int m = m0;
+      // batches of FF_B terms: all loads first (independent), then the arithmetic
+      for (; m + FF_B <= m1; m += FF_B, Rq += FF_B * N2) {
+        float rv[FF_B];
+        float2 ov[FF_B];
+#pragma unroll
+        for (int u = 0; u < FF_B; ++u) {
+          rv[u] = __ldg(Rq + u * N2);
+          ov[u] = omp[m + u - mb];
+        }
+#pragma unroll
+        for (int u = 0; u < FF_B; ++u) {
+          const float e = fmaf(sg, ov[u].x, chi) + fmaf(sg, ov[u].y, clo);
+          float r = rcp32(e);
+          r = (m + u >= lo && m + u < hi) ? 0.f : r;
+          const float t = rv[u] * r;
+          s += t;
+          d = fmaf(t, r, d);
+        }
+      }
+      for (; m < m1; ++m, Rq += N2) {
+        const float2 o = omp[m - mb];
         const float e = fmaf(sg, o.x, chi) + fmaf(sg, o.y, clo);
         float r = rcp32(e);
         r = (m >= lo && m < hi) ? 0.f : r;
-        const float t = __ldg(Rq + N2 * m) * r;
+        const float t = __ldg(Rq) * r;
         s += t;
         d = fmaf(t, r, d);
       }
@@ -575,10 +618,14 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
   a.doSRG = doSRG; a.eta = eta; a.flow = flow;
   a.eq = eq; a.wp = wp; a.Om = Om; a.rho = rho; a.list = list; a.nact = nact; a.part = part;
   if (ptiles > 0 && nS > 0) {
-    if (ff && !doSRG && eta == 0.0) {
-      SigFF f{ff->R, ff->OmF, ff->bad, ff->tau};
-      k_sigma_partial_ff<<<dim3(ptiles, nchunks), SIG_WARPS * 32, N * sizeof(double), ctx->stream>>>(
-          a, f);
+    const size_t base = (size_t)N * (sizeof(double) + sizeof(float2));
+    // the mixed sweep keeps e in shared memory twice; very large N takes the FP64 sweep
+    if (ff && !doSRG && eta == 0.0 && base <= 40 * 1024) {
+      const size_t with_om = base + (size_t)mper * sizeof(float2);
+      const int om_smem = with_om <= 40 * 1024;
+      SigFF f{ff->R, ff->OmF, ff->bad, ff->tau, om_smem};
+      k_sigma_partial_ff<<<dim3(ptiles, nchunks), SIG_WARPS * 32, om_smem ? with_om : base,
+                           ctx->stream>>>(a, f);
     } else {
       k_sigma_partial<<<dim3(ptiles, nchunks), SIG_WARPS * 32, N * sizeof(double), ctx->stream>>>(a);
     }

@@ -7,6 +7,7 @@
 //   sigma_chunks  m chunks per p tile of the pole sweeps, in units of SMs {2,4,8}   (size = nS)
 //   sytrd_grid    CTAs of the cooperative tridiagonalisation, quarters of the SMs {2,3,4}
 //                 (size = n)
+//   dgemm_path    FP64 GEMM on DFMA (1) or on the DMMA tensor path (2)           (size = m*n)
 // qk_autotune times every candidate on buffers of the caller's problem sizes (CUDA events on the
 // context stream, best of two runs) and records the fastest; qk_tune_save / qk_tune_load keep
 // the table as JSON so that a later process starts tuned.
@@ -18,7 +19,7 @@
 #include "qk_internal.cuh"
 
 static const char* k_tune_names[TUNE_NUM] = {"bf16x3_chunk", "splitk_mult", "sigma_chunks",
-                                             "sytrd_grid"};
+                                             "sytrd_grid", "dgemm_path"};
 
 static int bucket_of(long long size) {
   int b = 0;
@@ -180,6 +181,25 @@ int qk_autotune(qk_ctx* ctx, int N, int nS, int flags) {
         if (t < tbest) { tbest = t; best = gq; }
       }
       ctx->tune[TUNE_SYTRD_GRID][bucket_of(nS)] = best;
+    }
+  }
+  // 5. FP64 GEMM path on the back-transformation shapes and the FP64 excitation density
+  {
+    struct Shape { int m, n, k; };
+    const Shape shapes[3] = {{nS, 128, nS}, {nS, nS, 128}, {(int)N2, nS, nS}};
+    for (const Shape& sh : shapes) {
+      const long long key = (long long)sh.m * sh.n;
+      int best = 1;
+      float tbest = 1e30f;
+      for (int path : {1, 2}) {
+        ctx->tune[TUNE_DGEMM_PATH][bucket_of(key)] = path;
+        const float t = time_best(ctx, [&] {
+          return qk_dgemm(ctx, 'N', 'N', sh.m, sh.n, sh.k, 1.0, sh.m == (int)N2 ? A : B, sh.m, 0,
+                          B + nB, sh.k, 0, 0.0, Cm, sh.m, 0, 1);
+        }, 1);
+        if (t < tbest) { tbest = t; best = path; }
+      }
+      ctx->tune[TUNE_DGEMM_PATH][bucket_of(key)] = best;
     }
   }
   cudaStreamSynchronize(ctx->stream);

@@ -492,12 +492,13 @@ def test_autotuner_roundtrip_and_parity(ctx, tmp_path):
     assert ctx.tune_query("bf16x3_chunk", (nS + 63) // 64 * 64) in (1, 2, 4)
     assert ctx.tune_query("splitk_mult", nS) in (1, 2, 4)
     assert ctx.tune_query("sytrd_grid", nS) in (2, 3, 4)
+    assert ctx.tune_query("dgemm_path", nS * nS) in (1, 2)
     path = tmp_path / "tune.json"
     ctx.tune_save(path)
     c2 = api.Context(0)
     c2.tune_load(path)
     for name, size in (("bf16x3_chunk", (nS + 63) // 64 * 64), ("splitk_mult", nS),
-                       ("sytrd_grid", nS)):
+                       ("sytrd_grid", nS), ("dgemm_path", nS * nS)):
         assert c2.tune_query(name, size) == ctx.tune_query(name, size)
     c2.close()
     r = api.RG0W0(api.GWOptions(), N, N, 0, nO, N - nO, 0, nS, E, f["eHF"], ctx=ctx)
