@@ -37,7 +37,8 @@ constexpr double QP_THRESH = 1e-6;  // RGW_QP_graph.f90:39
 
 struct SigArgs {
   int N, nC, nO, nR, nS;
-  int nchunks, mper;  // m chunks and m per chunk
+  int nchunks, mper;  // chunks (all of them) and m per chunk
+  int mchunks, qper;  // mixed sweep: chunk y covers m chunk y % mchunks, q group y / mchunks
   int doSRG;
   double eta, flow;
   const double* eq;    // energies in the poles (e or eOld)
@@ -159,11 +160,12 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial(SigArgs a) {
   }
 }
 
-// Mixed-tier sweep (eta = 0, no SRG).  Same CTA layout and outputs as k_sigma_partial (lanes =
-// orbitals p, CTAs over (p tile, m chunk)), but the 8 warps split the q index and each warp runs
-// over the whole m chunk, so that the per-(p,q) setup is done once: c = w - e_q in FP64 and its
-// float pair (c_hi, c_lo), and the window [lo, hi) of the m with |w - e_q +- Om_m| < tau (Om
-// ascending: two bisections).  Outside the window, eps = (c_hi +- Om_hi) + (c_lo +- Om_lo) is
+// Mixed-tier sweep (eta = 0, no SRG).  Same outputs as k_sigma_partial (lanes = orbitals p, CTAs
+// over (p tile, chunk)), but a chunk is an (m range, q range) pair and the 8 warps split the q
+// of their range, each warp running over the whole m range, so that the per-(p,q) setup is done
+// once: c = w - e_q as a float pair (c_hi, c_lo) by TwoSum in FP32 from float pairs of w and e_q,
+// and the window [lo, hi) of the m with |w - e_q +- Om_m| < tau (Om ascending: two bisections).
+// Splitting q over CTAs keeps the GPU busy when only a few orbitals are still searching.  Outside the window, eps = (c_hi +- Om_hi) + (c_lo +- Om_lo) is
 // accurate to a few FP32 ulps and the term R/eps with R = 2 rho^2 (FP32) runs on the FP32 pipe;
 // the per-(p,q) FP32 partials are added into float-float (TwoSum) accumulators.  Inside the
 // window the term is evaluated exactly as in k_sigma_partial (FP64).  All lanes step through the
@@ -211,7 +213,8 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial_ff(SigArgs a, 
   if (a.list && (int)blockIdx.x * 32 >= nl) return;
   const int N = a.N;
   float2* eF = (float2*)(se + N);
-  const int m0 = blockIdx.y * a.mper;
+  const int mc = blockIdx.y % a.mchunks, qg = blockIdx.y / a.mchunks;
+  const int m0 = mc * a.mper;
   const int m1 = min(a.nS, m0 + a.mper);
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const double e = a.eq[i];
@@ -252,7 +255,8 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial_ff(SigArgs a, 
     const double* rp = a.rho + p;
     float so_h = 0.f, so_l = 0.f, sv_h = 0.f, sv_l = 0.f, d_h = 0.f, d_l = 0.f;
     double Sn_o = 0.0, Sn_v = 0.0, Dn = 0.0;  // near-pole (FP64) parts
-    for (int q = a.nC + warp; q < pend; q += SIG_WARPS) {
+    const int qend = min(pend, a.nC + (qg + 1) * a.qper);
+    for (int q = a.nC + qg * a.qper + warp; q < qend; q += SIG_WARPS) {
       const bool occ = q < a.nO;
       // c = w - e_q as a float pair, FP32 only: TwoSum of the high parts plus the low parts
       const float2 eq = eF[q];
@@ -444,15 +448,23 @@ __global__ void k_qp_restart(int N, int nC, int nR, const double* __restrict__ e
 // one Newton step for every still-active p (RGW_QP_graph.f90:56-76)
 __global__ void k_qp_update(int N, int nchunks, const double* __restrict__ part,
                             const double* __restrict__ eHF, QPState s, int maxit) {
-  if (*s.nact == 0) return;
+  const int nl = *s.nact;
+  if (nl == 0) return;
   const size_t stride = (size_t)nchunks * N;
-  for (int p = threadIdx.x; p < N; p += blockDim.x) {
-    if (!s.active[p]) continue;
+  // one warp per active orbital: the lanes split the chunk partials, then a butterfly
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int idx = warp; idx < nl; idx += nw) {
+    const int p = s.list[idx];
     double sig = 0.0, dsig = 0.0;
-    for (int c = 0; c < nchunks; ++c) {
+    for (int c = lane; c < nchunks; c += 32) {
       sig += part[(size_t)c * N + p];
       dsig += part[(size_t)c * N + p + stride];
     }
+    for (int o = 16; o > 0; o >>= 1) {
+      sig += __shfl_xor_sync(0xffffffffu, sig, o);
+      dsig += __shfl_xor_sync(0xffffffffu, dsig, o);
+    }
+    if (lane != 0) continue;
     const int nIt = s.nit[p] + 1;
     s.nit[p] = nIt;
     s.evals[p] += 1;
@@ -599,28 +611,47 @@ __global__ void k_diis(int n_err, int n_e, int nd_host, double* __restrict__ err
 static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                        int nS, const double* eq, const double* wp, const double* Om,
                        const double* rho, const int* list, const int* nact, double** part_out,
-                       int* nchunks_out, const qk_sigma_ff* ff = nullptr) {
-  const int nact_p = N - nR - nC;
+                       int* nchunks_out, const qk_sigma_ff* ff = nullptr, int nact_max = -1) {
+  // p tiles: all orbitals, or (with a compacted list) an upper bound on the active count
+  int nact_p = N - nR - nC;
+  if (list && nact_max >= 0 && nact_max < nact_p) nact_p = nact_max;
   const int ptiles = (nact_p + 31) / 32;
   const int cm = qk_tune_get(ctx, TUNE_SIGMA_CHUNKS, (long long)nS, 4);
-  int nchunks = (cm * ctx->num_sms + ptiles - 1) / (ptiles > 0 ? ptiles : 1);
-  const int maxch = (nS + SIG_WARPS - 1) / SIG_WARPS;
-  if (nchunks > maxch) nchunks = maxch;
-  if (nchunks < 1) nchunks = 1;
-  const int mper = (nS + nchunks - 1) / nchunks;
-  nchunks = (nS + mper - 1) / mper;
+  const int target = (cm * ctx->num_sms + (ptiles > 0 ? ptiles : 1) - 1) / (ptiles > 0 ? ptiles : 1);
+  const size_t base = (size_t)N * (sizeof(double) + sizeof(float2));
+  // the mixed sweep keeps e in shared memory twice; very large N takes the FP64 sweep
+  const bool use_ff = ff && !doSRG && eta == 0.0 && base <= 40 * 1024;
+  int mchunks = target;
+  int maxch = (nS + SIG_WARPS - 1) / SIG_WARPS;
+  if (use_ff) maxch = (nS + 2 * FF_B - 1) / (2 * FF_B);  // at least two load batches per q
+  if (mchunks > maxch) mchunks = maxch;
+  if (mchunks < 1) mchunks = 1;
+  const int mper = (nS + mchunks - 1) / mchunks;
+  mchunks = (nS + mper - 1) / mper;
+  // mixed sweep: when few orbitals are active, the q range is split over CTAs too
+  const int nq = N - nR - nC;
+  int qgroups = 1;
+  if (use_ff) {
+    const int gmax = nq / (2 * SIG_WARPS) > 1 ? nq / (2 * SIG_WARPS) : 1;
+    qgroups = target / mchunks;
+    if (qgroups > gmax) qgroups = gmax;
+    if (qgroups < 1) qgroups = 1;
+  }
+  int qper = (nq + qgroups - 1) / qgroups;
+  qper = (qper + SIG_WARPS - 1) / SIG_WARPS * SIG_WARPS;
+  qgroups = (nq + qper - 1) / qper;
+  if (qgroups < 1) qgroups = 1;
+  const int nchunks = mchunks * qgroups;
   double* part = nullptr;
   // every (chunk, p) entry the consumers read is written by the sweep: no clearing needed
   QK_TRY(qk_wst(ctx, W_MISC, (size_t)3 * nchunks * N + 64, &part));
   SigArgs a;
   a.N = N; a.nC = nC; a.nO = nO; a.nR = nR; a.nS = nS;
-  a.nchunks = nchunks; a.mper = mper;
+  a.nchunks = nchunks; a.mper = mper; a.mchunks = mchunks; a.qper = qper;
   a.doSRG = doSRG; a.eta = eta; a.flow = flow;
   a.eq = eq; a.wp = wp; a.Om = Om; a.rho = rho; a.list = list; a.nact = nact; a.part = part;
   if (ptiles > 0 && nS > 0) {
-    const size_t base = (size_t)N * (sizeof(double) + sizeof(float2));
-    // the mixed sweep keeps e in shared memory twice; very large N takes the FP64 sweep
-    if (ff && !doSRG && eta == 0.0 && base <= 40 * 1024) {
+    if (use_ff) {
       const size_t with_om = base + (size_t)mper * sizeof(float2);
       const int om_smem = with_om <= 40 * 1024;
       SigFF f{ff->R, ff->OmF, ff->bad, ff->tau, om_smem};
@@ -697,12 +728,12 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
       k_qp_restart<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, eGWlin, eHF, s);
       QK_LAUNCHED();
     }
-    int hact = 1;
+    int hact = N;  // upper bound on the active count, refreshed by the polls
     for (int it = 0; it < maxit; ++it) {
       double* part;
       int nch;
       QK_TRY(sigma_sweep(ctx, doSRG, eta, flow, N, nC, nO, nR, nS, eOld, s.w, Om, rho, s.list,
-                         s.nact, &part, &nch, ff));
+                         s.nact, &part, &nch, ff, hact));
       k_qp_update<<<1, 1024, 0, ctx->stream>>>(N, nch, part, eHF, s, maxit);
       QK_LAUNCHED();
       if (!ctx->capturing && (it & 3) == 3) {  // poll the active count every 4 steps
