@@ -262,7 +262,8 @@ def run_ours(args):
         torch.cuda.synchronize()
         ms_e2e = ev0.elapsed_time(ev1)
         e2e = {"value": ws * Ke / (ms_e2e * 1e-3), "unit": "systems/s",
-               "h2d_bytes_per_step": int(hE.numel() * 8 + N * 8),
+               # the driver uploads the ERI(p,j,q,b) block it reads, plus the energies
+               "h2d_bytes_per_step": int(N * nO * N * (N - nO) * 8 + N * 8),
                "d2h_bytes_per_step": int((3 * N + nS) * 8 + 16), "steps": Ke,
                "api": "qk_RG0W0 (host pointers, pinned)"}
         del hE
