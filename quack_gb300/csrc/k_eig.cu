@@ -8,11 +8,11 @@
 //      (read+write) and every element costs 4 FMAs (LAPACK's 4/3 n^3 flops); every CTA
 //      recomputes the O(n) vector work redundantly (bitwise identical in all CTAs), leaving
 //      one bounded grid barrier per column.
-//   2. k_stebz: Sturm-count bisection, one thread per eigenvalue, full FP64 precision.
+//   2. k_stebz: Sturm-count k-section (K lanes per eigenvalue), full FP64 precision.
 //   3. k_stein: inverse iteration on T - lambda I (tridiagonal GEPP), one thread per cluster of
 //      close eigenvalues, modified Gram-Schmidt inside clusters; eigenvectors written as rows.
-//   4. Blocked back-transformation E <- E * Q^T with compact-WY blocks of 64 reflectors on the
-//      DMMA GEMM.
+//   4. Blocked back-transformation E <- E * Q^T with compact-WY blocks of 128 reflectors on the
+//      FP64 GEMM (all T factors from one batched GEMM and one launch).
 // Eigenvalues come out ascending (as dsyev).  Eigenvectors are defined up to sign/rotation in
 // degenerate subspaces, which every downstream GW quantity is invariant to.
 #include <cmath>
@@ -402,7 +402,9 @@ __global__ void __launch_bounds__(128) k_stebz(int n, const double* __restrict__
 void launch_stebz(qk_ctx* ctx, int n, const double* d, const double* e2, const double* prep,
                   double* w) {
   const long long slots = 4LL * 32 * ctx->num_sms;  // one warp per SM sub-partition
-  const int K = slots >= 8LL * n ? 8 : slots >= 4LL * n ? 4 : slots >= 2LL * n ? 2 : 1;
+  int K = slots >= 8LL * n ? 8 : slots >= 4LL * n ? 4 : slots >= 2LL * n ? 2 : 1;
+  const int tk = qk_tune_get(ctx, TUNE_STEBZ_K, n, 0);  // tuned width, if any
+  if (tk == 1 || tk == 2 || tk == 4 || tk == 8) K = tk;
   const int blocks = (int)((K * (long long)n + 127) / 128);
   switch (K) {
     case 8: k_stebz<8><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, w); break;

@@ -8,6 +8,7 @@
 //   sytrd_grid    CTAs of the cooperative tridiagonalisation, quarters of the SMs {2,3,4}
 //                 (size = n)
 //   dgemm_path    FP64 GEMM on DFMA (1) or on the DMMA tensor path (2)           (size = m*n)
+//   stebz_k       lanes per eigenvalue of the k-section bisection {2,4,8}        (size = n)
 // qk_autotune times every candidate on buffers of the caller's problem sizes (CUDA events on the
 // context stream, best of two runs) and records the fastest; qk_tune_save / qk_tune_load keep
 // the table as JSON so that a later process starts tuned.
@@ -19,7 +20,7 @@
 #include "qk_internal.cuh"
 
 static const char* k_tune_names[TUNE_NUM] = {"bf16x3_chunk", "splitk_mult", "sigma_chunks",
-                                             "sytrd_grid", "dgemm_path"};
+                                             "sytrd_grid", "dgemm_path", "stebz_k"};
 
 static int bucket_of(long long size) {
   int b = 0;
@@ -183,7 +184,32 @@ int qk_autotune(qk_ctx* ctx, int N, int nS, int flags) {
       ctx->tune[TUNE_SYTRD_GRID][bucket_of(nS)] = best;
     }
   }
-  // 5. FP64 GEMM path on the back-transformation shapes and the FP64 excitation density
+  // 5. k-section width of the bisection (eigenvalues of a random symmetric nS x nS matrix; the
+  //    tridiagonalisation is part of each timing and the same for every candidate)
+  if (st == QK_OK) {
+    double* w = nullptr;
+    st = qk_wst(ctx, W_TUNE, (size_t)nS + 16, &w);
+    if (st == QK_OK) {
+      int best = 0;
+      float tbest = 1e30f;
+      for (int kk : {2, 4, 8}) {
+        ctx->tune[TUNE_STEBZ_K][bucket_of(nS)] = kk;
+        const float t = time_best(ctx, [&] {
+          k_fill<<<1024, 256, 0, ctx->stream>>>((long long)nB, B + nB, 1.0, 3);
+          k_symmetrise<<<1024, 256, 0, ctx->stream>>>(nS, B + nB);
+          ctx->launches += 2;
+          const bool tm = ctx->time_eig;
+          ctx->time_eig = false;
+          const int r = qk_eig_sym(ctx, nS, B + nB, nS, w, nullptr, 0);
+          ctx->time_eig = tm;
+          return r;
+        }, 1);
+        if (t < tbest) { tbest = t; best = kk; }
+      }
+      ctx->tune[TUNE_STEBZ_K][bucket_of(nS)] = best;
+    }
+  }
+  // 6. FP64 GEMM path on the back-transformation shapes and the FP64 excitation density
   {
     struct Shape { int m, n, k; };
     const Shape shapes[3] = {{nS, 128, nS}, {nS, nS, 128}, {(int)N2, nS, nS}};

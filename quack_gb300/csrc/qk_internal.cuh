@@ -26,7 +26,7 @@ enum {
 };
 
 // runtime-tunable launch parameters (chosen by qk_autotune, looked up by size bucket)
-enum { TUNE_BF16X3_CHUNK = 0, TUNE_SPLITK_MULT, TUNE_SIGMA_CHUNKS, TUNE_SYTRD_GRID, TUNE_DGEMM_PATH, TUNE_NUM };
+enum { TUNE_BF16X3_CHUNK = 0, TUNE_SPLITK_MULT, TUNE_SIGMA_CHUNKS, TUNE_SYTRD_GRID, TUNE_DGEMM_PATH, TUNE_STEBZ_K, TUNE_NUM };
 constexpr int TUNE_BUCKETS = 40;
 
 struct DevBuf {

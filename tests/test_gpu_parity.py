@@ -493,6 +493,7 @@ def test_autotuner_roundtrip_and_parity(ctx, tmp_path):
     assert ctx.tune_query("splitk_mult", nS) in (1, 2, 4)
     assert ctx.tune_query("sytrd_grid", nS) in (2, 3, 4)
     assert ctx.tune_query("dgemm_path", nS * nS) in (1, 2)
+    assert ctx.tune_query("stebz_k", nS) in (2, 4, 8)
     path = tmp_path / "tune.json"
     ctx.tune_save(path)
     c2 = api.Context(0)
