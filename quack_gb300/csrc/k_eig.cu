@@ -711,6 +711,9 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
     // small problems do not need the whole GPU
     const int want = (int)((N * N) / (32 * 128)) + 1;
     if (grid > want) grid = want < 1 ? 1 : want;
+    // several systems at once (batch workers): each takes a share of the SMs, so that their
+    // latency-bound per-column phases overlap instead of queueing for the whole GPU
+    if (ctx->sytrd_max_ctas > 0 && grid > ctx->sytrd_max_ctas) grid = ctx->sytrd_max_ctas;
     double* gvec = nullptr;
     if (!use_smem) QK_TRY(qk_wst(ctx, W_VEC, (size_t)grid * 3 * N, &gvec));
     TriArgs ta;

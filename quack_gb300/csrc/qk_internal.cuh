@@ -50,7 +50,8 @@ struct qk_ctx {
   unsigned* d_bar = nullptr;    // grid-barrier counters (zeroed before each cooperative launch)
   DevBuf buf[W_NUMBUF];
   long long launches = 0;
-  int stage_precision = QK_PREC_FP64;  // tier of the stage-level drop-ins (qk_set_stage_precision)
+  int stage_precision = QK_PREC_FP64;
+  int sytrd_max_ctas = 0;  // cap on the tridiagonalisation grid (batch workers share the GPU)  // tier of the stage-level drop-ins (qk_set_stage_precision)
   int last_dev_status = 0;
   bool time_eig = true;  // stage timers inside the eigensolver (off for the eigenvalue-only pass)
   std::vector<int> qp_iters;  // Newton steps per orbital of the last QP solve
