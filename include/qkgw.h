@@ -129,7 +129,7 @@ int qk_DIIS_extrapolation(qk_ctx* ctx, double* rcond, int n_err, int n_e, int n_
 /* ---- driver-level (host pointers) --------------------------------------------------------- */
 /* ERI(nOrb,nOrb,nOrb,nOrb) is the full MO tensor as in the reference, but the drivers read (and
  * copy to the device) only the entries ERI(p,j,q,b) with j active occupied and b active virtual
- * (the excitation-density slab, which contains the Casida block): 2*nO*nV/nOrb^2 of it. */
+ * (the excitation-density slab, which contains the Casida block): nO*nV/nOrb^2 of it. */
 /* GW/RG0W0.f90:109-233.  Om receives the screening (first Casida) energies; EcRPA the
  * correlation energy of the second Casida at eGW (the dumped "G0W0 correlation energy"). */
 int qk_RG0W0(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
