@@ -66,10 +66,17 @@ def batch_systems(nsys: int, Nmin: int, Nmax: int, seed: int, naux_per_N: int = 
 
 
 def eri_phys_numpy(L: np.ndarray) -> np.ndarray:
-    """ERI[p,q,r,s] = (pr|qs) as a numpy array indexed like the Fortran ERI(p,q,r,s)."""
+    """ERI[p,q,r,s] = (pr|qs) as a numpy array indexed like the Fortran ERI(p,q,r,s).  Built a
+    few p at a time, so that no second N^4 copy and no single huge GEMM is needed."""
     naux, N, _ = L.shape
-    chem = (L.reshape(naux, N * N).T @ L.reshape(naux, N * N)).reshape(N, N, N, N)
-    return chem.transpose(0, 2, 1, 3).copy()
+    out = np.empty((N, N, N, N))
+    Lf = L.reshape(naux, N * N)
+    pb = max(1, min(N, (1 << 27) // (N * N * N)))  # ~1 GB blocks of (pr|..)
+    for p0 in range(0, N, pb):
+        p1 = min(N, p0 + pb)
+        blk = (L[:, p0:p1, :].reshape(naux, (p1 - p0) * N).T @ Lf).reshape(p1 - p0, N, N, N)
+        out[p0:p1] = blk.transpose(0, 2, 1, 3)
+    return out
 
 
 def eri_fortran_flat_torch(L: np.ndarray, device="cuda"):
