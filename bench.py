@@ -530,14 +530,43 @@ def run_profile_case(args):
     JSON line of CUDA-event times; not a bench result).
       tridiag   : eigenvalues of a random symmetric n x n matrix (k_sytrd + k_stebz)
       g0w0_L    : the N=200 G0W0 from its factor L (no N^4 tensor on the device), mixed tier
-      g0w0_mixed: the bench's G0W0 step, mixed tier only (launch list of one step)"""
+      g0w0_mixed: the bench's G0W0 step, mixed tier only (launch list of one step)
+      c4        : the N=400 system (nS=14400) through the factorised drivers, both tiers"""
     import numpy as np
     import torch
     from quack_gb300 import api, synth
 
     ctx = api.Context(0)
     out = {"case": args.profile_case}
-    if args.profile_case == "tridiag":
+    if args.profile_case == "c4":
+        # configuration 4: N=400, nO=40, naux=1200, seed 2 (nS=14400), factorised drivers;
+        # both tiers, Newton and linearised QP, per-stage times and the tier difference
+        N, nO, naux = 400, 40, 1200
+        nS = nO * (N - nO)
+        s = synth.gen_system(N, nO, naux, np.random.default_rng(2))
+        dL = torch.from_numpy(api.L_fortran_flat(s["L"])).cuda()
+        de = torch.from_numpy(s["eHF"]).cuda()
+        res = {}
+        for prec, name in ((api.QK_PREC_BF16X3, "mixed"), (api.QK_PREC_FP64, "fp64")):
+            for lin in (True, False):
+                b = [torch.empty(N, dtype=torch.float64, device="cuda") for _ in range(3)]
+                dOm = torch.empty(nS, dtype=torch.float64, device="cuda")
+                torch.cuda.synchronize()
+                t0 = time.time()
+                api.RG0W0_L_dev(api.GWOptions(precision=prec, linearize=lin), N, 0, nO, 0, naux,
+                                dL.data_ptr(), de.data_ptr(), b[0].data_ptr(), b[1].data_ptr(),
+                                b[2].data_ptr(), dOm.data_ptr(), ctx=ctx)
+                torch.cuda.synchronize()
+                key = "%s_%s" % (name, "lin" if lin else "newton")
+                res[key] = (b[0].cpu().numpy(), dOm.cpu().numpy())
+                out[key] = {"seconds": time.time() - t0, "stages": ctx.timings()}
+        for q in ("lin", "newton"):
+            d = np.abs(res["mixed_" + q][0] - res["fp64_" + q][0])
+            out["diff_" + q] = {"max_abs_Ha": float(d.max()), "median_abs_Ha": float(np.median(d)),
+                                "n_over_1meV": int((d > MEV).sum()),
+                                "Om_max_abs_Ha": float(np.abs(res["mixed_" + q][1] -
+                                                              res["fp64_" + q][1]).max())}
+    elif args.profile_case == "tridiag":
         n = args.case_n
         A = np.random.default_rng(n).standard_normal((n, n))
         A = A + A.T
@@ -599,7 +628,7 @@ def main():
     ap.add_argument("--batch-workers", type=int, default=8)
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-systems", type=int, default=120)
-    ap.add_argument("--profile-case", choices=["tridiag", "g0w0_L", "g0w0_mixed"], default=None,
+    ap.add_argument("--profile-case", choices=["tridiag", "g0w0_L", "g0w0_mixed", "c4"], default=None,
                     help="run one small kernel case for an ncu capture instead of the bench")
     ap.add_argument("--case-n", type=int, default=3600)
     ap.add_argument("--case-reps", type=int, default=1)
