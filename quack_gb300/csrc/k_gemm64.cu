@@ -321,7 +321,7 @@ int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, c
   if (grid.y > 65535 || grid.z > 65535) return qk_fail(ctx, QK_ERR_ARG, "qk_dgemm: grid too large");
   const long long tiles = (long long)grid.x * grid.y;
   // fewer output tiles than mult CTAs per SM and a long K: split K and reduce
-  const int mult = qk_tune_get(ctx, TUNE_SPLITK_MULT, k, 2);
+  const int mult = qk_tune_get(ctx, TUNE_SPLITK_MULT, k, 4);
   if (batch == 1 && tiles < (long long)mult * ctx->num_sms && k >= 4 * BK) {
     int S = (int)(((long long)mult * ctx->num_sms + tiles - 1) / tiles);
     const int maxS = k / (2 * BK);

@@ -3,7 +3,7 @@
 // Tunable launch parameters (all runtime-selectable, looked up per size bucket
 // floor(log2(size)) by the kernels' host launchers):
 //   bf16x3_chunk  k blocks per TMEM accumulation chunk of the BF16x3 GEMM {1,2,4}   (size = K)
-//   splitk_mult   target CTAs / SMs for split-K DMMA GEMMs {1,2,4}                  (size = K)
+//   splitk_mult   target CTAs per SM below which FP64 GEMMs split K {1,2,4}       (size = K)
 //   sigma_chunks  m chunks per p tile of the pole sweeps, in units of SMs {2,4,8}   (size = nS)
 //   sytrd_grid    CTAs of the cooperative tridiagonalisation, quarters of the SMs {2,3,4}
 //                 (size = n)
