@@ -371,10 +371,24 @@ __device__ __forceinline__ int sturm_count(int n, const double* __restrict__ d,
 // bracket follows from a popcount of the group's ballot.  K trades extra sweeps for parallelism:
 // the FP64 pipe of an SM sub-partition issues one warp instruction per 64 cycles, so the launch
 // picks the largest K whose warps still fit one per sub-partition.
+// Sturm counts at G+1 equally spaced points of the Gershgorin interval (one thread per point):
+// every eigenvalue then starts its k-section from the grid cell that holds it, log2(G) halvings
+// below the full interval.
+constexpr int STEBZ_GRID = 16384;
+__global__ void k_stebz_grid(int n, const double* __restrict__ d, const double* __restrict__ e2,
+                             const double* __restrict__ prep, int G, int* __restrict__ cnt) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g > G) return;
+  const double lo = prep[0], hi = prep[1];
+  const double h = (hi - lo) / G;
+  cnt[g] = g == 0 ? 0 : (g == G ? n : sturm_count(n, d, e2, lo + h * g));
+}
+
 template <int K>
 __global__ void __launch_bounds__(128) k_stebz(int n, const double* __restrict__ d,
                                                const double* __restrict__ e2,
                                                const double* __restrict__ prep,
+                                               const int* __restrict__ cnt, int G,
                                                double* __restrict__ w) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = gt / K, t = gt % K;
@@ -383,6 +397,20 @@ __global__ void __launch_bounds__(128) k_stebz(int n, const double* __restrict__
   const unsigned gmask = (K == 32 ? 0xffffffffu : ((1u << K) - 1u)) << (lane & ~(K - 1));
   double lo = prep[0], hi = prep[1];
   const double pivmin = prep[2];
+  if (cnt && valid) {
+    // the cell [x_g, x_{g+1}) with cnt[g] <= j < cnt[g+1] (cnt[0] = 0, cnt[G] = n)
+    int a = 0, b = G;
+    while (b - a > 1) {
+      const int mid = (a + b) >> 1;
+      if (cnt[mid] <= j) a = mid;
+      else b = mid;
+    }
+    const double h = (hi - lo) / G;
+    const double x0 = lo + h * a;
+    const double x1 = b == G ? hi : lo + h * b;
+    lo = x0;
+    hi = x1;
+  }
   for (int it = 0; it < 128; ++it) {
     if (hi - lo <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + 2.0 * pivmin) break;
     const double h = (hi - lo) / (K + 1);
@@ -400,17 +428,17 @@ __global__ void __launch_bounds__(128) k_stebz(int n, const double* __restrict__
 }
 
 void launch_stebz(qk_ctx* ctx, int n, const double* d, const double* e2, const double* prep,
-                  double* w) {
+                  const int* cnt, int G, double* w) {
   const long long slots = 4LL * 32 * ctx->num_sms;  // one warp per SM sub-partition
   int K = slots >= 8LL * n ? 8 : slots >= 4LL * n ? 4 : slots >= 2LL * n ? 2 : 1;
   const int tk = qk_tune_get(ctx, TUNE_STEBZ_K, n, 0);  // tuned width, if any
   if (tk == 1 || tk == 2 || tk == 4 || tk == 8) K = tk;
   const int blocks = (int)((K * (long long)n + 127) / 128);
   switch (K) {
-    case 8: k_stebz<8><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, w); break;
-    case 4: k_stebz<4><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, w); break;
-    case 2: k_stebz<2><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, w); break;
-    default: k_stebz<1><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, w); break;
+    case 8: k_stebz<8><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, cnt, G, w); break;
+    case 4: k_stebz<4><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, cnt, G, w); break;
+    case 2: k_stebz<2><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, cnt, G, w); break;
+    default: k_stebz<1><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, cnt, G, w); break;
   }
 }
 
@@ -750,7 +778,14 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   if (tm) qk_tic(ctx, T_BISECT);
   k_tri_prep<<<1, 1024, 0, ctx->stream>>>(n, d, e, e2, prep);
   QK_LAUNCHED();
-  launch_stebz(ctx, n, d, e2, prep, w);
+  int* cnt = nullptr;
+  if (n >= 256) {
+    QK_TRY(qk_wst(ctx, W_STEBZ, (size_t)STEBZ_GRID + 64, &cnt));
+    k_stebz_grid<<<(STEBZ_GRID + 128) / 128, 128, 0, ctx->stream>>>(n, d, e2, prep, STEBZ_GRID,
+                                                                     cnt);
+    QK_LAUNCHED();
+  }
+  launch_stebz(ctx, n, d, e2, prep, cnt, STEBZ_GRID, w);
   QK_LAUNCHED();
   if (tm) qk_toc(ctx, T_BISECT);
   if (!want_vectors) return QK_OK;

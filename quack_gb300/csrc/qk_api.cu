@@ -34,20 +34,17 @@ int h2d(qk_ctx* ctx, void* dst, const void* src, size_t bytes) {
 }
 // Upload only the part of ERI(p,q,r,s) the G0W0/evGW drivers read: q occupied (active), s
 // virtual (active), all p and r -- the excitation-density slab ERI(p,j,q,b), which contains the
-// Casida block ERI(b,i,j,a) as well.  One 3D copy (rows of N doubles) per virtual s; the other
-// entries of the device tensor are never read.  At N=200, nO=20 that is 1.15 GB instead of 12.8.
+// Casida block ERI(b,i,j,a) as well.  For fixed (r, s) the entries with q in the occupied range
+// and any p are one contiguous run of no*N doubles, so each virtual s is one 2D copy of N such
+// runs; the other entries of the device tensor are never read.  At N=200, nO=20 that is
+// 1.15 GB instead of 12.8.
 int h2d_eri_used(qk_ctx* ctx, double* dERI, const double* hERI, const Dims& d) {
-  const size_t N = d.N, N3 = N * N * N;
-  const int no = d.nO - d.nC;
+  const size_t N = d.N, N2 = N * N, N3 = N2 * N;
+  const size_t run = (size_t)(d.nO - d.nC) * N * sizeof(double);
   for (int s = d.nO; s < d.N - d.nR; ++s) {
-    cudaMemcpy3DParms p = {};
-    p.srcPtr = make_cudaPitchedPtr((void*)(hERI + N3 * s), N * sizeof(double), N, N);
-    p.dstPtr = make_cudaPitchedPtr((void*)(dERI + N3 * s), N * sizeof(double), N, N);
-    p.srcPos = make_cudaPos(0, d.nC, 0);
-    p.dstPos = make_cudaPos(0, d.nC, 0);
-    p.extent = make_cudaExtent(N * sizeof(double), no, N);
-    p.kind = cudaMemcpyHostToDevice;
-    QK_CK(cudaMemcpy3DAsync(&p, ctx->stream));
+    const size_t off = N3 * s + N * d.nC;
+    QK_CK(cudaMemcpy2DAsync(dERI + off, N2 * sizeof(double), hERI + off, N2 * sizeof(double), run,
+                            N, cudaMemcpyHostToDevice, ctx->stream));
   }
   return QK_OK;
 }
