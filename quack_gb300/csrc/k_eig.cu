@@ -164,9 +164,11 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
             beta = alpha;
           } else {
             beta = -copysign(sqrt(alpha * alpha + sigma), alpha);
-            t1 = (beta - alpha) / beta;
+            // reciprocals by qk_rcp (a few ulps) instead of IEEE divisions: this runs on the
+            // per-column critical path, where each FP64 instruction costs ~64 cycles
+            t1 = (beta - alpha) * qk_rcp(beta);
             inv = alpha - beta;
-            scal = 1.0 / inv;
+            scal = qk_rcp(inv);
           }
           vk1[j + 1] = inv;  // u_{j+1} = 1/scal, so that scal * u_{j+1} = 1
         }
@@ -177,9 +179,10 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       const double dj = s_dj;
       tau1 = s_sc[4];
       scal1 = s_sc[5];
-      if (j <= n - 2 && blockIdx.x == 0) {
-        if (tid == 0) { a.e[j] = s_sc[3]; a.tau[j] = tau1; }
-        for (int i = j + 1 + tid; i < n; i += nt)
+      if (j <= n - 2) {
+        // every CTA holds the reflector: the V column is written by all of them, a slice each
+        if (blockIdx.x == 0 && tid == 0) { a.e[j] = s_sc[3]; a.tau[j] = tau1; }
+        for (int i = j + 1 + gthread; i < n; i += totthreads)
           a.V[i + a.ldv * j] = (i == j + 1) ? 1.0 : vk1[i] * scal1;
       }
       if (blockIdx.x == 0 && tid == 0) a.d[j] = dj;
