@@ -414,6 +414,7 @@ def run_learned(args, ctx):
     return {"train_systems": ntr, "test_systems": n - ntr, "train_orbitals": int(len(T)),
             "collect_s": t1 - t0, "train_s": t2 - t1, "train_mse_normalised": mse,
             "newton_sigma_evals_reference": ev_ref, "newton_sigma_evals_guess": ev_g,
+            "newton_sigma_evals_hf_start": sum(r["evals_hf_start"] for r in rows),
             "eval_ratio": ev_g / max(1, ev_ref),
             "qp_ms_reference": sum(r["qp_ms_ref"] for r in rows),
             "qp_ms_guess": sum(r["qp_ms_guess"] for r in rows),

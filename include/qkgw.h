@@ -62,7 +62,8 @@ typedef struct qk_gw_params {
   int precision;     /* QK_PREC_* */
   int qp_guess;      /* 0: Newton from the reference start (eGWlin); 1: Newton from the learned
                         guess of the context's model (qk_set_qp_model), restarted from the
-                        reference start for orbitals that do not converge within 8 steps */
+                        reference start for orbitals that do not converge within 8 steps;
+                        2: the same protocol started from eHF (a comparison baseline) */
 } qk_gw_params;
 
 /* ---- context ------------------------------------------------------------------------------ */

@@ -292,7 +292,7 @@ class GWOptions:
     TDA_W: bool = False
     reg: bool = False
     precision: int = QK_PREC_FP64
-    qp_guess: bool = False
+    qp_guess: int = 0  # 0 reference start, 1 learned guess, 2 HF start (comparison)
 
     def c(self):
         return qk_gw_params(self.eta, int(self.linearize), int(self.reg), int(self.TDA_W),

@@ -228,15 +228,15 @@ int sigma_tier(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double
   return QK_OK;
 }
 
-// Newton QP of RG0W0 (reference start eGWlin) or, with prm->qp_guess, from the learned guess;
-// captures the per-orbital features when requested.
+// Newton QP of RG0W0 (reference start eGWlin) or, with prm->qp_guess, from the learned guess (1)
+// or from eHF (2, a comparison baseline); captures the per-orbital features when requested.
 int g0w0_qp(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, double flow, const double* eHF,
             const double* Om, const double* rho, const double* SigC, double* Z,
             const double* eGWlin, double* eGW, const qk_sigma_ff* ff) {
   const int N = d.N, nS = d.nS;
   float* F = nullptr;
   double* gbuf = nullptr;  // [0, N): start; [N, 2N): Halley step; then N ints: fromref
-  const bool need_f = ctx->capture_features || prm->qp_guess;
+  const bool need_f = ctx->capture_features || prm->qp_guess == 1;
   if (need_f) {
     QK_TRY(qk_wst(ctx, W_FEAT, (size_t)N * QK_MLP_NIN + 16, &F));
     QK_TRY(qk_wst(ctx, W_GUESS, (size_t)3 * N + 16, &gbuf));
@@ -250,10 +250,16 @@ int g0w0_qp(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, double flow, co
   }
   double* w0 = nullptr;
   int* fromref = nullptr;
-  if (prm->qp_guess && !prm->linearize) {
+  if (prm->qp_guess == 1 && !prm->linearize) {
     w0 = gbuf;
     fromref = (int*)(gbuf + 2 * N);
     QK_TRY(qk_guess_from_model(ctx, N, F, eGWlin, gbuf + N, w0, fromref));
+  }
+  if (prm->qp_guess == 2 && !prm->linearize) {
+    // comparison start: the HF energies, same 8-step protocol as the learned guess
+    QK_TRY(qk_wst(ctx, W_GUESS, (size_t)3 * N + 16, &gbuf));
+    w0 = gbuf;
+    QK_CK(cudaMemcpyAsync(w0, eHF, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   }
   if (prm->linearize) {
     QK_CK(cudaMemcpyAsync(eGW, eGWlin, N * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));

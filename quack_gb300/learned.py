@@ -163,11 +163,13 @@ def evaluate(ctx, model, systems, tol=1e-8):
         t0 = time.time()
         a = run_g0w0_L(ctx, s, api.GWOptions())
         t1 = time.time()
-        b = run_g0w0_L(ctx, s, api.GWOptions(qp_guess=True))
+        b = run_g0w0_L(ctx, s, api.GWOptions(qp_guess=1))
         t2 = time.time()
+        h = run_g0w0_L(ctx, s, api.GWOptions(qp_guess=2))
         both = (a["iters"] < 64) & np.isfinite(a["eGW"])
         d = np.abs(a["eGW"] - b["eGW"])
         rows.append(dict(N=s["N"], evals_ref=a["evals"], evals_guess=b["evals"],
+                         evals_hf_start=h["evals"],
                          qp_ms_ref=a["qp_ms"], qp_ms_guess=b["qp_ms"], wall_ref=t1 - t0,
                          wall_guess=t2 - t1, n_conv=int(both.sum()),
                          max_diff_conv=float(d[both].max()) if both.any() else 0.0,

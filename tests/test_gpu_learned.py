@@ -85,7 +85,9 @@ def test_learned_guess_saves_newton_evaluations(ctx):
     ev_g = sum(r["evals_guess"] for r in rows)
     n_conv = sum(r["n_conv"] for r in rows)
     n_same = sum(r["n_same"] for r in rows)
-    print("newton evals: reference %d, learned guess %d (%.1f%% fewer); same root %d/%d"
-          % (ev_ref, ev_g, 100.0 * (1.0 - ev_g / ev_ref), n_same, n_conv))
+    ev_hf = sum(r["evals_hf_start"] for r in rows)
+    print("newton evals: reference %d, learned guess %d (%.1f%% fewer), HF start %d; same root %d/%d"
+          % (ev_ref, ev_g, 100.0 * (1.0 - ev_g / ev_ref), ev_hf, n_same, n_conv))
+    assert ev_g < ev_hf
     assert ev_g < ev_ref
     assert n_same >= 0.95 * n_conv
