@@ -219,13 +219,19 @@ int qk_dsyev_dev(qk_ctx* ctx, int n, double* d_A, int lda, double* d_w, double* 
                  int want_vectors);
 
 /* ---- contraction kernels on device buffers (column-major) --------------------------------
- * qk_dgemm_dev: C = alpha*op(A)*op(B) + beta*C on the FP64 tensor path (DMMA); replaces the
+ * qk_dgemm_dev: C = alpha*op(A)*op(B) + beta*C in FP64 (DFMA, or DMMA where tuned); replaces the
  *   dgemm calls of AOtoMO/AOtoMO_ERI_RHF.f90:26-53 and GW/RGW_excitation_density.f90:48-50.
+ * qk_dgemm_f32p_dev: the same contract with FP64 operands and result but FP32 products (the
+ *   16 products of each k tile summed in FP32, the tiles folded into a compensated FP32 pair);
+ *   the mixed tier's eigenvector back-transformation (dsyev's dormtr step).
  * qk_gemm_bf16x3_dev: C = A * B^T with the three-way BF16 split on tcgen05 (FP32 accumulate),
  *   the precision tier of the same excitation-density dgemm. */
 int qk_dgemm_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, double alpha,
                  const double* d_A, int lda, const double* d_B, int ldb, double beta, double* d_C,
                  int ldc);
+int qk_dgemm_f32p_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, double alpha,
+                      const double* d_A, int lda, const double* d_B, int ldb, double beta,
+                      double* d_C, int ldc);
 int qk_gemm_bf16x3_dev(qk_ctx* ctx, int m, int n, int k, const double* d_A, int lda,
                        const double* d_B, int ldb, double* d_C, int ldc);
 

@@ -352,11 +352,19 @@ def dsyev_dev(n, d_A, lda, d_w, d_Zt, want_vectors=True, ctx=None):
 
 
 def dgemm_dev(transa, transb, m, n, k, alpha, d_A, lda, d_B, ldb, beta, d_C, ldc, ctx=None):
-    """FP64 (DMMA) GEMM on device buffers, column-major."""
+    """FP64 GEMM on device buffers, column-major."""
     c = _ctx(ctx)
     c.check(lib().qk_dgemm_dev(c.handle, C.c_char(transa.encode()), C.c_char(transb.encode()), m,
                                n, k, C.c_double(alpha), C.c_void_p(d_A), lda, C.c_void_p(d_B), ldb,
                                C.c_double(beta), C.c_void_p(d_C), ldc))
+
+
+def dgemm_f32p_dev(transa, transb, m, n, k, alpha, d_A, lda, d_B, ldb, beta, d_C, ldc, ctx=None):
+    """The dgemm_dev contract with FP32 products (compensated FP32 sums, FP64 in/out)."""
+    c = _ctx(ctx)
+    c.check(lib().qk_dgemm_f32p_dev(c.handle, C.c_char(transa.encode()), C.c_char(transb.encode()),
+                                    m, n, k, C.c_double(alpha), C.c_void_p(d_A), lda,
+                                    C.c_void_p(d_B), ldb, C.c_double(beta), C.c_void_p(d_C), ldc))
 
 
 def gemm_bf16x3_dev(m, n, k, d_A, lda, d_B, ldb, d_C, ldc, ctx=None):

@@ -12,7 +12,8 @@
 //   3. k_stein: inverse iteration on T - lambda I (tridiagonal GEPP), one thread per cluster of
 //      close eigenvalues, modified Gram-Schmidt inside clusters; eigenvectors written as rows.
 //   4. Blocked back-transformation E <- E * Q^T with compact-WY blocks of 128 reflectors on the
-//      FP64 GEMM (all T factors from one batched GEMM and one launch).
+//      FP64 GEMM, or with FP32 products in the mixed tier (all T factors from one batched GEMM
+//      and one launch).
 // Eigenvalues come out ascending (as dsyev).  Eigenvectors are defined up to sign/rotation in
 // degenerate subspaces, which every downstream GW quantity is invariant to.
 #include <cmath>
@@ -32,28 +33,30 @@ constexpr double CLUSTER_REL = 1e-7;  // eigenvalues closer than this * ||T||_1 
 constexpr int SB = 8;                 // inverse iteration: steps per batch of prefetched loads
 
 // Sum over the CTA with few FP64 operations (the FP64 pipe is the scarce resource here): the
-// per-thread partials go to shared memory and warp 0 adds them with four independent chains per
-// lane, then one butterfly.  Thread 0 then runs fin(total) -- the scalar follow-up work, done
-// once instead of by every warp -- before the closing barrier publishes its results.
-// scratch holds blockDim.x doubles.
+// per-thread partials go to shared memory and warps 0-3 (one per SM sub-partition, so their
+// FP64 issue runs in parallel) add the first cnt of them (the rest are zero) in two chains per
+// lane, then one butterfly each.  Thread 0 adds the four warp sums and runs fin(total) -- the
+// scalar follow-up work, done once instead of by every warp -- before the closing barrier
+// publishes its results.  scratch holds blockDim.x + 4 doubles; blockDim.x >= 128.
 template <class Fin>
-__device__ __forceinline__ void tri_block_sum(double v, double* scratch, Fin fin) {
-  const int tid = threadIdx.x, nt = blockDim.x;
+__device__ __forceinline__ void tri_block_sum(double v, double* scratch, int cnt, Fin fin) {
+  const int tid = threadIdx.x;
   scratch[tid] = v;
   __syncthreads();
-  if (tid < 32) {
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  if (tid < 128) {
+    double a0 = 0.0, a1 = 0.0;
     int i = tid;
-    for (; i + 96 < nt; i += 128) {
+    for (; i + 128 < cnt; i += 256) {
       a0 += scratch[i];
-      a1 += scratch[i + 32];
-      a2 += scratch[i + 64];
-      a3 += scratch[i + 96];
+      a1 += scratch[i + 128];
     }
-    for (; i < nt; i += 32) a0 += scratch[i];
-    double t = (a0 + a1) + (a2 + a3);
+    if (i < cnt) a0 += scratch[i];
+    double t = a0 + a1;
     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (tid == 0) fin(t);
+    double* red4 = scratch + blockDim.x;
+    if ((tid & 31) == 0) red4[tid >> 5] = t;
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    if (tid == 0) fin((red4[0] + red4[1]) + (red4[2] + red4[3]));
   }
   __syncthreads();
 }
@@ -111,6 +114,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
     // pass over the vector (the big pass computes p~ = A' u, so p = scal p~, and with
     // w' = scal w the update A - v w^T - w v^T = A - u w'^T - w' u^T keeps its form).
     const int j = k + 1;
+    const int cnt = n - j < nt ? n - j : nt;  // threads holding a non-zero partial sum
     double tau1 = 0.0, scal1 = 1.0;
     {
       const double* p = a.pbuf + (size_t)((k + 3) % 3) * n;
@@ -126,7 +130,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       }
       if (k >= 0) {
         // (the barriers publish vk1, wk and s_pj as well)
-        tri_block_sum(dot, ytile, [&](double t) {
+        tri_block_sum(dot, ytile, cnt, [&](double t) {
           // true dot p.v = scal^2 p~.u;  c = tau^2 dot / 2;  w' = scal^2 (tau p~ - c u)
           const double s2 = scal_k * scal_k;
           const double cc = 0.5 * tau_k * tau_k * (s2 * t);
@@ -156,7 +160,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
         else ss = fma(x, x, ss);
       }
       // Householder reflector of the updated column (dlarfg), computed once by thread 0
-      tri_block_sum(ss, ytile, [&](double sigma) {
+      tri_block_sum(ss, ytile, cnt, [&](double sigma) {
         double beta = 0.0, t1 = 0.0, scal = 1.0, inv = 1.0;
         if (j <= n - 2) {
           const double alpha = s_alpha;
@@ -660,7 +664,8 @@ __global__ void __launch_bounds__(BT_NB) k_larft_all(int nref, const double* __r
 // T factors of all reflector blocks of the last tridiagonalisation on this context:
 // G_b = V_b^T V_b for the full blocks in one batched GEMM (V is zero above its unit diagonal,
 // so all n rows can be used), the last partial block on its own, then k_larft_all.
-int eig_tfactors(qk_ctx* ctx, int n, const double* V, const double* tau, const double** T_out) {
+int eig_tfactors(qk_ctx* ctx, int n, const double* V, const double* tau, const double** T_out,
+                 bool fp32) {
   const int nref = n - 2;
   const int nblk = (nref + BT_NB - 1) / BT_NB;
   const size_t B2 = (size_t)BT_NB * BT_NB;
@@ -670,14 +675,15 @@ int eig_tfactors(qk_ctx* ctx, int n, const double* V, const double* tau, const d
   double* T = buf + B2 * nblk;
   const int full = nref / BT_NB;
   const long long bstride = (long long)n * BT_NB;
+  auto gemm = fp32 ? qk_gemm_f32p : qk_dgemm;
   if (full > 0)
-    QK_TRY(qk_dgemm(ctx, 'T', 'N', BT_NB, BT_NB, n, 1.0, V, n, bstride, V, n, bstride, 0.0, G,
-                    BT_NB, (long long)B2, full));
+    QK_TRY(gemm(ctx, 'T', 'N', BT_NB, BT_NB, n, 1.0, V, n, bstride, V, n, bstride, 0.0, G, BT_NB,
+                (long long)B2, full));
   if (full < nblk) {
     const int kb = full * BT_NB, nb = nref - kb;
     const double* Vb = V + (size_t)n * kb;
-    QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, nb, n, 1.0, Vb, n, 0, Vb, n, 0, 0.0, G + B2 * full, BT_NB,
-                    0, 1));
+    QK_TRY(gemm(ctx, 'T', 'N', nb, nb, n, 1.0, Vb, n, 0, Vb, n, 0, 0.0, G + B2 * full, BT_NB, 0,
+                1));
   }
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
@@ -802,11 +808,13 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
 
   if (!backtransform) return QK_OK;  // caller applies Q^T itself (qk_eig_apply_qt)
   // ---- 4. back-transformation Zt <- Zt * Q^T, blocks from last to first ----
+  // (backtransform == 2: the block products in FP32, Zt kept in FP64; the mixed tier)
+  auto gemm = backtransform == 2 ? qk_gemm_f32p : qk_dgemm;
   if (tm) qk_tic(ctx, T_BACKTRANS);
   const int nref = n - 2;  // reflectors 0..n-3 can be non-trivial
   if (nref > 0) {
     const double* Tall = nullptr;
-    QK_TRY(eig_tfactors(ctx, n, V, tau, &Tall));
+    QK_TRY(eig_tfactors(ctx, n, V, tau, &Tall, backtransform == 2));
     double* bt = nullptr;
     QK_TRY(qk_wst(ctx, W_PART, 2 * N * BT_NB, &bt));
     double* W1 = bt;
@@ -819,9 +827,9 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
       const double* Vb = V + (kb + 1) + N * kb;
       const double* Tb = Tall + (size_t)b * BT_NB * BT_NB;
       double* Es = Zt + N * (kb + 1);
-      QK_TRY(qk_dgemm(ctx, 'N', 'N', n, nb, m, 1.0, Es, n, 0, Vb, n, 0, 0.0, W1, n, 0, 1));
-      QK_TRY(qk_dgemm(ctx, 'N', 'T', n, nb, nb, 1.0, W1, n, 0, Tb, BT_NB, 0, 0.0, W2, n, 0, 1));
-      QK_TRY(qk_dgemm(ctx, 'N', 'T', n, m, nb, -1.0, W2, n, 0, Vb, n, 0, 1.0, Es, n, 0, 1));
+      QK_TRY(gemm(ctx, 'N', 'N', n, nb, m, 1.0, Es, n, 0, Vb, n, 0, 0.0, W1, n, 0, 1));
+      QK_TRY(gemm(ctx, 'N', 'T', n, nb, nb, 1.0, W1, n, 0, Tb, BT_NB, 0, 0.0, W2, n, 0, 1));
+      QK_TRY(gemm(ctx, 'N', 'T', n, m, nb, -1.0, W2, n, 0, Vb, n, 0, 1.0, Es, n, 0, 1));
     }
   }
   if (tm) qk_toc(ctx, T_BACKTRANS);
@@ -830,8 +838,8 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
 
 // X (n x ncols, ldx) <- Q^T X with the reflectors of the last qk_eig_sym call on this context
 // (Q = H_0 H_1 ... H_{n-3}); compact-WY blocks applied first to last:
-//   X <- X - V (T^T (V^T X)) on rows kb+1..n-1.
-int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols) {
+//   X <- X - V (T^T (V^T X)) on rows kb+1..n-1;  fp32: the block products in FP32.
+int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols, int fp32) {
   const int nref = n - 2;
   if (nref <= 0 || ncols <= 0) return QK_OK;
   const size_t N = (size_t)n;
@@ -840,11 +848,12 @@ int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols) {
   QK_TRY(qk_wst(ctx, W_TRI, 8 * N + 64, &tri));
   double* tau = tri + 2 * N;
   const double* Tall = nullptr;
-  QK_TRY(eig_tfactors(ctx, n, V, tau, &Tall));
+  QK_TRY(eig_tfactors(ctx, n, V, tau, &Tall, fp32 != 0));
   QK_TRY(qk_wst(ctx, W_PART, 2 * (size_t)ncols * BT_NB, &bt));
   double* W1 = bt;
   double* W2 = bt + (size_t)ncols * BT_NB;
   const int nblk = (nref + BT_NB - 1) / BT_NB;
+  auto gemm = fp32 ? qk_gemm_f32p : qk_dgemm;
   for (int b = 0; b < nblk; ++b) {
     const int kb = b * BT_NB;
     const int nb = (nref - kb) < BT_NB ? (nref - kb) : BT_NB;
@@ -853,9 +862,9 @@ int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols) {
     const double* Tb = Tall + (size_t)b * BT_NB * BT_NB;
     double* Xs = X + (kb + 1);
     // W1 = V^T X (nb x ncols), W2 = T^T W1, X -= V W2
-    QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, ncols, m, 1.0, Vb, n, 0, Xs, ldx, 0, 0.0, W1, nb, 0, 1));
-    QK_TRY(qk_dgemm(ctx, 'T', 'N', nb, ncols, nb, 1.0, Tb, BT_NB, 0, W1, nb, 0, 0.0, W2, nb, 0, 1));
-    QK_TRY(qk_dgemm(ctx, 'N', 'N', m, ncols, nb, -1.0, Vb, n, 0, W2, nb, 0, 1.0, Xs, ldx, 0, 1));
+    QK_TRY(gemm(ctx, 'T', 'N', nb, ncols, m, 1.0, Vb, n, 0, Xs, ldx, 0, 0.0, W1, nb, 0, 1));
+    QK_TRY(gemm(ctx, 'T', 'N', nb, ncols, nb, 1.0, Tb, BT_NB, 0, W1, nb, 0, 0.0, W2, nb, 0, 1));
+    QK_TRY(gemm(ctx, 'N', 'N', m, ncols, nb, -1.0, Vb, n, 0, W2, nb, 0, 1.0, Xs, ldx, 0, 1));
   }
   return QK_OK;
 }

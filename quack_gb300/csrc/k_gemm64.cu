@@ -1,4 +1,6 @@
-// k_gemm64.cu -- FP64 GEMM: the FP64 tensor path (DMMA, mma.sync.m8n8k4.f64) and a DFMA path.
+// k_gemm64.cu -- FP64 GEMM: the FP64 tensor path (DMMA, mma.sync.m8n8k4.f64) and a DFMA path,
+// plus an FP32-product variant with FP64 operands and result (the mixed tier's eigenvector
+// back-transformation).
 //
 // Column-major C = alpha*op(A)*op(B) + beta*C, strided batch.  Used for the AO->MO quarter
 // transforms (AOtoMO/AOtoMO_ERI_RHF.f90:26-53), the FP64 excitation density
@@ -141,19 +143,21 @@ __global__ void __launch_bounds__(128) k_dgemm_dmma(int M, int N, int K, double 
   }
 }
 
-// The same GEMM on the FP64 FMA path (DFMA).  On GB300 DFMA and DMMA share one FP64 datapath
-// and DFMA issues slightly faster (1.2 vs 1.05 TFLOP/s measured), so a plain register-tiled
-// kernel can beat the tensor path: 256 threads, each a 4x4 block of C (rows tx + 16 i, columns
-// ty + 16 j) with 16 independent FMA chains, 8 shared loads per 16 DFMA.
-template <bool TA, bool TB>
-__global__ void __launch_bounds__(256) k_dgemm_simt(int M, int N, int K, double alpha,
+// The same GEMM on the FMA path.  With T = double (DFMA): on GB300 DFMA and DMMA share one FP64
+// datapath and DFMA issues slightly faster (1.2 vs 1.05 TFLOP/s measured), so a plain
+// register-tiled kernel can beat the tensor path: 256 threads, each a 4x4 block of C (rows
+// tx + 16 i, columns ty + 16 j) with 16 independent FMA chains, 8 shared loads per 16 FMA.
+// With T = float the FP64 operands are rounded to FP32 as they are staged and the products and
+// partial sums are FP32 (64x the FP64 issue rate); C stays FP64 (alpha, beta applied in FP64).
+template <bool TA, bool TB, typename T>
+__global__ void __launch_bounds__(256) k_gemm_simt(int M, int N, int K, double alpha,
                                                      const double* __restrict__ A, long long lda,
                                                      long long sA, const double* __restrict__ B,
                                                      long long ldb, long long sB, double beta,
                                                      double* __restrict__ C, long long ldc,
                                                      long long sC, int kc) {
-  __shared__ double As[2][BK][BM];
-  __shared__ double Bs[2][BK][BN];
+  __shared__ T As[2][BK][BM];
+  __shared__ T Bs[2][BK][BN];
   const long long bz = blockIdx.z;
   int kbeg = 0, kend = K;
   if (kc > 0) {
@@ -168,13 +172,16 @@ __global__ void __launch_bounds__(256) k_dgemm_simt(int M, int N, int K, double 
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
 
-  double acc[4][4];
+  constexpr bool kF32 = sizeof(T) == 4;
+  // FP32: each k tile's 16 products are summed in FP32 and folded into a compensated (hi, lo)
+  // pair by TwoSum, so the rounding of the long sum does not grow with K
+  T acc[4][4], lo[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    for (int j = 0; j < 4; ++j) acc[i][j] = lo[i][j] = T(0);
 
-  double ra[4], rb[4];
+  T ra[4], rb[4];
   auto ldA = [&](int k0) {
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -184,7 +191,7 @@ __global__ void __launch_bounds__(256) k_dgemm_simt(int M, int N, int K, double 
       const int gm = m0 + mm, gk = k0 + kk;
       double v = 0.0;
       if (gm < M && gk < kend) v = !TA ? A[gm + lda * gk] : A[gk + lda * gm];
-      ra[r] = v;
+      ra[r] = (T)v;
     }
   };
   auto stA = [&](int st) {
@@ -205,7 +212,7 @@ __global__ void __launch_bounds__(256) k_dgemm_simt(int M, int N, int K, double 
       const int gn = n0 + nn, gk = k0 + kk;
       double v = 0.0;
       if (gn < N && gk < kend) v = !TB ? B[gk + ldb * gn] : B[gn + ldb * gk];
-      rb[r] = v;
+      rb[r] = (T)v;
     }
   };
   auto stB = [&](int st) {
@@ -227,9 +234,14 @@ __global__ void __launch_bounds__(256) k_dgemm_simt(int M, int N, int K, double 
   for (int k0 = kbeg; k0 < kend; k0 += BK) {
     const bool more = (k0 + BK) < kend;
     if (more) { ldA(k0 + BK); ldB(k0 + BK); }
+    T part[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) part[i][j] = kF32 ? T(0) : acc[i][j];
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
-      double af[4], bf[4];
+      T af[4], bf[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) af[i] = As[st][kk][tx + 16 * i];
 #pragma unroll
@@ -237,8 +249,21 @@ __global__ void __launch_bounds__(256) k_dgemm_simt(int M, int N, int K, double 
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(af[i], bf[j], acc[i][j]);
+        for (int j = 0; j < 4; ++j) part[i][j] = fma(af[i], bf[j], part[i][j]);
     }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (kF32) {
+          const T a0 = acc[i][j], b0 = part[i][j];
+          const T sum = a0 + b0, bp = sum - a0;
+          lo[i][j] += (a0 - (sum - bp)) + (b0 - bp);
+          acc[i][j] = sum;
+        } else {
+          acc[i][j] = part[i][j];
+        }
+      }
     if (more) { stA(st ^ 1); stB(st ^ 1); }
     __syncthreads();
     st ^= 1;
@@ -253,7 +278,7 @@ __global__ void __launch_bounds__(256) k_dgemm_simt(int M, int N, int K, double 
       const int gn = n0 + ty + 16 * j;
       if (gn < N) {
         double* c = C + gm + ldc * (long long)gn;
-        double v = alpha * acc[i][j];
+        double v = alpha * ((double)acc[i][j] + (double)lo[i][j]);
         if (beta != 0.0) v += beta * (*c);
         *c = v;
       }
@@ -278,33 +303,40 @@ __global__ void k_splitk_reduce(int m, int n, int S, const double* __restrict__ 
   }
 }
 
+// path: 0 = DMMA, 1 = DFMA, 2 = FP32 products
 template <bool TA, bool TB>
-void launch(bool simt, dim3 grid, cudaStream_t st, int m, int n, int k, double alpha,
+void launch(int path, dim3 grid, cudaStream_t st, int m, int n, int k, double alpha,
             const double* A, long long lda, long long sA, const double* B, long long ldb,
             long long sB, double beta, double* C, long long ldc, long long sC, int kc) {
-  if (simt)
-    k_dgemm_simt<TA, TB><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C,
-                                               ldc, sC, kc);
+  if (path == 1)
+    k_gemm_simt<TA, TB, double><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB,
+                                                      beta, C, ldc, sC, kc);
+  else if (path == 2)
+    k_gemm_simt<TA, TB, float><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB,
+                                                     beta, C, ldc, sC, kc);
   else
     k_dgemm_dmma<TA, TB><<<grid, 128, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C,
                                                ldc, sC, kc);
 }
 
-void launch_any(bool simt, bool TA, bool TB, dim3 grid, cudaStream_t st, int m, int n, int k,
+void launch_any(int path, bool TA, bool TB, dim3 grid, cudaStream_t st, int m, int n, int k,
                 double alpha, const double* A, long long lda, long long sA, const double* B,
                 long long ldb, long long sB, double beta, double* C, long long ldc, long long sC,
                 int kc) {
-  if (!TA && !TB) launch<false, false>(simt, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
-  else if (!TA && TB) launch<false, true>(simt, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
-  else if (TA && !TB) launch<true, false>(simt, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
-  else launch<true, true>(simt, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+  if (!TA && !TB) launch<false, false>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+  else if (!TA && TB) launch<false, true>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+  else if (TA && !TB) launch<true, false>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+  else launch<true, true>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
 }
 
 }  // namespace
 
-int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, const double* A,
-             long long lda, long long strideA, const double* B, long long ldb, long long strideB,
-             double beta, double* C, long long ldc, long long strideC, int batch) {
+namespace {
+
+int gemm_impl(qk_ctx* ctx, bool fp32, char ta, char tb, int m, int n, int k, double alpha,
+              const double* A, long long lda, long long strideA, const double* B, long long ldb,
+              long long strideB, double beta, double* C, long long ldc, long long strideC,
+              int batch) {
   if (m <= 0 || n <= 0 || batch <= 0) return QK_OK;
   if (k <= 0) {
     // C = beta*C: only beta == 0 is needed by callers
@@ -316,7 +348,7 @@ int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, c
   }
   const bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
   // FP64 path: 1 = DFMA (default), 2 = DMMA tensor path; tunable per size of the product
-  const bool simt = qk_tune_get(ctx, TUNE_DGEMM_PATH, (long long)m * n, 1) != 2;
+  const int path = fp32 ? 2 : (qk_tune_get(ctx, TUNE_DGEMM_PATH, (long long)m * n, 1) != 2 ? 1 : 0);
   dim3 grid((m + BM - 1) / BM, (n + BN - 1) / BN, batch);
   if (grid.y > 65535 || grid.z > 65535) return qk_fail(ctx, QK_ERR_ARG, "qk_dgemm: grid too large");
   const long long tiles = (long long)grid.x * grid.y;
@@ -333,7 +365,7 @@ int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, c
       double* W = nullptr;
       QK_TRY(qk_wst(ctx, W_SPLITK, (size_t)S * m * n, &W));
       grid.z = S;
-      launch_any(simt, TA, TB, grid, ctx->stream, m, n, k, 1.0, A, lda, 0, B, ldb, 0, 0.0, W, m,
+      launch_any(path, TA, TB, grid, ctx->stream, m, n, k, 1.0, A, lda, 0, B, ldb, 0, 0.0, W, m,
                  (long long)m * n, kc);
       QK_LAUNCHED();
       long long total = (long long)m * n;
@@ -344,8 +376,25 @@ int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, c
       return QK_OK;
     }
   }
-  launch_any(simt, TA, TB, grid, ctx->stream, m, n, k, alpha, A, lda, strideA, B, ldb, strideB,
+  launch_any(path, TA, TB, grid, ctx->stream, m, n, k, alpha, A, lda, strideA, B, ldb, strideB,
              beta, C, ldc, strideC, 0);
   QK_LAUNCHED();
   return QK_OK;
+}
+
+}  // namespace
+
+int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, const double* A,
+             long long lda, long long strideA, const double* B, long long ldb, long long strideB,
+             double beta, double* C, long long ldc, long long strideC, int batch) {
+  return gemm_impl(ctx, false, ta, tb, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C,
+                   ldc, strideC, batch);
+}
+
+int qk_gemm_f32p(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
+                 const double* A, long long lda, long long strideA, const double* B, long long ldb,
+                 long long strideB, double beta, double* C, long long ldc, long long strideC,
+                 int batch) {
+  return gemm_impl(ctx, true, ta, tb, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C,
+                   ldc, strideC, batch);
 }

@@ -151,9 +151,10 @@ int factor_prep(qk_ctx* ctx, const Dims& d, int naux, const double* L, double** 
 // and, with XpY = D_Om^-1/2 Z_M^T D_s and Z_M = Q Z_T (Householder Q, tridiagonal vectors Z_T):
 //   T = D_Om^-1/2 Z_T^T (Q^T (D_s Lov)),
 // so the eigenvectors of M are never back-transformed: Q^T is applied to the nS x naux factor
-// (2 nS^2 naux flops instead of 2 nS^3) -- all in FP64, the same numbers in another order.
-int casida_factored(qk_ctx* ctx, const Dims& d, const double* e, const double* K, const double* Lov,
-                    int naux, double* Om, double* T, double* scal) {
+// (2 nS^2 naux flops instead of 2 nS^3) -- the same numbers in another order, with FP64
+// products (FP32 products in the mixed tier, whose excitation densities are BF16x3).
+int casida_factored(qk_ctx* ctx, int prec, const Dims& d, const double* e, const double* K,
+                    const double* Lov, int naux, double* Om, double* T, double* scal) {
   const int nS = d.nS;
   const size_t S2 = (size_t)nS * nS;
   double *M = nullptr, *Zt = nullptr, *sq = nullptr, *X = nullptr;
@@ -169,8 +170,10 @@ int casida_factored(qk_ctx* ctx, const Dims& d, const double* e, const double* K
   QK_TRY(qk_launch_omega(ctx, nS, w, Om));
   qk_tic(ctx, T_BACKTRANS);
   QK_TRY(qk_launch_rowscale(ctx, nS, naux, sq, 0, Lov, nS, X, nS));           // D_s Lov
-  QK_TRY(qk_eig_apply_qt(ctx, nS, X, nS, naux));                             // Q^T (.)
-  QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, naux, nS, 1.0, Zt, nS, 0, X, nS, 0, 0.0, T, nS, 0, 1));
+  const int f32 = prec == QK_PREC_BF16X3;  // mixed tier: FP32 products, FP64 storage
+  QK_TRY(qk_eig_apply_qt(ctx, nS, X, nS, naux, f32));                        // Q^T (.)
+  QK_TRY((f32 ? qk_gemm_f32p : qk_dgemm)(ctx, 'N', 'N', nS, naux, nS, 1.0, Zt, nS, 0, X, nS, 0,
+                                         0.0, T, nS, 0, 1));
   QK_TRY(qk_launch_rowscale(ctx, nS, naux, w, 1, T, nS, T, nS));             // D_Om^-1/2
   qk_toc(ctx, T_BACKTRANS);
   QK_TRY(qk_launch_sum_sqrt(ctx, nS, w, scal + 1));
@@ -193,7 +196,7 @@ int rho_from_T(qk_ctx* ctx, int prec, const Dims& d, int naux, const double* L, 
 // Outputs: Om (nS), XpY (nS*nS), optional XmY, sumOm/trA (device scalars) for EcRPA.
 int casida_dev(qk_ctx* ctx, const Dims& d, const double* e, const double* ERI, double* Om,
                double* XpY, double* XmY, double* scal /* [0]=trA [1]=sumOm [2]=EcRPA */,
-               int want_vectors, const double* K = nullptr) {
+               int want_vectors, const double* K = nullptr, int prec = QK_PREC_FP64) {
   const size_t S2 = (size_t)d.nS * d.nS;
   double *M = nullptr, *Zt = nullptr, *sq = nullptr;
   QK_TRY(qk_wst(ctx, W_M, S2, &M));
@@ -207,7 +210,10 @@ int casida_dev(qk_ctx* ctx, const Dims& d, const double* e, const double* ERI, d
   qk_toc(ctx, T_BUILD);
   if (want_vectors) QK_TRY(qk_wst(ctx, W_ZT, S2, &Zt));
   ctx->time_eig = want_vectors != 0;
-  const int est = qk_eig_sym(ctx, d.nS, M, d.nS, w, Zt, want_vectors);
+  // the mixed tier back-transforms the eigenvectors with FP32 products (they feed the BF16x3
+  // excitation densities); eigenvalues, and so Om and EcRPA, are FP64 in every tier
+  const int est = qk_eig_sym(ctx, d.nS, M, d.nS, w, Zt, want_vectors,
+                             prec == QK_PREC_BF16X3 ? 2 : 1);
   ctx->time_eig = true;
   QK_TRY(est);
   if (want_vectors) QK_TRY(qk_launch_xpy(ctx, d.nS, w, Zt, sq, Om, XpY, XmY, XmY != nullptr));
@@ -287,7 +293,7 @@ int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   double* EcGM_d = scal + 8;
   qk_timings_clear(ctx);
   // screening at eHF
-  QK_TRY(casida_dev(ctx, d, eHF, ERI, Om, XpY, nullptr, scal, 1));
+  QK_TRY(casida_dev(ctx, d, eHF, ERI, Om, XpY, nullptr, scal, 1, nullptr, prm->precision));
   // excitation densities
   qk_tic(ctx, T_SLAB);
   QK_TRY(qk_launch_slab_gather(ctx, N, d.nC, d.nO, d.nR, ERI, slab));
@@ -356,12 +362,12 @@ int evgw_cycle(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const EvBufs
   if (b.L) {
     double* T = nullptr;
     QK_TRY(qk_wst(ctx, W_TMAT, (size_t)nS * b.naux, &T));
-    QK_TRY(casida_factored(ctx, d, b.eGW, b.K, b.Lov, b.naux, b.Om, T, b.scal));
+    QK_TRY(casida_factored(ctx, prm->precision, d, b.eGW, b.K, b.Lov, b.naux, b.Om, T, b.scal));
     qk_tic(ctx, T_RHO);
     QK_TRY(rho_from_T(ctx, prm->precision, d, b.naux, b.L, T, b.rho));
     qk_toc(ctx, T_RHO);
   } else {
-    QK_TRY(casida_dev(ctx, d, b.eGW, b.ERI, b.Om, b.XpY, nullptr, b.scal, 1, b.K));
+    QK_TRY(casida_dev(ctx, d, b.eGW, b.ERI, b.Om, b.XpY, nullptr, b.scal, 1, b.K, prm->precision));
     qk_tic(ctx, T_RHO);
     QK_TRY(rho_gemm(ctx, prm->precision, N, nS, b.slab, b.XpY, b.rho));
     qk_toc(ctx, T_RHO);
@@ -535,7 +541,7 @@ int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   double* eGWlin = small + 16;
   double* T = nullptr;
   QK_TRY(qk_wst(ctx, W_TMAT, (size_t)nS * naux, &T));
-  QK_TRY(casida_factored(ctx, d, eHF, K, Lov, naux, Om, T, scal));
+  QK_TRY(casida_factored(ctx, prm->precision, d, eHF, K, Lov, naux, Om, T, scal));
   qk_tic(ctx, T_RHO);
   QK_TRY(rho_from_T(ctx, prm->precision, d, naux, L, T, rho));
   qk_toc(ctx, T_RHO);
@@ -1005,6 +1011,15 @@ int qk_dgemm_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, dou
   QK_TRY(begin(ctx));
   const int st = qk_dgemm(ctx, transa, transb, m, n, k, alpha, d_A, lda, 0, d_B, ldb, 0, beta, d_C,
                           ldc, 0, 1);
+  return end(ctx, st);
+}
+
+int qk_dgemm_f32p_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, double alpha,
+                      const double* d_A, int lda, const double* d_B, int ldb, double beta,
+                      double* d_C, int ldc) {
+  QK_TRY(begin(ctx));
+  const int st = qk_gemm_f32p(ctx, transa, transb, m, n, k, alpha, d_A, lda, 0, d_B, ldb, 0, beta,
+                              d_C, ldc, 0, 1);
   return end(ctx, st);
 }
 

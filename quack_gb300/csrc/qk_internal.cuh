@@ -124,15 +124,21 @@ void qk_timings_collect(qk_ctx* ctx);
 // ------------------------------------------------------------------------------------------
 // kernel-level entry points (all enqueue on ctx->stream; device pointers)
 // ------------------------------------------------------------------------------------------
-// DMMA FP64 GEMM, column-major: C = alpha*op(A)*op(B) + beta*C, batched by strides.
+// FP64 GEMM (DFMA or DMMA), column-major: C = alpha*op(A)*op(B) + beta*C, batched by strides.
 int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, const double* A,
              long long lda, long long strideA, const double* B, long long ldb, long long strideB,
              double beta, double* C, long long ldc, long long strideC, int batch);
+// The same contract with FP32 products and FP32 partial sums (split-K slices added in FP64).
+int qk_gemm_f32p(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
+                 const double* A, long long lda, long long strideA, const double* B, long long ldb,
+                 long long strideB, double beta, double* C, long long ldc, long long strideC,
+                 int batch);
 
-// dense symmetric eigensolver pieces
+// dense symmetric eigensolver pieces.  backtransform: 0 = leave Zt as the eigenvectors of the
+// tridiagonal matrix, 1 = back-transform in FP64, 2 = back-transform with FP32 products.
 int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, int want_vectors,
                int backtransform = 1);
-int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols);
+int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols, int fp32 = 0);
 
 // Casida pieces (k_casida.cu)
 int qk_launch_build_AB(qk_ctx* ctx, int which, int ispin, int dRPA, int N, int nC, int nO, int nR,

@@ -59,6 +59,31 @@ def test_dgemm_dev_matches_numpy(ctx, path):
         ctx.tune_set("dgemm_path", key, max(v, 0))
 
 
+def test_dgemm_f32p_dev_error_bound(ctx):
+    """FP32-product GEMM (the mixed tier's back-transformation): every transpose, ragged sizes
+    and the split-K shape; the error stays within a few FP32 roundings of sum |a_ik b_kj|."""
+    import torch
+    rng = np.random.default_rng(2)
+    shapes = (("N", "N", (70, 33, 45)), ("T", "N", (64, 65, 66)), ("N", "T", (129, 17, 3)),
+              ("T", "T", (5, 200, 77)), ("N", "N", (300, 128, 2000)), ("N", "T", (257, 300, 128)))
+    for ta, tb, (m, n, k) in shapes:
+        A = rng.standard_normal((k, m) if ta == "T" else (m, k))
+        B = rng.standard_normal((n, k) if tb == "T" else (k, n))
+        C0 = rng.standard_normal((m, n))
+        dA = torch.from_numpy(np.asfortranarray(A).ravel(order="F")).cuda()
+        dB = torch.from_numpy(np.asfortranarray(B).ravel(order="F")).cuda()
+        dC = torch.from_numpy(np.asfortranarray(C0).ravel(order="F")).cuda()
+        api.dgemm_f32p_dev(ta, tb, m, n, k, 0.5, dA.data_ptr(), A.shape[0], dB.data_ptr(),
+                           B.shape[0], -1.5, dC.data_ptr(), m, ctx=ctx)
+        opA = A.T if ta == "T" else A
+        opB = B.T if tb == "T" else B
+        ref = 0.5 * opA @ opB - 1.5 * C0
+        scale = 0.5 * np.abs(opA) @ np.abs(opB)
+        C = dC.cpu().numpy().reshape((m, n), order="F")
+        # FP32 rounding of both operands (2^-23 per product) plus the 16-term FP32 tile sums
+        assert np.all(np.abs(C - ref) <= 1e-6 * scale + 1e-13 * np.abs(ref)), (ta, tb)
+
+
 @pytest.mark.parametrize("N,nO,seed", [(40, 5, 21), (64, 8, 24)])
 def test_mixed_g0w0_within_1mev(ctx, N, nO, seed):
     s = synth.small_system(N, nO, 3 * N, seed)
