@@ -218,6 +218,23 @@ int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int method, int nsys
 int qk_dsyev_dev(qk_ctx* ctx, int n, double* d_A, int lda, double* d_w, double* d_Zt,
                  int want_vectors);
 
+/* ---- dRPA correlation energy by frequency quadrature (device pointers) ---------------------
+ * qk_RPA_ecorr_quad_dev: EcRPA = (sum Omega - tr A)/2 of the singlet dRPA problem at orbital
+ *   energies d_e (the quantity phRLR returns, LR/phRLR.f90) without the nS x nS eigenproblem:
+ *   EcRPA = 1/(2 pi) int_0^inf [ln det(1 + Q(w)) - tr Q(w)] dw, Q(w) = 4 L^T diag(d/(d^2+w^2)) L
+ *   for a factor (ia|jb) = L L^T -- the pivoted Cholesky of the (ia|jb) block of d_ERI
+ *   (ERI(nOrb,nOrb,nOrb,nOrb), the block ERI(b,i,j,a) is read), or d_L (L(nOrb,nOrb,naux)); pass
+ *   exactly one.  24-64 Gauss-Legendre points by the width of the e_a - e_i spectrum;
+ *   Q with compensated FP32 products, ln det by FP64 Cholesky; agrees with the eigenvalue
+ *   route to ~1e-8 Ha.  *applied = 0 (EcRPA untouched) when it does not apply: a non-positive
+ *   e_a - e_i, d_max/d_min > 12000, or a numerical rank of (ia|jb) above nS/3.  The mixed tier
+ *   of qk_RG0W0 / qk_RG0W0_L_dev uses it for the EcRPA at the G0W0 energies.
+ * qk_gauss_legendre: the quadrature's nodes x (ascending) and weights w on [-1, 1], host only. */
+int qk_RPA_ecorr_quad_dev(qk_ctx* ctx, int nOrb, int nC, int nO, int nR, int naux,
+                          const double* d_e, const double* d_ERI, const double* d_L,
+                          double* EcRPA, int* applied);
+int qk_gauss_legendre(int n, double* x, double* w);
+
 /* ---- contraction kernels on device buffers (column-major) --------------------------------
  * qk_dgemm_dev: C = alpha*op(A)*op(B) + beta*C in FP64 (DFMA, or DMMA where tuned); replaces the
  *   dgemm calls of AOtoMO/AOtoMO_ERI_RHF.f90:26-53 and GW/RGW_excitation_density.f90:48-50.

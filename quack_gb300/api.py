@@ -359,6 +359,30 @@ def dgemm_dev(transa, transb, m, n, k, alpha, d_A, lda, d_B, ldb, beta, d_C, ldc
                                C.c_double(beta), C.c_void_p(d_C), ldc))
 
 
+def rpa_ecorr_quad_dev(nOrb, nC, nO, nR, d_e, d_ERI=None, d_L=None, naux=0, ctx=None):
+    """dRPA correlation energy at orbital energies d_e by imaginary-frequency quadrature, from
+    the device ERI tensor or the device factor L (one of the two).  Returns EcRPA, or None when
+    the quadrature does not apply (the caller then uses the Casida eigenvalues)."""
+    c = _ctx(ctx)
+    ec = C.c_double(0.0)
+    applied = C.c_int(0)
+    c.check(lib().qk_RPA_ecorr_quad_dev(c.handle, nOrb, nC, nO, nR, naux, C.c_void_p(d_e),
+                                        C.c_void_p(d_ERI or None), C.c_void_p(d_L or None),
+                                        C.byref(ec), C.byref(applied)))
+    return ec.value if applied.value else None
+
+
+def gauss_legendre(n):
+    """Nodes (ascending) and weights of the n-point Gauss-Legendre rule on [-1, 1] (host code
+    of the library; no GPU needed)."""
+    x = np.zeros(n)
+    w = np.zeros(n)
+    rc = lib().qk_gauss_legendre(n, _ptr(x), _ptr(w))
+    if rc != 0:
+        raise QkError(rc, "qk_gauss_legendre")
+    return x, w
+
+
 def dgemm_f32p_dev(transa, transb, m, n, k, alpha, d_A, lda, d_B, ldb, beta, d_C, ldc, ctx=None):
     """The dgemm_dev contract with FP32 products (compensated FP32 sums, FP64 in/out)."""
     c = _ctx(ctx)

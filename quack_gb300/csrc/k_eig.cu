@@ -106,53 +106,71 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       double* pz = a.pbuf + (size_t)((k + 2) % 3) * n;
       for (int i = gthread; i < n; i += totthreads) __stcg(pz + i, 0.0);
     }
-    // ---- small phase (redundant in every CTA): w_k, then v_{k+1} from column j = k+1 ----
+    // ---- small phase (redundant in every CTA): step k's scalars, then v_{k+1} from column j ----
     // FP64 is the scarce resource (one warp instruction per 64 cycles per SM sub-partition), so
-    // the passes are fused: p_k and the raw column j are loaded together and one pass forms w_k,
-    // the updated column and its norm.  The reflector is kept unscaled, u = v / scal with
-    // u_{j+1} = 1/scal: the scale factor goes into the scalars of the next step instead of a
-    // pass over the vector (the big pass computes p~ = A' u, so p = scal p~, and with
-    // w' = scal w the update A - v w^T - w v^T = A - u w'^T - w' u^T keeps its form).
+    // the O(n) work is kept to 4 FMAs per element.  The reflector is kept unscaled, u = v / scal
+    // with u_{j+1} = 1/scal: the scale factor goes into the scalars of the next step instead of
+    // a pass over the vector (the big pass computes p~ = A' u, so p = scal p~).  The rank-2
+    // update A - u w^T - w u^T with w = a1 p~ - a2 u is never formed through w: it is
+    //   A_ic - (a1 u_i) p~_c - (a1 p~_i - 2 a2 u_i) u_c,
+    // two FMAs per element with row scalars, and the column j it exposes is
+    //   A_ij + (a2 u_j - w_j) u_i - (a1 u_j) p~_i.
     const int j = k + 1;
     const int cnt = n - j < nt ? n - j : nt;  // threads holding a non-zero partial sum
     double tau1 = 0.0, scal1 = 1.0;
+    double a1 = 0.0, a2x2 = 0.0;  // step k's update scalars, kept for the big pass
     {
       const double* p = a.pbuf + (size_t)((k + 3) % 3) * n;
       double dot = 0.0;
-      for (int i = j + tid; i < n; i += nt) {
-        vk1[i] = __ldcg(a.A + i + a.lda * j);
-        if (k >= 0) {
-          const double pi = __ldcg(p + i);
-          wk[i] = pi;
-          if (i == j) s_pj = pi;
-          dot = fma(pi, vk[i], dot);
+      // four elements per thread per round, their loads issued together
+      for (int i0 = j + tid; i0 < n; i0 += 4 * nt) {
+        double xv[4], pv[4], uv[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int i = i0 + r * nt;
+          xv[r] = i < n ? __ldcg(a.A + i + a.lda * j) : 0.0;
+          pv[r] = (k >= 0 && i < n) ? __ldcg(p + i) : 0.0;
+          uv[r] = (k >= 0 && i < n) ? vk[i] : 0.0;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int i = i0 + r * nt;
+          if (i < n) {
+            vk1[i] = xv[r];
+            if (k >= 0) {
+              wk[i] = pv[r];
+              if (i == j) s_pj = pv[r];
+              dot = fma(pv[r], uv[r], dot);
+            }
+          }
         }
       }
       if (k >= 0) {
         // (the barriers publish vk1, wk and s_pj as well)
         tri_block_sum(dot, ytile, cnt, [&](double t) {
-          // true dot p.v = scal^2 p~.u;  c = tau^2 dot / 2;  w' = scal^2 (tau p~ - c u)
+          // true dot p.v = scal^2 p~.u;  c = tau^2 dot / 2;  w = scal^2 (tau p~ - c u)
           const double s2 = scal_k * scal_k;
           const double cc = 0.5 * tau_k * tau_k * (s2 * t);
-          const double a1 = tau_k * s2, a2 = cc * s2;
+          const double b1 = tau_k * s2, b2 = cc * s2;
           const double u = vk[j];
-          s_sc[0] = a1;
-          s_sc[1] = a2;
-          s_sc[2] = u;
-          s_sc[6] = a1 * s_pj - a2 * u;
+          const double wj = b1 * s_pj - b2 * u;
+          s_sc[0] = b1;
+          s_sc[1] = b2 + b2;
+          s_sc[2] = b2 * u - wj;  // coefficient of u_i in column j
+          s_sc[6] = -b1 * u;      // coefficient of p~_i in column j
         });
       } else {
         if (tid == 0) s_sc[0] = s_sc[1] = s_sc[2] = s_sc[6] = 0.0;
         __syncthreads();
       }
-      const double a1 = s_sc[0], a2 = s_sc[1], uj = s_sc[2], wj = s_sc[6];
+      a1 = s_sc[0];
+      a2x2 = s_sc[1];
+      const double cu = s_sc[2], cp = s_sc[6];
       double ss = 0.0;
       for (int i = j + tid; i < n; i += nt) {
         double x = vk1[i];
         if (k >= 0) {
-          const double w = a1 * wk[i] - a2 * vk[i];
-          wk[i] = w;
-          x = x - vk[i] * wj - w * uj;
+          x = fma(cp, wk[i], fma(cu, vk[i], x));
           vk1[i] = x;
         }
         if (i == j) s_dj = x;
@@ -219,7 +237,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
         int cur = -1;
         int i = 0;
         bool rowok = false;
-        double vi = 0.0, wi = 0.0, rowacc = 0.0;
+        double ri = 0.0, si = 0.0, rowacc = 0.0;
         for (int it = it0; it < it1; ++it) {
           while (it >= off + 2 * bi + 2) {
             off += 2 * bi + 2;
@@ -230,8 +248,10 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
             cur = bi;
             i = r0 + 32 * bi + lane;
             rowok = i < n;
-            vi = (upd && rowok) ? vk[i] : 0.0;
-            wi = (upd && rowok) ? wk[i] : 0.0;
+            const double ui = (upd && rowok) ? vk[i] : 0.0;
+            const double pi = (upd && rowok) ? wk[i] : 0.0;
+            ri = a1 * ui;                  // row scalars of the rank-2 update
+            si = fma(a1, pi, -a2x2 * ui);
             rowacc = 0.0;
           }
           const int c0 = r0 + TRI_TC * (it - off);
@@ -251,7 +271,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
               const bool ok = rowok && c <= i;
               double y = 0.0;
               if (ok) {
-                y = upd ? x[u] - vi * wk[c] - wi * vk[c] : x[u];
+                y = upd ? x[u] - ri * wk[c] - si * vk[c] : x[u];
                 __stcg(col + a.lda * c, y);
                 rowacc += y * vk1[c];
               }
@@ -873,6 +893,7 @@ extern "C" int qk_dsyev_dev(qk_ctx* ctx, int n, double* d_A, int lda, double* d_
                             int want_vectors) {
   if (!ctx || n < 0 || lda < n) return QK_ERR_ARG;
   cudaSetDevice(ctx->device);
+  QK_TRY(qk_order_after_default(ctx));
   QK_TRY(qk_status_reset(ctx));
   QK_TRY(qk_eig_sym(ctx, n, d_A, lda, d_w, d_Zt, want_vectors, 1));
   return qk_status_check(ctx, QKD_BARRIER_TIMEOUT | QKD_BAD_INDEX);

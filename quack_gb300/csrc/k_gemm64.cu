@@ -32,6 +32,8 @@ __global__ void __launch_bounds__(128) k_dgemm_dmma(int M, int N, int K, double 
   __shared__ double As[2][BK][LDS];
   __shared__ double Bs[2][BK][LDS];
   const long long bz = blockIdx.z;
+  // kc < 0: only the lower triangle of C is wanted, tiles strictly above the diagonal exit
+  if (kc < 0 && (int)(blockIdx.x + 1) * BM <= (int)blockIdx.y * BN) return;
   int kbeg = 0, kend = K;
   if (kc > 0) {  // split-K: slice bz covers [bz*kc, min(K, bz*kc+kc)) and writes its own C slice
     kbeg = (int)bz * kc;
@@ -159,6 +161,7 @@ __global__ void __launch_bounds__(256) k_gemm_simt(int M, int N, int K, double a
   __shared__ T As[2][BK][BM];
   __shared__ T Bs[2][BK][BN];
   const long long bz = blockIdx.z;
+  if (kc < 0 && (int)(blockIdx.x + 1) * BM <= (int)blockIdx.y * BN) return;  // lower C only
   int kbeg = 0, kend = K;
   if (kc > 0) {
     kbeg = (int)bz * kc;
@@ -336,7 +339,7 @@ namespace {
 int gemm_impl(qk_ctx* ctx, bool fp32, char ta, char tb, int m, int n, int k, double alpha,
               const double* A, long long lda, long long strideA, const double* B, long long ldb,
               long long strideB, double beta, double* C, long long ldc, long long strideC,
-              int batch) {
+              int batch, bool lower = false) {
   if (m <= 0 || n <= 0 || batch <= 0) return QK_OK;
   if (k <= 0) {
     // C = beta*C: only beta == 0 is needed by callers
@@ -354,7 +357,7 @@ int gemm_impl(qk_ctx* ctx, bool fp32, char ta, char tb, int m, int n, int k, dou
   const long long tiles = (long long)grid.x * grid.y;
   // fewer output tiles than mult CTAs per SM and a long K: split K and reduce
   const int mult = qk_tune_get(ctx, TUNE_SPLITK_MULT, k, 4);
-  if (batch == 1 && tiles < (long long)mult * ctx->num_sms && k >= 4 * BK) {
+  if (!lower && batch == 1 && tiles < (long long)mult * ctx->num_sms && k >= 4 * BK) {
     int S = (int)(((long long)mult * ctx->num_sms + tiles - 1) / tiles);
     const int maxS = k / (2 * BK);
     if (S > maxS) S = maxS;
@@ -377,7 +380,7 @@ int gemm_impl(qk_ctx* ctx, bool fp32, char ta, char tb, int m, int n, int k, dou
     }
   }
   launch_any(path, TA, TB, grid, ctx->stream, m, n, k, alpha, A, lda, strideA, B, ldb, strideB,
-             beta, C, ldc, strideC, 0);
+             beta, C, ldc, strideC, lower ? -1 : 0);
   QK_LAUNCHED();
   return QK_OK;
 }
@@ -397,4 +400,20 @@ int qk_gemm_f32p(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alph
                  int batch) {
   return gemm_impl(ctx, true, ta, tb, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C,
                    ldc, strideC, batch);
+}
+
+int qk_gemm_f32p_lower(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
+                       const double* A, long long lda, long long strideA, const double* B,
+                       long long ldb, long long strideB, double beta, double* C, long long ldc,
+                       long long strideC, int batch) {
+  return gemm_impl(ctx, true, ta, tb, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C,
+                   ldc, strideC, batch, true);
+}
+
+int qk_dgemm_lower(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
+                   const double* A, long long lda, long long strideA, const double* B,
+                   long long ldb, long long strideB, double beta, double* C, long long ldc,
+                   long long strideC, int batch) {
+  return gemm_impl(ctx, false, ta, tb, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C,
+                   ldc, strideC, batch, true);
 }

@@ -321,6 +321,7 @@ int qk_mlp_set_scaling(qk_mlp* m, const float* xmean, const float* xstd, float y
 int qk_mlp_grad_dev(qk_ctx* ctx, qk_mlp* m, int B, const float* d_X, const float* d_T,
                     float* d_grad, float* loss) {
   if (!ctx || !m || B <= 0) return QK_ERR_ARG;
+  QK_TRY(qk_order_after_default(ctx));
   QK_TRY(mlp_work(ctx, m, B));
   float* Z1 = m->work;
   float* Z2 = Z1 + (size_t)B * NH;
@@ -350,6 +351,7 @@ int qk_mlp_grad_dev(qk_ctx* ctx, qk_mlp* m, int B, const float* d_X, const float
 int qk_mlp_train_dev(qk_ctx* ctx, qk_mlp* m, int n, const float* d_X, const float* d_T, int epochs,
                      int batch, float lr, float* final_loss) {
   if (!ctx || !m || n <= 0 || batch <= 0 || epochs < 0) return QK_ERR_ARG;
+  QK_TRY(qk_order_after_default(ctx));
   if (batch > n) batch = n;
   QK_TRY(mlp_work(ctx, m, batch));
   float* Z1 = m->work;
@@ -393,6 +395,7 @@ int qk_mlp_train_dev(qk_ctx* ctx, qk_mlp* m, int n, const float* d_X, const floa
 // predictions for n samples (normalised inputs) in FP32 or BF16
 int qk_mlp_predict_dev(qk_ctx* ctx, qk_mlp* m, int n, const float* d_X, float* d_Y, int bf16) {
   if (!ctx || !m || n < 0) return QK_ERR_ARG;
+  QK_TRY(qk_order_after_default(ctx));
   if (n == 0) return QK_OK;
   if (bf16)
     k_mlp_infer_bf16<<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, d_X, m->P, d_Y);

@@ -1,0 +1,560 @@
+// k_rpa_quad.cu -- dRPA correlation energy by imaginary-frequency quadrature.
+//
+// The reference computes EcRPA = (sum_m Omega_m - tr A) / 2 from the eigenvalues of the Casida
+// problem (LR/phRLR.f90, called a second time at the G0W0 energies by RG0W0.f90:222-225).  With
+// D = diag(e_a - e_i) and K = (ia|jb), the singlet dRPA problem is M = D^1/2 (D + 4K) D^1/2,
+// Omega^2 = eig(M), tr A = tr D + 2 tr K, and for any factor K = L L^T (L: nS x r)
+//   det(M + w^2) / det(D^2 + w^2) = det(I_r + Q(w)),   Q(w) = 4 L^T diag(d / (d^2 + w^2)) L,
+// while  int_0^inf ln((x + w^2)/(y + w^2)) dw = pi (sqrt(x) - sqrt(y))  and
+// int_0^inf tr Q(w) dw = 2 pi tr K, so that
+//   EcRPA = 1/(2 pi) int_0^inf [ ln det(I + Q(w)) - tr Q(w) ] dw
+// exactly.  The integrand is smooth and decays as w^-4; Gauss-Legendre on w = w0 (1+x)/(1-x)
+// with w0 = sqrt(d_min d_max) and 24-64 points (by the width d_max/d_min of the spectrum)
+// reproduces the eigenvalue route to ~1e-10 Ha.  Cost: r x r problems instead of nS x nS:
+//   * the factor: Lov (factorised integrals, r = naux) or a pivoted Cholesky of K (ERI input,
+//     stopped at 1e-12 of the largest diagonal; r = the numerical rank);
+//   * Q for all points: one batched GEMM with compensated FP32 products (error ~1e-9 Ha);
+//   * ln det(I + Q) - tr Q: blocked FP64 Cholesky carried on S = (Schur complement) - I, so that
+//     each pivot contributes (log1p(s) - s) - (Q_ii - s), both second order in Q: no
+//     cancellation of the two first-order terms at large w.
+// Used by the mixed tier for the EcRPA of the G0W0 energies; every other EcRPA comes from the
+// Casida eigenvalues.
+#include <cmath>
+#include <mutex>
+#include <vector>
+#include "qk_internal.cuh"
+
+namespace {
+
+constexpr int CB = 64;  // Cholesky block
+
+// d_ia = e_a - e_i (ia = i * nv + a, the Casida ordering) and [min, max] of d
+__global__ void k_quad_delta(int nS, int nv, int nC, int nO, const double* __restrict__ e,
+                             double* __restrict__ dd, double* __restrict__ mm) {
+  __shared__ double smin[32], smax[32];
+  double lo = INFINITY, hi = -INFINITY;
+  for (int ia = threadIdx.x; ia < nS; ia += blockDim.x) {
+    const int ip = ia / nv, ap = ia - ip * nv;
+    const double v = e[ap + nO] - e[ip + nC];
+    dd[ia] = v;
+    lo = fmin(lo, v);
+    hi = fmax(hi, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { smin[w] = lo; smax[w] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) { lo = fmin(lo, smin[i]); hi = fmax(hi, smax[i]); }
+    mm[0] = fmin(lo, smin[0]);
+    mm[1] = fmax(hi, smax[0]);
+  }
+}
+
+// K(ia, jb) = (ia|jb) = ERI(b, i, j, a) (Fortran ERI(p,q,r,s) at p + N q + N^2 r + N^3 s),
+// column-major nS x nS; tiles of 32 a x 32 b for one (i, j), read along b, written along a.
+__global__ void k_gather_K(int N, int nC, int nO, int nR, const double* __restrict__ ERI,
+                           double* __restrict__ K) {
+  __shared__ double t[32][33];
+  const int no = nO - nC, nv = N - nO - nR;
+  const long long nS = (long long)no * nv;
+  const int ij = blockIdx.z;
+  const int ip = ij / no, jp = ij - ip * no;
+  const long long N1 = N, N2 = N1 * N1, N3 = N2 * N1;
+  const int a0 = blockIdx.x * 32, b0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    const int ap = a0 + r, bp = b0 + tx;
+    t[r][tx] = (ap < nv && bp < nv)
+                   ? __ldg(ERI + (bp + nO) + N1 * (ip + nC) + N2 * (jp + nC) + N3 * (ap + nO))
+                   : 0.0;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int ap = a0 + tx, bp = b0 + r;
+    if (ap < nv && bp < nv) K[(long long)ip * nv + ap + nS * ((long long)jp * nv + bp)] = t[tx][r];
+  }
+}
+
+struct PcArgs {
+  const double* K;
+  long long ldk;
+  int nS, rmax;
+  double tol_rel;
+  double* Lt;      // rmax x nS, column-major: Lt[t + rmax * i] = L(i, t)
+  double* r;       // residual diagonal
+  int* done;       // pivoted rows
+  double* sval;    // per-CTA argmax candidates, two sets (even / odd steps)
+  int* sidx;
+  int* rank;
+  unsigned* bar;
+  int* status;
+};
+
+// argmax with ties to the lowest index (so that every CTA picks the same pivot)
+__device__ __forceinline__ void amax_merge(double& v, int& i, double v2, int i2) {
+  if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+}
+
+// Left-looking pivoted Cholesky of K in one cooperative launch: per pivot, every CTA finds the
+// global pivot from the per-CTA candidates, each warp forms one row of the new column
+// (l_i = (K_ip - L_i . L_p) / sqrt(r_p)) and updates r_i, and one bounded grid barrier closes
+// the step.  Deterministic: no atomics on the data, fixed reduction orders.
+__global__ void __launch_bounds__(1024) k_pchol(PcArgs a) {
+  extern __shared__ double lp[];  // row p of L (a.rmax doubles)
+  __shared__ double wv[32];
+  __shared__ int wi[32];
+  __shared__ double s_rp, s_inv, s_tol;
+  __shared__ int s_p;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int gw = blockIdx.x * 32 + warp, totw = gridDim.x * 32;
+  unsigned epoch = 0;
+
+  int par = 0;  // candidate set written this step (the other one may still be read)
+  auto cta_candidate = [&](double v, int i) {
+    for (int o = 16; o > 0; o >>= 1) {
+      const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+      amax_merge(v, i, v2, i2);
+    }
+    if (lane == 0) { wv[warp] = v; wi[warp] = i; }
+    __syncthreads();
+    if (warp == 0) {
+      v = lane < (int)(blockDim.x >> 5) ? wv[lane] : -INFINITY;
+      i = lane < (int)(blockDim.x >> 5) ? wi[lane] : 0x7fffffff;
+      for (int o = 16; o > 0; o >>= 1) {
+        const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+        amax_merge(v, i, v2, i2);
+      }
+      if (lane == 0) {
+        a.sval[par * gridDim.x + blockIdx.x] = v;
+        a.sidx[par * gridDim.x + blockIdx.x] = i;
+      }
+    }
+  };
+  auto global_pivot = [&]() {
+    if (warp == 0) {
+      double v = -INFINITY;
+      int i = 0x7fffffff;
+      for (int c = lane; c < (int)gridDim.x; c += 32)
+        amax_merge(v, i, __ldcg(a.sval + par * gridDim.x + c), __ldcg(a.sidx + par * gridDim.x + c));
+      for (int o = 16; o > 0; o >>= 1) {
+        const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+        amax_merge(v, i, v2, i2);
+      }
+      if (lane == 0) {
+        s_rp = v;
+        s_p = i;
+        s_inv = v > 0.0 ? 1.0 / sqrt(v) : 0.0;
+      }
+    }
+    __syncthreads();
+  };
+
+  // residual diagonal = diag(K); candidates
+  {
+    double v = -INFINITY;
+    int vi = 0x7fffffff;
+    for (int i = blockIdx.x * blockDim.x + tid; i < a.nS; i += gridDim.x * blockDim.x) {
+      const double x = a.K[i + a.ldk * i];
+      a.r[i] = x;
+      a.done[i] = 0;
+      amax_merge(v, vi, x, i);
+    }
+    cta_candidate(v, vi);
+  }
+  if (!qk_grid_barrier(a.bar, gridDim.x, epoch, a.status)) return;
+  global_pivot();
+  par ^= 1;
+  if (tid == 0) s_tol = a.tol_rel * s_rp;
+  __syncthreads();
+  const double tol = s_tol;
+  int q = 0;
+  for (; q < a.rmax; ++q) {
+    if (q > 0) {
+      global_pivot();
+      par ^= 1;
+    }
+    const double rp = s_rp;
+    const int p = s_p;
+    if (!(rp > tol) || p < 0 || p >= a.nS) break;  // uniform: every CTA read the same candidates
+    for (int t = tid; t < q; t += blockDim.x) lp[t] = __ldcg(a.Lt + t + (long long)a.rmax * p);
+    __syncthreads();
+    const double inv = s_inv;
+    double v = -INFINITY;
+    int vi = 0x7fffffff;
+    for (int i = gw; i < a.nS; i += totw) {
+      double* li = a.Lt + (long long)a.rmax * i;
+      double s0 = 0.0, s1 = 0.0;
+      int t = lane;
+      for (; t + 32 < q; t += 64) {
+        s0 = fma(li[t], lp[t], s0);
+        s1 = fma(li[t + 32], lp[t + 32], s1);
+      }
+      if (t < q) s0 = fma(li[t], lp[t], s0);
+      double s = s0 + s1;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) {
+        double l = 0.0, rn = a.r[i];
+        if (i == p) {
+          l = sqrt(rp);  // L_pp
+          rn = 0.0;
+          a.done[i] = 1;
+        } else if (!a.done[i]) {
+          l = (a.K[i + a.ldk * p] - s) * inv;
+          rn = rn - l * l;
+        }
+        li[q] = l;
+        a.r[i] = rn;
+        if (!a.done[i]) amax_merge(v, vi, rn, i);
+      }
+    }
+    cta_candidate(v, vi);
+    if (!qk_grid_barrier(a.bar, gridDim.x, epoch, a.status)) return;
+  }
+  if (blockIdx.x == 0 && tid == 0) *a.rank = q;
+}
+
+// L (nS x r, column-major) from Lt (rmax x nS): 32 x 32 tiles through shared memory
+__global__ void k_lt_transpose(int nS, int r, int rmax, const double* __restrict__ Lt,
+                               double* __restrict__ L) {
+  __shared__ double t[32][33];
+  const int i0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int k = ty; k < 32; k += 8) {
+    const int i = i0 + k, tt = t0 + tx;
+    t[k][tx] = (i < nS && tt < r) ? Lt[tt + (long long)rmax * i] : 0.0;
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int i = i0 + tx, tt = t0 + k;
+    if (i < nS && tt < r) L[i + (long long)nS * tt] = t[tx][k];
+  }
+}
+
+// X_q(i, t) = L(i, t) * sqrt(4 d_i / (d_i^2 + w_q^2)) for the points of one chunk
+__global__ void k_quad_scale(int nS, int r, const double* __restrict__ L, long long ldl,
+                             const double* __restrict__ dd, const double* __restrict__ om,
+                             int nch, double* __restrict__ X) {
+  const long long per = (long long)nS * r;
+  const long long total = per * nch;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(idx / per);
+    const long long rem = idx - per * q;
+    const int t = (int)(rem / nS), i = (int)(rem - (long long)t * nS);
+    const double d = dd[i], w = om[q];
+    X[idx] = L[i + ldl * t] * sqrt(4.0 * d / fma(d, d, w * w));
+  }
+}
+
+// diag(Q_q) saved before the factorisation overwrites it
+__global__ void k_quad_diag(int r, int nch, const double* __restrict__ Q, double* __restrict__ qd) {
+  const int total = r * nch;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    const int q = idx / r, i = idx - q * r;
+    qd[idx] = Q[(long long)q * r * r + i + (long long)r * i];
+  }
+}
+
+// Diagonal block kb..kb+nb of every matrix: unblocked Cholesky of I + S (S stored, the identity
+// implicit), L11 written back, and the pivots' contributions to ln det(I+Q) - tr Q added to acc.
+__global__ void __launch_bounds__(256) k_chol_blk(int r, int kb, int nb, double* __restrict__ S,
+                                                  const double* __restrict__ qd,
+                                                  double* __restrict__ acc) {
+  __shared__ double A[CB][CB + 1];
+  __shared__ double sv[CB];
+  __shared__ double s_inv;
+  __shared__ double red[8];
+  const int q = blockIdx.x, tid = threadIdx.x;
+  double* Sq = S + (long long)q * r * r;
+  for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+    const int j = idx % nb, k = idx / nb;
+    A[j][k] = (j >= k) ? Sq[(kb + j) + (long long)r * (kb + k)] : 0.0;
+  }
+  __syncthreads();
+  for (int c = 0; c < nb; ++c) {
+    if (tid == 0) {
+      const double s = A[c][c];
+      sv[c] = s;
+      const double l = sqrt(1.0 + s);
+      A[c][c] = l;
+      s_inv = 1.0 / l;
+    }
+    __syncthreads();
+    const double inv = s_inv;
+    for (int j = c + 1 + tid; j < nb; j += blockDim.x) A[j][c] *= inv;
+    __syncthreads();
+    const int m = nb - c - 1;
+    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+      const int jj = idx % m, kk = idx / m;
+      if (jj >= kk) {
+        const int j = c + 1 + jj, k = c + 1 + kk;
+        A[j][k] = fma(-A[j][c], A[k][c], A[j][k]);
+      }
+    }
+    __syncthreads();
+  }
+  double t = 0.0;
+  for (int c = tid; c < nb; c += blockDim.x) {
+    const double s = sv[c];
+    t += (log1p(s) - s) - (qd[(long long)q * r + kb + c] - s);
+  }
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((tid & 31) == 0) red[tid >> 5] = t;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    acc[q] += s;
+  }
+  for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+    const int j = idx % nb, k = idx / nb;
+    if (j >= k) Sq[(kb + j) + (long long)r * (kb + k)] = A[j][k];
+  }
+}
+
+// Panel below the diagonal block: P = S(rows, kb:kb+nb) L11^-T, one row per thread, held in
+// registers; column-oriented so that the updates of one step are independent.
+__global__ void __launch_bounds__(128) k_chol_trsm(int r, int kb, int nb, double* __restrict__ S) {
+  __shared__ double L[CB][CB + 1];
+  __shared__ double rinv[CB];
+  const int q = blockIdx.y, tid = threadIdx.x;
+  double* Sq = S + (long long)q * r * r;
+  for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+    const int j = idx % nb, k = idx / nb;
+    L[j][k] = (j >= k) ? Sq[(kb + j) + (long long)r * (kb + k)] : 0.0;
+  }
+  __syncthreads();
+  for (int c = tid; c < nb; c += blockDim.x) rinv[c] = 1.0 / L[c][c];
+  __syncthreads();
+  const int row = kb + nb + blockIdx.x * blockDim.x + tid;
+  if (row >= r) return;
+  double x[CB];
+#pragma unroll
+  for (int c = 0; c < CB; ++c) x[c] = c < nb ? Sq[row + (long long)r * (kb + c)] : 0.0;
+#pragma unroll
+  for (int c = 0; c < CB; ++c) {
+    if (c < nb) {
+      x[c] *= rinv[c];
+#pragma unroll
+      for (int k = c + 1; k < CB; ++k)
+        if (k < nb) x[k] = fma(-x[c], L[k][c], x[k]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < CB; ++c)
+    if (c < nb) Sq[row + (long long)r * (kb + c)] = x[c];
+}
+
+__global__ void k_quad_final(int nq, const double* __restrict__ wt, const double* __restrict__ acc,
+                             double* __restrict__ Ec) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < nq; ++q) s = fma(wt[q], acc[q], s);
+    *Ec = s * (0.5 / M_PI);
+  }
+}
+
+// points for the width d_max / d_min of the spectrum (0: too wide, use the eigenvalues)
+int quad_points(double ratio) {
+  if (ratio <= 40.0) return 24;
+  if (ratio <= 300.0) return 32;
+  if (ratio <= 2500.0) return 48;
+  if (ratio <= 12000.0) return 64;
+  return 0;
+}
+
+}  // namespace
+
+void qk_gauss_legendre_host(int n, double* x, double* w) {
+  // roots of P_n by Newton from the asymptotic guesses cos(pi (k - 1/4) / (n + 1/2)); P_n and
+  // P_n' by the three-term recurrence; weights 2 / ((1 - x^2) P_n'(x)^2); nodes ascending
+  for (int k = 0; k < (n + 1) / 2; ++k) {
+    double z = cos(M_PI * (k + 0.75) / (n + 0.5));
+    double dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int j = 2; j <= n; ++j) {
+        const double p2 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p0) / j;
+        p0 = p1;
+        p1 = p2;
+      }
+      if (n == 1) { p1 = z; p0 = 1.0; }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-16) break;
+    }
+    {
+      double p0 = 1.0, p1 = z;
+      for (int j = 2; j <= n; ++j) {
+        const double p2 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p0) / j;
+        p0 = p1;
+        p1 = p2;
+      }
+      if (n == 1) { p1 = z; p0 = 1.0; }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+    }
+    const double wk = 2.0 / ((1.0 - z * z) * dp * dp);
+    x[k] = -z;
+    x[n - 1 - k] = z;
+    w[k] = w[n - 1 - k] = wk;
+  }
+  if (n % 2 == 1) x[n / 2] = 0.0;
+}
+
+int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, const double* ERI,
+                   const double* Lov, int naux, double* Ec, int* applied) {
+  *applied = 0;
+  const int no = nO - nC, nv = N - nO - nR, nS = no * nv;
+  if (nS <= 0 || (!ERI && !Lov)) return QK_OK;
+  double *dd = nullptr, *small = nullptr;
+  QK_TRY(qk_wst(ctx, W_QUAD, (size_t)nS + 1024, &dd));
+  small = dd + nS;  // [0,2): d range; [8,8+64): nodes; [72,136): weights; [136,200): acc
+  k_quad_delta<<<1, 1024, 0, ctx->stream>>>(nS, nv, nC, nO, e, dd, small);
+  QK_LAUNCHED();
+  double mm[2];
+  QK_CK(cudaMemcpyAsync(mm, small, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QK_CK(cudaStreamSynchronize(ctx->stream));
+  if (!(mm[0] > 0.0) || !(mm[1] >= mm[0])) return QK_OK;
+  const int nq = quad_points(mm[1] / mm[0]);
+  if (nq == 0) return QK_OK;
+
+  // the factor L (nS x r)
+  const double* L = Lov;
+  long long ldl = nS;
+  int r = naux;
+  if (!Lov) {
+    const int rmax = nS / 3 > (nS < 64 ? nS : 64) ? nS / 3 : (nS < 64 ? nS : 64);
+    double *K = nullptr, *Lt = nullptr, *Lc = nullptr, *pv = nullptr;
+    QK_TRY(qk_wst(ctx, W_M, (size_t)nS * nS, &K));
+    QK_TRY(qk_wst(ctx, W_QLT, (size_t)rmax * nS, &Lt));
+    QK_TRY(qk_wst(ctx, W_QPV, (size_t)2 * nS + 4 * ctx->num_sms + 64, &pv));
+    dim3 gg((nv + 31) / 32, (nv + 31) / 32, no * no);
+    if (gg.z > 65535) return QK_OK;
+    k_gather_K<<<gg, dim3(32, 8), 0, ctx->stream>>>(N, nC, nO, nR, ERI, K);
+    QK_LAUNCHED();
+    PcArgs pa;
+    pa.K = K;
+    pa.ldk = nS;
+    pa.nS = nS;
+    pa.rmax = rmax;
+    pa.tol_rel = 1e-12;
+    pa.Lt = Lt;
+    pa.r = pv;
+    pa.done = (int*)(pv + nS);
+    pa.sval = pv + 2 * nS;                              // 2 * grid doubles
+    pa.sidx = (int*)(pv + 2 * nS + 2 * ctx->num_sms);   // 2 * grid ints
+    pa.rank = (int*)(pv + 2 * nS + 3 * ctx->num_sms);
+    pa.bar = ctx->d_bar;
+    pa.status = ctx->d_status;
+    int grid = (nS + 31) / 32;
+    if (grid > ctx->num_sms) grid = ctx->num_sms;
+    const size_t smem = (size_t)rmax * sizeof(double);
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+      attr_err = cudaFuncSetAttribute(k_pchol, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      160 * 1024);
+    });
+    QK_CK(attr_err);
+    if (smem > 160 * 1024) return QK_OK;
+    int per_sm = 0;
+    QK_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pchol, 1024, smem));
+    if (per_sm < 1) return QK_OK;
+    QK_CK(cudaMemsetAsync(ctx->d_bar, 0, 16 * sizeof(unsigned), ctx->stream));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(1024);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    QK_CK(cudaLaunchKernelEx(&cfg, k_pchol, pa));
+    ctx->launches++;
+    int rank = 0;
+    QK_CK(cudaMemcpyAsync(&rank, pa.rank, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    QK_CK(cudaStreamSynchronize(ctx->stream));
+    int hst = 0;
+    QK_CK(cudaMemcpy(&hst, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (hst & QKD_BARRIER_TIMEOUT)
+      return qk_fail(ctx, QK_ERR_DEVICE, "pivoted Cholesky: grid barrier timed out");
+    if (rank <= 0 || rank >= rmax) return QK_OK;  // numerically full rank: eigenvalue route
+    QK_TRY(qk_wst(ctx, W_QL, (size_t)nS * rank, &Lc));
+    dim3 tg((nS + 31) / 32, (rank + 31) / 32);
+    k_lt_transpose<<<tg, dim3(32, 8), 0, ctx->stream>>>(nS, rank, rmax, Lt, Lc);
+    QK_LAUNCHED();
+    L = Lc;
+    ldl = nS;
+    r = rank;
+  }
+
+  // quadrature points
+  std::vector<double> x(nq), wg(nq), hb(2 * nq);
+  qk_gauss_legendre_host(nq, x.data(), wg.data());
+  const double w0 = sqrt(mm[0] * mm[1]);
+  for (int k = 0; k < nq; ++k) {
+    hb[k] = w0 * (1.0 + x[k]) / (1.0 - x[k]);
+    hb[nq + k] = wg[k] * 2.0 * w0 / ((1.0 - x[k]) * (1.0 - x[k]));
+  }
+  double* om = small + 8;
+  double* wt = small + 72;
+  double* acc = small + 136;
+  QK_CK(cudaMemcpyAsync(om, hb.data(), nq * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  QK_CK(cudaMemcpyAsync(wt, hb.data() + nq, nq * sizeof(double), cudaMemcpyHostToDevice,
+                        ctx->stream));
+  QK_CK(cudaMemsetAsync(acc, 0, nq * sizeof(double), ctx->stream));
+  // the host copies above read hb before this function returns
+  QK_CK(cudaStreamSynchronize(ctx->stream));
+
+  // chunks of points: X (nch x nS x r) at most ~4 GB
+  const size_t per = (size_t)nS * r;
+  int nch = (int)((size_t)(512u << 20) / (per > 0 ? per : 1));
+  if (nch < 1) nch = 1;
+  if (nch > nq) nch = nq;
+  double *X = nullptr, *Q = nullptr, *qd = nullptr;
+  QK_TRY(qk_wst(ctx, W_QX, per * nch, &X));
+  QK_TRY(qk_wst(ctx, W_QQ, (size_t)r * r * nch, &Q));
+  QK_TRY(qk_wst(ctx, W_QD, (size_t)r * nch, &qd));
+  const long long r2 = (long long)r * r;
+  for (int q0 = 0; q0 < nq; q0 += nch) {
+    const int nc = nq - q0 < nch ? nq - q0 : nch;
+    {
+      const long long total = (long long)per * nc;
+      int blocks = (int)((total + 255) / 256);
+      if (blocks > 16 * ctx->num_sms) blocks = 16 * ctx->num_sms;
+      k_quad_scale<<<blocks, 256, 0, ctx->stream>>>(nS, r, L, ldl, dd, om + q0, nc, X);
+      QK_LAUNCHED();
+    }
+    // the lower triangle of Q_q = X_q^T X_q (all the factorisation reads)
+    QK_TRY(qk_gemm_f32p_lower(ctx, 'T', 'N', r, r, nS, 1.0, X, nS, (long long)per, X, nS,
+                              (long long)per, 0.0, Q, r, r2, nc));
+    k_quad_diag<<<(r * nc + 255) / 256, 256, 0, ctx->stream>>>(r, nc, Q, qd);
+    QK_LAUNCHED();
+    for (int kb = 0; kb < r; kb += CB) {
+      const int nb = r - kb < CB ? r - kb : CB;
+      k_chol_blk<<<nc, 256, 0, ctx->stream>>>(r, kb, nb, Q, qd, acc + q0);
+      QK_LAUNCHED();
+      const int m = r - kb - nb;
+      if (m <= 0) break;
+      k_chol_trsm<<<dim3((m + 127) / 128, nc), 128, 0, ctx->stream>>>(r, kb, nb, Q);
+      QK_LAUNCHED();
+      double* P = Q + (kb + nb) + (long long)r * kb;
+      double* S22 = Q + (kb + nb) + (long long)r * (kb + nb);
+      QK_TRY(qk_dgemm_lower(ctx, 'N', 'T', m, m, nb, -1.0, P, r, r2, P, r, r2, 1.0, S22, r, r2, nc));
+    }
+  }
+  k_quad_final<<<1, 32, 0, ctx->stream>>>(nq, wt, acc, Ec);
+  QK_LAUNCHED();
+  *applied = 1;
+  return QK_OK;
+}

@@ -313,9 +313,13 @@ int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   qk_tic(ctx, T_QP);
   QK_TRY(g0w0_qp(ctx, prm, d, flow, eHF, Om, rho, SigC, Z, eGWlin, eGW, ffp));
   qk_toc(ctx, T_QP);
-  // second Casida at eGW for EcRPA (RG0W0.f90:222-225): eigenvalues only
+  // second Casida at eGW for EcRPA (RG0W0.f90:222-225): eigenvalues only; the mixed tier
+  // takes the frequency quadrature of the same energy (r x r problems instead of nS x nS)
   qk_tic(ctx, T_CASIDA2);
-  QK_TRY(casida_dev(ctx, d, eGW, ERI, nullptr, nullptr, nullptr, scal + 3, 0));
+  int quad = 0;
+  if (prm->precision == QK_PREC_BF16X3)
+    QK_TRY(qk_rpa_ec_quad(ctx, N, d.nC, d.nO, d.nR, eGW, ERI, nullptr, 0, scal + 5, &quad));
+  if (!quad) QK_TRY(casida_dev(ctx, d, eGW, ERI, nullptr, nullptr, nullptr, scal + 3, 0));
   qk_toc(ctx, T_CASIDA2);
   double h[16];
   QK_TRY(d2h(ctx, h, scal, 16 * sizeof(double)));
@@ -557,7 +561,10 @@ int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   QK_TRY(g0w0_qp(ctx, prm, d, flow, eHF, Om, rho, SigC, Z, eGWlin, eGW, ffp));
   qk_toc(ctx, T_QP);
   qk_tic(ctx, T_CASIDA2);
-  QK_TRY(casida_dev(ctx, d, eGW, nullptr, nullptr, nullptr, nullptr, scal + 3, 0, K));
+  int quad = 0;
+  if (prm->precision == QK_PREC_BF16X3)
+    QK_TRY(qk_rpa_ec_quad(ctx, N, d.nC, d.nO, d.nR, eGW, nullptr, Lov, naux, scal + 5, &quad));
+  if (!quad) QK_TRY(casida_dev(ctx, d, eGW, nullptr, nullptr, nullptr, nullptr, scal + 3, 0, K));
   qk_toc(ctx, T_CASIDA2);
   double h[16];
   QK_TRY(d2h(ctx, h, scal, 16 * sizeof(double)));
@@ -639,6 +646,7 @@ int begin(qk_ctx* ctx) {
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return qk_cuda_fail(ctx, e, "cudaSetDevice", __FILE__, __LINE__);
   ctx->err.clear();
+  QK_TRY(qk_order_after_default(ctx));
   return qk_status_reset(ctx);
 }
 
@@ -1012,6 +1020,37 @@ int qk_dgemm_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, dou
   const int st = qk_dgemm(ctx, transa, transb, m, n, k, alpha, d_A, lda, 0, d_B, ldb, 0, beta, d_C,
                           ldc, 0, 1);
   return end(ctx, st);
+}
+
+int qk_RPA_ecorr_quad_dev(qk_ctx* ctx, int nOrb, int nC, int nO, int nR, int naux,
+                          const double* d_e, const double* d_ERI, const double* d_L,
+                          double* EcRPA, int* applied) {
+  QK_TRY(begin(ctx));
+  if (!EcRPA || !applied || (!d_ERI) == (!d_L) || (d_L && naux <= 0))
+    return qk_fail(ctx, QK_ERR_ARG, "one of ERI / L (with naux > 0) and the outputs required");
+  Dims d;
+  const int nS = (nO - nC) * (nOrb - nO - nR);
+  QK_TRY(check_dims(ctx, nOrb, nOrb, nC, nO, nOrb - nO, nR, nS, &d));
+  double* Lov = nullptr;
+  if (d_L) {
+    QK_TRY(qk_wst(ctx, W_VEC2, (size_t)nS * naux, &Lov));
+    QK_TRY(qk_launch_gather_ov(ctx, nOrb, nC, nO, nR, naux, d_L, Lov));
+  }
+  double* dEc = nullptr;
+  QK_TRY(qk_wst(ctx, W_HOST_A, 8, &dEc));
+  int used = 0;
+  const int st = qk_rpa_ec_quad(ctx, nOrb, nC, nO, nR, d_e, d_ERI, Lov, naux, dEc, &used);
+  if (st != QK_OK) return end(ctx, st);
+  *applied = used;
+  *EcRPA = 0.0;
+  if (used) QK_TRY(d2h(ctx, EcRPA, dEc, sizeof(double)));
+  return end(ctx, QK_OK);
+}
+
+int qk_gauss_legendre(int n, double* x, double* w) {
+  if (n < 1 || n > 4096 || !x || !w) return QK_ERR_ARG;
+  qk_gauss_legendre_host(n, x, w);
+  return QK_OK;
 }
 
 int qk_dgemm_f32p_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, double alpha,

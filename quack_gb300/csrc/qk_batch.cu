@@ -46,9 +46,13 @@ extern "C" int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int metho
     if (rc != QK_OK) return qk_fail(ctx, rc, "could not create batch worker context");
     ctx->workers.push_back(w);
   }
-  // each worker's cooperative tridiagonalisation gets a share of the SMs
+  // each worker's cooperative tridiagonalisation gets a share of the SMs; every worker stream
+  // starts after the caller's default-stream work (the packed inputs)
   const int share = ctx->num_sms / n_workers > 16 ? ctx->num_sms / n_workers : 16;
-  for (int wi = 0; wi < n_workers; ++wi) ctx->workers[wi]->sytrd_max_ctas = share;
+  for (int wi = 0; wi < n_workers; ++wi) {
+    ctx->workers[wi]->sytrd_max_ctas = share;
+    QK_TRY(qk_order_after_default(ctx->workers[wi]));
+  }
   std::vector<Item> order(nsys);
   for (int i = 0; i < nsys; ++i) {
     const double nS = (double)(desc[i].nO - desc[i].nC) * (desc[i].nOrb - desc[i].nO - desc[i].nR);

@@ -63,6 +63,12 @@ int qk_status_check(qk_ctx* ctx, int fatal_mask) {
   return QK_OK;
 }
 
+int qk_order_after_default(qk_ctx* ctx) {
+  QK_CK(cudaEventRecord(ctx->ev_in, cudaStreamLegacy));
+  QK_CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_in, 0));
+  return QK_OK;
+}
+
 void qk_tic(qk_ctx* ctx, int stage) {
   if (ctx->timing && !ctx->capturing) cudaEventRecord(ctx->ev[2 * stage], ctx->stream);
 }
@@ -107,6 +113,7 @@ int qk_init(int device, qk_ctx** out) {
     return QK_ERR_CUDA;
   }
   for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+  cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming);
   if (cudaMalloc(&ctx->d_status, 256) != cudaSuccess ||
       cudaMalloc(&ctx->d_bar, 256 * sizeof(unsigned)) != cudaSuccess) {
     qk_finalize(ctx);
@@ -132,6 +139,7 @@ int qk_finalize(qk_ctx* ctx) {
   if (ctx->d_bar) cudaFree(ctx->d_bar);
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
+  if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return QK_OK;

@@ -36,7 +36,8 @@ struct DevBuf {
 
 enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
-  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_TMAT2, W_RHO32, W_OMF, W_TFAC, W_STEBZ, W_NUMBUF
+  W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_TMAT2, W_RHO32, W_OMF, W_TFAC, W_STEBZ,
+  W_QUAD, W_QLT, W_QPV, W_QL, W_QX, W_QQ, W_QD, W_NUMBUF
 };
 
 struct qk_ctx {
@@ -44,6 +45,7 @@ struct qk_ctx {
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2 * T_NUM + 2] = {};
+  cudaEvent_t ev_in = nullptr;  // orders the stream after the caller's default-stream work
   double timings[T_NUM] = {};
   std::string err;
   int* d_status = nullptr;      // device status word
@@ -111,6 +113,9 @@ template <class T>
 inline int qk_wst(qk_ctx* ctx, int slot, size_t count, T** out) {
   return qk_ws(ctx, slot, count * sizeof(T), (void**)out);
 }
+// make ctx->stream wait for the work already enqueued on the legacy default stream (where a
+// caller such as PyTorch writes the device inputs), without a host synchronisation
+int qk_order_after_default(qk_ctx* ctx);
 // reset and read back the device status word
 int qk_status_reset(qk_ctx* ctx);
 int qk_status_check(qk_ctx* ctx, int fatal_mask);
@@ -128,11 +133,33 @@ void qk_timings_collect(qk_ctx* ctx);
 int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, const double* A,
              long long lda, long long strideA, const double* B, long long ldb, long long strideB,
              double beta, double* C, long long ldc, long long strideC, int batch);
-// The same contract with FP32 products and FP32 partial sums (split-K slices added in FP64).
+// The same contract with FP32 products and FP32 partial sums (split-K slices added in FP64);
+// the _lower form computes only the tiles touching the lower triangle of C.
 int qk_gemm_f32p(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
                  const double* A, long long lda, long long strideA, const double* B, long long ldb,
                  long long strideB, double beta, double* C, long long ldc, long long strideC,
                  int batch);
+int qk_gemm_f32p_lower(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
+                       const double* A, long long lda, long long strideA, const double* B,
+                       long long ldb, long long strideB, double beta, double* C, long long ldc,
+                       long long strideC, int batch);
+
+// FP64 GEMM that computes only the 64x64 tiles of C touching its lower triangle (rows >= cols);
+// for symmetric rank-k updates whose consumer reads the lower triangle.
+int qk_dgemm_lower(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
+                   const double* A, long long lda, long long strideA, const double* B,
+                   long long ldb, long long strideB, double beta, double* C, long long ldc,
+                   long long strideC, int batch);
+
+// dRPA correlation energy at orbital energies e by imaginary-frequency quadrature (k_rpa_quad.cu);
+// from the (ia|jb) block of ERI (pivoted Cholesky) or from Lov (nS x naux).  Writes the energy
+// to the device scalar Ec.  *applied = 0 (and nothing written) when the quadrature does not
+// apply (a non-positive e_a - e_i, a spectrum too wide for the grids, or a factor rank above
+// nS/3); the caller then takes the eigenvalue route.
+int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, const double* ERI,
+                   const double* Lov, int naux, double* Ec, int* applied);
+// Gauss-Legendre nodes and weights on [-1, 1] (Newton iteration on P_n).
+void qk_gauss_legendre_host(int n, double* x, double* w);
 
 // dense symmetric eigensolver pieces.  backtransform: 0 = leave Zt as the eigenvectors of the
 // tridiagonal matrix, 1 = back-transform in FP64, 2 = back-transform with FP32 products.

@@ -52,3 +52,14 @@ def test_init_without_gpu_reports_no_device(libpath):
     h = ctypes.c_void_p()
     rc = lib.qk_init(0, ctypes.byref(h))
     assert rc == 8  # QK_ERR_NO_DEVICE, and no exit()/abort
+
+
+def test_gauss_legendre_nodes_match_numpy(libpath):
+    """Host code of the frequency quadrature: the Gauss-Legendre rule against numpy."""
+    import numpy as np
+    from quack_gb300 import api
+    for n in (1, 2, 5, 24, 32, 48, 64):
+        x, w = api.gauss_legendre(n)
+        xr, wr = np.polynomial.legendre.leggauss(n)
+        assert np.allclose(x, xr, rtol=0, atol=1e-14), n
+        assert np.allclose(w, wr, rtol=1e-11, atol=1e-15), n  # end weights: P_n' cancellation
