@@ -318,6 +318,12 @@ def run_ours(args):
         "qp_error_mixed_vs_fp64": qp_err,
         "fp64_peak_tflops": {"dmma": dmma_peak, "dfma": dfma_peak},
     }
+    # the QP spectrum of this synthetic system closes its gap (some e_a < e_i after the Newton
+    # solve), so EcRPA at the G0W0 energies is NaN in both tiers, as in the reference; the
+    # quadrature that the mixed tier uses for a positive gap is timed on the HF energies
+    res["qp_gap_min_Ha"] = {"mixed": float(e_mix[nO:].min() - e_mix[:nO].max()),
+                            "plain_fp64": float(e_fp[nO:].min() - e_fp[:nO].max())}
+    res["ecrpa_quadrature"] = run_ecrpa_quad(ctx, stream, N, nO, naux, s, dE, de)
     if not args.no_batch:
         res["batched_evgw"] = run_batched(args, ctx)
     if not args.no_learned:
@@ -526,13 +532,63 @@ def run_reference(args):
     print(json.dumps(res))
 
 
+def run_ecrpa_quad(ctx, stream, N, nO, naux, s, dE, de):
+    """EcRPA of the N=200 system at its HF energies: the frequency quadrature (from the ERI
+    tensor and from the factor L) against the FP64 eigenvalue route (M built on the device,
+    eigenvalues by this library's eigensolver), CUDA-event times on the library stream."""
+    import torch
+    from quack_gb300 import api
+    nV = N - nO
+    nS = nO * nV
+    dL = torch.from_numpy(api.L_fortran_flat(s["L"])).cuda()
+    T = dE.view(N, N, N, N)                        # T[s, r, q, p] = ERI(p, q, r, s)
+    K = T[nO:, :nO, :nO, nO:].permute(2, 0, 1, 3).reshape(nS, nS).contiguous()  # (ia|jb)
+    e = de
+    d = (e[nO:].view(1, nV) - e[:nO].view(nO, 1)).reshape(-1)
+    sd = torch.sqrt(d)
+    M0 = (sd.view(-1, 1) * (torch.diag(d) + 4.0 * K) * sd.view(1, -1)).t().contiguous()
+    trA = float(d.sum() + 2.0 * torch.diagonal(K).sum())
+    dw = torch.empty(nS, dtype=torch.float64, device="cuda")
+
+    def timed(fn, reps=3):
+        ts, v = [], None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            v = fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return v, min(ts)
+
+    def eig_route():
+        M = M0.clone()
+        torch.cuda.synchronize()
+        api.dsyev_dev(nS, M.data_ptr(), nS, dw.data_ptr(), 0, False, ctx=ctx)
+        return 0.5 * (float(torch.sqrt(dw).sum()) - trA)
+
+    ec_eig, t_eig = timed(eig_route)
+    ec_eri, t_eri = timed(lambda: api.rpa_ecorr_quad_dev(N, 0, nO, 0, de.data_ptr(),
+                                                         d_ERI=dE.data_ptr(), ctx=ctx))
+    ec_l, t_l = timed(lambda: api.rpa_ecorr_quad_dev(N, 0, nO, 0, de.data_ptr(),
+                                                     d_L=dL.data_ptr(), naux=naux, ctx=ctx))
+    del K, M0
+    return {"energies": "HF", "EcRPA_eigenvalues": ec_eig, "ms_eigenvalues_fp64": t_eig,
+            "EcRPA_quad_eri": ec_eri, "ms_quad_eri": t_eri, "EcRPA_quad_L": ec_l,
+            "ms_quad_L": t_l,
+            "abs_diff_eri_Ha": abs(ec_eri - ec_eig) if ec_eri is not None else None,
+            "abs_diff_L_Ha": abs(ec_l - ec_eig) if ec_l is not None else None}
+
+
 def run_profile_case(args):
     """One small, self-contained case of a single kernel family, for ncu captures (prints one
     JSON line of CUDA-event times; not a bench result).
       tridiag   : eigenvalues of a random symmetric n x n matrix (k_sytrd + k_stebz)
       g0w0_L    : the N=200 G0W0 from its factor L (no N^4 tensor on the device), mixed tier
       g0w0_mixed: the bench's G0W0 step, mixed tier only (launch list of one step)
-      c4        : the N=400 system (nS=14400) through the factorised drivers, both tiers"""
+      c4        : the N=400 system (nS=14400) through the factorised drivers, both tiers
+      rpa_quad  : the frequency-quadrature EcRPA of the N=200 system (ERI and factor inputs)"""
     import numpy as np
     import torch
     from quack_gb300 import api, synth
@@ -567,6 +623,26 @@ def run_profile_case(args):
                                 "n_over_1meV": int((d > MEV).sum()),
                                 "Om_max_abs_Ha": float(np.abs(res["mixed_" + q][1] -
                                                               res["fp64_" + q][1]).max())}
+    elif args.profile_case == "rpa_quad":
+        # the frequency-quadrature EcRPA of the N=200 system at its HF energies, from the ERI
+        # tensor (pivoted Cholesky of (ia|jb)) and from the factor L
+        N, nO, naux, seed = WORKLOAD["N"], WORKLOAD["nO"], WORKLOAD["naux"], WORKLOAD["seed"]
+        s = synth.gen_system(N, nO, naux, np.random.default_rng(seed))
+        de = torch.from_numpy(s["eHF"]).cuda()
+        dL = torch.from_numpy(api.L_fortran_flat(s["L"])).cuda()
+        dE = synth.eri_fortran_flat_torch(s["L"], device="cuda")
+        stream = torch.cuda.ExternalStream(api.stream_handle(ctx))
+        for name, kw in (("eri", dict(d_ERI=dE.data_ptr())), ("L", dict(d_L=dL.data_ptr(), naux=naux))):
+            ts, ec = [], None
+            for _ in range(args.case_reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                e0.record(stream)
+                ec = api.rpa_ecorr_quad_dev(N, 0, nO, 0, de.data_ptr(), ctx=ctx, **kw)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            out[name] = {"EcRPA": ec, "ms": ts}
     elif args.profile_case == "tridiag":
         n = args.case_n
         A = np.random.default_rng(n).standard_normal((n, n))
@@ -608,7 +684,9 @@ def run_profile_case(args):
             run()
             torch.cuda.synchronize()
             stages.append(ctx.timings())
-        out.update(stages=stages, qp_evals=ctx.qp_evals())
+        eg = b[0].cpu().numpy()
+        out.update(stages=stages, qp_evals=ctx.qp_evals(),
+                   qp_gap_min_Ha=float(eg[nO:].min() - eg[:nO].max()))
     print(json.dumps(out))
     ctx.close()
 
@@ -629,7 +707,8 @@ def main():
     ap.add_argument("--batch-workers", type=int, default=8)
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-systems", type=int, default=120)
-    ap.add_argument("--profile-case", choices=["tridiag", "g0w0_L", "g0w0_mixed", "c4"], default=None,
+    ap.add_argument("--profile-case", choices=["tridiag", "g0w0_L", "g0w0_mixed", "c4", "rpa_quad"],
+                    default=None,
                     help="run one small kernel case for an ncu capture instead of the bench")
     ap.add_argument("--case-n", type=int, default=3600)
     ap.add_argument("--case-reps", type=int, default=1)

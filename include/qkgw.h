@@ -224,10 +224,11 @@ int qk_dsyev_dev(qk_ctx* ctx, int n, double* d_A, int lda, double* d_w, double* 
  *   EcRPA = 1/(2 pi) int_0^inf [ln det(1 + Q(w)) - tr Q(w)] dw, Q(w) = 4 L^T diag(d/(d^2+w^2)) L
  *   for a factor (ia|jb) = L L^T -- the pivoted Cholesky of the (ia|jb) block of d_ERI
  *   (ERI(nOrb,nOrb,nOrb,nOrb), the block ERI(b,i,j,a) is read), or d_L (L(nOrb,nOrb,naux)); pass
- *   exactly one.  24-64 Gauss-Legendre points by the width of the e_a - e_i spectrum;
+ *   exactly one.  24-128 Gauss-Legendre points by the width of the e_a - e_i spectrum;
  *   Q with compensated FP32 products, ln det by FP64 Cholesky; agrees with the eigenvalue
- *   route to ~1e-8 Ha.  *applied = 0 (EcRPA untouched) when it does not apply: a non-positive
- *   e_a - e_i, d_max/d_min > 12000, or a numerical rank of (ia|jb) above nS/3.  The mixed tier
+ *   route to ~1e-8 Ha.  A negative e_a - e_i gives NaN (as the Casida square roots do) and the
+ *   QKD_NEG_AMB status.  *applied = 0 (EcRPA untouched) when it does not apply: a zero
+ *   e_a - e_i, d_max/d_min > 60000, or a numerical rank of (ia|jb) above nS/3.  The mixed tier
  *   of qk_RG0W0 / qk_RG0W0_L_dev uses it for the EcRPA at the G0W0 energies.
  * qk_gauss_legendre: the quadrature's nodes x (ascending) and weights w on [-1, 1], host only. */
 int qk_RPA_ecorr_quad_dev(qk_ctx* ctx, int nOrb, int nC, int nO, int nR, int naux,

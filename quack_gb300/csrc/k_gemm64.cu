@@ -151,13 +151,17 @@ __global__ void __launch_bounds__(128) k_dgemm_dmma(int M, int N, int K, double 
 // tx + 16 i, columns ty + 16 j) with 16 independent FMA chains, 8 shared loads per 16 FMA.
 // With T = float the FP64 operands are rounded to FP32 as they are staged and the products and
 // partial sums are FP32 (64x the FP64 issue rate); C stays FP64 (alpha, beta applied in FP64).
+// kscale (FP32 path, batched, no split-K): op(B)(k, n) is scaled by kscale[batch * sK + k] as it
+// is staged, i.e. C = alpha op(A) diag(kscale) op(B) + beta C.
 template <bool TA, bool TB, typename T>
 __global__ void __launch_bounds__(256) k_gemm_simt(int M, int N, int K, double alpha,
                                                      const double* __restrict__ A, long long lda,
                                                      long long sA, const double* __restrict__ B,
                                                      long long ldb, long long sB, double beta,
                                                      double* __restrict__ C, long long ldc,
-                                                     long long sC, int kc) {
+                                                     long long sC, int kc,
+                                                     const float* __restrict__ kscale,
+                                                     long long sK) {
   __shared__ T As[2][BK][BM];
   __shared__ T Bs[2][BK][BN];
   const long long bz = blockIdx.z;
@@ -171,6 +175,7 @@ __global__ void __launch_bounds__(256) k_gemm_simt(int M, int N, int K, double a
     A += bz * sA;
     B += bz * sB;
     C += bz * sC;
+    if (kscale) kscale += bz * sK;
   }
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -216,6 +221,7 @@ __global__ void __launch_bounds__(256) k_gemm_simt(int M, int N, int K, double a
       double v = 0.0;
       if (gn < N && gk < kend) v = !TB ? B[gk + ldb * gn] : B[gn + ldb * gk];
       rb[r] = (T)v;
+      if (sizeof(T) == 4 && kscale && gk < kend) rb[r] *= (T)kscale[gk];
     }
   };
   auto stB = [&](int st) {
@@ -310,13 +316,14 @@ __global__ void k_splitk_reduce(int m, int n, int S, const double* __restrict__ 
 template <bool TA, bool TB>
 void launch(int path, dim3 grid, cudaStream_t st, int m, int n, int k, double alpha,
             const double* A, long long lda, long long sA, const double* B, long long ldb,
-            long long sB, double beta, double* C, long long ldc, long long sC, int kc) {
+            long long sB, double beta, double* C, long long ldc, long long sC, int kc,
+            const float* kscale, long long sK) {
   if (path == 1)
     k_gemm_simt<TA, TB, double><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB,
-                                                      beta, C, ldc, sC, kc);
+                                                      beta, C, ldc, sC, kc, nullptr, 0);
   else if (path == 2)
     k_gemm_simt<TA, TB, float><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB,
-                                                     beta, C, ldc, sC, kc);
+                                                     beta, C, ldc, sC, kc, kscale, sK);
   else
     k_dgemm_dmma<TA, TB><<<grid, 128, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C,
                                                ldc, sC, kc);
@@ -325,11 +332,11 @@ void launch(int path, dim3 grid, cudaStream_t st, int m, int n, int k, double al
 void launch_any(int path, bool TA, bool TB, dim3 grid, cudaStream_t st, int m, int n, int k,
                 double alpha, const double* A, long long lda, long long sA, const double* B,
                 long long ldb, long long sB, double beta, double* C, long long ldc, long long sC,
-                int kc) {
-  if (!TA && !TB) launch<false, false>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
-  else if (!TA && TB) launch<false, true>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
-  else if (TA && !TB) launch<true, false>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
-  else launch<true, true>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc);
+                int kc, const float* ks = nullptr, long long sK = 0) {
+  if (!TA && !TB) launch<false, false>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc, ks, sK);
+  else if (!TA && TB) launch<false, true>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc, ks, sK);
+  else if (TA && !TB) launch<true, false>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc, ks, sK);
+  else launch<true, true>(path, grid, st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, kc, ks, sK);
 }
 
 }  // namespace
@@ -339,7 +346,7 @@ namespace {
 int gemm_impl(qk_ctx* ctx, bool fp32, char ta, char tb, int m, int n, int k, double alpha,
               const double* A, long long lda, long long strideA, const double* B, long long ldb,
               long long strideB, double beta, double* C, long long ldc, long long strideC,
-              int batch, bool lower = false) {
+              int batch, bool lower = false, const float* kscale = nullptr, long long sK = 0) {
   if (m <= 0 || n <= 0 || batch <= 0) return QK_OK;
   if (k <= 0) {
     // C = beta*C: only beta == 0 is needed by callers
@@ -357,7 +364,7 @@ int gemm_impl(qk_ctx* ctx, bool fp32, char ta, char tb, int m, int n, int k, dou
   const long long tiles = (long long)grid.x * grid.y;
   // fewer output tiles than mult CTAs per SM and a long K: split K and reduce
   const int mult = qk_tune_get(ctx, TUNE_SPLITK_MULT, k, 4);
-  if (!lower && batch == 1 && tiles < (long long)mult * ctx->num_sms && k >= 4 * BK) {
+  if (!lower && !kscale && batch == 1 && tiles < (long long)mult * ctx->num_sms && k >= 4 * BK) {
     int S = (int)(((long long)mult * ctx->num_sms + tiles - 1) / tiles);
     const int maxS = k / (2 * BK);
     if (S > maxS) S = maxS;
@@ -380,7 +387,7 @@ int gemm_impl(qk_ctx* ctx, bool fp32, char ta, char tb, int m, int n, int k, dou
     }
   }
   launch_any(path, TA, TB, grid, ctx->stream, m, n, k, alpha, A, lda, strideA, B, ldb, strideB,
-             beta, C, ldc, strideC, lower ? -1 : 0);
+             beta, C, ldc, strideC, lower ? -1 : 0, kscale, sK);
   QK_LAUNCHED();
   return QK_OK;
 }
@@ -405,9 +412,9 @@ int qk_gemm_f32p(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alph
 int qk_gemm_f32p_lower(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
                        const double* A, long long lda, long long strideA, const double* B,
                        long long ldb, long long strideB, double beta, double* C, long long ldc,
-                       long long strideC, int batch) {
+                       long long strideC, int batch, const float* kscale, long long sK) {
   return gemm_impl(ctx, true, ta, tb, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C,
-                   ldc, strideC, batch, true);
+                   ldc, strideC, batch, true, kscale, sK);
 }
 
 int qk_dgemm_lower(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,

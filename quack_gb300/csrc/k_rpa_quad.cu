@@ -9,11 +9,12 @@
 // int_0^inf tr Q(w) dw = 2 pi tr K, so that
 //   EcRPA = 1/(2 pi) int_0^inf [ ln det(I + Q(w)) - tr Q(w) ] dw
 // exactly.  The integrand is smooth and decays as w^-4; Gauss-Legendre on w = w0 (1+x)/(1-x)
-// with w0 = sqrt(d_min d_max) and 24-64 points (by the width d_max/d_min of the spectrum)
+// with w0 = sqrt(d_min d_max) and 24-128 points (by the width d_max/d_min of the spectrum)
 // reproduces the eigenvalue route to ~1e-10 Ha.  Cost: r x r problems instead of nS x nS:
 //   * the factor: Lov (factorised integrals, r = naux) or a pivoted Cholesky of K (ERI input,
 //     stopped at 1e-12 of the largest diagonal; r = the numerical rank);
-//   * Q for all points: one batched GEMM with compensated FP32 products (error ~1e-9 Ha);
+//   * Q for all points: one batched GEMM with compensated FP32 products, the weights applied
+//     as the operand is staged (error ~1e-9 Ha);
 //   * ln det(I + Q) - tr Q: blocked FP64 Cholesky carried on S = (Schur complement) - I, so that
 //     each pivot contributes (log1p(s) - s) - (Q_ii - s), both second order in Q: no
 //     cancellation of the two first-order terms at large w.
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(1024) k_pchol(PcArgs a) {
       if (lane == 0) {
         s_rp = v;
         s_p = i;
-        s_inv = v > 0.0 ? 1.0 / sqrt(v) : 0.0;
+        s_inv = v > 0.0 ? qk_rsqrt(v) : 0.0;
       }
     }
     __syncthreads();
@@ -190,6 +191,7 @@ __global__ void __launch_bounds__(1024) k_pchol(PcArgs a) {
     int vi = 0x7fffffff;
     for (int i = gw; i < a.nS; i += totw) {
       double* li = a.Lt + (long long)a.rmax * i;
+      const double kip = lane == 0 ? a.K[i + a.ldk * p] : 0.0;  // issued ahead of the dot
       double s0 = 0.0, s1 = 0.0;
       int t = lane;
       for (; t + 32 < q; t += 64) {
@@ -206,7 +208,7 @@ __global__ void __launch_bounds__(1024) k_pchol(PcArgs a) {
           rn = 0.0;
           a.done[i] = 1;
         } else if (!a.done[i]) {
-          l = (a.K[i + a.ldk * p] - s) * inv;
+          l = (kip - s) * inv;
           rn = rn - l * l;
         }
         li[q] = l;
@@ -237,19 +239,14 @@ __global__ void k_lt_transpose(int nS, int r, int rmax, const double* __restrict
   }
 }
 
-// X_q(i, t) = L(i, t) * sqrt(4 d_i / (d_i^2 + w_q^2)) for the points of one chunk
-__global__ void k_quad_scale(int nS, int r, const double* __restrict__ L, long long ldl,
-                             const double* __restrict__ dd, const double* __restrict__ om,
-                             int nch, double* __restrict__ X) {
-  const long long per = (long long)nS * r;
-  const long long total = per * nch;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int q = (int)(idx / per);
-    const long long rem = idx - per * q;
-    const int t = (int)(rem / nS), i = (int)(rem - (long long)t * nS);
+// FP32 weights c_q(i) = 4 d_i / (d_i^2 + w_q^2) of every point (Q_q = L^T diag(c_q) L)
+__global__ void k_quad_weights(int nS, int nq, const double* __restrict__ dd,
+                               const double* __restrict__ om, float* __restrict__ wq) {
+  const int total = nS * nq;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    const int q = idx / nS, i = idx - q * nS;
     const double d = dd[i], w = om[q];
-    X[idx] = L[i + ldl * t] * sqrt(4.0 * d / fma(d, d, w * w));
+    wq[idx] = (float)(4.0 * d / fma(d, d, w * w));
   }
 }
 
@@ -361,13 +358,21 @@ __global__ void k_quad_final(int nq, const double* __restrict__ wt, const double
   }
 }
 
-// points for the width d_max / d_min of the spectrum (0: too wide, use the eigenvalues)
+// points for the width d_max / d_min of the spectrum (0: too wide, use the eigenvalues); the
+// table keeps the quadrature error below ~1e-9 Ha on dRPA problems of each width
 int quad_points(double ratio) {
   if (ratio <= 40.0) return 24;
-  if (ratio <= 300.0) return 32;
-  if (ratio <= 2500.0) return 48;
-  if (ratio <= 12000.0) return 64;
+  if (ratio <= 250.0) return 32;
+  if (ratio <= 2000.0) return 48;
+  if (ratio <= 6000.0) return 64;
+  if (ratio <= 20000.0) return 96;
+  if (ratio <= 60000.0) return 128;
   return 0;
+}
+
+__global__ void k_quad_nan(double* Ec, int* status) {
+  *Ec = NAN;
+  atomicOr(status, QKD_NEG_AMB);
 }
 
 }  // namespace
@@ -410,19 +415,27 @@ void qk_gauss_legendre_host(int n, double* x, double* w) {
 }
 
 int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, const double* ERI,
-                   const double* Lov, int naux, double* Ec, int* applied) {
+                   const double* Lov, int naux, double* Ec, int* applied, bool gap_only) {
   *applied = 0;
   const int no = nO - nC, nv = N - nO - nR, nS = no * nv;
   if (nS <= 0 || (!ERI && !Lov)) return QK_OK;
   double *dd = nullptr, *small = nullptr;
   QK_TRY(qk_wst(ctx, W_QUAD, (size_t)nS + 1024, &dd));
-  small = dd + nS;  // [0,2): d range; [8,8+64): nodes; [72,136): weights; [136,200): acc
+  small = dd + nS;  // [0,2): d range; [8,136): nodes; [136,264): weights; [264,392): acc
   k_quad_delta<<<1, 1024, 0, ctx->stream>>>(nS, nv, nC, nO, e, dd, small);
   QK_LAUNCHED();
   double mm[2];
   QK_CK(cudaMemcpyAsync(mm, small, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   QK_CK(cudaStreamSynchronize(ctx->stream));
-  if (!(mm[0] > 0.0) || !(mm[1] >= mm[0])) return QK_OK;
+  if (mm[0] < 0.0) {
+    // some e_a < e_i: A - B is not positive definite and the Casida energy is not a number
+    // (its square roots are of negative values); no factorisation is needed to say so
+    k_quad_nan<<<1, 1, 0, ctx->stream>>>(Ec, ctx->d_status);
+    QK_LAUNCHED();
+    *applied = 1;
+    return QK_OK;
+  }
+  if (gap_only || !(mm[0] > 0.0) || !(mm[1] >= mm[0])) return QK_OK;
   const int nq = quad_points(mm[1] / mm[0]);
   if (nq == 0) return QK_OK;
 
@@ -507,8 +520,8 @@ int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, 
     hb[nq + k] = wg[k] * 2.0 * w0 / ((1.0 - x[k]) * (1.0 - x[k]));
   }
   double* om = small + 8;
-  double* wt = small + 72;
-  double* acc = small + 136;
+  double* wt = small + 136;
+  double* acc = small + 264;
   QK_CK(cudaMemcpyAsync(om, hb.data(), nq * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   QK_CK(cudaMemcpyAsync(wt, hb.data() + nq, nq * sizeof(double), cudaMemcpyHostToDevice,
                         ctx->stream));
@@ -516,28 +529,23 @@ int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, 
   // the host copies above read hb before this function returns
   QK_CK(cudaStreamSynchronize(ctx->stream));
 
-  // chunks of points: X (nch x nS x r) at most ~4 GB
-  const size_t per = (size_t)nS * r;
-  int nch = (int)((size_t)(512u << 20) / (per > 0 ? per : 1));
+  // weights of all points; chunks of points with their Q (nch x r x r) at most ~2 GB
+  float* wq = nullptr;
+  QK_TRY(qk_wst(ctx, W_QX, (size_t)nS * nq, &wq));
+  k_quad_weights<<<(nS * nq + 255) / 256, 256, 0, ctx->stream>>>(nS, nq, dd, om, wq);
+  QK_LAUNCHED();
+  const long long r2 = (long long)r * r;
+  int nch = (int)((size_t)(256u << 20) / (size_t)r2);
   if (nch < 1) nch = 1;
   if (nch > nq) nch = nq;
-  double *X = nullptr, *Q = nullptr, *qd = nullptr;
-  QK_TRY(qk_wst(ctx, W_QX, per * nch, &X));
-  QK_TRY(qk_wst(ctx, W_QQ, (size_t)r * r * nch, &Q));
+  double *Q = nullptr, *qd = nullptr;
+  QK_TRY(qk_wst(ctx, W_QQ, (size_t)r2 * nch, &Q));
   QK_TRY(qk_wst(ctx, W_QD, (size_t)r * nch, &qd));
-  const long long r2 = (long long)r * r;
   for (int q0 = 0; q0 < nq; q0 += nch) {
     const int nc = nq - q0 < nch ? nq - q0 : nch;
-    {
-      const long long total = (long long)per * nc;
-      int blocks = (int)((total + 255) / 256);
-      if (blocks > 16 * ctx->num_sms) blocks = 16 * ctx->num_sms;
-      k_quad_scale<<<blocks, 256, 0, ctx->stream>>>(nS, r, L, ldl, dd, om + q0, nc, X);
-      QK_LAUNCHED();
-    }
-    // the lower triangle of Q_q = X_q^T X_q (all the factorisation reads)
-    QK_TRY(qk_gemm_f32p_lower(ctx, 'T', 'N', r, r, nS, 1.0, X, nS, (long long)per, X, nS,
-                              (long long)per, 0.0, Q, r, r2, nc));
+    // the lower triangle of Q_q = L^T diag(c_q) L (all the factorisation reads), FP32 products
+    QK_TRY(qk_gemm_f32p_lower(ctx, 'T', 'N', r, r, nS, 1.0, L, ldl, 0, L, ldl, 0, 0.0, Q, r, r2,
+                              nc, wq + (size_t)q0 * nS, nS));
     k_quad_diag<<<(r * nc + 255) / 256, 256, 0, ctx->stream>>>(r, nc, Q, qd);
     QK_LAUNCHED();
     for (int kb = 0; kb < r; kb += CB) {

@@ -314,11 +314,13 @@ int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   QK_TRY(g0w0_qp(ctx, prm, d, flow, eHF, Om, rho, SigC, Z, eGWlin, eGW, ffp));
   qk_toc(ctx, T_QP);
   // second Casida at eGW for EcRPA (RG0W0.f90:222-225): eigenvalues only; the mixed tier
-  // takes the frequency quadrature of the same energy (r x r problems instead of nS x nS)
+  // takes the frequency quadrature of the same energy (r x r problems instead of nS x nS).
+  // Both tiers first check the QP gap: a virtual level below an occupied one makes A - B
+  // indefinite and the energy NaN (phRLR's square roots), which needs no eigenproblem.
   qk_tic(ctx, T_CASIDA2);
   int quad = 0;
-  if (prm->precision == QK_PREC_BF16X3)
-    QK_TRY(qk_rpa_ec_quad(ctx, N, d.nC, d.nO, d.nR, eGW, ERI, nullptr, 0, scal + 5, &quad));
+  QK_TRY(qk_rpa_ec_quad(ctx, N, d.nC, d.nO, d.nR, eGW, ERI, nullptr, 0, scal + 5, &quad,
+                        prm->precision != QK_PREC_BF16X3));
   if (!quad) QK_TRY(casida_dev(ctx, d, eGW, ERI, nullptr, nullptr, nullptr, scal + 3, 0));
   qk_toc(ctx, T_CASIDA2);
   double h[16];
@@ -562,8 +564,8 @@ int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   qk_toc(ctx, T_QP);
   qk_tic(ctx, T_CASIDA2);
   int quad = 0;
-  if (prm->precision == QK_PREC_BF16X3)
-    QK_TRY(qk_rpa_ec_quad(ctx, N, d.nC, d.nO, d.nR, eGW, nullptr, Lov, naux, scal + 5, &quad));
+  QK_TRY(qk_rpa_ec_quad(ctx, N, d.nC, d.nO, d.nR, eGW, nullptr, Lov, naux, scal + 5, &quad,
+                        prm->precision != QK_PREC_BF16X3));
   if (!quad) QK_TRY(casida_dev(ctx, d, eGW, nullptr, nullptr, nullptr, nullptr, scal + 3, 0, K));
   qk_toc(ctx, T_CASIDA2);
   double h[16];

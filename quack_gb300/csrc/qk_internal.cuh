@@ -134,7 +134,8 @@ int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, c
              long long lda, long long strideA, const double* B, long long ldb, long long strideB,
              double beta, double* C, long long ldc, long long strideC, int batch);
 // The same contract with FP32 products and FP32 partial sums (split-K slices added in FP64);
-// the _lower form computes only the tiles touching the lower triangle of C.
+// the _lower form computes only the tiles touching the lower triangle of C and can scale the
+// k index of op(B) by kscale[batch * sK + k] (C = alpha op(A) diag(kscale) op(B) + beta C).
 int qk_gemm_f32p(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
                  const double* A, long long lda, long long strideA, const double* B, long long ldb,
                  long long strideB, double beta, double* C, long long ldc, long long strideC,
@@ -142,7 +143,8 @@ int qk_gemm_f32p(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alph
 int qk_gemm_f32p_lower(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
                        const double* A, long long lda, long long strideA, const double* B,
                        long long ldb, long long strideB, double beta, double* C, long long ldc,
-                       long long strideC, int batch);
+                       long long strideC, int batch, const float* kscale = nullptr,
+                       long long sK = 0);
 
 // FP64 GEMM that computes only the 64x64 tiles of C touching its lower triangle (rows >= cols);
 // for symmetric rank-k updates whose consumer reads the lower triangle.
@@ -153,11 +155,12 @@ int qk_dgemm_lower(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double al
 
 // dRPA correlation energy at orbital energies e by imaginary-frequency quadrature (k_rpa_quad.cu);
 // from the (ia|jb) block of ERI (pivoted Cholesky) or from Lov (nS x naux).  Writes the energy
-// to the device scalar Ec.  *applied = 0 (and nothing written) when the quadrature does not
-// apply (a non-positive e_a - e_i, a spectrum too wide for the grids, or a factor rank above
-// nS/3); the caller then takes the eigenvalue route.
+// to the device scalar Ec.  A negative e_a - e_i writes NaN (what the Casida square roots give).
+// *applied = 0 (and nothing written) when the quadrature does not apply (a zero e_a - e_i, a
+// spectrum too wide for the grids, or a factor rank above nS/3) or, with gap_only, whenever
+// the gap is not negative; the caller then takes the eigenvalue route.
 int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, const double* ERI,
-                   const double* Lov, int naux, double* Ec, int* applied);
+                   const double* Lov, int naux, double* Ec, int* applied, bool gap_only = false);
 // Gauss-Legendre nodes and weights on [-1, 1] (Newton iteration on P_n).
 void qk_gauss_legendre_host(int n, double* x, double* w);
 
@@ -277,6 +280,18 @@ __device__ __forceinline__ double qk_rcp(double x) {
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
   r = r * fma(-x, r, 2.0);
   r = r * fma(-x, r, 2.0);
+  return r;
+}
+
+// 1/sqrt(x) for x > 0 in FP64: the hardware approximation (rsqrt.approx.ftz.f64) refined by two
+// Newton-Raphson steps r <- r (3 - x r^2) / 2; x outside [1e-300, 1e300] takes 1 / sqrt(x).
+__device__ __forceinline__ double qk_rsqrt(double x) {
+  if (!(x > 1e-300 && x < 1e300)) return 1.0 / sqrt(x);
+  double r;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  const double hx = 0.5 * x;
+  r = r * fma(-hx * r, r, 1.5);
+  r = r * fma(-hx * r, r, 1.5);
   return r;
 }
 

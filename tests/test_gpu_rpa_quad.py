@@ -41,14 +41,21 @@ def test_quadrature_matches_casida_eigenvalues(ctx, N, nO, naux, seed):
         assert ec_E is None  # (ia|jb) of numerical rank above nS/3: the eigenvalue route
 
 
-def test_quadrature_declines_nonpositive_gap(ctx):
+def test_quadrature_negative_gap_is_nan_and_zero_gap_declines(ctx):
+    """A virtual below an occupied orbital makes A - B indefinite: the Casida energy is NaN (the
+    reference takes square roots of negative values) -- the quadrature says so without a
+    factorisation; an exactly zero e_a - e_i is left to the eigenvalue route."""
     import torch
     N, nO, naux = 40, 5, 40
     s = synth.small_system(N, nO, naux, 36)
-    e = s["eHF"].copy()
-    e[nO] = e[nO - 1] - 0.01  # LUMO below HOMO: e_a - e_i <= 0 somewhere
-    de = torch.from_numpy(e).cuda()
     dL = torch.from_numpy(api.L_fortran_flat(s["L"])).cuda()
+    e = s["eHF"].copy()
+    e[nO] = e[nO - 1] - 0.01
+    de = torch.from_numpy(e).cuda()
+    ec = api.rpa_ecorr_quad_dev(N, 0, nO, 0, de.data_ptr(), d_L=dL.data_ptr(), naux=naux, ctx=ctx)
+    assert ec is not None and np.isnan(ec)
+    e[nO] = e[nO - 1]
+    de = torch.from_numpy(e).cuda()
     assert api.rpa_ecorr_quad_dev(N, 0, nO, 0, de.data_ptr(), d_L=dL.data_ptr(), naux=naux,
                                   ctx=ctx) is None
 
