@@ -49,6 +49,39 @@ int h2d_eri_used(qk_ctx* ctx, double* dERI, const double* hERI, const Dims& d) {
   return QK_OK;
 }
 
+// The same block in two parts for the G0W0 driver: the rows r of the Casida matrix's sub-block
+// ERI(b,i,j,a) (r = j occupied, 1/N of the bytes per occupied row) on the compute stream, the
+// other rows -- only the excitation-density slab reads them -- on the copy stream, where they
+// overlap with the Casida eigensolve; the slab gather waits for ctx->ev_copy.
+int h2d_eri_split(qk_ctx* ctx, double* dERI, const double* hERI, const Dims& d) {
+  if (!ctx->copy_stream) {
+    QK_CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    QK_CK(cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming));
+  }
+  const size_t N = d.N, N2 = N * N, N3 = N2 * N;
+  const size_t run = (size_t)(d.nO - d.nC) * N * sizeof(double);
+  for (int s = d.nO; s < d.N - d.nR; ++s) {
+    const size_t off = N3 * s + N * d.nC + N2 * d.nC;
+    QK_CK(cudaMemcpy2DAsync(dERI + off, N2 * sizeof(double), hERI + off, N2 * sizeof(double), run,
+                            d.nO - d.nC, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  // the copy stream starts after the compute stream's earlier work (which may read dERI)
+  QK_CK(cudaEventRecord(ctx->ev_copy, ctx->stream));
+  QK_CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_copy, 0));
+  for (int s = d.nO; s < d.N - d.nR; ++s) {
+    const size_t base = N3 * s + N * d.nC;
+    if (d.nC > 0)
+      QK_CK(cudaMemcpy2DAsync(dERI + base, N2 * sizeof(double), hERI + base, N2 * sizeof(double),
+                              run, d.nC, cudaMemcpyHostToDevice, ctx->copy_stream));
+    const size_t off = base + N2 * d.nO;
+    QK_CK(cudaMemcpy2DAsync(dERI + off, N2 * sizeof(double), hERI + off, N2 * sizeof(double), run,
+                            d.N - d.nO, cudaMemcpyHostToDevice, ctx->copy_stream));
+  }
+  QK_CK(cudaEventRecord(ctx->ev_copy, ctx->copy_stream));
+  ctx->eri_pending = true;
+  return QK_OK;
+}
+
 int d2h(qk_ctx* ctx, void* dst, const void* src, size_t bytes) {
   QK_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   return QK_OK;
@@ -294,7 +327,11 @@ int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   qk_timings_clear(ctx);
   // screening at eHF
   QK_TRY(casida_dev(ctx, d, eHF, ERI, Om, XpY, nullptr, scal, 1, nullptr, prm->precision));
-  // excitation densities
+  // excitation densities (the slab reads rows of ERI that may still be arriving)
+  if (ctx->eri_pending) {
+    QK_CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0));
+    ctx->eri_pending = false;
+  }
   qk_tic(ctx, T_SLAB);
   QK_TRY(qk_launch_slab_gather(ctx, N, d.nC, d.nO, d.nR, ERI, slab));
   qk_toc(ctx, T_SLAB);
@@ -979,9 +1016,13 @@ int qk_RG0W0(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, i
   double* dSig = io + 2 * N;
   double* dZ = io + 3 * N;
   double* dOm = io + 4 * N;
-  QK_TRY(h2d_eri_used(ctx, dERI, ERI, d));
   QK_TRY(h2d(ctx, de, eHF, N * 8));
+  QK_TRY(h2d_eri_split(ctx, dERI, ERI, d));
   int st = g0w0_dev(ctx, prm, d, de, dERI, dGW, dSig, dZ, dOm, EcRPA, EcGM);
+  if (ctx->eri_pending) {  // an early return: the copies still end before the next call
+    cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0);
+    ctx->eri_pending = false;
+  }
   if (st != QK_OK) return end(ctx, st);
   QK_TRY(d2h(ctx, eGW, dGW, N * 8));
   QK_TRY(d2h(ctx, SigC, dSig, N * 8));

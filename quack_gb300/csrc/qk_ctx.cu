@@ -140,6 +140,11 @@ int qk_finalize(qk_ctx* ctx) {
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
+  if (ctx->copy_stream) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
+  }
+  if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return QK_OK;

@@ -46,6 +46,9 @@ struct qk_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2 * T_NUM + 2] = {};
   cudaEvent_t ev_in = nullptr;  // orders the stream after the caller's default-stream work
+  cudaStream_t copy_stream = nullptr;  // host->device copies overlapped with the kernels
+  cudaEvent_t ev_copy = nullptr;       // end of the overlapped ERI upload
+  bool eri_pending = false;            // the slab gather must wait for ev_copy first
   double timings[T_NUM] = {};
   std::string err;
   int* d_status = nullptr;      // device status word
