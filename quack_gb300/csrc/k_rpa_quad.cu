@@ -85,120 +85,110 @@ struct PcArgs {
   long long ldk;
   int nS, rmax;
   double tol_rel;
-  double* Lt;      // rmax x nS, column-major: Lt[t + rmax * i] = L(i, t)
-  double* r;       // residual diagonal
-  int* done;       // pivoted rows
-  double* sval;    // per-CTA argmax candidates, two sets (even / odd steps)
-  int* sidx;
+  double* Lt;                // rmax x nS, column-major: Lt[t + rmax * i] = L(i, t)
+  double* r;                 // residual diagonal
+  int* done;                 // pivoted rows
+  unsigned long long* gkey;  // pivot candidates of three consecutive steps (zeroed before launch)
   int* rank;
   unsigned* bar;
   int* status;
 };
 
-// argmax with ties to the lowest index (so that every CTA picks the same pivot)
-__device__ __forceinline__ void amax_merge(double& v, int& i, double v2, int i2) {
-  if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+// Pivot candidate key: the residual rounded to FP32 (whose bit pattern orders non-negative
+// values) in the high word, the complemented row index (ties to the lowest row) in the low word;
+// integer max then selects a pivot of (to FP32 rounding) the largest residual.
+__device__ __forceinline__ unsigned long long pc_key(double v, int i) {
+  const float f = v > 0.0 ? (float)v : 0.0f;
+  return ((unsigned long long)__float_as_uint(f) << 32) |
+         (unsigned long long)(0xFFFFFFFFu - (unsigned)i);
 }
 
-// Left-looking pivoted Cholesky of K in one cooperative launch: per pivot, every CTA finds the
-// global pivot from the per-CTA candidates, each warp forms one row of the new column
-// (l_i = (K_ip - L_i . L_p) / sqrt(r_p)) and updates r_i, and one bounded grid barrier closes
-// the step.  Deterministic: no atomics on the data, fixed reduction orders.
+// Left-looking pivoted Cholesky of K in one cooperative launch.  Per pivot: thread 0 of every
+// CTA reads the winning key of the previous step and the pivot's exact residual, each warp forms
+// one row of the new column (l_i = (K_ip - L_i . L_p) / sqrt(r_p)) and folds its residual's key into the CTA's shared maximum, and one bounded grid barrier
+// -- whose arrival carries the CTA's key to a global atomic maximum -- closes the step.  The
+// factor does not depend on the order of the atomics: every CTA reads the same final maximum.
+// The pivot row is staged in shared memory and each row's entries are loaded 4 per lane at once,
+// so a step costs a few L2 round trips plus the barrier (~12 us per pivot at nS = 3600).
 __global__ void __launch_bounds__(1024) k_pchol(PcArgs a) {
-  extern __shared__ double lp[];  // row p of L (a.rmax doubles)
-  __shared__ double wv[32];
-  __shared__ int wi[32];
+  extern __shared__ double lp[];  // the pivot row of L (a.rmax doubles)
+  __shared__ unsigned long long s_key;
   __shared__ double s_rp, s_inv, s_tol;
-  __shared__ int s_p;
+  __shared__ int s_p, s_ok;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int gw = blockIdx.x * 32 + warp, totw = gridDim.x * 32;
   unsigned epoch = 0;
-
-  int par = 0;  // candidate set written this step (the other one may still be read)
-  auto cta_candidate = [&](double v, int i) {
-    for (int o = 16; o > 0; o >>= 1) {
-      const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
-      const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
-      amax_merge(v, i, v2, i2);
-    }
-    if (lane == 0) { wv[warp] = v; wi[warp] = i; }
+  // grid barrier (bounded) that first publishes the CTA's candidate into gkey[slot]
+  auto barrier = [&](int slot) -> bool {
     __syncthreads();
-    if (warp == 0) {
-      v = lane < (int)(blockDim.x >> 5) ? wv[lane] : -INFINITY;
-      i = lane < (int)(blockDim.x >> 5) ? wi[lane] : 0x7fffffff;
-      for (int o = 16; o > 0; o >>= 1) {
-        const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
-        const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
-        amax_merge(v, i, v2, i2);
+    if (tid == 0) {
+      int ok = 1;
+      atomicMax(a.gkey + slot, s_key);
+      s_key = 0ull;
+      epoch++;
+      const unsigned target = epoch * gridDim.x;
+      __threadfence();
+      atomicAdd(a.bar, 1u);
+      unsigned spins = 0;
+      while (qk_ld_acquire(a.bar) < target) {
+        if (++spins > QK_MAX_SPIN) { atomicOr(a.status, QKD_BARRIER_TIMEOUT); ok = 0; break; }
+        if (spins > 64) __nanosleep(32);
       }
-      if (lane == 0) {
-        a.sval[par * gridDim.x + blockIdx.x] = v;
-        a.sidx[par * gridDim.x + blockIdx.x] = i;
-      }
-    }
-  };
-  auto global_pivot = [&]() {
-    if (warp == 0) {
-      double v = -INFINITY;
-      int i = 0x7fffffff;
-      for (int c = lane; c < (int)gridDim.x; c += 32)
-        amax_merge(v, i, __ldcg(a.sval + par * gridDim.x + c), __ldcg(a.sidx + par * gridDim.x + c));
-      for (int o = 16; o > 0; o >>= 1) {
-        const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
-        const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
-        amax_merge(v, i, v2, i2);
-      }
-      if (lane == 0) {
-        s_rp = v;
-        s_p = i;
-        s_inv = v > 0.0 ? qk_rsqrt(v) : 0.0;
-      }
+      if (ok && (*((volatile int*)a.status) & QKD_BARRIER_TIMEOUT)) ok = 0;
+      __threadfence();
+      s_ok = ok;
     }
     __syncthreads();
+    return s_ok != 0;
   };
 
-  // residual diagonal = diag(K); candidates
-  {
-    double v = -INFINITY;
-    int vi = 0x7fffffff;
-    for (int i = blockIdx.x * blockDim.x + tid; i < a.nS; i += gridDim.x * blockDim.x) {
-      const double x = a.K[i + a.ldk * i];
-      a.r[i] = x;
-      a.done[i] = 0;
-      amax_merge(v, vi, x, i);
-    }
-    cta_candidate(v, vi);
-  }
-  if (!qk_grid_barrier(a.bar, gridDim.x, epoch, a.status)) return;
-  global_pivot();
-  par ^= 1;
-  if (tid == 0) s_tol = a.tol_rel * s_rp;
+  if (tid == 0) s_key = 0ull;
   __syncthreads();
-  const double tol = s_tol;
+  for (int i = blockIdx.x * blockDim.x + tid; i < a.nS; i += gridDim.x * blockDim.x) {
+    const double x = a.K[i + a.ldk * i];
+    a.r[i] = x;
+    a.done[i] = 0;
+    atomicMax(&s_key, pc_key(x, i));
+  }
+  if (!barrier(0)) return;
   int q = 0;
   for (; q < a.rmax; ++q) {
-    if (q > 0) {
-      global_pivot();
-      par ^= 1;
+    if (tid == 0) {
+      const unsigned long long k = __ldcg(a.gkey + q % 3);
+      const int p = (int)(0xFFFFFFFFu - (unsigned)(k & 0xFFFFFFFFull));
+      double rp = -1.0;
+      if (k != 0ull && p >= 0 && p < a.nS) rp = __ldcg(a.r + p);
+      s_p = p;
+      s_rp = rp;
+      s_inv = rp > 0.0 ? qk_rsqrt(rp) : 0.0;
+      if (q == 0) s_tol = a.tol_rel * rp;  // relative to the largest diagonal
+      if (blockIdx.x == 0) a.gkey[(q + 2) % 3] = 0ull;  // read two steps ago, written next step
     }
-    const double rp = s_rp;
+    __syncthreads();
+    const double rp = s_rp, tol = s_tol, inv = s_inv;
     const int p = s_p;
-    if (!(rp > tol) || p < 0 || p >= a.nS) break;  // uniform: every CTA read the same candidates
+    if (!(rp > tol) || p < 0 || p >= a.nS) break;  // uniform: every CTA read the same key
     for (int t = tid; t < q; t += blockDim.x) lp[t] = __ldcg(a.Lt + t + (long long)a.rmax * p);
     __syncthreads();
-    const double inv = s_inv;
-    double v = -INFINITY;
-    int vi = 0x7fffffff;
     for (int i = gw; i < a.nS; i += totw) {
       double* li = a.Lt + (long long)a.rmax * i;
       const double kip = lane == 0 ? a.K[i + a.ldk * p] : 0.0;  // issued ahead of the dot
       double s0 = 0.0, s1 = 0.0;
-      int t = lane;
-      for (; t + 32 < q; t += 64) {
-        s0 = fma(li[t], lp[t], s0);
-        s1 = fma(li[t + 32], lp[t + 32], s1);
+      // the row's entries in batches of 4 loads per lane, issued before their FMAs
+      for (int t0 = 0; t0 < q; t0 += 128) {
+        double x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = t0 + lane + 32 * u;
+          x[u] = t < q ? li[t] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u += 2) {
+          const int t = t0 + lane + 32 * u;
+          if (t < q) s0 = fma(x[u], lp[t], s0);
+          if (t + 32 < q) s1 = fma(x[u + 1], lp[t + 32], s1);
+        }
       }
-      if (t < q) s0 = fma(li[t], lp[t], s0);
       double s = s0 + s1;
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if (lane == 0) {
@@ -210,14 +200,13 @@ __global__ void __launch_bounds__(1024) k_pchol(PcArgs a) {
         } else if (!a.done[i]) {
           l = (kip - s) * inv;
           rn = rn - l * l;
+          atomicMax(&s_key, pc_key(rn, i));
         }
         li[q] = l;
         a.r[i] = rn;
-        if (!a.done[i]) amax_merge(v, vi, rn, i);
       }
     }
-    cta_candidate(v, vi);
-    if (!qk_grid_barrier(a.bar, gridDim.x, epoch, a.status)) return;
+    if (!barrier((q + 1) % 3)) return;
   }
   if (blockIdx.x == 0 && tid == 0) *a.rank = q;
 }
@@ -448,7 +437,7 @@ int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, 
     double *K = nullptr, *Lt = nullptr, *Lc = nullptr, *pv = nullptr;
     QK_TRY(qk_wst(ctx, W_M, (size_t)nS * nS, &K));
     QK_TRY(qk_wst(ctx, W_QLT, (size_t)rmax * nS, &Lt));
-    QK_TRY(qk_wst(ctx, W_QPV, (size_t)2 * nS + 4 * ctx->num_sms + 64, &pv));
+    QK_TRY(qk_wst(ctx, W_QPV, (size_t)2 * nS + 64, &pv));
     dim3 gg((nv + 31) / 32, (nv + 31) / 32, no * no);
     if (gg.z > 65535) return QK_OK;
     k_gather_K<<<gg, dim3(32, 8), 0, ctx->stream>>>(N, nC, nO, nR, ERI, K);
@@ -462,9 +451,8 @@ int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, 
     pa.Lt = Lt;
     pa.r = pv;
     pa.done = (int*)(pv + nS);
-    pa.sval = pv + 2 * nS;                              // 2 * grid doubles
-    pa.sidx = (int*)(pv + 2 * nS + 2 * ctx->num_sms);   // 2 * grid ints
-    pa.rank = (int*)(pv + 2 * nS + 3 * ctx->num_sms);
+    pa.gkey = (unsigned long long*)(pv + 2 * nS);  // 3 keys
+    pa.rank = (int*)(pv + 2 * nS + 4);
     pa.bar = ctx->d_bar;
     pa.status = ctx->d_status;
     int grid = (nS + 31) / 32;
@@ -482,6 +470,7 @@ int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, 
     QK_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pchol, 1024, smem));
     if (per_sm < 1) return QK_OK;
     QK_CK(cudaMemsetAsync(ctx->d_bar, 0, 16 * sizeof(unsigned), ctx->stream));
+    QK_CK(cudaMemsetAsync(pa.gkey, 0, 3 * sizeof(unsigned long long), ctx->stream));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(1024);
