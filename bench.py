@@ -704,7 +704,7 @@ def main():
     ap.add_argument("--reference-budget-s", type=float, default=150.0)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-systems", type=int, default=32)
-    ap.add_argument("--batch-workers", type=int, default=8)
+    ap.add_argument("--batch-workers", type=int, default=4)
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-systems", type=int, default=120)
     ap.add_argument("--profile-case", choices=["tridiag", "g0w0_L", "g0w0_mixed", "c4", "rpa_quad"],
