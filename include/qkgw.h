@@ -43,11 +43,13 @@ enum {
 enum {
   QK_PREC_FP64 = 0,        /* FP64 throughout (plain form) */
   QK_PREC_BF16X3 = 1       /* mixed: the excitation-density contraction as BF16x3 split products
-                              on tcgen05 (FP32 accumulation, compensated); with eta = 0 and no SRG
-                              the pole sums of Sigma/dSigma (linearised stage and Newton) take the
-                              terms with |w - e +- Om| >= 0.1 Ha in FP32 and the near-pole terms in
-                              FP64.  The Casida build and eigensolve, the Newton update and DIIS
-                              stay FP64. */
+                              on tcgen05 (FP32 accumulation, compensated) and the eigenvector
+                              back-transformation on compensated FP32 products; with eta = 0 and
+                              no SRG the pole sums of Sigma/dSigma (linearised stage and Newton)
+                              take the terms with |w - e +- Om| >= 0.01 Ha in FP32 and the
+                              near-pole terms in FP64; G0W0's EcRPA at eGW by frequency
+                              quadrature.  The Casida eigenvalues, the Newton update and DIIS stay
+                              FP64. */
 };
 
 /* Options of the GW line of QuAcK's input/options (QuAcK/read_options.f90:242-267). */

@@ -685,7 +685,7 @@ int qk_sigma_ff_prep(qk_ctx* ctx, int N, int nS, const double* rho, const double
   ff->R = R;
   ff->OmF = OmF;
   ff->bad = bad;
-  ff->tau = 0.1f;
+  ff->tau = 0.01f;  // Ha: the FP32-pair denominators are exact to ~1e-12 Ha outside
   return QK_OK;
 }
 
