@@ -245,7 +245,10 @@ int qk_gauss_legendre(int n, double* x, double* w);
  *   16 products of each k tile summed in FP32, the tiles folded into a compensated FP32 pair);
  *   the mixed tier's eigenvector back-transformation (dsyev's dormtr step).
  * qk_gemm_bf16x3_dev: C = A * B^T with the three-way BF16 split on tcgen05 (FP32 accumulate),
- *   the precision tier of the same excitation-density dgemm. */
+ *   the precision tier of the same excitation-density dgemm.
+ * qk_gemm_bf16x3_ex_dev: the qk_dgemm_dev contract (transposes, alpha, beta) on the same tensor-core
+ *   path; few output tiles with a long k split k over CTAs.  The mixed tier's back-transformation
+ *   and quadrature products use it. */
 int qk_dgemm_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, double alpha,
                  const double* d_A, int lda, const double* d_B, int ldb, double beta, double* d_C,
                  int ldc);
@@ -254,6 +257,9 @@ int qk_dgemm_f32p_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k
                       double* d_C, int ldc);
 int qk_gemm_bf16x3_dev(qk_ctx* ctx, int m, int n, int k, const double* d_A, int lda,
                        const double* d_B, int ldb, double* d_C, int ldc);
+int qk_gemm_bf16x3_ex_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k,
+                          double alpha, const double* d_A, int lda, const double* d_B, int ldb,
+                          double beta, double* d_C, int ldc);
 
 /* ---- allocation-free self-energy (device pointers) -----------------------------------------
  * No counterpart in the reference.  For hosts that own all device memory themselves (one

@@ -391,6 +391,16 @@ def dgemm_f32p_dev(transa, transb, m, n, k, alpha, d_A, lda, d_B, ldb, beta, d_C
                                     C.c_void_p(d_B), ldb, C.c_double(beta), C.c_void_p(d_C), ldc))
 
 
+def gemm_bf16x3_ex_dev(transa, transb, m, n, k, alpha, d_A, lda, d_B, ldb, beta, d_C, ldc,
+                       ctx=None):
+    """C = alpha op(A) op(B) + beta C with the BF16x3 split on the tensor cores (FP64 in/out)."""
+    c = _ctx(ctx)
+    c.check(lib().qk_gemm_bf16x3_ex_dev(c.handle, C.c_char(transa.encode()),
+                                        C.c_char(transb.encode()), m, n, k, C.c_double(alpha),
+                                        C.c_void_p(d_A), lda, C.c_void_p(d_B), ldb,
+                                        C.c_double(beta), C.c_void_p(d_C), ldc))
+
+
 def gemm_bf16x3_dev(m, n, k, d_A, lda, d_B, ldb, d_C, ldc, ctx=None):
     """C = A B^T with the BF16x3 split on the tensor cores (FP64 in/out, FP32 accumulate)."""
     c = _ctx(ctx)

@@ -162,11 +162,33 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bp)) + (b - bp);
 }
 
+// Launch geometry: blockIdx.x = output tile, blockIdx.y = batch entry, blockIdx.z = k slice.
+struct GemmX {
+  int M, N, Kpad, rowsA, rowsB;
+  int a_batched, b_batched;  // operand planes per batch entry (else shared by all)
+  int kb_per_slice;          // k blocks per z slice (split-K), >= the total when not split
+  int n_tiles, lower;        // lower: only tiles touching the lower triangle of C
+  double alpha, beta;
+  double* C;
+  long long ldc, sC;         // C of batch entry y at C + y * sC; slice z at C + z * sC too
+};
+
 template <int CHUNK_KB>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_gemm_bf16x3(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                  int M, int N, int Kpad, int rowsA, int rowsB, double* __restrict__ C,
-                  long long ldc, int n_tiles, int* status) {
+                  GemmX g, int* status) {
+  const int M = g.M, N = g.N, rowsA = g.rowsA, rowsB = g.rowsB;
+  const int tile0 = blockIdx.x;
+  const int m_tile0 = tile0 / g.n_tiles, n_tile0 = tile0 - m_tile0 * g.n_tiles;
+  if (g.lower && (m_tile0 + 1) * BM <= n_tile0 * BN) return;  // strictly above the diagonal
+  const int kb_first = (int)blockIdx.z * g.kb_per_slice;
+  const int num_kb_all = g.Kpad / BK;
+  const int num_kb = min(g.kb_per_slice, num_kb_all - kb_first);
+  if (num_kb <= 0) return;
+  const int rowA0 = g.a_batched ? (int)blockIdx.y * 3 * rowsA : 0;
+  const int rowB0 = g.b_batched ? (int)blockIdx.y * 3 * rowsB : 0;
+  double* __restrict__ C = g.C + (long long)(blockIdx.y + blockIdx.z) * g.sC;
+  const long long ldc = g.ldc;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
@@ -177,10 +199,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   int* abort_flag = (int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tile = blockIdx.x;
-  const int m_tile = tile / n_tiles, n_tile = tile - m_tile * n_tiles;
-  const int m0 = m_tile * BM, n0 = n_tile * BN;
-  const int num_kb = Kpad / BK;
+  const int m0 = m_tile0 * BM, n0 = n_tile0 * BN;
   const int nch = (num_kb + CHUNK_KB - 1) / CHUNK_KB;
 
   if (threadIdx.x == 0) {
@@ -218,10 +237,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (*(volatile int*)abort_flag) break;
         uint8_t* st = smem + s * STAGE_BYTES;
         mbar_expect_tx(&full[s], STAGE_BYTES);
-        const int k0 = kb * BK;
+        const int k0 = (kb_first + kb) * BK;
         for (int p = 0; p < 3; ++p) {
-          tma_load_2d(st + p * TILE_BYTES, &mapA, &full[s], k0, p * rowsA + m0);
-          tma_load_2d(st + (3 + p) * TILE_BYTES, &mapB, &full[s], k0, p * rowsB + n0);
+          tma_load_2d(st + p * TILE_BYTES, &mapA, &full[s], k0, rowA0 + p * rowsA + m0);
+          tma_load_2d(st + (3 + p) * TILE_BYTES, &mapB, &full[s], k0, rowB0 + p * rowsB + n0);
         }
         issued = kb + 1;
       }
@@ -317,9 +336,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int col = n0 + half * 64 + c * 16 + j;
-            if (col < N)
-              C[(long long)row + ldc * col] =
-                  (double)__uint_as_float(h[j]) + (double)__uint_as_float(l[j]);
+            if (col < N) {
+              double* cp = C + (long long)row + ldc * col;
+              double v = g.alpha * ((double)__uint_as_float(h[j]) + (double)__uint_as_float(l[j]));
+              if (g.beta != 0.0) v += g.beta * *cp;
+              *cp = v;
+            }
           }
         }
       }
@@ -331,36 +353,71 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(TMEM_COLS)
                  : "memory");
-  (void)rowsB;
 }
 
-// Split a column-major FP64 matrix X (rows x K, ld) into three BF16 parts stored K-major:
-// P[p*rows_pad*Kpad + r*Kpad + k], zero padded to rows_pad x Kpad.
-__global__ void k_split3(int rows, int K, const double* __restrict__ X, long long ld, int rows_pad,
-                         int Kpad, __nv_bfloat16* __restrict__ P) {
+// Split the FP64 matrix X (rows x K) into three BF16 parts stored K-major:
+// P[p*rows_pad*Kpad + r*Kpad + k], zero padded to rows_pad x Kpad.  X(r, k) = X[r + ld*k]
+// (trans = 0, read through a shared-memory transpose) or X[k + ld*r] (trans = 1, read along k
+// directly); kscale (optional) multiplies X(r, k) by kscale[k] first.
+__device__ __forceinline__ void split_store(double x, __nv_bfloat16* __restrict__ P, size_t o,
+                                            size_t plane) {
+  const __nv_bfloat16 x0 = __double2bfloat16(x);
+  const double r1 = x - (double)__bfloat162float(x0);
+  const __nv_bfloat16 x1 = __double2bfloat16(r1);
+  const double r2 = r1 - (double)__bfloat162float(x1);
+  const __nv_bfloat16 x2 = __double2bfloat16(r2);
+  P[o] = x0;
+  P[o + plane] = x1;
+  P[o + 2 * plane] = x2;
+}
+
+__global__ void k_split3(int rows, int K, const double* __restrict__ X, long long ld, int trans,
+                         const float* __restrict__ kscale, int rows_pad, int Kpad,
+                         __nv_bfloat16* __restrict__ P) {
   __shared__ double t[32][33];
   const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  const size_t plane = (size_t)rows_pad * Kpad;
+  if (trans) {
+    for (int i = ty; i < 32; i += 8) {
+      const int r = r0 + i, k = k0 + tx;
+      if (r < rows_pad && k < Kpad) {
+        double x = (r < rows && k < K) ? X[(long long)k + ld * r] : 0.0;
+        if (kscale && k < K) x *= (double)kscale[k];
+        split_store(x, P, (size_t)r * Kpad + k, plane);
+      }
+    }
+    return;
+  }
   for (int i = ty; i < 32; i += 8) {
     const int r = r0 + tx, k = k0 + i;
     t[i][tx] = (r < rows && k < K) ? X[(long long)r + ld * k] : 0.0;
   }
   __syncthreads();
-  const size_t plane = (size_t)rows_pad * Kpad;
   for (int i = ty; i < 32; i += 8) {
     const int r = r0 + i, k = k0 + tx;
     if (r < rows_pad && k < Kpad) {
-      const double x = t[tx][i];
-      const __nv_bfloat16 x0 = __double2bfloat16(x);
-      const double r1 = x - (double)__bfloat162float(x0);
-      const __nv_bfloat16 x1 = __double2bfloat16(r1);
-      const double r2 = r1 - (double)__bfloat162float(x1);
-      const __nv_bfloat16 x2 = __double2bfloat16(r2);
-      const size_t o = (size_t)r * Kpad + k;
-      P[o] = x0;
-      P[o + plane] = x1;
-      P[o + 2 * plane] = x2;
+      double x = t[tx][i];
+      if (kscale && k < K) x *= (double)kscale[k];
+      split_store(x, P, (size_t)r * Kpad + k, plane);
     }
+  }
+}
+
+// C = alpha * sum_s W[s] + beta * C  (split-K reduction, column-major m x n, W slices m x n)
+__global__ void k_bf16x3_reduce(int m, int n, int S, const double* __restrict__ W, double alpha,
+                                double beta, double* __restrict__ C, long long ldc) {
+  const long long total = (long long)m * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int s = 0; s < S; ++s) acc += W[(long long)s * total + i];
+    const int r = (int)(i % m);
+    const long long c = i / m;
+    double* cp = C + r + ldc * c;
+    double v = alpha * acc;
+    if (beta != 0.0) v += beta * (*cp);
+    *cp = v;
   }
 }
 
@@ -393,21 +450,20 @@ int make_map(qk_ctx* ctx, CUtensorMap* map, const void* base, int Kpad, long lon
 
 }  // namespace
 
-int qk_split3(qk_ctx* ctx, int rows, int K, const double* X, long long ld, int rows_pad, int Kpad,
-              void* parts) {
+static int qk_split3(qk_ctx* ctx, int rows, int K, const double* X, long long ld, int trans,
+                     const float* kscale, int rows_pad, int Kpad, void* parts) {
   dim3 grid((rows_pad + 31) / 32, (Kpad + 31) / 32);
   if (grid.y > 65535) return qk_fail(ctx, QK_ERR_ARG, "split: K too large");
-  k_split3<<<grid, dim3(32, 8), 0, ctx->stream>>>(rows, K, X, ld, rows_pad, Kpad,
+  k_split3<<<grid, dim3(32, 8), 0, ctx->stream>>>(rows, K, X, ld, trans, kscale, rows_pad, Kpad,
                                                   (__nv_bfloat16*)parts);
   QK_LAUNCHED();
   return QK_OK;
 }
 
-int qk_gemm_bf16x3_parts(qk_ctx* ctx, int m, int n, const void* Ap, int rowsA, const void* Bp,
-                         int rowsB, int Kpad, double* C, long long ldc) {
-  CUtensorMap ma, mb;
-  QK_TRY(make_map(ctx, &ma, Ap, Kpad, 3LL * rowsA));
-  QK_TRY(make_map(ctx, &mb, Bp, Kpad, 3LL * rowsB));
+namespace {
+
+int launch_gemm(qk_ctx* ctx, const CUtensorMap& ma, const CUtensorMap& mb, const GemmX& g,
+                dim3 grid) {
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
@@ -421,33 +477,88 @@ int qk_gemm_bf16x3_parts(qk_ctx* ctx, int m, int n, const void* Ap, int rowsA, c
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
   });
   QK_CK(attr_err);
-  const int m_tiles = rowsA / BM, n_tiles = rowsB / BN;
-  const long long tiles = (long long)m_tiles * n_tiles;
-  if (tiles > 0x7fffffffLL) return qk_fail(ctx, QK_ERR_ARG, "bf16x3: too many tiles");
-  const int chunk = qk_tune_get(ctx, TUNE_BF16X3_CHUNK, Kpad, 2);
+  const int chunk = qk_tune_get(ctx, TUNE_BF16X3_CHUNK, g.Kpad, 2);
   if (chunk == 1)
-    k_gemm_bf16x3<1><<<(unsigned)tiles, NTHREADS, SMEM_BYTES, ctx->stream>>>(
-        ma, mb, m, n, Kpad, rowsA, rowsB, C, ldc, n_tiles, ctx->d_status);
+    k_gemm_bf16x3<1><<<grid, NTHREADS, SMEM_BYTES, ctx->stream>>>(ma, mb, g, ctx->d_status);
   else if (chunk == 4)
-    k_gemm_bf16x3<4><<<(unsigned)tiles, NTHREADS, SMEM_BYTES, ctx->stream>>>(
-        ma, mb, m, n, Kpad, rowsA, rowsB, C, ldc, n_tiles, ctx->d_status);
+    k_gemm_bf16x3<4><<<grid, NTHREADS, SMEM_BYTES, ctx->stream>>>(ma, mb, g, ctx->d_status);
   else
-    k_gemm_bf16x3<2><<<(unsigned)tiles, NTHREADS, SMEM_BYTES, ctx->stream>>>(
-        ma, mb, m, n, Kpad, rowsA, rowsB, C, ldc, n_tiles, ctx->d_status);
+    k_gemm_bf16x3<2><<<grid, NTHREADS, SMEM_BYTES, ctx->stream>>>(ma, mb, g, ctx->d_status);
   QK_LAUNCHED();
   return QK_OK;
+}
+
+}  // namespace
+
+int qk_gemm_bf16x3(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
+                   const double* A, long long lda, long long sA, const double* B, long long ldb,
+                   long long sB, const float* bscale, long long sBS, double beta, double* C,
+                   long long ldc, long long sC, int batch, bool lower) {
+  if (m <= 0 || n <= 0 || batch <= 0) return QK_OK;
+  if (k <= 0) return qk_fail(ctx, QK_ERR_ARG, "bf16x3: k must be positive");
+  const bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
+  const int rowsA = (m + BM - 1) / BM * BM;
+  const int rowsB = (n + BN - 1) / BN * BN;
+  const int Kpad = (k + BK - 1) / BK * BK;
+  const bool a_b = batch > 1 && sA != 0;
+  const bool b_b = batch > 1 && (sB != 0 || (bscale && sBS != 0));
+  const size_t planeA = (size_t)3 * rowsA * Kpad, planeB = (size_t)3 * rowsB * Kpad;
+  __nv_bfloat16 *Ap = nullptr, *Bp = nullptr;
+  QK_TRY(qk_wst(ctx, W_SPLIT_A, planeA * (a_b ? batch : 1), &Ap));
+  QK_TRY(qk_wst(ctx, W_SPLIT_B, planeB * (b_b ? batch : 1), &Bp));
+  // op(A) (m x k) as rows x K: X(i, kk) = A[i + lda kk] ('N') or A[kk + lda i] ('T');
+  // op(B)^T (n x k): X(j, kk) = op(B)(kk, j) = B[kk + ldb j] ('N') or B[j + ldb kk] ('T')
+  for (int b = 0; b < (a_b ? batch : 1); ++b)
+    QK_TRY(qk_split3(ctx, m, k, A + b * sA, lda, TA ? 1 : 0, nullptr, rowsA, Kpad, Ap + b * planeA));
+  for (int b = 0; b < (b_b ? batch : 1); ++b)
+    QK_TRY(qk_split3(ctx, n, k, B + b * sB, ldb, TB ? 0 : 1, bscale ? bscale + b * sBS : nullptr,
+                     rowsB, Kpad, Bp + b * planeB));
+  CUtensorMap ma, mb;
+  QK_TRY(make_map(ctx, &ma, Ap, Kpad, 3LL * rowsA * (a_b ? batch : 1)));
+  QK_TRY(make_map(ctx, &mb, Bp, Kpad, 3LL * rowsB * (b_b ? batch : 1)));
+  const int m_tiles = rowsA / BM, n_tiles = rowsB / BN;
+  const long long tiles = (long long)m_tiles * n_tiles;
+  if (tiles > 0x7fffffffLL || batch > 65535) return qk_fail(ctx, QK_ERR_ARG, "bf16x3: too many tiles");
+  GemmX g;
+  g.M = m; g.N = n; g.Kpad = Kpad; g.rowsA = rowsA; g.rowsB = rowsB;
+  g.a_batched = a_b; g.b_batched = b_b;
+  g.n_tiles = n_tiles; g.lower = lower ? 1 : 0;
+  const int num_kb = Kpad / BK;
+  // few output tiles and a long k: split k over CTAs, FP64 slices, one reduction (not with
+  // lower: the reduction would write the skipped upper tiles)
+  const long long eff = tiles;
+  int S = 1;
+  if (!lower && batch == 1 && eff * 2 < ctx->num_sms && num_kb >= 8) {
+    S = (int)((ctx->num_sms + eff - 1) / eff);
+    if (S > num_kb / 4) S = num_kb / 4;
+    if (S > 16) S = 16;
+    if (S < 1) S = 1;
+  }
+  if (S > 1) {
+    const int kbs = (num_kb + S - 1) / S;
+    S = (num_kb + kbs - 1) / kbs;
+    double* W = nullptr;
+    QK_TRY(qk_wst(ctx, W_SPLITK, (size_t)S * m * n, &W));
+    g.kb_per_slice = kbs;
+    g.alpha = 1.0; g.beta = 0.0;
+    g.C = W; g.ldc = m; g.sC = (long long)m * n;
+    QK_TRY(launch_gemm(ctx, ma, mb, g, dim3((unsigned)tiles, 1, S)));
+    const long long total = (long long)m * n;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 16 * ctx->num_sms) blocks = 16 * ctx->num_sms;
+    k_bf16x3_reduce<<<blocks, 256, 0, ctx->stream>>>(m, n, S, W, alpha, beta, C, ldc);
+    QK_LAUNCHED();
+    return QK_OK;
+  }
+  g.kb_per_slice = num_kb;
+  g.alpha = alpha; g.beta = beta;
+  g.C = C; g.ldc = ldc; g.sC = sC;
+  return launch_gemm(ctx, ma, mb, g, dim3((unsigned)tiles, batch, 1));
 }
 
 int qk_gemm_bf16x3_nt(qk_ctx* ctx, int m, int n, int k, const double* A, long long lda,
                       const double* B, long long ldb, double* C, long long ldc) {
   if (m <= 0 || n <= 0 || k <= 0) return QK_OK;
-  const int rowsA = (m + BM - 1) / BM * BM;
-  const int rowsB = (n + BN - 1) / BN * BN;
-  const int Kpad = (k + BK - 1) / BK * BK;
-  void *Ap = nullptr, *Bp = nullptr;
-  QK_TRY(qk_ws(ctx, W_SPLIT_A, (size_t)3 * rowsA * Kpad * 2, &Ap));
-  QK_TRY(qk_ws(ctx, W_SPLIT_B, (size_t)3 * rowsB * Kpad * 2, &Bp));
-  QK_TRY(qk_split3(ctx, m, k, A, lda, rowsA, Kpad, Ap));
-  QK_TRY(qk_split3(ctx, n, k, B, ldb, rowsB, Kpad, Bp));
-  return qk_gemm_bf16x3_parts(ctx, m, n, Ap, rowsA, Bp, rowsB, Kpad, C, ldc);
+  return qk_gemm_bf16x3(ctx, 'N', 'T', m, n, k, 1.0, A, lda, 0, B, ldb, 0, nullptr, 0, 0.0, C, ldc,
+                        0, 1, false);
 }

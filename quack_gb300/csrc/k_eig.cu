@@ -12,8 +12,8 @@
 //   3. k_stein: inverse iteration on T - lambda I (tridiagonal GEPP), one thread per cluster of
 //      close eigenvalues, modified Gram-Schmidt inside clusters; eigenvectors written as rows.
 //   4. Blocked back-transformation E <- E * Q^T with compact-WY blocks of 128 reflectors on the
-//      FP64 GEMM, or with FP32 products in the mixed tier (all T factors from one batched GEMM
-//      and one launch).
+//      FP64 GEMM, or with compensated FP32 products in the mixed tier (all T factors from one
+//      batched GEMM and one launch).
 // Eigenvalues come out ascending (as dsyev).  Eigenvectors are defined up to sign/rotation in
 // degenerate subspaces, which every downstream GW quantity is invariant to.
 #include <cmath>
@@ -681,6 +681,18 @@ __global__ void __launch_bounds__(BT_NB) k_larft_all(int nref, const double* __r
   }
 }
 
+// The two large products of a back-transformation block: FP64 GEMM, or (mixed tier) the
+// compensated FP32-product GEMM.  (The BF16x3 tensor-core GEMM is ~7x less accurate here: its
+// FP32 tensor-memory accumulator sums 6 x 128 products per chunk against 16 per compensated
+// tile, and over the 28 blocks of nS = 3600 that moved the linearised QP energies past 1 meV.)
+int bt_big_gemm(qk_ctx* ctx, bool mixed, char ta, char tb, int m, int n, int k, double alpha,
+                const double* A, long long lda, const double* B, long long ldb, double beta,
+                double* C, long long ldc) {
+  if (mixed)
+    return qk_gemm_f32p(ctx, ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1);
+  return qk_dgemm(ctx, ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1);
+}
+
 // T factors of all reflector blocks of the last tridiagonalisation on this context:
 // G_b = V_b^T V_b for the full blocks in one batched GEMM (V is zero above its unit diagonal,
 // so all n rows can be used), the last partial block on its own, then k_larft_all.
@@ -828,7 +840,8 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
 
   if (!backtransform) return QK_OK;  // caller applies Q^T itself (qk_eig_apply_qt)
   // ---- 4. back-transformation Zt <- Zt * Q^T, blocks from last to first ----
-  // (backtransform == 2: the block products in FP32, Zt kept in FP64; the mixed tier)
+  // (backtransform == 2, the mixed tier: the block products and the T factors with compensated
+  // FP32 products; Zt stays FP64)
   auto gemm = backtransform == 2 ? qk_gemm_f32p : qk_dgemm;
   if (tm) qk_tic(ctx, T_BACKTRANS);
   const int nref = n - 2;  // reflectors 0..n-3 can be non-trivial
@@ -847,9 +860,11 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
       const double* Vb = V + (kb + 1) + N * kb;
       const double* Tb = Tall + (size_t)b * BT_NB * BT_NB;
       double* Es = Zt + N * (kb + 1);
-      QK_TRY(gemm(ctx, 'N', 'N', n, nb, m, 1.0, Es, n, 0, Vb, n, 0, 0.0, W1, n, 0, 1));
+      QK_TRY(bt_big_gemm(ctx, backtransform == 2, 'N', 'N', n, nb, m, 1.0, Es, n, Vb, n, 0.0, W1,
+                         n));
       QK_TRY(gemm(ctx, 'N', 'T', n, nb, nb, 1.0, W1, n, 0, Tb, BT_NB, 0, 0.0, W2, n, 0, 1));
-      QK_TRY(gemm(ctx, 'N', 'T', n, m, nb, -1.0, W2, n, 0, Vb, n, 0, 1.0, Es, n, 0, 1));
+      QK_TRY(bt_big_gemm(ctx, backtransform == 2, 'N', 'T', n, m, nb, -1.0, W2, n, Vb, n, 1.0, Es,
+                         n));
     }
   }
   if (tm) qk_toc(ctx, T_BACKTRANS);
@@ -882,9 +897,9 @@ int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols, int
     const double* Tb = Tall + (size_t)b * BT_NB * BT_NB;
     double* Xs = X + (kb + 1);
     // W1 = V^T X (nb x ncols), W2 = T^T W1, X -= V W2
-    QK_TRY(gemm(ctx, 'T', 'N', nb, ncols, m, 1.0, Vb, n, 0, Xs, ldx, 0, 0.0, W1, nb, 0, 1));
+    QK_TRY(bt_big_gemm(ctx, fp32 != 0, 'T', 'N', nb, ncols, m, 1.0, Vb, n, Xs, ldx, 0.0, W1, nb));
     QK_TRY(gemm(ctx, 'T', 'N', nb, ncols, nb, 1.0, Tb, BT_NB, 0, W1, nb, 0, 0.0, W2, nb, 0, 1));
-    QK_TRY(gemm(ctx, 'N', 'N', m, ncols, nb, -1.0, Vb, n, 0, W2, nb, 0, 1.0, Xs, ldx, 0, 1));
+    QK_TRY(bt_big_gemm(ctx, fp32 != 0, 'N', 'N', m, ncols, nb, -1.0, Vb, n, W2, nb, 1.0, Xs, ldx));
   }
   return QK_OK;
 }

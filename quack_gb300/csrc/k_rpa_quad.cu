@@ -532,7 +532,10 @@ int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, 
   QK_TRY(qk_wst(ctx, W_QD, (size_t)r * nch, &qd));
   for (int q0 = 0; q0 < nq; q0 += nch) {
     const int nc = nq - q0 < nch ? nq - q0 : nch;
-    // the lower triangle of Q_q = L^T diag(c_q) L (all the factorisation reads), FP32 products
+    // the lower triangle of Q_q = L^T diag(c_q) L (all the factorisation reads), compensated FP32
+    // products.  (The BF16x3 tensor-core GEMM was measured at 1.3e-5 Ha here: its FP32 tensor-
+    // memory accumulation leaves ~1e-6 relative errors in Q, and ln det(1 + Q) - tr Q, second order
+    // in Q, does not forgive first-order errors.)
     QK_TRY(qk_gemm_f32p_lower(ctx, 'T', 'N', r, r, nS, 1.0, L, ldl, 0, L, ldl, 0, 0.0, Q, r, r2,
                               nc, wq + (size_t)q0 * nS, nS));
     k_quad_diag<<<(r * nc + 255) / 256, 256, 0, ctx->stream>>>(r, nc, Q, qd);

@@ -1113,6 +1113,18 @@ int qk_gemm_bf16x3_dev(qk_ctx* ctx, int m, int n, int k, const double* d_A, int 
   return end(ctx, st);
 }
 
+int qk_gemm_bf16x3_ex_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k,
+                          double alpha, const double* d_A, int lda, const double* d_B, int ldb,
+                          double beta, double* d_C, int ldc) {
+  QK_TRY(begin(ctx));
+  const bool TA = (transa == 'T' || transa == 't'), TB = (transb == 'T' || transb == 't');
+  if (lda < (TA ? k : m) || ldb < (TB ? n : k) || ldc < m)
+    return qk_fail(ctx, QK_ERR_ARG, "bad leading dimensions");
+  const int st = qk_gemm_bf16x3(ctx, transa, transb, m, n, k, alpha, d_A, lda, 0, d_B, ldb, 0,
+                                nullptr, 0, beta, d_C, ldc, 0, 1, false);
+  return end(ctx, st);
+}
+
 int qk_RG0W0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int nOrb, int nC, int nO, int nR,
                    int naux, const double* d_L, const double* d_eHF, double* d_eGW, double* d_SigC,
                    double* d_Z, double* d_Om, double* EcRPA, double* EcGM) {

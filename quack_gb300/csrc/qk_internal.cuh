@@ -233,6 +233,14 @@ int qk_max_abs_diff(qk_ctx* ctx, int n, const double* a, const double* b, double
 
 // BF16x3 tensor-core GEMM (k_bf16x3.cu): C(m x n, ldc) = A(m x k) * B(n x k)^T, column-major,
 // FP64 in/out, three-way BF16 split, FP32 accumulation in TMEM.
+// The general form: C_b = alpha op(A_b) diag(bscale_b) op(B_b) + beta C_b for b < batch (operands
+// with stride 0 are shared; bscale, if given, scales the k index of op(B)), lower: only the
+// 128x128 tiles touching the lower triangle of C.  Few output tiles with a long k split k over
+// CTAs (FP64 slices and one reduction).
+int qk_gemm_bf16x3(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,
+                   const double* A, long long lda, long long sA, const double* B, long long ldb,
+                   long long sB, const float* bscale, long long sBS, double beta, double* C,
+                   long long ldc, long long sC, int batch, bool lower);
 int qk_gemm_bf16x3_nt(qk_ctx* ctx, int m, int n, int k, const double* A, long long lda,
                       const double* B, long long ldb, double* C, long long ldc);
 

@@ -59,6 +59,32 @@ def test_dgemm_dev_matches_numpy(ctx, path):
         ctx.tune_set("dgemm_path", key, max(v, 0))
 
 
+@pytest.mark.parametrize("ta,tb,m,n,k", [("N", "N", 70, 33, 45), ("T", "N", 64, 65, 66),
+                                         ("N", "T", 129, 17, 3), ("T", "T", 5, 200, 77),
+                                         ("N", "N", 300, 128, 3000), ("T", "N", 128, 600, 3600),
+                                         ("N", "T", 257, 300, 128)])
+def test_gemm_bf16x3_ex_transposes_alpha_beta_splitk(ctx, ta, tb, m, n, k):
+    """General BF16x3 GEMM: every transpose, alpha and beta, ragged sizes, and the split-K shapes
+    of the back-transformation (few output tiles, long k)."""
+    import torch
+    rng = np.random.default_rng(m + 3 * n + 7 * k)
+    A = rng.standard_normal((k, m) if ta == "T" else (m, k))
+    B = rng.standard_normal((n, k) if tb == "T" else (k, n))
+    C0 = rng.standard_normal((m, n))
+    dA = torch.from_numpy(np.asfortranarray(A).ravel(order="F")).cuda()
+    dB = torch.from_numpy(np.asfortranarray(B).ravel(order="F")).cuda()
+    dC = torch.from_numpy(np.asfortranarray(C0).ravel(order="F")).cuda()
+    api.gemm_bf16x3_ex_dev(ta, tb, m, n, k, -0.75, dA.data_ptr(), A.shape[0], dB.data_ptr(),
+                           B.shape[0], 1.25, dC.data_ptr(), m, ctx=ctx)
+    opA = A.T if ta == "T" else A
+    opB = B.T if tb == "T" else B
+    ref = -0.75 * opA @ opB + 1.25 * C0
+    scale = 0.75 * np.abs(opA) @ np.abs(opB)
+    C = dC.cpu().numpy().reshape((m, n), order="F")
+    assert np.all(np.abs(C - ref) <= 4e-6 * max(1.0, np.sqrt(k / 64.0)) * scale
+                  + 1e-13 * np.abs(ref)), (ta, tb)
+
+
 def test_dgemm_f32p_dev_error_bound(ctx):
     """FP32-product GEMM (the mixed tier's back-transformation): every transpose, ragged sizes
     and the split-K shape; the error stays within a few FP32 roundings of sum |a_ik b_kj|."""
