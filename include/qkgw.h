@@ -220,6 +220,31 @@ int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int method, int nsys
 int qk_dsyev_dev(qk_ctx* ctx, int n, double* d_A, int lda, double* d_w, double* d_Zt,
                  int want_vectors);
 
+/* ---- Bethe-Salpeter excitation energies on top of GW (GW/RGW_phBSE.f90) -------------------
+ * qk_RGW_phBSE: static phBSE@GW -- the dRPA singlet screening at the energies eW (the G0W0 caller
+ *   passes eHF, GW/RG0W0.f90:241-242), its static kernels KA/KB
+ *   (GW/RGW_phBSE_static_kernel_A/B.f90), and per spin the Casida problem of
+ *   A = phRLR_A(ispin, dRPA = false, eGW) + KA, B = phRLR_B + KB (full, or TDA).  Outputs the
+ *   correlation energies EcBSE[2] (singlet, 3 x triplet; halved with exchange_kernel, :183-187)
+ *   and the excitation energies of the manifolds asked for (OmBSE_* of length nS, or NULL).
+ *   The second-order kernel (dophBSE2), the dynamical correction (dBSE) and the transition
+ *   dipoles are not computed.  All arithmetic FP64.  ERI is the full ERI(nOrb,nOrb,nOrb,nOrb). */
+typedef struct {
+  int TDA_W;            /* Tamm-Dancoff screening */
+  int TDA;              /* Tamm-Dancoff BSE */
+  int singlet;          /* compute the singlet manifold */
+  int triplet;          /* compute the triplet manifold */
+  int exchange_kernel;  /* halve EcBSE (RGW_phBSE.f90:186-187) */
+  double eta;           /* the GW broadening of the static kernels */
+} qk_bse_params;
+
+int qk_RGW_phBSE(qk_ctx* ctx, const qk_bse_params* prm, int nBas, int nOrb, int nC, int nO,
+                 int nV, int nR, int nS, const double* ERI, const double* eW, const double* eGW,
+                 double* EcBSE, double* OmBSE_singlet, double* OmBSE_triplet);
+int qk_RGW_phBSE_dev(qk_ctx* ctx, const qk_bse_params* prm, int nOrb, int nC, int nO, int nR,
+                     const double* d_ERI, const double* d_eW, const double* d_eGW, double* EcBSE,
+                     double* d_OmBSE_singlet, double* d_OmBSE_triplet);
+
 /* ---- dRPA correlation energy by frequency quadrature (device pointers) ---------------------
  * qk_RPA_ecorr_quad_dev: EcRPA = (sum Omega - tr A)/2 of the singlet dRPA problem at orbital
  *   energies d_e (the quantity phRLR returns, LR/phRLR.f90) without the nS x nS eigenproblem:

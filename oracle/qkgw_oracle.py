@@ -362,6 +362,65 @@ def AOtoMO_ERI_RHF(nBas, nOrb, c, ERI_AO):
 
 
 # ---------------------------------------------------------------------------
+# Bethe-Salpeter equation on top of GW (src/GW/RGW_phBSE*.f90)
+# ---------------------------------------------------------------------------
+def RGW_phBSE_static_kernel_A(eta, nBas, nC, nO, nV, nR, nS, lam, Om, rho):
+    """Static BSE kernel, resonant block -- GW/RGW_phBSE_static_kernel_A.f90:32-52.
+
+    KA(ia,jb) = 4 lam^2 sum_kc rho(i,j,kc) rho(a,b,kc) Om(kc) / (Om(kc)^2 + eta^2).
+    """
+    occ, vir = _ov(nBas, nC, nO, nR)
+    f = Om / (Om ** 2 + eta ** 2)
+    roo = rho[np.ix_(occ, occ)]                       # [i,j,kc]
+    rvv = rho[np.ix_(vir, vir)]                       # [a,b,kc]
+    K = np.einsum("ijk,abk,k->iajb", roo, rvv, f, optimize=True)
+    return 4.0 * lam ** 2 * K.reshape(nS, nS)
+
+
+def RGW_phBSE_static_kernel_B(eta, nBas, nC, nO, nV, nR, nS, lam, Om, rho):
+    """Static BSE kernel, coupling block -- GW/RGW_phBSE_static_kernel_B.f90:32-52.
+
+    KB(ia,jb) = 4 lam^2 sum_kc rho(i,b,kc) rho(a,j,kc) Om(kc) / (Om(kc)^2 + eta^2).
+    """
+    occ, vir = _ov(nBas, nC, nO, nR)
+    f = Om / (Om ** 2 + eta ** 2)
+    rov = rho[np.ix_(occ, vir)]                       # [i,b,kc]
+    rvo = rho[np.ix_(vir, occ)]                       # [a,j,kc]
+    K = np.einsum("ibk,ajk,k->iajb", rov, rvo, f, optimize=True)
+    return 4.0 * lam ** 2 * K.reshape(nS, nS)
+
+
+def RGW_phBSE(TDA_W, TDA, singlet, triplet, exchange_kernel, eta, nOrb, nC, nO, nV, nR, nS, ERI,
+              eW, eGW):
+    """Static phBSE@GW excitation energies -- GW/RGW_phBSE.f90:83-190 (no second-order kernel,
+    no dynamical correction).  Screening: dRPA singlet at eW (:89-95); kernels from its Om, rho
+    (:97-98); per spin A = phRLR_A(ispin, dRPA=False, eGW) + KA, B = phRLR_B + KB (:110-133,
+    :146-154).  Returns dict(EcBSE=[singlet, triplet], Om_singlet, Om_triplet, Om_RPA)."""
+    Aw = phRLR_A(1, True, nOrb, nC, nO, nV, nR, nS, 1.0, eW, ERI)
+    Bw = np.zeros((nS, nS)) if TDA_W else phRLR_B(1, True, nOrb, nC, nO, nV, nR, nS, 1.0, ERI)
+    _, OmRPA, XpY, _ = phRLR(TDA_W, nS, Aw, Bw)
+    rho = RGW_excitation_density(nOrb, nC, nO, nR, nS, ERI, XpY)
+    KA = RGW_phBSE_static_kernel_A(eta, nOrb, nC, nO, nV, nR, nS, 1.0, OmRPA, rho)
+    KB = np.zeros((nS, nS)) if TDA else RGW_phBSE_static_kernel_B(eta, nOrb, nC, nO, nV, nR, nS,
+                                                                    1.0, OmRPA, rho)
+    EcBSE = [0.0, 0.0]
+    out = dict(Om_RPA=OmRPA, Om_singlet=None, Om_triplet=None)
+    for ispin, on, key in ((1, singlet, "Om_singlet"), (2, triplet, "Om_triplet")):
+        if not on:
+            continue
+        A = phRLR_A(ispin, False, nOrb, nC, nO, nV, nR, nS, 1.0, eGW, ERI) + KA
+        B = np.zeros((nS, nS)) if TDA else phRLR_B(ispin, False, nOrb, nC, nO, nV, nR, nS, 1.0,
+                                                   ERI) + KB
+        EcBSE[ispin - 1], Om, _, _ = phRLR(TDA, nS, A, B)
+        out[key] = Om
+    EcBSE[1] = 3.0 * EcBSE[1]                                          # :184
+    if exchange_kernel:
+        EcBSE = [0.5 * x for x in EcBSE]                               # :186-187
+    out["EcBSE"] = EcBSE
+    return out
+
+
+# ---------------------------------------------------------------------------
 # Drivers (src/GW/RG0W0.f90, src/GW/evRGW.f90)
 # ---------------------------------------------------------------------------
 def RG0W0(linearize, eta, doSRG, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eHF, TDA_W=False):

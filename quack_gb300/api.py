@@ -62,6 +62,11 @@ def _f(a):
     return np.asfortranarray(np.asarray(a, dtype=np.float64))
 
 
+class qk_bse_params(C.Structure):
+    _fields_ = [("TDA_W", C.c_int), ("TDA", C.c_int), ("singlet", C.c_int), ("triplet", C.c_int),
+                ("exchange_kernel", C.c_int), ("eta", C.c_double)]
+
+
 class qk_sys_desc(C.Structure):
     _fields_ = [("nOrb", C.c_int), ("nC", C.c_int), ("nO", C.c_int), ("nR", C.c_int),
                 ("naux", C.c_int), ("offset_L", C.c_longlong), ("offset_e", C.c_longlong)]
@@ -298,6 +303,36 @@ class GWOptions:
         return qk_gw_params(self.eta, int(self.linearize), int(self.reg), int(self.TDA_W),
                             self.maxSCF, self.thresh, self.max_diis, self.precision,
                             int(self.qp_guess))
+
+
+@dataclass
+class BSEOptions:
+    """BSE line of QuAcK's options (phBSE with TDA / singlet / triplet / exchange kernel)."""
+    TDA_W: bool = False
+    TDA: bool = False
+    singlet: bool = True
+    triplet: bool = True
+    exchange_kernel: bool = False
+    eta: float = 0.0
+
+    def c(self):
+        return qk_bse_params(int(self.TDA_W), int(self.TDA), int(self.singlet), int(self.triplet),
+                             int(self.exchange_kernel), self.eta)
+
+
+def RGW_phBSE(opts: BSEOptions, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eW, eGW, ctx=None):
+    """GW/RGW_phBSE.f90 (static kernel).  Returns dict(EcBSE=[singlet, triplet], Om_singlet,
+    Om_triplet) -- the excitation energies of the manifolds asked for (else None)."""
+    c = _ctx(ctx)
+    ERI, eW, eGW = _f(ERI), _f(eW), _f(eGW)
+    ec = (C.c_double * 2)()
+    oms = np.empty(nS) if opts.singlet else None
+    omt = np.empty(nS) if opts.triplet else None
+    prm = opts.c()
+    c.check(lib().qk_RGW_phBSE(c.handle, C.byref(prm), nBas, nOrb, nC, nO, nV, nR, nS, _ptr(ERI),
+                               _ptr(eW), _ptr(eGW), ec, _ptr(oms) if oms is not None else None,
+                               _ptr(omt) if omt is not None else None))
+    return dict(EcBSE=[ec[0], ec[1]], Om_singlet=oms, Om_triplet=omt)
 
 
 def RG0W0(opts: GWOptions, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eHF, ctx=None):

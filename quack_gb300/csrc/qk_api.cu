@@ -679,6 +679,114 @@ int qk_evgw_L(qk_ctx* ctx, const qk_gw_params* prm, int N, int nC, int nO, int n
 
 namespace {
 
+__global__ void k_vsum(int n, const double* __restrict__ v, double* out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += v[i];
+  s = qk_block_sum(s, red);
+  if (threadIdx.x == 0) *out = s;
+}
+
+__global__ void k_copy_om(int n, const double* __restrict__ w, double* __restrict__ Om) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) Om[i] = w[i];
+}
+
+}  // namespace
+
+// Casida solve on device buffers (LR/phRLR.f90:45-95): A (and B unless TDA) nS x nS column-major,
+// A and B are overwritten.  TDA: Om = eig(A), XpY = XmY = eigenvectors as rows.  Otherwise the
+// diagonal-A-B (dRPA) fast path or the general path eig(A-B) -> AmBSq, AmBIv -> eig(AmBSq (A+B)
+// AmBSq).  scal[0] = tr A, [1] = sum Om, [2] = EcRPA = (sum Om - tr A)/2.  want_vectors = 0 skips
+// the eigenvectors of the final eigenproblem (and XpY, XmY); *XpY / *XmY point at the context's
+// buffers on return.
+int phrlr_dev(qk_ctx* ctx, int TDA, int nS, double* dA, double* dB, double* dOm, double** XpY,
+              double** XmY, double* scal, int want_vectors) {
+  const size_t S2 = (size_t)nS * nS;
+  double *dM, *dZt = nullptr, *dX = nullptr, *dY = nullptr, *sm;
+  QK_TRY(qk_wst(ctx, W_M, S2, &dM));
+  QK_TRY(qk_wst(ctx, W_E, 3 * (size_t)nS + 64, &sm));
+  if (want_vectors) {
+    QK_TRY(qk_wst(ctx, W_ZT, S2, &dZt));
+    QK_TRY(qk_wst(ctx, W_XPY, S2, &dX));
+    QK_TRY(qk_wst(ctx, W_XMY, S2, &dY));
+  }
+  double* sq = sm;
+  double* w = sm + nS;
+  QK_CK(cudaMemsetAsync(scal, 0, 4 * sizeof(double), ctx->stream));
+  if (XpY) *XpY = want_vectors ? (TDA ? dZt : dX) : nullptr;
+  if (XmY) *XmY = want_vectors ? (TDA ? dZt : dY) : nullptr;
+  if (TDA) {
+    k_trace<<<1, 1024, 0, ctx->stream>>>(nS, dA, scal + 0);
+    QK_LAUNCHED();
+    QK_TRY(qk_eig_sym(ctx, nS, dA, nS, w, dZt, want_vectors));  // Om = eig(A)
+    k_copy_om<<<grid_for(ctx, nS), 256, 0, ctx->stream>>>(nS, w, dOm);
+    QK_LAUNCHED();
+    k_vsum<<<1, 1024, 0, ctx->stream>>>(nS, w, scal + 1);
+    QK_LAUNCHED();
+    k_ecrpa<<<1, 1, 0, ctx->stream>>>(scal + 1, scal + 0, scal + 2);
+    QK_LAUNCHED();
+    return QK_OK;
+  }
+  k_offdiag_maxabs<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, dA, dB, scal + 3);
+  QK_LAUNCHED();
+  double offmax = 0.0;
+  QK_TRY(d2h(ctx, &offmax, scal + 3, 8));
+  QK_CK(cudaStreamSynchronize(ctx->stream));
+  if (offmax == 0.0) {
+    // A-B diagonal (dRPA): M = AmBSq.(A+B).AmBSq directly
+    QK_TRY(qk_launch_casida_M_from_AB(ctx, nS, dA, dB, dM, sq, scal + 0));
+    QK_TRY(qk_eig_sym(ctx, nS, dM, nS, w, dZt, want_vectors));
+    if (want_vectors) {
+      QK_TRY(qk_launch_xpy(ctx, nS, w, dZt, sq, dOm, dX, dY, 1));
+    } else {
+      QK_TRY(qk_launch_omega(ctx, nS, w, dOm));
+    }
+  } else {
+    // general A-B (phRLR.f90:50-81): eig(A-B), AmBSq = U sqrt(l) U^T, AmBIv = U l^-1/2 U^T
+    double *amb, *sqm, *ivm, *tmp, *ut;
+    QK_TRY(qk_wst(ctx, W_SLAB, 4 * S2, &amb));
+    sqm = amb + S2;
+    ivm = sqm + S2;
+    tmp = ivm + S2;
+    QK_TRY(qk_wst(ctx, W_BSEU, S2, &ut));  // U^T of A-B
+    k_axpby<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>((long long)S2, 1.0, dA, -1.0, dB, amb);
+    QK_LAUNCHED();
+    k_trace<<<1, 1024, 0, ctx->stream>>>(nS, dA, scal + 0);
+    QK_LAUNCHED();
+    double* lam = sm + 2 * nS;
+    QK_TRY(qk_eig_sym(ctx, nS, amb, nS, lam, ut, 1));
+    // AmBSq = U diag(sqrt l) U^T = Ut^T (D Ut)
+    k_rowscale<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, lam, 0, ut, tmp);
+    QK_LAUNCHED();
+    QK_TRY(qk_dgemm(ctx, 'T', 'N', nS, nS, nS, 1.0, ut, nS, 0, tmp, nS, 0, 0.0, sqm, nS, 0, 1));
+    if (want_vectors) {
+      k_rowscale<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, lam, 1, ut, tmp);
+      QK_LAUNCHED();
+      QK_TRY(qk_dgemm(ctx, 'T', 'N', nS, nS, nS, 1.0, ut, nS, 0, tmp, nS, 0, 0.0, ivm, nS, 0, 1));
+    }
+    // ApB into amb, tmp = ApB.AmBSq, M = AmBSq.tmp
+    k_axpby<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>((long long)S2, 1.0, dA, 1.0, dB, amb);
+    QK_LAUNCHED();
+    QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, amb, nS, 0, sqm, nS, 0, 0.0, tmp, nS, 0, 1));
+    QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, sqm, nS, 0, tmp, nS, 0, 0.0, dM, nS, 0, 1));
+    QK_TRY(qk_eig_sym(ctx, nS, dM, nS, w, dZt, want_vectors));  // dZt = Z^T
+    if (want_vectors) {
+      QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, dZt, nS, 0, sqm, nS, 0, 0.0, dX, nS, 0, 1));
+      QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, dZt, nS, 0, ivm, nS, 0, 0.0, dY, nS, 0, 1));
+      k_xpy_general<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, w, dOm, dX, dY, ctx->d_status);
+      QK_LAUNCHED();
+    } else {
+      QK_TRY(qk_launch_omega(ctx, nS, w, dOm));
+    }
+  }
+  QK_TRY(qk_launch_sum_sqrt(ctx, nS, w, scal + 1));
+  k_ecrpa<<<1, 1, 0, ctx->stream>>>(scal + 1, scal + 0, scal + 2);
+  QK_LAUNCHED();
+  return QK_OK;
+}
+
+namespace {
+
 int begin(qk_ctx* ctx) {
   if (!ctx) return QK_ERR_ARG;
   (void)cudaGetLastError();  // drop a non-sticky error left in this host thread by an earlier call
@@ -746,70 +854,20 @@ int qk_phRLR_B(qk_ctx* ctx, int ispin, int dRPA, int nBas, int nC, int nO, int n
 int qk_phRLR(qk_ctx* ctx, int TDA, int nS, const double* Aph, const double* Bph, double* EcRPA,
              double* Om, double* XpY, double* XmY) {
   QK_TRY(begin(ctx));
-  if (TDA) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA screening is not supported");
   if (nS <= 0) return qk_fail(ctx, QK_ERR_ARG, "nS must be positive");
   const size_t S2 = (size_t)nS * nS;
-  double *dA, *dB, *dM, *dZt, *dX, *dY, *sm;
+  double *dA, *dOm, *scal;
   QK_TRY(qk_wst(ctx, W_HOST_A, 2 * S2, &dA));
-  dB = dA + S2;
-  QK_TRY(qk_wst(ctx, W_M, S2, &dM));
-  QK_TRY(qk_wst(ctx, W_ZT, S2, &dZt));
-  QK_TRY(qk_wst(ctx, W_XPY, S2, &dX));
-  QK_TRY(qk_wst(ctx, W_XMY, S2, &dY));
-  QK_TRY(qk_wst(ctx, W_E, 3 * (size_t)nS + 64, &sm));
-  double* sq = sm;
-  double* w = sm + nS;
-  double* dOm = sm + 2 * nS;
-  double* scal = sm + 3 * nS;  // [0] trA [1] sumOm [2] EcRPA [3] offdiag max
+  double* dB = dA + S2;
+  QK_TRY(qk_wst(ctx, W_BSE, (size_t)nS + 16, &dOm));
+  scal = dOm + nS;
   QK_TRY(h2d(ctx, dA, Aph, S2 * 8));
-  QK_TRY(h2d(ctx, dB, Bph, S2 * 8));
-  QK_CK(cudaMemsetAsync(scal, 0, 8 * sizeof(double), ctx->stream));
-  k_offdiag_maxabs<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, dA, dB, scal + 3);
-  QK_LAUNCHED();
-  double offmax = 0.0;
-  QK_TRY(d2h(ctx, &offmax, scal + 3, 8));
-  QK_CK(cudaStreamSynchronize(ctx->stream));
-  if (offmax == 0.0) {
-    // A-B diagonal (dRPA): M = AmBSq.(A+B).AmBSq directly
-    QK_TRY(qk_launch_casida_M_from_AB(ctx, nS, dA, dB, dM, sq, scal + 0));
-    QK_TRY(qk_eig_sym(ctx, nS, dM, nS, w, dZt, 1));
-    QK_TRY(qk_launch_xpy(ctx, nS, w, dZt, sq, dOm, dX, dY, 1));
-  } else {
-    // general A-B (phRLR.f90:50-81): eig(A-B), AmBSq = U sqrt(l) U^T, AmBIv = U l^-1/2 U^T
-    double *amb, *sqm, *ivm, *tmp;
-    QK_TRY(qk_wst(ctx, W_SLAB, 4 * S2, &amb));
-    sqm = amb + S2;
-    ivm = sqm + S2;
-    tmp = ivm + S2;
-    k_axpby<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>((long long)S2, 1.0, dA, -1.0, dB, amb);
-    QK_LAUNCHED();
-    k_trace<<<1, 1024, 0, ctx->stream>>>(nS, dA, scal + 0);
-    QK_LAUNCHED();
-    QK_TRY(qk_eig_sym(ctx, nS, amb, nS, w, dZt, 1));  // dZt = U^T
-    // AmBSq = U diag(sqrt l) U^T = Zt^T (D Zt)
-    k_rowscale<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, w, 0, dZt, tmp);
-    QK_LAUNCHED();
-    QK_TRY(qk_dgemm(ctx, 'T', 'N', nS, nS, nS, 1.0, dZt, nS, 0, tmp, nS, 0, 0.0, sqm, nS, 0, 1));
-    k_rowscale<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, w, 1, dZt, tmp);
-    QK_LAUNCHED();
-    QK_TRY(qk_dgemm(ctx, 'T', 'N', nS, nS, nS, 1.0, dZt, nS, 0, tmp, nS, 0, 0.0, ivm, nS, 0, 1));
-    // ApB into amb, tmp = ApB.AmBSq, M = AmBSq.tmp
-    k_axpby<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>((long long)S2, 1.0, dA, 1.0, dB, amb);
-    QK_LAUNCHED();
-    QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, amb, nS, 0, sqm, nS, 0, 0.0, tmp, nS, 0, 1));
-    QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, sqm, nS, 0, tmp, nS, 0, 0.0, dM, nS, 0, 1));
-    QK_TRY(qk_eig_sym(ctx, nS, dM, nS, w, dZt, 1));  // dZt = Z^T
-    QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, dZt, nS, 0, sqm, nS, 0, 0.0, dX, nS, 0, 1));
-    QK_TRY(qk_dgemm(ctx, 'N', 'N', nS, nS, nS, 1.0, dZt, nS, 0, ivm, nS, 0, 0.0, dY, nS, 0, 1));
-    k_xpy_general<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(nS, w, dOm, dX, dY, ctx->d_status);
-    QK_LAUNCHED();
-  }
-  QK_TRY(qk_launch_sum_sqrt(ctx, nS, w, scal + 1));
-  k_ecrpa<<<1, 1, 0, ctx->stream>>>(scal + 1, scal + 0, scal + 2);
-  QK_LAUNCHED();
+  if (!TDA) QK_TRY(h2d(ctx, dB, Bph, S2 * 8));
+  double *dX = nullptr, *dY = nullptr;
+  QK_TRY(phrlr_dev(ctx, TDA, nS, dA, dB, dOm, &dX, &dY, scal, 1));
   QK_TRY(d2h(ctx, Om, dOm, nS * 8));
   QK_TRY(d2h(ctx, XpY, dX, S2 * 8));
-  QK_TRY(d2h(ctx, XmY, dY, S2 * 8));
+  QK_TRY(d2h(ctx, XmY, TDA ? dX : dY, S2 * 8));
   QK_TRY(d2h(ctx, EcRPA, scal + 2, 8));
   return end(ctx, QK_OK);
 }
@@ -1063,6 +1121,47 @@ int qk_dgemm_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, dou
   const int st = qk_dgemm(ctx, transa, transb, m, n, k, alpha, d_A, lda, 0, d_B, ldb, 0, beta, d_C,
                           ldc, 0, 1);
   return end(ctx, st);
+}
+
+int qk_RGW_phBSE_dev(qk_ctx* ctx, const qk_bse_params* prm, int nOrb, int nC, int nO, int nR,
+                     const double* d_ERI, const double* d_eW, const double* d_eGW, double* EcBSE,
+                     double* d_OmBSE_singlet, double* d_OmBSE_triplet) {
+  QK_TRY(begin(ctx));
+  if (!prm || !d_ERI || !d_eW || !d_eGW) return qk_fail(ctx, QK_ERR_ARG, "inputs required");
+  Dims d;
+  const int nS = (nO - nC) * (nOrb - nO - nR);
+  QK_TRY(check_dims(ctx, nOrb, nOrb, nC, nO, nOrb - nO, nR, nS, &d));
+  const int st = qk_bse_dev(ctx, prm->TDA_W, prm->TDA, prm->singlet, prm->triplet,
+                            prm->exchange_kernel, prm->eta, nOrb, nC, nO, nR, d_ERI, d_eW, d_eGW,
+                            EcBSE, d_OmBSE_singlet, d_OmBSE_triplet);
+  return end(ctx, st);
+}
+
+int qk_RGW_phBSE(qk_ctx* ctx, const qk_bse_params* prm, int nBas, int nOrb, int nC, int nO,
+                 int nV, int nR, int nS, const double* ERI, const double* eW, const double* eGW,
+                 double* EcBSE, double* OmBSE_singlet, double* OmBSE_triplet) {
+  QK_TRY(begin(ctx));
+  if (!prm || !ERI || !eW || !eGW) return qk_fail(ctx, QK_ERR_ARG, "inputs required");
+  Dims d;
+  QK_TRY(check_dims(ctx, nBas, nOrb, nC, nO, nV, nR, nS, &d));
+  const size_t N = nOrb, N4 = N * N * N * N;
+  double *dERI, *io;
+  QK_TRY(qk_wst(ctx, W_ERI, N4, &dERI));
+  QK_TRY(qk_wst(ctx, W_HOST_B, 2 * N + 2 * (size_t)nS + 16, &io));
+  double* deW = io;
+  double* deGW = io + N;
+  double* dOS = io + 2 * N;
+  double* dOT = dOS + nS;
+  QK_TRY(h2d(ctx, dERI, ERI, N4 * 8));
+  QK_TRY(h2d(ctx, deW, eW, N * 8));
+  QK_TRY(h2d(ctx, deGW, eGW, N * 8));
+  const int st = qk_bse_dev(ctx, prm->TDA_W, prm->TDA, prm->singlet, prm->triplet,
+                            prm->exchange_kernel, prm->eta, nOrb, nC, nO, nR, dERI, deW, deGW,
+                            EcBSE, OmBSE_singlet ? dOS : nullptr, OmBSE_triplet ? dOT : nullptr);
+  if (st != QK_OK) return end(ctx, st);
+  if (OmBSE_singlet) QK_TRY(d2h(ctx, OmBSE_singlet, dOS, (size_t)nS * 8));
+  if (OmBSE_triplet) QK_TRY(d2h(ctx, OmBSE_triplet, dOT, (size_t)nS * 8));
+  return end(ctx, QK_OK);
 }
 
 int qk_RPA_ecorr_quad_dev(qk_ctx* ctx, int nOrb, int nC, int nO, int nR, int naux,

@@ -37,7 +37,7 @@ struct DevBuf {
 enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
   W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_TMAT2, W_RHO32, W_OMF, W_TFAC, W_STEBZ,
-  W_QUAD, W_QLT, W_QPV, W_QL, W_QX, W_QQ, W_QD, W_NUMBUF
+  W_QUAD, W_QLT, W_QPV, W_QL, W_QX, W_QQ, W_QD, W_BSE, W_BSEU, W_BSER, W_BSEK, W_NUMBUF
 };
 
 struct qk_ctx {
@@ -166,6 +166,17 @@ int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, 
                    const double* Lov, int naux, double* Ec, int* applied, bool gap_only = false);
 // Gauss-Legendre nodes and weights on [-1, 1] (Newton iteration on P_n).
 void qk_gauss_legendre_host(int n, double* x, double* w);
+
+// Casida solve on device buffers (qk_api.cu; LR/phRLR.f90:45-95), A and B overwritten; TDA or
+// full; scal[0..2] = tr A, sum Om, EcRPA; want_vectors = 0 skips the final eigenvectors.
+int phrlr_dev(qk_ctx* ctx, int TDA, int nS, double* dA, double* dB, double* dOm, double** XpY,
+              double** XmY, double* scal, int want_vectors);
+
+// static phBSE@GW excitation energies (k_bse.cu; GW/RGW_phBSE.f90:83-190): device ERI (full
+// N^4), eW (screening energies), eGW; EcBSE[2] on the host; OmS / OmT (device, nS) optional.
+int qk_bse_dev(qk_ctx* ctx, int TDA_W, int TDA, int singlet, int triplet, int exchange_kernel,
+               double eta, int N, int nC, int nO, int nR, const double* ERI, const double* eW,
+               const double* eGW, double* hEcBSE, double* OmS, double* OmT);
 
 // dense symmetric eigensolver pieces.  backtransform: 0 = leave Zt as the eigenvectors of the
 // tridiagonal matrix, 1 = back-transform in FP64, 2 = back-transform with FP32 products.

@@ -51,6 +51,46 @@ def test_he_evgw_with_diis_within_threshold(he):
     assert r["nSCF"] == 3
 
 
+def test_he_cis_matches_reference_test_data(he):
+    """The non-dRPA ph blocks that the BSE builds on: CIS = TDA of phRLR_A(ispin, dRPA=False) at
+    eHF, against the reference's own test data (test/Rtest_ref.dat:27-30, He/6-31G; its RHF energy
+    there differs from FeatherBench's by 7e-10 Ha, hence the 1e-8 bar)."""
+    E, e = he["ERI_MO"], he["eHF"]
+    for ispin, ref in ((1, 1.911193619935257), (2, 1.455852629402236)):
+        A = O.phRLR_A(ispin, False, 2, 0, 1, 1, 0, 1, 1.0, e, E)
+        _, Om, _, _ = O.phRLR(True, 1, A, np.zeros((1, 1)))
+        assert abs(Om[0] - ref) < 1e-8, (ispin, Om[0], ref)
+
+
+def test_bse_static_kernels_match_reference_loops():
+    """The einsum form of RGW_phBSE_static_kernel_A/B against the reference's loop nest
+    (GW/RGW_phBSE_static_kernel_A.f90:32-52, _B.f90:32-52) on a small random rho with a frozen
+    core and a frozen virtual."""
+    rng = np.random.default_rng(5)
+    N, nC, nO, nR = 9, 1, 4, 1
+    no, nv = nO - nC, N - nO - nR
+    nS = no * nv
+    rho = rng.standard_normal((N, N, nS))
+    Om = np.sort(rng.uniform(0.2, 3.0, nS))
+    eta = 0.05
+    KA = O.RGW_phBSE_static_kernel_A(eta, N, nC, nO, N - nO, nR, nS, 1.0, Om, rho)
+    KB = O.RGW_phBSE_static_kernel_B(eta, N, nC, nO, N - nO, nR, nS, 1.0, Om, rho)
+    ia = 0
+    for i in range(nC, nO):
+        for a in range(nO, N - nR):
+            jb = 0
+            for j in range(nC, nO):
+                for b in range(nO, N - nR):
+                    ca = sum(rho[i, j, k] * rho[a, b, k] * Om[k] / (Om[k] ** 2 + eta ** 2)
+                             for k in range(nS))
+                    cb = sum(rho[i, b, k] * rho[a, j, k] * Om[k] / (Om[k] ** 2 + eta ** 2)
+                             for k in range(nS))
+                    assert abs(KA[ia, jb] - 4.0 * ca) < 1e-12 * max(1.0, abs(ca))
+                    assert abs(KB[ia, jb] - 4.0 * cb) < 1e-12 * max(1.0, abs(cb))
+                    jb += 1
+            ia += 1
+
+
 def test_casida_closed_form_ns1(he):
     """nS = 1: Omega = sqrt(Delta (Delta + 4 (ia|ia)))."""
     E, e = he["ERI_MO"], he["eHF"]
