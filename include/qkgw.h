@@ -34,7 +34,7 @@ enum {
   QK_ERR_NOMEM = 3,        /* device allocation failed */
   QK_ERR_NOT_PD = 4,       /* reserved: A-B not positive definite (reported as warning flag) */
   QK_ERR_NO_CONV = 5,      /* evGW did not converge in maxSCF cycles (evRGW.f90:190-198 stops) */
-  QK_ERR_UNSUPPORTED = 6,  /* option outside the supported path (e.g. TDA_W, triplet W in drivers) */
+  QK_ERR_UNSUPPORTED = 6,  /* option outside the supported path */
   QK_ERR_DEVICE = 7,       /* a device-side check failed (bounded wait expired, bad index) */
   QK_ERR_NO_DEVICE = 8     /* no CUDA device / library not built for this GPU */
 };
@@ -57,7 +57,7 @@ typedef struct qk_gw_params {
   double eta;        /* eta_GW */
   int linearize;     /* lin_GW */
   int doSRG;         /* reg_GW  (SRG regularisation, flow s = 500, RG0W0.f90:98) */
-  int TDA_W;         /* must be 0: TDA screening is rejected with QK_ERR_UNSUPPORTED */
+  int TDA_W;         /* Tamm-Dancoff screening: Om = eig(A), XpY = XmY = eigenvectors */
   int maxSCF;        /* maxSCF_GW (evGW) */
   double thresh;     /* thresh_GW (evGW) */
   int max_diis;      /* max_diis_GW (evGW) */

@@ -429,13 +429,12 @@ def RG0W0(linearize, eta, doSRG, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eHF, TDA_W
     Returns a dict with eGW, SigC, Z, Om, XpY, rho, EcRPA (second Casida at
     eGW, :222-225), EcGM, eGWlin and the first-Casida EcRPA.
     """
-    if TDA_W:
-        raise NotImplementedError("TDA_W screening is not on the supported path")
     flow = 500.0                                                     # :98
     isp_W, dRPA_W = 1, True
     Aph = phRLR_A(isp_W, dRPA_W, nOrb, nC, nO, nV, nR, nS, 1.0, eHF, ERI)
-    Bph = phRLR_B(isp_W, dRPA_W, nOrb, nC, nO, nV, nR, nS, 1.0, ERI)
-    EcRPA0, Om, XpY, XmY = phRLR(False, nS, Aph, Bph)
+    Bph = np.zeros((nS, nS)) if TDA_W else phRLR_B(isp_W, dRPA_W, nOrb, nC, nO, nV, nR, nS, 1.0,
+                                                   ERI)                # :116-117
+    EcRPA0, Om, XpY, XmY = phRLR(TDA_W, nS, Aph, Bph)                 # :119
     rho = RGW_excitation_density(nOrb, nC, nO, nR, nS, ERI, XpY)
     if doSRG:
         EcGM, SigC, Z = RGW_SRG_self_energy_diag(flow, nBas, nOrb, nC, nO, nV, nR, nS, eHF, Om, rho)
@@ -449,8 +448,9 @@ def RG0W0(linearize, eta, doSRG, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eHF, TDA_W
         eGW, Z, iters = RGW_QP_graph(doSRG, eta, flow, nOrb, nC, nO, nV, nR, nS, eHF, Om, rho,
                                      eGWlin, eHF, Z, return_iters=True)
     Aph2 = phRLR_A(isp_W, dRPA_W, nOrb, nC, nO, nV, nR, nS, 1.0, eGW, ERI)
-    Bph2 = phRLR_B(isp_W, dRPA_W, nOrb, nC, nO, nV, nR, nS, 1.0, ERI)
-    EcRPA, Om2, _, _ = phRLR(False, nS, Aph2, Bph2)
+    Bph2 = np.zeros((nS, nS)) if TDA_W else phRLR_B(isp_W, dRPA_W, nOrb, nC, nO, nV, nR, nS, 1.0,
+                                                    ERI)               # :222-223
+    EcRPA, Om2, _, _ = phRLR(TDA_W, nS, Aph2, Bph2)                   # :225
     return dict(eGW=eGW, SigC=SigC, Z=Z, Om=Om, XpY=XpY, XmY=XmY, rho=rho, EcRPA=EcRPA,
                 EcRPA_HF=EcRPA0, EcGM=EcGM, eGWlin=eGWlin, Om_GW=Om2, qp_iters=iters)
 
@@ -462,8 +462,6 @@ def evRGW(maxSCF, thresh, max_diis, linearize, eta, doSRG, nBas, nOrb, nC, nO, n
     Returns a dict with eGW (after the last DIIS step), EcRPA (Casida of the
     last cycle), SigC, Z, Conv, nSCF and the per-cycle Conv history.
     """
-    if TDA_W:
-        raise NotImplementedError("TDA_W screening is not on the supported path")
     flow = 500.0
     ispin, dRPA = 1, True
     nSCF = 0
@@ -479,8 +477,9 @@ def evRGW(maxSCF, thresh, max_diis, linearize, eta, doSRG, nBas, nOrb, nC, nO, n
     SigC = np.zeros(nOrb)
     while Conv > thresh and nSCF <= maxSCF:                          # :119
         Aph = phRLR_A(ispin, dRPA, nOrb, nC, nO, nV, nR, nS, 1.0, eGW, ERI)
-        Bph = phRLR_B(ispin, dRPA, nOrb, nC, nO, nV, nR, nS, 1.0, ERI)
-        EcRPA, Om, XpY, XmY = phRLR(False, nS, Aph, Bph)
+        Bph = np.zeros((nS, nS)) if TDA_W else phRLR_B(ispin, dRPA, nOrb, nC, nO, nV, nR, nS, 1.0,
+                                                       ERI)            # :123-124
+        EcRPA, Om, XpY, XmY = phRLR(TDA_W, nS, Aph, Bph)               # :126
         rho = RGW_excitation_density(nOrb, nC, nO, nR, nS, ERI, XpY)
         if doSRG:
             EcGM, SigC, Z = RGW_SRG_self_energy_diag(flow, nBas, nOrb, nC, nO, nV, nR, nS, eGW, Om, rho)

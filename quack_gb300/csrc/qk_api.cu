@@ -11,6 +11,14 @@ struct Dims {
   int N, nC, nO, nR, nS, no, nv;
 };
 
+// the drivers' screening form for the duration of one call (the Casida helpers read ctx->tda_w)
+struct TdaScope {
+  qk_ctx* ctx;
+  bool old;
+  TdaScope(qk_ctx* c, bool on) : ctx(c), old(c->tda_w) { c->tda_w = on; }
+  ~TdaScope() { ctx->tda_w = old; }
+};
+
 int check_dims(qk_ctx* ctx, int nBas, int nOrb, int nC, int nO, int nV, int nR, int nS, Dims* d) {
   (void)nV;
   if (nBas != nOrb)
@@ -129,6 +137,32 @@ __global__ void k_trace(int n, const double* __restrict__ A, double* out) {
   s = qk_block_sum(s, red);
   if (threadIdx.x == 0) *out = s;
 }
+// dRPA singlet A = Delta + 2K from K = (ia|jb) (phRLR_A.f90:43-72, evaluation order (2K + e_a) - e_i)
+__global__ void k_build_A_from_K(int nS, int nv, int nC, int nO, const double* __restrict__ e,
+                                 const double* __restrict__ K, double* __restrict__ A) {
+  const long long total = (long long)nS * nS;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i % nS), c = (int)(i / nS);
+    double v = 2.0 * K[i];
+    if (r == c) {
+      const int ip = r / nv, ap = r - ip * nv;
+      v = (v + e[ap + nO]) - e[ip + nC];
+    }
+    A[i] = v;
+  }
+}
+__global__ void k_vsum_om(int n, const double* __restrict__ w, double* __restrict__ Om,
+                          double* out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    s += w[i];
+    if (Om) Om[i] = w[i];
+  }
+  s = qk_block_sum(s, red);
+  if (threadIdx.x == 0) *out = s;
+}
 __global__ void k_xpy_general(int nS, const double* __restrict__ w, double* __restrict__ Om,
                               double* __restrict__ XpY, double* __restrict__ XmY, int* status) {
   const long long total = (long long)nS * nS;
@@ -196,6 +230,31 @@ int casida_factored(qk_ctx* ctx, int prec, const Dims& d, const double* e, const
   QK_TRY(qk_wst(ctx, W_ZT, S2, &Zt));
   QK_TRY(qk_wst(ctx, W_TMAT2, (size_t)nS * naux, &X));
   double* w = sq + nS;
+  const int f32 = prec == QK_PREC_BF16X3;  // mixed tier: FP32 products, FP64 storage
+  if (ctx->tda_w) {
+    // Tamm-Dancoff screening (phRLR.f90 with TDA): Om = eig(A), XpY = Z^T = Z_T^T Q^T, so
+    // T = Z_T^T (Q^T Lov)
+    qk_tic(ctx, T_BUILD);
+    k_build_A_from_K<<<grid_for(ctx, (long long)nS * nS), 256, 0, ctx->stream>>>(
+        nS, d.nv, d.nC, d.nO, e, K, M);
+    QK_LAUNCHED();
+    k_trace<<<1, 1024, 0, ctx->stream>>>(nS, M, scal + 0);
+    QK_LAUNCHED();
+    qk_toc(ctx, T_BUILD);
+    QK_TRY(qk_eig_sym(ctx, nS, M, nS, w, Zt, 1, 0));
+    qk_tic(ctx, T_BACKTRANS);
+    QK_CK(cudaMemcpyAsync(X, Lov, (size_t)nS * naux * sizeof(double), cudaMemcpyDeviceToDevice,
+                          ctx->stream));
+    QK_TRY(qk_eig_apply_qt(ctx, nS, X, nS, naux, f32));
+    QK_TRY((f32 ? qk_gemm_f32p : qk_dgemm)(ctx, 'N', 'N', nS, naux, nS, 1.0, Zt, nS, 0, X, nS, 0,
+                                           0.0, T, nS, 0, 1));
+    qk_toc(ctx, T_BACKTRANS);
+    k_vsum_om<<<1, 1024, 0, ctx->stream>>>(nS, w, Om, scal + 1);
+    QK_LAUNCHED();
+    k_ecrpa<<<1, 1, 0, ctx->stream>>>(scal + 1, scal + 0, scal + 2);
+    QK_LAUNCHED();
+    return QK_OK;
+  }
   qk_tic(ctx, T_BUILD);
   QK_TRY(qk_launch_casida_M_K(ctx, d.N, d.nC, d.nO, d.nR, e, K, M, sq, scal + 0));
   qk_toc(ctx, T_BUILD);
@@ -203,7 +262,6 @@ int casida_factored(qk_ctx* ctx, int prec, const Dims& d, const double* e, const
   QK_TRY(qk_launch_omega(ctx, nS, w, Om));
   qk_tic(ctx, T_BACKTRANS);
   QK_TRY(qk_launch_rowscale(ctx, nS, naux, sq, 0, Lov, nS, X, nS));           // D_s Lov
-  const int f32 = prec == QK_PREC_BF16X3;  // mixed tier: FP32 products, FP64 storage
   QK_TRY(qk_eig_apply_qt(ctx, nS, X, nS, naux, f32));                        // Q^T (.)
   QK_TRY((f32 ? qk_gemm_f32p : qk_dgemm)(ctx, 'N', 'N', nS, naux, nS, 1.0, Zt, nS, 0, X, nS, 0,
                                          0.0, T, nS, 0, 1));
@@ -235,6 +293,32 @@ int casida_dev(qk_ctx* ctx, const Dims& d, const double* e, const double* ERI, d
   QK_TRY(qk_wst(ctx, W_M, S2, &M));
   QK_TRY(qk_wst(ctx, W_E, 2 * (size_t)d.nS + 64, &sq));
   double* w = sq + d.nS;
+  if (ctx->tda_w) {
+    // Tamm-Dancoff screening (phRLR.f90 with TDA): Om = eig(A), XpY = XmY = eigenvectors as rows
+    qk_tic(ctx, T_BUILD);
+    if (K) {
+      k_build_A_from_K<<<grid_for(ctx, (long long)S2), 256, 0, ctx->stream>>>(d.nS, d.nv, d.nC,
+                                                                               d.nO, e, K, M);
+      QK_LAUNCHED();
+    } else {
+      QK_TRY(qk_launch_build_AB(ctx, 0, 1, 1, d.N, d.nC, d.nO, d.nR, 1.0, e, ERI, M));
+    }
+    k_trace<<<1, 1024, 0, ctx->stream>>>(d.nS, M, scal + 0);
+    QK_LAUNCHED();
+    qk_toc(ctx, T_BUILD);
+    ctx->time_eig = want_vectors != 0;
+    const int est = qk_eig_sym(ctx, d.nS, M, d.nS, w, want_vectors ? XpY : nullptr, want_vectors,
+                               prec == QK_PREC_BF16X3 ? 2 : 1);
+    ctx->time_eig = true;
+    QK_TRY(est);
+    if (want_vectors && XmY)
+      QK_CK(cudaMemcpyAsync(XmY, XpY, S2 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    k_vsum_om<<<1, 1024, 0, ctx->stream>>>(d.nS, w, Om, scal + 1);
+    QK_LAUNCHED();
+    k_ecrpa<<<1, 1, 0, ctx->stream>>>(scal + 1, scal + 0, scal + 2);
+    QK_LAUNCHED();
+    return QK_OK;
+  }
   qk_tic(ctx, T_BUILD);
   if (K)
     QK_TRY(qk_launch_casida_M_K(ctx, d.N, d.nC, d.nO, d.nR, e, K, M, sq, scal + 0));
@@ -311,7 +395,7 @@ int g0w0_qp(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, double flow, co
 int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* eHF,
              const double* ERI, double* eGW, double* SigC, double* Z, double* Om, double* hEcRPA,
              double* hEcGM) {
-  if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
+  TdaScope tda(ctx, prm->TDA_W != 0);
   const double flow = 500.0;  // RG0W0.f90:98
   const int N = d.N, nS = d.nS;
   const size_t S2 = (size_t)nS * nS, N2S = (size_t)N * N * nS;
@@ -356,8 +440,9 @@ int g0w0_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
   // indefinite and the energy NaN (phRLR's square roots), which needs no eigenproblem.
   qk_tic(ctx, T_CASIDA2);
   int quad = 0;
-  QK_TRY(qk_rpa_ec_quad(ctx, N, d.nC, d.nO, d.nR, eGW, ERI, nullptr, 0, scal + 5, &quad,
-                        prm->precision != QK_PREC_BF16X3));
+  if (!prm->TDA_W)  // (with TDA screening A - B plays no part: no square roots, no quadrature)
+    QK_TRY(qk_rpa_ec_quad(ctx, N, d.nC, d.nO, d.nR, eGW, ERI, nullptr, 0, scal + 5, &quad,
+                          prm->precision != QK_PREC_BF16X3));
   if (!quad) QK_TRY(casida_dev(ctx, d, eGW, ERI, nullptr, nullptr, nullptr, scal + 3, 0));
   qk_toc(ctx, T_CASIDA2);
   double h[16];
@@ -451,7 +536,7 @@ int evgw_graph_run(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const Ev
                                 (long long)(prm->thresh * 1e15), (long long)(prm->eta * 1e15),
                                 (long long)b.ERI, (long long)b.K, (long long)b.slab,
                                 (long long)b.eHF, (long long)b.eGW, (long long)b.dstate,
-                                (long long)b.L, (long long)b.naux};
+                                (long long)b.L, (long long)b.naux, prm->TDA_W};
   if (!ctx->evgw_exec || ctx->evgw_key != key) {
     if (ctx->evgw_exec) {
       cudaGraphExecDestroy(ctx->evgw_exec);
@@ -526,7 +611,7 @@ int evgw_loop(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const EvBufs&
 int evgw_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* eHF,
              const double* ERI, double* eGW, double* SigC, double* Z, double* hEcRPA,
              double* hEcGM, int* hnSCF, double* hConv) {
-  if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
+  TdaScope tda(ctx, prm->TDA_W != 0);
   const int N = d.N, nS = d.nS;
   const size_t S2 = (size_t)nS * nS, N2S = (size_t)N * N * nS;
   const int maxd = prm->max_diis > 1 ? prm->max_diis : 1;
@@ -571,7 +656,7 @@ int evgw_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const double* 
 int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, const double* L,
                const double* eHF, double* eGW, double* SigC, double* Z, double* Om,
                double* hEcRPA, double* hEcGM) {
-  if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
+  TdaScope tda(ctx, prm->TDA_W != 0);
   const double flow = 500.0;
   const int N = d.N, nS = d.nS;
   const size_t N2S = (size_t)N * N * nS;
@@ -601,8 +686,9 @@ int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
   qk_toc(ctx, T_QP);
   qk_tic(ctx, T_CASIDA2);
   int quad = 0;
-  QK_TRY(qk_rpa_ec_quad(ctx, N, d.nC, d.nO, d.nR, eGW, nullptr, Lov, naux, scal + 5, &quad,
-                        prm->precision != QK_PREC_BF16X3));
+  if (!prm->TDA_W)
+    QK_TRY(qk_rpa_ec_quad(ctx, N, d.nC, d.nO, d.nR, eGW, nullptr, Lov, naux, scal + 5, &quad,
+                          prm->precision != QK_PREC_BF16X3));
   if (!quad) QK_TRY(casida_dev(ctx, d, eGW, nullptr, nullptr, nullptr, nullptr, scal + 3, 0, K));
   qk_toc(ctx, T_CASIDA2);
   double h[16];
@@ -617,7 +703,7 @@ int g0w0_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, co
 int evgw_L_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, int naux, const double* L,
                const double* eHF, double* eGW, double* SigC, double* Z, double* hEcRPA,
                double* hEcGM, int* hnSCF, double* hConv) {
-  if (prm->TDA_W) return qk_fail(ctx, QK_ERR_UNSUPPORTED, "TDA_W screening is not supported");
+  TdaScope tda(ctx, prm->TDA_W != 0);
   const int N = d.N, nS = d.nS;
   const size_t N2S = (size_t)N * N * nS;
   const int maxd = prm->max_diis > 1 ? prm->max_diis : 1;

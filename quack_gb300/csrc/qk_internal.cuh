@@ -49,6 +49,7 @@ struct qk_ctx {
   cudaStream_t copy_stream = nullptr;  // host->device copies overlapped with the kernels
   cudaEvent_t ev_copy = nullptr;       // end of the overlapped ERI upload
   bool eri_pending = false;            // the slab gather must wait for ev_copy first
+  bool tda_w = false;                  // the drivers' screening Casida in the Tamm-Dancoff form
   double timings[T_NUM] = {};
   std::string err;
   int* d_status = nullptr;      // device status word

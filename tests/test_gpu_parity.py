@@ -278,9 +278,56 @@ def test_bad_arguments_rejected(ctx):
     with pytest.raises(api.QkError) as ei:
         api.RG0W0(api.GWOptions(), 24, 24, 0, 5, 19, 0, 96, E, f["eHF"], ctx=ctx)
     assert ei.value.code == api.QK_ERR_ARG
-    with pytest.raises(api.QkError) as ei:
-        api.RG0W0(api.GWOptions(TDA_W=True), 24, 24, 0, 5, 19, 0, 95, E, f["eHF"], ctx=ctx)
-    assert ei.value.code == api.QK_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("lin", [True, False])
+def test_g0w0_tda_screening_matches_oracle(ctx, lin):
+    """TDA_W: the screening Casida in the Tamm-Dancoff form (Om = eig(A), XpY = eigenvectors),
+    RG0W0.f90:116-119,222-225; ERI driver and factorised driver."""
+    import torch
+    f = np.load(os.path.join(GOLD, "synth_n24.npz"))
+    N, nO = 24, 5
+    nS = nO * (N - nO)
+    E = synth.eri_phys_numpy(f["L"])
+    ref = O.RG0W0(lin, 0.0, False, N, N, 0, nO, N - nO, 0, nS, E, f["eHF"], TDA_W=True)
+    r = api.RG0W0(api.GWOptions(TDA_W=True, linearize=lin), N, N, 0, nO, N - nO, 0, nS, E,
+                  f["eHF"], ctx=ctx)
+    assert np.max(np.abs(r["Om"] - ref["Om"])) < 1e-10
+    assert abs(r["EcRPA"] - ref["EcRPA"]) < 1e-9
+    assert abs(r["EcGM"] - ref["EcGM"]) < 1e-9 * max(1.0, abs(ref["EcGM"]))
+    ok = np.ones(N, bool) if lin else (ref["qp_iters"] <= 10)
+    assert np.max(np.abs(r["eGW"][ok] - ref["eGW"][ok])) < 1e-8
+    naux = f["L"].shape[0]
+    dL = torch.from_numpy(api.L_fortran_flat(f["L"])).cuda()
+    de = torch.from_numpy(f["eHF"]).cuda()
+    out = [torch.empty(N, dtype=torch.float64, device="cuda") for _ in range(3)]
+    dOm = torch.empty(nS, dtype=torch.float64, device="cuda")
+    ec, gm = api.RG0W0_L_dev(api.GWOptions(TDA_W=True, linearize=lin), N, 0, nO, 0, naux,
+                             dL.data_ptr(), de.data_ptr(), out[0].data_ptr(), out[1].data_ptr(),
+                             out[2].data_ptr(), dOm.data_ptr(), ctx=ctx)
+    assert np.max(np.abs(dOm.cpu().numpy() - ref["Om"])) < 1e-10
+    assert np.max(np.abs(out[0].cpu().numpy()[ok] - ref["eGW"][ok])) < 1e-8
+
+
+def test_evgw_tda_screening_matches_oracle_and_graph(ctx):
+    f = np.load(os.path.join(GOLD, "synth_n24.npz"))
+    N, nO = 24, 5
+    nS = nO * (N - nO)
+    E = synth.eri_phys_numpy(f["L"])
+    ref = O.evRGW(5, 1e-5, 5, True, 0.0, False, N, N, 0, nO, N - nO, 0, nS, E, f["eHF"],
+                  TDA_W=True, raise_on_fail=False)
+    opts = api.GWOptions(TDA_W=True, linearize=True, maxSCF=5, thresh=1e-5, max_diis=5)
+    r = api.evRGW(opts, N, N, 0, nO, N - nO, 0, nS, E, f["eHF"], ctx=ctx, raise_on_fail=False)
+    assert r["nSCF"] == ref["nSCF"]
+    assert np.max(np.abs(r["eGW"] - ref["eGW"])) < 1e-8
+    assert abs(r["EcRPA"] - ref["EcRPA"]) < 1e-9
+    ctx.set_graph_mode(True)
+    try:
+        g = api.evRGW(opts, N, N, 0, nO, N - nO, 0, nS, E, f["eHF"], ctx=ctx, raise_on_fail=False)
+    finally:
+        ctx.set_graph_mode(False)
+    assert g["nSCF"] == r["nSCF"]
+    assert np.max(np.abs(g["eGW"] - r["eGW"])) < 1e-12
 
 
 def newton_stable_mask(N, nO, nS, eHF, Om, rho, eGWlin, Z, iters):
