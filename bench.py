@@ -324,6 +324,8 @@ def run_ours(args):
     res["qp_gap_min_Ha"] = {"mixed": float(e_mix[nO:].min() - e_mix[:nO].max()),
                             "plain_fp64": float(e_fp[nO:].min() - e_fp[:nO].max())}
     res["ecrpa_quadrature"] = run_ecrpa_quad(ctx, stream, N, nO, naux, s, dE, de)
+    if not args.no_bse:
+        res["bse"] = run_bse(ctx, stream, args)
     if not args.no_batch:
         res["batched_evgw"] = run_batched(args, ctx)
     if not args.no_learned:
@@ -532,6 +534,52 @@ def run_reference(args):
     print(json.dumps(res))
 
 
+def run_bse(ctx, stream, args):
+    """Static phBSE@GW (singlet and triplet, full BSE on full screening) of the N=100 synthetic
+    system (nO=13, naux=300, seed 0; nS=1131) at eW = eHF and a seeded eGW: CUDA-event time of
+    qk_RGW_phBSE_dev (ERI resident) and the oracle on the host cores, with the largest difference
+    of the excitation energies."""
+    import numpy as np
+    import torch
+    from quack_gb300 import api, synth
+    from oracle import qkgw_oracle as O
+    N, nO, naux = 100, 13, 300
+    nS = nO * (N - nO)
+    s = synth.gen_system(N, nO, naux, np.random.default_rng(0))
+    eGW = s["eHF"] + 0.01 * np.random.default_rng(1).standard_normal(N)
+    dE = synth.eri_fortran_flat_torch(s["L"], device="cuda")
+    deW = torch.from_numpy(s["eHF"]).cuda()
+    deG = torch.from_numpy(eGW).cuda()
+    dS = torch.empty(nS, dtype=torch.float64, device="cuda")
+    dT = torch.empty(nS, dtype=torch.float64, device="cuda")
+    opts = api.BSEOptions()
+    ts, ec = [], None
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ec = api.RGW_phBSE_dev(opts, N, 0, nO, 0, dE.data_ptr(), deW.data_ptr(), deG.data_ptr(),
+                               dS.data_ptr(), dT.data_ptr(), ctx=ctx)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    out = {"system": "synthetic N=100 nO=13 naux=300 seed 0 (nS=1131), singlet+triplet, full BSE",
+           "ms_gpu": min(ts), "EcBSE": ec}
+    if not args.no_cpu:
+        E = dE.view(N, N, N, N).permute(3, 2, 1, 0).cpu().numpy()  # ERI[p,q,r,s]
+        t0 = time.time()
+        ref = O.RGW_phBSE(False, False, True, True, False, 0.0, N, 0, nO, N - nO, 0, nS, E,
+                          s["eHF"], eGW)
+        out["seconds_cpu_oracle"] = time.time() - t0
+        out["cpu_cores"] = os.cpu_count()
+        out["max_abs_diff_Om_Ha"] = float(max(np.max(np.abs(dS.cpu().numpy() - ref["Om_singlet"])),
+                                              np.max(np.abs(dT.cpu().numpy() - ref["Om_triplet"]))))
+        out["abs_diff_EcBSE_Ha"] = float(max(abs(ec[0] - ref["EcBSE"][0]),
+                                             abs(ec[1] - ref["EcBSE"][1])))
+    del dE
+    return out
+
+
 def run_ecrpa_quad(ctx, stream, N, nO, naux, s, dE, de):
     """EcRPA of the N=200 system at its HF energies: the frequency quadrature (from the ERI
     tensor and from the factor L) against the FP64 eigenvalue route (M built on the device,
@@ -703,6 +751,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--reference-budget-s", type=float, default=150.0)
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-bse", action="store_true", help="skip the phBSE@GW leg")
     ap.add_argument("--batch-systems", type=int, default=32)
     ap.add_argument("--batch-workers", type=int, default=4)
     ap.add_argument("--no-learned", action="store_true")

@@ -335,6 +335,18 @@ def RGW_phBSE(opts: BSEOptions, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eW, eGW, ct
     return dict(EcBSE=[ec[0], ec[1]], Om_singlet=oms, Om_triplet=omt)
 
 
+def RGW_phBSE_dev(opts: BSEOptions, nOrb, nC, nO, nR, d_ERI, d_eW, d_eGW, d_OmS=None, d_OmT=None,
+                  ctx=None):
+    """Static phBSE@GW on device buffers (full ERI tensor).  Returns [EcBSE singlet, triplet]."""
+    c = _ctx(ctx)
+    ec = (C.c_double * 2)()
+    prm = opts.c()
+    c.check(lib().qk_RGW_phBSE_dev(c.handle, C.byref(prm), nOrb, nC, nO, nR, C.c_void_p(d_ERI),
+                                   C.c_void_p(d_eW), C.c_void_p(d_eGW), ec,
+                                   C.c_void_p(d_OmS or None), C.c_void_p(d_OmT or None)))
+    return [ec[0], ec[1]]
+
+
 def RG0W0(opts: GWOptions, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eHF, ctx=None):
     """GW/RG0W0.f90 (dRPA singlet W).  Returns dict(eGW, SigC, Z, Om, EcRPA, EcGM)."""
     c = _ctx(ctx)
