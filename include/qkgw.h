@@ -121,6 +121,23 @@ int qk_RGW_SRG_self_energy_diag(qk_ctx* ctx, double flow, int nBas, int nOrb, in
 int qk_RGW_QP_graph(qk_ctx* ctx, int doSRG, double eta, double flow, int nBas, int nC, int nO,
                     int nV, int nR, int nS, const double* eHF, const double* Om, const double* rho,
                     const double* eGWlin, const double* eOld, double* eGW, double* Z);
+/* ---- integrals from the reference's files into device memory --------------------------------
+ * qk_read_eri_bin: int/ERI.bin (utils/read_2e_integrals.f90:55-63; nBas^4 doubles, <pq|rs> in
+ *   the column-major layout every ERI argument here takes) streamed into d_ERI through two
+ *   pinned staging buffers, reading overlapped with the copies.
+ * qk_read_eri_chem_bin: int/ERI_chem.bin (read_2e_integrals.f90:85-107; the 8-fold symmetric
+ *   chemist integrals, pair(i,j) = i(i+1)/2 + j for i >= j, nested once more over the pairs, as
+ *   AOtoMO/Hartree_matrix_AO_basis.f90:71-93 indexes them) streamed to the device and expanded
+ *   into the full <pq|rs> tensor d_ERI (nBas^4).
+ * qk_unpack_eri_s8_dev: that expansion alone, from a packed array already on the device.
+ * qk_AOtoMO_ERI_RHF_dev: the AO->MO transform of qk_AOtoMO_ERI_RHF on device buffers (d_ERI_AO
+ *   is left unchanged). */
+int qk_read_eri_bin(qk_ctx* ctx, const char* path, int nBas, double* d_ERI);
+int qk_read_eri_chem_bin(qk_ctx* ctx, const char* path, int nBas, double* d_ERI);
+int qk_unpack_eri_s8_dev(qk_ctx* ctx, int nBas, const double* d_packed, double* d_ERI);
+int qk_AOtoMO_ERI_RHF_dev(qk_ctx* ctx, int nBas, int nOrb, const double* d_c,
+                          const double* d_ERI_AO, double* d_ERI_MO);
+
 /* AOtoMO/AOtoMO_ERI_RHF.f90:1-55 */
 int qk_AOtoMO_ERI_RHF(qk_ctx* ctx, int nBas, int nOrb, const double* c, const double* ERI_AO,
                       double* ERI_MO);

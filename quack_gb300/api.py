@@ -430,6 +430,30 @@ def gauss_legendre(n):
     return x, w
 
 
+def read_eri_bin(path, nBas, d_ERI, ctx=None):
+    """int/ERI.bin (nBas^4 doubles, <pq|rs> column-major) streamed into the device buffer."""
+    c = _ctx(ctx)
+    c.check(lib().qk_read_eri_bin(c.handle, str(path).encode(), nBas, C.c_void_p(d_ERI)))
+
+
+def read_eri_chem_bin(path, nBas, d_ERI, ctx=None):
+    """int/ERI_chem.bin (8-fold packed chemist integrals) streamed to the device and expanded
+    into the full <pq|rs> tensor."""
+    c = _ctx(ctx)
+    c.check(lib().qk_read_eri_chem_bin(c.handle, str(path).encode(), nBas, C.c_void_p(d_ERI)))
+
+
+def unpack_eri_s8_dev(nBas, d_packed, d_ERI, ctx=None):
+    c = _ctx(ctx)
+    c.check(lib().qk_unpack_eri_s8_dev(c.handle, nBas, C.c_void_p(d_packed), C.c_void_p(d_ERI)))
+
+
+def AOtoMO_ERI_RHF_dev(nBas, nOrb, d_c, d_ERI_AO, d_ERI_MO, ctx=None):
+    c = _ctx(ctx)
+    c.check(lib().qk_AOtoMO_ERI_RHF_dev(c.handle, nBas, nOrb, C.c_void_p(d_c), C.c_void_p(d_ERI_AO),
+                                        C.c_void_p(d_ERI_MO)))
+
+
 def dgemm_f32p_dev(transa, transb, m, n, k, alpha, d_A, lda, d_B, ldb, beta, d_C, ldc, ctx=None):
     """The dgemm_dev contract with FP32 products (compensated FP32 sums, FP64 in/out)."""
     c = _ctx(ctx)

@@ -1067,18 +1067,13 @@ int qk_RGW_QP_graph(qk_ctx* ctx, int doSRG, double eta, double flow, int nBas, i
   return end(ctx, QK_OK);
 }
 
-int qk_AOtoMO_ERI_RHF(qk_ctx* ctx, int nBas, int nOrb, const double* c, const double* ERI_AO,
-                      double* ERI_MO) {
-  QK_TRY(begin(ctx));
-  if (nBas <= 0 || nOrb <= 0 || nOrb > nBas) return qk_fail(ctx, QK_ERR_ARG, "bad sizes");
-  const size_t B = nBas, O = nOrb, B4 = B * B * B * B;
-  double *X, *Y, *dc;
-  QK_TRY(qk_wst(ctx, W_ERI, B4, &X));
-  QK_TRY(qk_wst(ctx, W_SLAB, B4, &Y));
-  QK_TRY(qk_wst(ctx, W_HOST_A, B * O, &dc));
-  QK_TRY(h2d(ctx, X, ERI_AO, B4 * 8));
-  QK_TRY(h2d(ctx, dc, c, B * O * 8));
-  // four dgemm('T','N') quarter transforms (AOtoMO_ERI_RHF.f90:26-53)
+namespace {
+
+// four dgemm('T','N') quarter transforms (AOtoMO_ERI_RHF.f90:26-53) on device buffers; X holds
+// the AO tensor and is overwritten, Y is scratch; returns the buffer that holds the result
+int aotomo_dev(qk_ctx* ctx, int nBas, int nOrb, const double* dc, double* X, double* Y,
+               double** result) {
+  const size_t B = nBas, O = nOrb;
   long long R[4] = {(long long)(B * B * B), (long long)(B * B * O), (long long)(B * O * O),
                     (long long)(O * O * O)};
   double* src = X;
@@ -1090,7 +1085,39 @@ int qk_AOtoMO_ERI_RHF(qk_ctx* ctx, int nBas, int nOrb, const double* c, const do
     src = dst;
     dst = t;
   }
-  QK_TRY(d2h(ctx, ERI_MO, src, O * O * O * O * 8));
+  *result = src;
+  return QK_OK;
+}
+
+}  // namespace
+
+int qk_AOtoMO_ERI_RHF(qk_ctx* ctx, int nBas, int nOrb, const double* c, const double* ERI_AO,
+                      double* ERI_MO) {
+  QK_TRY(begin(ctx));
+  if (nBas <= 0 || nOrb <= 0 || nOrb > nBas) return qk_fail(ctx, QK_ERR_ARG, "bad sizes");
+  const size_t B = nBas, O = nOrb, B4 = B * B * B * B;
+  double *X, *Y, *dc, *res;
+  QK_TRY(qk_wst(ctx, W_ERI, B4, &X));
+  QK_TRY(qk_wst(ctx, W_SLAB, B4, &Y));
+  QK_TRY(qk_wst(ctx, W_HOST_A, B * O, &dc));
+  QK_TRY(h2d(ctx, X, ERI_AO, B4 * 8));
+  QK_TRY(h2d(ctx, dc, c, B * O * 8));
+  QK_TRY(aotomo_dev(ctx, nBas, nOrb, dc, X, Y, &res));
+  QK_TRY(d2h(ctx, ERI_MO, res, O * O * O * O * 8));
+  return end(ctx, QK_OK);
+}
+
+int qk_AOtoMO_ERI_RHF_dev(qk_ctx* ctx, int nBas, int nOrb, const double* d_c,
+                          const double* d_ERI_AO, double* d_ERI_MO) {
+  QK_TRY(begin(ctx));
+  if (nBas <= 0 || nOrb <= 0 || nOrb > nBas) return qk_fail(ctx, QK_ERR_ARG, "bad sizes");
+  const size_t B = nBas, O = nOrb, B4 = B * B * B * B;
+  double *X, *Y, *res;
+  QK_TRY(qk_wst(ctx, W_ERI, B4, &X));
+  QK_TRY(qk_wst(ctx, W_SLAB, B4, &Y));
+  QK_CK(cudaMemcpyAsync(X, d_ERI_AO, B4 * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  QK_TRY(aotomo_dev(ctx, nBas, nOrb, d_c, X, Y, &res));
+  QK_CK(cudaMemcpyAsync(d_ERI_MO, res, O * O * O * O * 8, cudaMemcpyDeviceToDevice, ctx->stream));
   return end(ctx, QK_OK);
 }
 

@@ -37,7 +37,7 @@ struct DevBuf {
 enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
   W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_TMAT2, W_RHO32, W_OMF, W_TFAC, W_STEBZ,
-  W_QUAD, W_QLT, W_QPV, W_QL, W_QX, W_QQ, W_QD, W_BSE, W_BSEU, W_BSER, W_BSEK, W_NUMBUF
+  W_QUAD, W_QLT, W_QPV, W_QL, W_QX, W_QQ, W_QD, W_BSE, W_BSEU, W_BSER, W_BSEK, W_ERIPACK, W_NUMBUF
 };
 
 struct qk_ctx {
