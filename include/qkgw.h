@@ -169,6 +169,28 @@ int qk_evRGW_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int n
                  double* d_SigC, double* d_Z, double* EcRPA, double* EcGM, int* nSCF,
                  double* Conv);
 
+/* ---- quasiparticle self-consistent GW (GW/qsRGW.f90:193-359) -------------------------------
+ * Replaces the call qsRGW(...) of GW/RGW.f90 for nBas = nOrb, without the linearised
+ * density-matrix correction (do_linDM_GW), the dipoles and the post-processing BSE.  AO inputs:
+ * S, T, V, Hc = T + V, X (orthogonalisation, Fp = X^T F X), ERI_AO(nBas^4) = <mu nu|la si>
+ * (physicist layout, 8-fold permutational symmetry of real integrals assumed), and the RHF
+ * start eHF, cHF, PHF.  prm: eta, doSRG, TDA_W, maxSCF, thresh, max_diis (<= 32) and
+ * precision are read.  Outputs: eGW, c, P, SigC = c^T SigCp c (MO basis), Z of the last cycle;
+ * EqsGW = ET + EV + EJ + EK (electronic, without ENuc), EcRPA, EcGM of the last cycle, nSCF,
+ * Conv.  c, P, SigC and Z may be NULL in the host-pointer form (SigC in both).  Returns
+ * QK_ERR_NO_CONV (results written) when nSCF reaches maxSCF, as the reference stops there. */
+int qk_qsRGW(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
+             int nR, int nS, const double* eHF, const double* cHF, const double* PHF,
+             const double* S, const double* T, const double* V, const double* Hc, const double* X,
+             const double* ERI_AO, double* eGW, double* c, double* P, double* SigC, double* Z,
+             double* EqsGW, double* EcRPA, double* EcGM, int* nSCF, double* Conv);
+int qk_qsRGW_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
+                 int nR, int nS, const double* d_eHF, const double* d_cHF, const double* d_PHF,
+                 const double* d_S, const double* d_T, const double* d_V, const double* d_Hc,
+                 const double* d_X, const double* d_ERI_AO, double* d_eGW, double* d_c,
+                 double* d_P, double* d_SigC, double* d_Z, double* EqsGW, double* EcRPA,
+                 double* EcGM, int* nSCF, double* Conv);
+
 /* ---- factorised-integral drivers (device pointers) ---------------------------------------
  * (pq|rs) = sum_P L(p,q,P) L(r,s,P) with L(nOrb,nOrb,naux) column-major (symmetric in p,q).
  * The slab (pq|jb) and the Casida coupling (ia|jb) are built on the device from L (in the

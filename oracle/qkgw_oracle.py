@@ -504,6 +504,133 @@ def evRGW(maxSCF, thresh, max_diis, linearize, eta, doSRG, nBas, nOrb, nC, nO, n
                 conv_hist=hist, failed=failed)
 
 
+# ---------------------------------------------------------------------------
+# Quasiparticle self-consistent GW (src/GW/qsRGW.f90)
+# ---------------------------------------------------------------------------
+def Hartree_matrix_AO_basis(nBas, P, ERI):
+    """J(mu,nu) = sum_{la,si} P(la,si) ERI(mu,la,nu,si) -- AOtoMO/Hartree_matrix_AO_basis.f90:23-31."""
+    return np.einsum("ls,mlns->mn", P, ERI, optimize=True)
+
+
+def exchange_matrix_AO_basis(nBas, P, ERI):
+    """K(mu,nu) = -sum_{la,si} P(la,si) ERI(mu,la,si,nu) -- AOtoMO/exchange_matrix_AO_basis.f90:22-31."""
+    return -np.einsum("ls,mlsn->mn", P, ERI, optimize=True)
+
+
+def AOtoMO(nBas, nOrb, c, M):
+    """c^T M c -- AOtoMO/AOtoMO.f90:21-29."""
+    return c.T @ (M @ c)
+
+
+def MOtoAO(nBas, nOrb, S, c, M):
+    """(S c) M (S c)^T -- AOtoMO/MOtoAO.f90:26-36."""
+    SC = S @ c
+    return SC @ (M @ SC.T)
+
+
+def RGW_self_energy(eta, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho):
+    """Full correlation self-energy matrix, Z and EcGM -- GW/RGW_self_energy.f90:40-156:
+    Sig(p,q) = sum_m [sum_i 2 rho(p,i,m) rho(q,i,m) eps/(eps^2+eta^2), eps = e(p)-e(i)+Om(m)]
+             + sum_m [sum_a 2 rho(p,a,m) rho(q,a,m) eps/(eps^2+eta^2), eps = e(p)-e(a)-Om(m)].
+    Returns (EcGM, Sig, Z)."""
+    occ, vir = _ov(nOrb, nC, nO, nR)
+    act = np.arange(nC, nOrb - nR)
+    eta2 = eta * eta
+    Sig = np.zeros((nOrb, nOrb))
+    dZ = np.zeros(nOrb)
+    for x, sgn in ((occ, 1.0), (vir, -1.0)):
+        eps = e[act][:, None, None] - e[x][None, :, None] + sgn * Om[None, None, :]   # [p,x,m]
+        w = eps / (eps ** 2 + eta2)
+        rp = rho[np.ix_(act, x)]                                                     # [p,x,m]
+        Sig[np.ix_(act, act)] += 2.0 * np.einsum("pxm,pxm,qxm->pq", w, rp, rp, optimize=True)
+        dZ[act] -= np.einsum("pxm,pxm->p", 2.0 * rp ** 2, (eps ** 2 - eta2) / (eps ** 2 + eta2) ** 2)
+    Z = 1.0 / (1.0 - dZ)
+    EcGM, _, _ = RGW_self_energy_diag(eta, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho)
+    return EcGM, Sig, Z
+
+
+def RGW_SRG_self_energy(flow, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho):
+    """SRG-regularised full self-energy -- GW/RGW_SRG_self_energy.f90:40-80:
+    Sig(p,q) = sum_(x,m) 2 rho(p,x,m) rho(q,x,m) (1 - exp(-s Dp^2) exp(-s Dq^2)) (Dp+Dq)/(Dp^2+Dq^2),
+    D = e - e_x + Om (x occupied) or e - e_x - Om (x virtual).  Z and EcGM are those of
+    RGW_SRG_self_energy_diag (RGW_SRG_self_energy.f90:86-130 has the same formulas)."""
+    occ, vir = _ov(nOrb, nC, nO, nR)
+    act = np.arange(nC, nOrb - nR)
+    s = flow
+    Sig = np.zeros((nOrb, nOrb))
+    for x, sgn in ((occ, 1.0), (vir, -1.0)):
+        D = e[act][:, None, None] - e[x][None, :, None] + sgn * Om[None, None, :]   # [p,x,m]
+        g = np.exp(-s * D * D)
+        r = rho[np.ix_(act, x)]
+        for ip, p in enumerate(act):
+            Dp, Dq = D[ip][None], D
+            f = (1.0 - g[ip][None] * g) * (Dp + Dq) / (Dp * Dp + Dq * Dq)
+            Sig[p, act] += np.einsum("xm,qxm->q", 2.0 * r[ip], r * f)
+    EcGM, _, Z = RGW_SRG_self_energy_diag(flow, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho)
+    return EcGM, Sig, Z
+
+
+def qsRGW(maxSCF, thresh, max_diis, eta, TDA_W, nBas, nOrb, nC, nO, nV, nR, nS, eHF, cHF, PHF, S,
+          T, V, Hc, X, ERI_AO, raise_on_fail=True, doSRG=False):
+    """Quasiparticle self-consistent GW@RHF -- GW/qsRGW.f90:193-359 (nBas = nOrb, without the
+    linearised density-matrix correction, dipoles, SRG and the post-processing BSE).
+    Returns dict(eGW, c, P, EqsGW (electronic), EcRPA, EcGM, SigC (MO), Z, nSCF, Conv, failed)."""
+    assert nBas == nOrb
+    nSCF = -1
+    n_diis = 0
+    Conv = 1.0
+    P = PHF.copy()
+    eGW = eHF.copy()
+    c = cHF.copy()
+    nsq = nBas * nBas
+    F_diis = np.zeros((nsq, max(max_diis, 1)))
+    err_diis = np.zeros((nsq, max(max_diis, 1)))
+    EcRPA = EcGM = EqsGW = 0.0
+    SigC = Z = None
+    while Conv > thresh and nSCF < maxSCF:                                     # :193
+        nSCF += 1
+        J = Hartree_matrix_AO_basis(nBas, P, ERI_AO)                           # :201
+        K = exchange_matrix_AO_basis(nBas, P, ERI_AO)                          # :202
+        ERI_MO = AOtoMO_ERI_RHF(nBas, nOrb, c, ERI_AO)                         # :210
+        Aph = phRLR_A(1, True, nOrb, nC, nO, nV, nR, nS, 1.0, eGW, ERI_MO)      # :214
+        Bph = np.zeros((nS, nS)) if TDA_W else phRLR_B(1, True, nOrb, nC, nO, nV, nR, nS, 1.0,
+                                                       ERI_MO)                  # :215
+        EcRPA, Om, XpY, XmY = phRLR(TDA_W, nS, Aph, Bph)                       # :217
+        rho = RGW_excitation_density(nOrb, nC, nO, nR, nS, ERI_MO, XpY)       # :220
+        if doSRG:                                                              # :257-264
+            EcGM, SigC, Z = RGW_SRG_self_energy(500.0, nBas, nOrb, nC, nO, nV, nR, nS, eGW, Om,
+                                                rho)
+        else:
+            EcGM, SigC, Z = RGW_self_energy(eta, nBas, nOrb, nC, nO, nV, nR, nS, eGW, Om, rho)
+        SigC = 0.5 * (SigC + SigC.T)                                           # :269
+        SigCp = MOtoAO(nBas, nOrb, S, c, SigC)                                 # :276
+        F = Hc + J + 0.5 * K + SigCp                                           # :280
+        err = F @ (P @ S) - (S @ P) @ F                                        # :288
+        if nSCF > 1:
+            Conv = float(np.max(np.abs(err)))                                  # :290
+        ET = trace_matrix(P @ T)                                               # :294
+        EV = trace_matrix(P @ V)                                               # :298
+        EJ = 0.5 * trace_matrix(P @ J)                                         # :302
+        EK = 0.25 * trace_matrix(P @ K)                                        # :306
+        EqsGW = ET + EV + EJ + EK                                              # :310
+        if max_diis > 1:                                                       # :314-319
+            n_diis = min(n_diis + 1, max_diis)
+            _, err_diis, F_diis, Fv = DIIS_extrapolation(n_diis, err_diis, F_diis,
+                                                         err.reshape(-1, order="F"),
+                                                         F.reshape(-1, order="F"))
+            F = Fv.reshape((nBas, nBas), order="F")
+        Fp = X.T @ (F @ X)                                                     # :324
+        cp, eGW = diagonalize_matrix(Fp)                                       # :326
+        c = X @ cp                                                             # :327
+        SigC = AOtoMO(nBas, nOrb, c, SigCp)                                    # :335
+        P = 2.0 * c[:, :nO] @ c[:, :nO].T                                      # :339
+    failed = (nSCF == maxSCF)                                                  # :354
+    if failed and raise_on_fail:
+        raise RuntimeError("qsGW convergence failed")
+    return dict(eGW=eGW, c=c, P=P, EqsGW=EqsGW, EcRPA=EcRPA, EcGM=EcGM, SigC=SigC, Z=Z,
+                nSCF=nSCF, Conv=Conv, failed=failed)
+
+
 def homo_lumo(eGW, nO):
     """print_RG0W0.f90:27-29."""
     return float(np.max(eGW[:nO])), float(np.min(eGW[nO:]))

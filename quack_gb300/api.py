@@ -376,6 +376,47 @@ def evRGW(opts: GWOptions, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eHF, ctx=None, r
                 Conv=conv.value, failed=(rc == QK_ERR_NO_CONV))
 
 
+def qsRGW(opts: GWOptions, nBas, nOrb, nC, nO, nV, nR, nS, eHF, cHF, PHF, S, T, V, Hc, X, ERI_AO,
+          ctx=None, raise_on_fail=True):
+    """GW/qsRGW.f90 (nBas = nOrb; opts.reg selects the SRG self-energy).  ERI_AO[mu,nu,la,si] =
+    <mu nu|la si>.  Returns dict(eGW, c, P, SigC (MO basis), Z, EqsGW (electronic), EcRPA, EcGM,
+    nSCF, Conv, failed)."""
+    c = _ctx(ctx)
+    ins = [_f(a) for a in (eHF, cHF, PHF, S, T, V, Hc, X, ERI_AO)]
+    eGW, Z = np.empty(nOrb), np.empty(nOrb)
+    cq, P, SigC = (np.empty((nBas, nOrb), order="F"), np.empty((nBas, nBas), order="F"),
+                   np.empty((nOrb, nOrb), order="F"))
+    E, Ec, gm, conv = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+    nscf = C.c_int()
+    prm = opts.c()
+    rc = c.check(lib().qk_qsRGW(c.handle, C.byref(prm), nBas, nOrb, nC, nO, nV, nR, nS,
+                                *[_ptr(a) for a in ins], _ptr(eGW), _ptr(cq), _ptr(P), _ptr(SigC),
+                                _ptr(Z), C.byref(E), C.byref(Ec), C.byref(gm), C.byref(nscf),
+                                C.byref(conv)),
+                 allow=() if raise_on_fail else (QK_ERR_NO_CONV,))
+    return dict(eGW=eGW, c=cq, P=P, SigC=SigC, Z=Z, EqsGW=E.value, EcRPA=Ec.value, EcGM=gm.value,
+                nSCF=nscf.value, Conv=conv.value, failed=(rc == QK_ERR_NO_CONV))
+
+
+def qsRGW_dev(opts: GWOptions, nOrb, nC, nO, nR, d_eHF, d_cHF, d_PHF, d_S, d_T, d_V, d_Hc, d_X,
+              d_ERI_AO, d_eGW, d_c, d_P, d_Z, d_SigC=None, ctx=None, raise_on_fail=True):
+    """Device-pointer qsGW (integer device addresses).  Returns dict(EqsGW, EcRPA, EcGM, nSCF,
+    Conv, failed)."""
+    c = _ctx(ctx)
+    nS = (nO - nC) * (nOrb - nO - nR)
+    E, Ec, gm, conv = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+    nscf = C.c_int()
+    prm = opts.c()
+    ptrs = [C.c_void_p(a) for a in (d_eHF, d_cHF, d_PHF, d_S, d_T, d_V, d_Hc, d_X, d_ERI_AO, d_eGW,
+                                    d_c, d_P, d_SigC, d_Z)]
+    rc = c.check(lib().qk_qsRGW_dev(c.handle, C.byref(prm), nOrb, nOrb, nC, nO, nOrb - nO, nR, nS,
+                                    *ptrs, C.byref(E), C.byref(Ec), C.byref(gm), C.byref(nscf),
+                                    C.byref(conv)),
+                 allow=() if raise_on_fail else (QK_ERR_NO_CONV,))
+    return dict(EqsGW=E.value, EcRPA=Ec.value, EcGM=gm.value, nSCF=nscf.value, Conv=conv.value,
+                failed=(rc == QK_ERR_NO_CONV))
+
+
 def RG0W0_dev(opts: GWOptions, nOrb, nC, nO, nR, d_ERI, d_eHF, d_eGW, d_SigC, d_Z, d_Om,
               ctx=None):
     """Device-pointer driver: arguments are integer device addresses (e.g. tensor.data_ptr()).

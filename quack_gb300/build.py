@@ -16,7 +16,7 @@ LIB = os.path.join(HERE, "libqkgw.so")
 
 SOURCES = ["qk_ctx.cu", "k_gemm64.cu", "k_eig.cu", "k_casida.cu", "k_sigma.cu", "k_bf16x3.cu",
            "k_mlp.cu", "k_probe.cu", "k_noalloc.cu", "k_tune.cu", "k_rpa_quad.cu", "k_bse.cu",
-           "k_eri_io.cu", "qk_api.cu", "qk_batch.cu"]
+           "k_eri_io.cu", "k_qsgw.cu", "qk_api.cu", "qk_batch.cu"]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-diag-suppress", "550"]

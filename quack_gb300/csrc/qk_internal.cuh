@@ -37,7 +37,8 @@ struct DevBuf {
 enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
   W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_TMAT2, W_RHO32, W_OMF, W_TFAC, W_STEBZ,
-  W_QUAD, W_QLT, W_QPV, W_QL, W_QX, W_QQ, W_QD, W_BSE, W_BSEU, W_BSER, W_BSEK, W_ERIPACK, W_NUMBUF
+  W_QUAD, W_QLT, W_QPV, W_QL, W_QX, W_QQ, W_QD, W_BSE, W_BSEU, W_BSER, W_BSEK, W_ERIPACK,
+  W_QSR1, W_QSR2, W_QSJK, W_QSMAT, W_QSDIIS, W_QSIN, W_NUMBUF
 };
 
 struct qk_ctx {
@@ -172,6 +173,24 @@ void qk_gauss_legendre_host(int n, double* x, double* w);
 // full; scal[0..2] = tr A, sum Om, EcRPA; want_vectors = 0 skips the final eigenvectors.
 int phrlr_dev(qk_ctx* ctx, int TDA, int nS, double* dA, double* dB, double* dOm, double** XpY,
               double** XmY, double* scal, int want_vectors);
+
+// quasiparticle self-consistent GW, AO-basis pieces (k_qsgw.cu):
+//   J = Hartree, K = exchange matrix of P over the AO tensor (part: 2 N^3 scratch);
+//   slab / Kmat from the partial MO transform with c (W1, W2: max(N^3 no, N^2 nS) each);
+//   Sig = full correlation self-energy (unsymmetrised, W: N^2 nS scratch);
+//   out[0..5] = ET, EV, EJ, EK, EqsGW, max|err|.
+int qk_qs_jk(qk_ctx* ctx, int N, const double* ERI, const double* P, double* part, double* J,
+             double* K);
+int qk_qs_mo_slab(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* c, const double* ERI,
+                  double* W1, double* W2, double* slab, double* Kmat);
+int qk_qs_sigma(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
+                int nS, const double* e, const double* Om, const double* rho, double* W,
+                double* Sig);
+int qk_qs_sym(qk_ctx* ctx, int N, int nC, int nR, const double* Sig, double* out);
+int qk_qs_fock(qk_ctx* ctx, int N, const double* Hc, const double* J, const double* K,
+               const double* SigCp, double* F);
+int qk_qs_energy(qk_ctx* ctx, int N, const double* P, const double* T, const double* V,
+                 const double* J, const double* K, const double* err, double* out);
 
 // static phBSE@GW excitation energies (k_bse.cu; GW/RGW_phBSE.f90:83-190): device ERI (full
 // N^4), eW (screening energies), eGW; EcBSE[2] on the host; OmS / OmT (device, nS) optional.
@@ -334,4 +353,20 @@ __device__ __forceinline__ T qk_block_sum(T v, T* red /* >= 32 entries */) {
   __syncthreads();
   s = red[0];
   return s;
+}
+
+// block-wide maximum, every thread gets the result (fmax semantics: NaN operands are ignored)
+__device__ __forceinline__ double qk_block_max(double v, double* red /* >= 32 entries */) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    double s = lane < nw ? red[lane] : -INFINITY;
+    for (int o = 16; o > 0; o >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, o));
+    if (lane == 0) red[0] = s;
+  }
+  __syncthreads();
+  return red[0];
 }
