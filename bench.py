@@ -326,6 +326,8 @@ def run_ours(args):
     res["ecrpa_quadrature"] = run_ecrpa_quad(ctx, stream, N, nO, naux, s, dE, de)
     if not args.no_bse:
         res["bse"] = run_bse(ctx, stream, args)
+    if not args.no_qsgw:
+        res["qsgw"] = run_qsgw(ctx, stream, args)
     if not args.no_batch:
         res["batched_evgw"] = run_batched(args, ctx)
     if not args.no_learned:
@@ -580,6 +582,113 @@ def run_bse(ctx, stream, args):
     return out
 
 
+def _rhf_start_torch(S, Hc, ERI, nO, tol=1e-10, maxit=300):
+    """RHF start (DIIS on F) computed with torch on the GPU: input preparation for the larger H
+    chains of the qsGW case, the same procedure as synth.rhf_start.  Returns numpy arrays
+    (E_elec, eps, C, P, X)."""
+    import torch
+    dS, dH = torch.from_numpy(S).cuda(), torch.from_numpy(Hc).cuda()
+    N = S.shape[0]
+    dE = torch.from_numpy(ERI).cuda()
+    Jm = dE.permute(0, 2, 1, 3).reshape(N * N, N * N)   # J(mu,nu) = sum ERI(mu,la,nu,si) P(la,si)
+    Km = dE.permute(0, 3, 1, 2).reshape(N * N, N * N)   # K(mu,nu) = -sum ERI(mu,la,si,nu) P(la,si)
+    s, U = torch.linalg.eigh(dS)
+    X = (U * s.rsqrt()) @ U.T
+    F, hist = dH.clone(), []
+    for _ in range(maxit):
+        eps, Cp = torch.linalg.eigh(X.T @ F @ X)
+        C = X @ Cp
+        P = 2.0 * C[:, :nO] @ C[:, :nO].T
+        F = dH + (Jm @ P.reshape(-1)).reshape(N, N) - 0.5 * (Km @ P.reshape(-1)).reshape(N, N)
+        err = F @ P @ dS - dS @ P @ F
+        if err.abs().max().item() < tol:
+            break
+        hist = (hist + [(F.clone(), err.reshape(-1))])[-8:]
+        m = len(hist)
+        B = -torch.ones(m + 1, m + 1, dtype=torch.float64, device="cuda")
+        B[m, m] = 0.0
+        E = torch.stack([h[1] for h in hist])
+        B[:m, :m] = E @ E.T
+        rhs = torch.zeros(m + 1, dtype=torch.float64, device="cuda")
+        rhs[m] = -1.0
+        w = torch.linalg.solve(B, rhs)[:m]
+        F = sum(w[i] * hist[i][0] for i in range(m))
+    eps, Cp = torch.linalg.eigh(X.T @ F @ X)
+    C = X @ Cp
+    P = 2.0 * C[:, :nO] @ C[:, :nO].T
+    Eel = 0.5 * float(torch.sum(P * (dH + F)))
+    del Jm, Km, dE
+    return Eel, eps.cpu().numpy(), C.cpu().numpy(), P.cpu().numpy(), X.cpu().numpy()
+
+
+def run_qsgw(ctx, stream, args, n_atoms=24):
+    """Quasiparticle self-consistent GW@RHF (qsRGW.f90) of a linear H chain (spacing 1.6 bohr,
+    3 s primitives per atom; H24: nBas = 72, nO = 12, nS = 720; eta = 0.05, DIIS 5, thresh 1e-5):
+    CUDA-event time of the converged qk_qsRGW_dev run in both tiers (AO integrals and RHF start
+    resident), and the first three cycles on the GPU and through the oracle on the host cores,
+    with their largest differences."""
+    import numpy as np
+    import torch
+    from quack_gb300 import api, synth
+    if n_atoms <= 24:
+        sy = synth.hchain_system(n_atoms, 1.6)
+    else:
+        S, T, V, ERI, ENuc = synth.hchain_integrals(n_atoms, 1.6)
+        Eel, eps, C, P0, X = _rhf_start_torch(S, T + V, ERI, n_atoms // 2)
+        sy = dict(nBas=S.shape[0], nO=n_atoms // 2, S=S, T=T, V=V, Hc=T + V, X=X, ERI_AO=ERI,
+                  ENuc=ENuc, ERHF=Eel, eHF=eps, cHF=C, PHF=P0)
+    n, nO = sy["nBas"], sy["nO"]
+    nS = nO * (n - nO)
+
+    def dev(a):
+        return torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).cuda()
+
+    names = ("eHF", "cHF", "PHF", "S", "T", "V", "Hc", "X", "ERI_AO")
+    d = {k: dev(sy[k]) for k in names}
+    eGW = torch.empty(n, dtype=torch.float64, device="cuda")
+    c = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    P = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    Z = torch.empty(n, dtype=torch.float64, device="cuda")
+
+    def run(maxSCF, prec=api.QK_PREC_FP64):
+        opts = api.GWOptions(maxSCF=maxSCF, thresh=1e-5, max_diis=5, eta=0.05, precision=prec)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        r = api.qsRGW_dev(opts, n, 0, nO, 0, *[d[k].data_ptr() for k in names], eGW.data_ptr(),
+                          c.data_ptr(), P.data_ptr(), Z.data_ptr(), ctx=ctx, raise_on_fail=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return r, e0.elapsed_time(e1)
+
+    out = {"system": "H%d chain, 1.6 bohr, 3 s primitives/atom (nBas=%d, nO=%d, nS=%d), "
+                     "eta=0.05, DIIS 5, thresh 1e-5" % (n_atoms, n, nO, nS),
+           "ERHF_plus_ENuc": sy["ERHF"] + sy["ENuc"]}
+    e_tier = {}
+    for prec, name in ((api.QK_PREC_FP64, "fp64"), (api.QK_PREC_BF16X3, "mixed")):
+        runs = [run(128, prec) for _ in range(3)]
+        r, _ = runs[-1]
+        ms = min(t for _, t in runs)
+        e_tier[name] = eGW.cpu().numpy()
+        out[name] = {"ms_gpu": ms, "nSCF": r["nSCF"], "converged": not r["failed"],
+                     "ms_gpu_per_cycle": ms / (r["nSCF"] + 1),
+                     "EqsGW_plus_ENuc": r["EqsGW"] + sy["ENuc"]}
+    out["mixed_vs_fp64_max_abs_eGW_Ha"] = float(np.max(np.abs(e_tier["mixed"] - e_tier["fp64"])))
+    if not args.no_cpu:
+        from oracle import qkgw_oracle as O
+        r3, ms3 = run(2)
+        e3 = eGW.cpu().numpy()
+        t0 = time.time()
+        ref = O.qsRGW(2, 1e-5, 5, 0.05, False, n, n, 0, nO, n - nO, 0, nS, sy["eHF"], sy["cHF"],
+                      sy["PHF"], sy["S"], sy["T"], sy["V"], sy["Hc"], sy["X"], sy["ERI_AO"],
+                      raise_on_fail=False)
+        out["three_cycles"] = {"ms_gpu": ms3, "seconds_cpu_oracle": time.time() - t0,
+                               "cpu_cores": os.cpu_count(),
+                               "max_abs_diff_eGW_Ha": float(np.max(np.abs(e3 - ref["eGW"]))),
+                               "abs_diff_EqsGW_Ha": abs(r3["EqsGW"] - ref["EqsGW"])}
+    return out
+
+
 def run_ecrpa_quad(ctx, stream, N, nO, naux, s, dE, de):
     """EcRPA of the N=200 system at its HF energies: the frequency quadrature (from the ERI
     tensor and from the factor L) against the FP64 eigenvalue route (M built on the device,
@@ -636,7 +745,8 @@ def run_profile_case(args):
       g0w0_L    : the N=200 G0W0 from its factor L (no N^4 tensor on the device), mixed tier
       g0w0_mixed: the bench's G0W0 step, mixed tier only (launch list of one step)
       c4        : the N=400 system (nS=14400) through the factorised drivers, both tiers
-      rpa_quad  : the frequency-quadrature EcRPA of the N=200 system (ERI and factor inputs)"""
+      rpa_quad  : the frequency-quadrature EcRPA of the N=200 system (ERI and factor inputs)
+      qsgw      : the qsGW leg without the oracle (H chain of --case-n atoms, default 24)"""
     import numpy as np
     import torch
     from quack_gb300 import api, synth
@@ -671,6 +781,12 @@ def run_profile_case(args):
                                 "n_over_1meV": int((d > MEV).sum()),
                                 "Om_max_abs_Ha": float(np.abs(res["mixed_" + q][1] -
                                                               res["fp64_" + q][1]).max())}
+    elif args.profile_case == "qsgw":
+        # an H chain of --case-n atoms (default 24; nBas = 3 x atoms), GPU only
+        args.no_cpu = True
+        n_atoms = args.case_n if args.case_n != 3600 else 24
+        out.update(run_qsgw(ctx, torch.cuda.ExternalStream(api.stream_handle(ctx)), args,
+                            n_atoms=n_atoms))
     elif args.profile_case == "rpa_quad":
         # the frequency-quadrature EcRPA of the N=200 system at its HF energies, from the ERI
         # tensor (pivoted Cholesky of (ia|jb)) and from the factor L
@@ -752,11 +868,13 @@ def main():
     ap.add_argument("--reference-budget-s", type=float, default=150.0)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-bse", action="store_true", help="skip the phBSE@GW leg")
+    ap.add_argument("--no-qsgw", action="store_true", help="skip the qsGW leg")
     ap.add_argument("--batch-systems", type=int, default=32)
     ap.add_argument("--batch-workers", type=int, default=4)
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-systems", type=int, default=120)
-    ap.add_argument("--profile-case", choices=["tridiag", "g0w0_L", "g0w0_mixed", "c4", "rpa_quad"],
+    ap.add_argument("--profile-case", choices=["tridiag", "g0w0_L", "g0w0_mixed", "c4", "rpa_quad",
+                                                  "qsgw"],
                     default=None,
                     help="run one small kernel case for an ncu capture instead of the bench")
     ap.add_argument("--case-n", type=int, default=3600)

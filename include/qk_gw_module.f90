@@ -137,6 +137,20 @@ module qk_gw_module
       integer(c_int), intent(out)   :: nSCF
     end function qk_evRGW
 
+    integer(c_int) function qk_qsRGW(ctx, prm, nBas, nOrb, nC, nO, nV, nR, nS, eHF, cHF, PHF, S, T, &
+        V, Hc, X, ERI_AO, eGW, c, P, SigC, Z, EqsGW, EcRPA, EcGM, nSCF, Conv) bind(C, name="qk_qsRGW")
+      import c_int, c_ptr, c_double, qk_gw_params
+      type(c_ptr), value            :: ctx
+      type(qk_gw_params), intent(in):: prm
+      integer(c_int), value         :: nBas, nOrb, nC, nO, nV, nR, nS
+      real(c_double), intent(in)    :: eHF(nOrb), cHF(nBas,nOrb), PHF(nBas,nBas)
+      real(c_double), intent(in)    :: S(nBas,nBas), T(nBas,nBas), V(nBas,nBas), Hc(nBas,nBas)
+      real(c_double), intent(in)    :: X(nBas,nOrb), ERI_AO(nBas,nBas,nBas,nBas)
+      real(c_double), intent(out)   :: eGW(nOrb), c(nBas,nOrb), P(nBas,nBas), SigC(nOrb,nOrb)
+      real(c_double), intent(out)   :: Z(nOrb), EqsGW, EcRPA, EcGM, Conv
+      integer(c_int), intent(out)   :: nSCF
+    end function qk_qsRGW
+
   end interface
 
 end module qk_gw_module
