@@ -170,9 +170,11 @@ int qk_evRGW_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int n
                  double* Conv);
 
 /* ---- quasiparticle self-consistent GW (GW/qsRGW.f90:193-359) -------------------------------
- * Replaces the call qsRGW(...) of GW/RGW.f90 for nBas = nOrb, without the linearised
- * density-matrix correction (do_linDM_GW), the dipoles and the post-processing BSE.  AO inputs:
- * S, T, V, Hc = T + V, X (orthogonalisation, Fp = X^T F X), ERI_AO(nBas^4) = <mu nu|la si>
+ * Replaces the call qsRGW(...) of GW/RGW.f90:116-124, without the linearised density-matrix
+ * correction (do_linDM_GW), the dipoles and the post-processing BSE.  nBas >= nOrb: with
+ * nOrb < nBas F is projected through c and Fp = c^T F c, as the reference does (qsRGW.f90:281-284,
+ * 328-333).  AO inputs: S, T, V, Hc = T + V (nBas^2), X (nBas x nOrb; Fp = X^T F X when nBas = nOrb),
+ * cHF (nBas x nOrb), PHF (nBas^2), ERI_AO(nBas^4) = <mu nu|la si>
  * (physicist layout, 8-fold permutational symmetry of real integrals assumed), and the RHF
  * start eHF, cHF, PHF.  prm: eta, doSRG, TDA_W, maxSCF, thresh, max_diis (<= 32) and
  * precision are read.  Outputs: eGW, c, P, SigC = c^T SigCp c (MO basis), Z of the last cycle;

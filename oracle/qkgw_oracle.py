@@ -545,7 +545,7 @@ def RGW_self_energy(eta, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho):
         Sig[np.ix_(act, act)] += 2.0 * np.einsum("pxm,pxm,qxm->pq", w, rp, rp, optimize=True)
         dZ[act] -= np.einsum("pxm,pxm->p", 2.0 * rp ** 2, (eps ** 2 - eta2) / (eps ** 2 + eta2) ** 2)
     Z = 1.0 / (1.0 - dZ)
-    EcGM, _, _ = RGW_self_energy_diag(eta, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho)
+    EcGM, _, _ = RGW_self_energy_diag(eta, nOrb, nOrb, nC, nO, nV, nR, nS, e, Om, rho)
     return EcGM, Sig, Z
 
 
@@ -566,16 +566,17 @@ def RGW_SRG_self_energy(flow, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho):
             Dp, Dq = D[ip][None], D
             f = (1.0 - g[ip][None] * g) * (Dp + Dq) / (Dp * Dp + Dq * Dq)
             Sig[p, act] += np.einsum("xm,qxm->q", 2.0 * r[ip], r * f)
-    EcGM, _, Z = RGW_SRG_self_energy_diag(flow, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho)
+    EcGM, _, Z = RGW_SRG_self_energy_diag(flow, nOrb, nOrb, nC, nO, nV, nR, nS, e, Om, rho)
     return EcGM, Sig, Z
 
 
 def qsRGW(maxSCF, thresh, max_diis, eta, TDA_W, nBas, nOrb, nC, nO, nV, nR, nS, eHF, cHF, PHF, S,
           T, V, Hc, X, ERI_AO, raise_on_fail=True, doSRG=False):
-    """Quasiparticle self-consistent GW@RHF -- GW/qsRGW.f90:193-359 (nBas = nOrb, without the
-    linearised density-matrix correction, dipoles, SRG and the post-processing BSE).
+    """Quasiparticle self-consistent GW@RHF -- GW/qsRGW.f90:193-359 (without the linearised
+    density-matrix correction, dipoles and the post-processing BSE).  nOrb < nBas follows the
+    reference's projected branch (:281-284, :329-333).
     Returns dict(eGW, c, P, EqsGW (electronic), EcRPA, EcGM, SigC (MO), Z, nSCF, Conv, failed)."""
-    assert nBas == nOrb
+    assert nOrb <= nBas
     nSCF = -1
     n_diis = 0
     Conv = 1.0
@@ -605,6 +606,8 @@ def qsRGW(maxSCF, thresh, max_diis, eta, TDA_W, nBas, nOrb, nC, nO, nV, nR, nS, 
         SigC = 0.5 * (SigC + SigC.T)                                           # :269
         SigCp = MOtoAO(nBas, nOrb, S, c, SigC)                                 # :276
         F = Hc + J + 0.5 * K + SigCp                                           # :280
+        if nBas != nOrb:                                                       # :281-284
+            F = MOtoAO(nBas, nOrb, S, c, AOtoMO(nBas, nOrb, c, F))
         err = F @ (P @ S) - (S @ P) @ F                                        # :288
         if nSCF > 1:
             Conv = float(np.max(np.abs(err)))                                  # :290
@@ -619,9 +622,14 @@ def qsRGW(maxSCF, thresh, max_diis, eta, TDA_W, nBas, nOrb, nC, nO, nV, nR, nS, 
                                                          err.reshape(-1, order="F"),
                                                          F.reshape(-1, order="F"))
             F = Fv.reshape((nBas, nBas), order="F")
-        Fp = X.T @ (F @ X)                                                     # :324
-        cp, eGW = diagonalize_matrix(Fp)                                       # :326
-        c = X @ cp                                                             # :327
+        if nBas == nOrb:
+            Fp = X.T @ (F @ X)                                                 # :324
+            cp, eGW = diagonalize_matrix(Fp)                                   # :326
+            c = X @ cp                                                         # :327
+        else:
+            Fp = c.T @ (F @ c)                                                 # :329
+            cp, eGW = diagonalize_matrix(Fp)                                   # :331
+            c = c @ cp                                                         # :332
         SigC = AOtoMO(nBas, nOrb, c, SigCp)                                    # :335
         P = 2.0 * c[:, :nO] @ c[:, :nO].T                                      # :339
     failed = (nSCF == maxSCF)                                                  # :354

@@ -378,7 +378,7 @@ def evRGW(opts: GWOptions, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eHF, ctx=None, r
 
 def qsRGW(opts: GWOptions, nBas, nOrb, nC, nO, nV, nR, nS, eHF, cHF, PHF, S, T, V, Hc, X, ERI_AO,
           ctx=None, raise_on_fail=True):
-    """GW/qsRGW.f90 (nBas = nOrb; opts.reg selects the SRG self-energy).  ERI_AO[mu,nu,la,si] =
+    """GW/qsRGW.f90 (nBas >= nOrb; opts.reg selects the SRG self-energy).  ERI_AO[mu,nu,la,si] =
     <mu nu|la si>.  Returns dict(eGW, c, P, SigC (MO basis), Z, EqsGW (electronic), EcRPA, EcGM,
     nSCF, Conv, failed)."""
     c = _ctx(ctx)
@@ -399,9 +399,11 @@ def qsRGW(opts: GWOptions, nBas, nOrb, nC, nO, nV, nR, nS, eHF, cHF, PHF, S, T, 
 
 
 def qsRGW_dev(opts: GWOptions, nOrb, nC, nO, nR, d_eHF, d_cHF, d_PHF, d_S, d_T, d_V, d_Hc, d_X,
-              d_ERI_AO, d_eGW, d_c, d_P, d_Z, d_SigC=None, ctx=None, raise_on_fail=True):
-    """Device-pointer qsGW (integer device addresses).  Returns dict(EqsGW, EcRPA, EcGM, nSCF,
-    Conv, failed)."""
+              d_ERI_AO, d_eGW, d_c, d_P, d_Z, d_SigC=None, ctx=None, raise_on_fail=True,
+              nBas=None):
+    """Device-pointer qsGW (integer device addresses; nBas defaults to nOrb).  Returns
+    dict(EqsGW, EcRPA, EcGM, nSCF, Conv, failed)."""
+    nBas = nOrb if nBas is None else nBas
     c = _ctx(ctx)
     nS = (nO - nC) * (nOrb - nO - nR)
     E, Ec, gm, conv = C.c_double(), C.c_double(), C.c_double(), C.c_double()
@@ -409,7 +411,7 @@ def qsRGW_dev(opts: GWOptions, nOrb, nC, nO, nR, d_eHF, d_cHF, d_PHF, d_S, d_T, 
     prm = opts.c()
     ptrs = [C.c_void_p(a) for a in (d_eHF, d_cHF, d_PHF, d_S, d_T, d_V, d_Hc, d_X, d_ERI_AO, d_eGW,
                                     d_c, d_P, d_SigC, d_Z)]
-    rc = c.check(lib().qk_qsRGW_dev(c.handle, C.byref(prm), nOrb, nOrb, nC, nO, nOrb - nO, nR, nS,
+    rc = c.check(lib().qk_qsRGW_dev(c.handle, C.byref(prm), nBas, nOrb, nC, nO, nOrb - nO, nR, nS,
                                     *ptrs, C.byref(E), C.byref(Ec), C.byref(gm), C.byref(nscf),
                                     C.byref(conv)),
                  allow=() if raise_on_fail else (QK_ERR_NO_CONV,))
@@ -430,6 +432,24 @@ def RG0W0_dev(opts: GWOptions, nOrb, nC, nO, nR, d_ERI, d_eHF, d_eGW, d_SigC, d_
                                C.c_void_p(d_SigC), C.c_void_p(d_Z), C.c_void_p(d_Om),
                                C.byref(Ec), C.byref(gm)))
     return Ec.value, gm.value
+
+
+def evRGW_dev(opts: GWOptions, nOrb, nC, nO, nR, d_ERI, d_eHF, d_eGW, d_SigC, d_Z, ctx=None,
+              raise_on_fail=True):
+    """Device-pointer evGW driver (integer device addresses).  Returns dict(EcRPA, EcGM, nSCF,
+    Conv, failed)."""
+    c = _ctx(ctx)
+    nS = (nO - nC) * (nOrb - nO - nR)
+    Ec, gm, conv = C.c_double(), C.c_double(), C.c_double()
+    nscf = C.c_int()
+    prm = opts.c()
+    rc = c.check(lib().qk_evRGW_dev(c.handle, C.byref(prm), nOrb, nOrb, nC, nO, nOrb - nO, nR, nS,
+                                    C.c_void_p(d_eHF), C.c_void_p(d_ERI), C.c_void_p(d_eGW),
+                                    C.c_void_p(d_SigC), C.c_void_p(d_Z), C.byref(Ec), C.byref(gm),
+                                    C.byref(nscf), C.byref(conv)),
+                 allow=() if raise_on_fail else (QK_ERR_NO_CONV,))
+    return dict(EcRPA=Ec.value, EcGM=gm.value, nSCF=nscf.value, Conv=conv.value,
+                failed=(rc == QK_ERR_NO_CONV))
 
 
 def dsyev_dev(n, d_A, lda, d_w, d_Zt, want_vectors=True, ctx=None):

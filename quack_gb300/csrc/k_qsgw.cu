@@ -267,20 +267,20 @@ int qk_qs_jk(qk_ctx* ctx, int N, const double* ERI, const double* P, double* par
   return QK_OK;
 }
 
-int qk_qs_mo_slab(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* c, const double* ERI,
-                  double* W1, double* W2, double* slab, double* Kmat) {
+int qk_qs_mo_slab(qk_ctx* ctx, int nBas, int N, int nC, int nO, int nR, const double* c,
+                  const double* ERI, double* W1, double* W2, double* slab, double* Kmat) {
   const int no = nO - nC, nv = N - nO - nR;
-  const long long N1 = N;
-  const double* cocc = c + N1 * nC;
-  const double* cvir = c + N1 * nO;
-  // <mu la|nu si> -> (la,nu,si,j) -> (nu,si,j,p) -> (si,j,p,b) -> (j,p,b,q)
-  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)(N1 * N1 * N1), no, N, 1.0, ERI, N1, 0, cocc, N1, 0, 0.0,
-                  W1, N1 * N1 * N1, 0, 1));
-  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)(N1 * N1 * no), N, N, 1.0, W1, N1, 0, c, N1, 0, 0.0, W2,
-                  N1 * N1 * no, 0, 1));
-  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)(N1 * no * N1), nv, N, 1.0, W2, N1, 0, cvir, N1, 0, 0.0, W1,
-                  N1 * no * N1, 0, 1));
-  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)((long long)no * N1 * nv), N, N, 1.0, W1, N1, 0, c, N1, 0,
+  const long long N1 = N, B = nBas;
+  const double* cocc = c + B * nC;
+  const double* cvir = c + B * nO;
+  // <mu la|nu si> -> (la,nu,si,j) -> (nu,si,j,p) -> (si,j,p,b) -> (j,p,b,q); c is nBas x nOrb
+  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)(B * B * B), no, nBas, 1.0, ERI, B, 0, cocc, B, 0, 0.0, W1,
+                  B * B * B, 0, 1));
+  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)(B * B * no), N, nBas, 1.0, W1, B, 0, c, B, 0, 0.0, W2,
+                  B * B * no, 0, 1));
+  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)(B * no * N1), nv, nBas, 1.0, W2, B, 0, cvir, B, 0, 0.0, W1,
+                  B * no * N1, 0, 1));
+  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)((long long)no * N1 * nv), N, nBas, 1.0, W1, B, 0, c, B, 0,
                   0.0, W2, (long long)no * N1 * nv, 0, 1));
   const long long nS = (long long)no * nv;
   k_qs_slab<<<grid_1d(ctx, N1 * N1 * nS), 256, 0, ctx->stream>>>(N, no, nv, W2, slab);

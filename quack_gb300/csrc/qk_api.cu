@@ -1103,63 +1103,68 @@ struct QsOut {
   double* Conv;
 };
 
-int qsgw_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const QsIn& in,
+int qsgw_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, const Dims& d, const QsIn& in,
              const QsOut& out) {
   if (prm->maxSCF < 0) return qk_fail(ctx, QK_ERR_ARG, "maxSCF must be >= 0");
   if (prm->max_diis > 32) return qk_fail(ctx, QK_ERR_ARG, "max_diis above 32");
+  if (nBas < d.N) return qk_fail(ctx, QK_ERR_ARG, "nBas (%d) < nOrb (%d)", nBas, d.N);
   TdaScope tda(ctx, prm->TDA_W != 0);
-  const int N = d.N, nS = d.nS;
+  const int N = d.N, nS = d.nS, B = nBas;
+  const bool proj = B != N;  // the reference's nBas /= nOrb branch (qsRGW.f90:281-284,328-333)
   const double flow = 500.0;
-  const size_t N1 = N, N2 = N1 * N1, N3 = N2 * N1;
-  const size_t rw = N3 * d.no > N2 * nS ? N3 * d.no : N2 * nS;
+  const size_t N1 = N, N2 = N1 * N1, B1 = B, B2 = B1 * B1, B3 = B2 * B1;
+  const size_t rw = B3 * d.no > N2 * nS ? B3 * d.no : N2 * nS;
   double *W1, *W2, *part, *mat, *slab, *rho, *Kmat, *XpY, *hist = nullptr;
   QK_TRY(qk_wst(ctx, W_QSR1, rw, &W1));
   QK_TRY(qk_wst(ctx, W_QSR2, rw, &W2));
-  QK_TRY(qk_wst(ctx, W_QSJK, 2 * N3, &part));
-  QK_TRY(qk_wst(ctx, W_QSMAT, 14 * N2 + N1 + nS + 64, &mat));
+  QK_TRY(qk_wst(ctx, W_QSJK, 2 * B3, &part));
+  QK_TRY(qk_wst(ctx, W_QSMAT, 14 * B2 + N1 + nS + 64, &mat));
   QK_TRY(qk_wst(ctx, W_SLAB, N2 * nS, &slab));
   QK_TRY(qk_wst(ctx, W_RHO, N2 * nS, &rho));
   QK_TRY(qk_wst(ctx, W_KMAT, (size_t)nS * nS, &Kmat));
   QK_TRY(qk_wst(ctx, W_XPY, (size_t)nS * nS, &XpY));
+  // every matrix slot holds nBas^2 doubles; AO matrices are nBas x nBas (ld nBas), MO matrices
+  // nOrb x nOrb (ld nOrb), mixed ones nBas x nOrb (ld nBas)
   double* J = mat;
-  double* K = J + N2;
-  double* F = K + N2;
-  double* err = F + N2;
-  double* Sraw = err + N2;
-  double* Smo = Sraw + N2;
-  double* SigCp = Smo + N2;
-  double* T1 = SigCp + N2;
-  double* T2 = T1 + N2;
-  double* Fp = T2 + N2;
-  double* Zt = Fp + N2;
-  double* SC = Zt + N2;
-  double* PS = SC + N2;
-  double* SP = PS + N2;
-  double* sdiag = SP + N2;
+  double* K = J + B2;
+  double* F = K + B2;
+  double* err = F + B2;
+  double* Sraw = err + B2;
+  double* Smo = Sraw + B2;
+  double* SigCp = Smo + B2;
+  double* T1 = SigCp + B2;
+  double* T2 = T1 + B2;
+  double* Fp = T2 + B2;
+  double* Zt = Fp + B2;
+  double* SC = Zt + B2;
+  double* PS = SC + B2;
+  double* SP = PS + B2;
+  double* sdiag = SP + B2;
   double* Om = sdiag + N1;
   double* sm = Om + nS;  // [0..2] Casida scalars, [8] EcGM, [16..21] energies + max|err|, [24] rcond
   const int md = prm->max_diis;
   if (md > 1) {
-    QK_TRY(qk_wst(ctx, W_QSDIIS, 2 * N2 * md, &hist));
-    QK_CK(cudaMemsetAsync(hist, 0, 2 * N2 * md * sizeof(double), ctx->stream));
+    QK_TRY(qk_wst(ctx, W_QSDIIS, 2 * B2 * md, &hist));
+    QK_CK(cudaMemsetAsync(hist, 0, 2 * B2 * md * sizeof(double), ctx->stream));
   }
   QK_CK(cudaMemsetAsync(sm, 0, 64 * sizeof(double), ctx->stream));
   if (out.eGW != in.eHF)
     QK_CK(cudaMemcpyAsync(out.eGW, in.eHF, N1 * 8, cudaMemcpyDeviceToDevice, ctx->stream));
   if (out.c != in.cHF)
-    QK_CK(cudaMemcpyAsync(out.c, in.cHF, N2 * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    QK_CK(cudaMemcpyAsync(out.c, in.cHF, B1 * N1 * 8, cudaMemcpyDeviceToDevice, ctx->stream));
   if (out.P != in.PHF)
-    QK_CK(cudaMemcpyAsync(out.P, in.PHF, N2 * 8, cudaMemcpyDeviceToDevice, ctx->stream));
-  auto gemm = [&](char ta, char tb, int k, double alpha, const double* A, const double* B,
-                  double beta, double* C) {
-    return qk_dgemm(ctx, ta, tb, N, N, k, alpha, A, N, 0, B, N, 0, beta, C, N, 0, 1);
+    QK_CK(cudaMemcpyAsync(out.P, in.PHF, B2 * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  auto gemm = [&](char ta, char tb, int m, int n, int k, double alpha, const double* A, int lda,
+                  const double* Bm, int ldb, double beta, double* C, int ldc) {
+    return qk_dgemm(ctx, ta, tb, m, n, k, alpha, A, lda, 0, Bm, ldb, 0, beta, C, ldc, 0, 1);
   };
   int nSCF = -1, n_diis = 0;
   double Conv = 1.0, hs[32] = {0.0};
   while (Conv > prm->thresh && nSCF < prm->maxSCF) {  // qsRGW.f90:193
     ++nSCF;
-    QK_TRY(qk_qs_jk(ctx, N, in.ERI, out.P, part, J, K));                             // :201-202
-    QK_TRY(qk_qs_mo_slab(ctx, N, d.nC, d.nO, d.nR, out.c, in.ERI, W1, W2, slab, Kmat));  // :210
+    QK_TRY(qk_qs_jk(ctx, B, in.ERI, out.P, part, J, K));                             // :201-202
+    QK_TRY(qk_qs_mo_slab(ctx, B, N, d.nC, d.nO, d.nR, out.c, in.ERI, W1, W2, slab,
+                         Kmat));                                                     // :210
     QK_TRY(casida_dev(ctx, d, out.eGW, nullptr, Om, XpY, nullptr, sm, 1, Kmat,
                       prm->precision));                                              // :214-217
     QK_TRY(rho_gemm(ctx, prm->precision, N, nS, slab, XpY, rho));                    // :220
@@ -1168,32 +1173,45 @@ int qsgw_dev(qk_ctx* ctx, const qk_gw_params* prm, const Dims& d, const QsIn& in
     QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, out.eGW, Om,
                          rho, sdiag, out.Z, sm + 8));                                // Z, EcGM
     QK_TRY(qk_qs_sym(ctx, N, d.nC, d.nR, Sraw, Smo));                                // :269
-    QK_TRY(gemm('N', 'N', N, 1.0, in.S, out.c, 0.0, SC));                            // :276
-    QK_TRY(gemm('N', 'N', N, 1.0, SC, Smo, 0.0, T1));
-    QK_TRY(gemm('N', 'T', N, 1.0, T1, SC, 0.0, SigCp));
-    QK_TRY(qk_qs_fock(ctx, N, in.Hc, J, K, SigCp, F));                               // :280
-    QK_TRY(gemm('N', 'N', N, 1.0, out.P, in.S, 0.0, PS));                            // :288
-    QK_TRY(gemm('N', 'N', N, 1.0, F, PS, 0.0, err));
-    QK_TRY(gemm('N', 'N', N, 1.0, in.S, out.P, 0.0, SP));
-    QK_TRY(gemm('N', 'N', N, -1.0, SP, F, 1.0, err));
-    QK_TRY(qk_qs_energy(ctx, N, out.P, in.T, in.V, J, K, err, sm + 16));             // :290-310
+    QK_TRY(gemm('N', 'N', B, N, B, 1.0, in.S, B, out.c, B, 0.0, SC, B));             // :276
+    QK_TRY(gemm('N', 'N', B, N, N, 1.0, SC, B, Smo, N, 0.0, T1, B));
+    QK_TRY(gemm('N', 'T', B, B, N, 1.0, T1, B, SC, B, 0.0, SigCp, B));
+    QK_TRY(qk_qs_fock(ctx, B, in.Hc, J, K, SigCp, F));                               // :280
+    if (proj) {                                                                      // :281-284
+      QK_TRY(gemm('N', 'N', B, N, B, 1.0, F, B, out.c, B, 0.0, T2, B));
+      QK_TRY(gemm('T', 'N', N, N, B, 1.0, out.c, B, T2, B, 0.0, Fp, N));
+      QK_TRY(gemm('N', 'N', B, N, N, 1.0, SC, B, Fp, N, 0.0, T1, B));
+      QK_TRY(gemm('N', 'T', B, B, N, 1.0, T1, B, SC, B, 0.0, F, B));
+    }
+    QK_TRY(gemm('N', 'N', B, B, B, 1.0, out.P, B, in.S, B, 0.0, PS, B));             // :288
+    QK_TRY(gemm('N', 'N', B, B, B, 1.0, F, B, PS, B, 0.0, err, B));
+    QK_TRY(gemm('N', 'N', B, B, B, 1.0, in.S, B, out.P, B, 0.0, SP, B));
+    QK_TRY(gemm('N', 'N', B, B, B, -1.0, SP, B, F, B, 1.0, err, B));
+    QK_TRY(qk_qs_energy(ctx, B, out.P, in.T, in.V, J, K, err, sm + 16));             // :290-310
     if (md > 1) {                                                                    // :314-319
       n_diis = n_diis + 1 < md ? n_diis + 1 : md;
-      QK_TRY(qk_diis_dev(ctx, (int)N2, (int)N2, n_diis, hist, hist + N2 * md, err, F, sm + 24));
+      QK_TRY(qk_diis_dev(ctx, (int)B2, (int)B2, n_diis, hist, hist + B2 * md, err, F, sm + 24));
     }
-    QK_TRY(gemm('N', 'N', N, 1.0, F, in.X, 0.0, T2));                                // :324
-    QK_TRY(gemm('T', 'N', N, 1.0, in.X, T2, 0.0, Fp));
-    QK_TRY(qk_eig_sym(ctx, N, Fp, N, out.eGW, Zt, 1, 1));                            // :326
-    QK_TRY(gemm('N', 'T', N, 1.0, in.X, Zt, 0.0, out.c));                            // :327
-    QK_TRY(qk_dgemm(ctx, 'N', 'T', N, N, d.nO, 2.0, out.c, N, 0, out.c, N, 0, 0.0, out.P, N, 0,
-                    1));                                                             // :339
+    if (!proj) {                                                                     // :323-327
+      QK_TRY(gemm('N', 'N', N, N, N, 1.0, F, N, in.X, N, 0.0, T2, N));
+      QK_TRY(gemm('T', 'N', N, N, N, 1.0, in.X, N, T2, N, 0.0, Fp, N));
+      QK_TRY(qk_eig_sym(ctx, N, Fp, N, out.eGW, Zt, 1, 1));
+      QK_TRY(gemm('N', 'T', N, N, N, 1.0, in.X, N, Zt, N, 0.0, out.c, N));
+    } else {                                                                         // :328-333
+      QK_TRY(gemm('N', 'N', B, N, B, 1.0, F, B, out.c, B, 0.0, T2, B));
+      QK_TRY(gemm('T', 'N', N, N, B, 1.0, out.c, B, T2, B, 0.0, Fp, N));
+      QK_TRY(qk_eig_sym(ctx, N, Fp, N, out.eGW, Zt, 1, 1));
+      QK_TRY(gemm('N', 'T', B, N, N, 1.0, out.c, B, Zt, N, 0.0, T1, B));
+      QK_CK(cudaMemcpyAsync(out.c, T1, B1 * N1 * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    QK_TRY(gemm('N', 'T', B, B, d.nO, 2.0, out.c, B, out.c, B, 0.0, out.P, B));      // :339
     QK_CK(cudaMemcpyAsync(hs, sm, 32 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     QK_CK(cudaStreamSynchronize(ctx->stream));
     if (nSCF > 1) Conv = hs[21];                                                     // :290
   }
   if (out.SigC) {                                                                    // :335
-    QK_TRY(gemm('N', 'N', N, 1.0, SigCp, out.c, 0.0, T1));
-    QK_TRY(gemm('T', 'N', N, 1.0, out.c, T1, 0.0, out.SigC));
+    QK_TRY(gemm('N', 'N', B, N, B, 1.0, SigCp, B, out.c, B, 0.0, T1, B));
+    QK_TRY(gemm('T', 'N', N, N, B, 1.0, out.c, B, T1, B, 0.0, out.SigC, N));
   }
   if (out.EqsGW) *out.EqsGW = hs[20];
   if (out.EcRPA) *out.EcRPA = hs[2];
@@ -1491,10 +1509,11 @@ int qk_qsRGW_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int n
       !d_eGW || !d_c || !d_P || !d_Z)
     return qk_fail(ctx, QK_ERR_ARG, "inputs and eGW, c, P, Z required");
   Dims d;
-  QK_TRY(check_dims(ctx, nBas, nOrb, nC, nO, nV, nR, nS, &d));
+  if (nBas < nOrb) return qk_fail(ctx, QK_ERR_ARG, "nBas (%d) < nOrb (%d)", nBas, nOrb);
+  QK_TRY(check_dims(ctx, nOrb, nOrb, nC, nO, nV, nR, nS, &d));
   const QsIn in{d_eHF, d_cHF, d_PHF, d_S, d_T, d_V, d_Hc, d_X, d_ERI_AO};
   const QsOut out{d_eGW, d_c, d_P, d_SigC, d_Z, EqsGW, EcRPA, EcGM, nSCF, Conv};
-  return end(ctx, qsgw_dev(ctx, prm, d, in, out));
+  return end(ctx, qsgw_dev(ctx, prm, nBas, d, in, out));
 }
 
 int qk_qsRGW(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, int nO, int nV,
@@ -1506,37 +1525,38 @@ int qk_qsRGW(qk_ctx* ctx, const qk_gw_params* prm, int nBas, int nOrb, int nC, i
   if (!prm || !eHF || !cHF || !PHF || !S || !T || !V || !Hc || !X || !ERI_AO || !eGW)
     return qk_fail(ctx, QK_ERR_ARG, "inputs and eGW required");
   Dims d;
-  QK_TRY(check_dims(ctx, nBas, nOrb, nC, nO, nV, nR, nS, &d));
-  const size_t N = nOrb, N2 = N * N, N4 = N2 * N2;
+  if (nBas < nOrb) return qk_fail(ctx, QK_ERR_ARG, "nBas (%d) < nOrb (%d)", nBas, nOrb);
+  QK_TRY(check_dims(ctx, nOrb, nOrb, nC, nO, nV, nR, nS, &d));
+  const size_t N = nOrb, N2 = N * N, Bn = nBas, B2 = Bn * Bn, B4 = B2 * B2;
   double *dERI, *io;
-  QK_TRY(qk_wst(ctx, W_ERI, N4, &dERI));
-  QK_TRY(qk_wst(ctx, W_QSIN, 8 * N2 + 2 * N + 16, &io));
+  QK_TRY(qk_wst(ctx, W_ERI, B4, &dERI));
+  QK_TRY(qk_wst(ctx, W_QSIN, 8 * B2 + 2 * N + 16, &io));
   double* dS = io;
-  double* dT = dS + N2;
-  double* dV = dT + N2;
-  double* dHc = dV + N2;
-  double* dX = dHc + N2;
-  double* dc = dX + N2;
-  double* dP = dc + N2;
-  double* dSig = dP + N2;
-  double* de = dSig + N2;
+  double* dT = dS + B2;
+  double* dV = dT + B2;
+  double* dHc = dV + B2;
+  double* dX = dHc + B2;     // nBas x nOrb
+  double* dc = dX + B2;      // nBas x nOrb
+  double* dP = dc + B2;
+  double* dSig = dP + B2;    // nOrb x nOrb
+  double* de = dSig + B2;
   double* dZ = de + N;
-  QK_TRY(h2d(ctx, dERI, ERI_AO, N4 * 8));
-  QK_TRY(h2d(ctx, dS, S, N2 * 8));
-  QK_TRY(h2d(ctx, dT, T, N2 * 8));
-  QK_TRY(h2d(ctx, dV, V, N2 * 8));
-  QK_TRY(h2d(ctx, dHc, Hc, N2 * 8));
-  QK_TRY(h2d(ctx, dX, X, N2 * 8));
-  QK_TRY(h2d(ctx, dc, cHF, N2 * 8));
-  QK_TRY(h2d(ctx, dP, PHF, N2 * 8));
+  QK_TRY(h2d(ctx, dERI, ERI_AO, B4 * 8));
+  QK_TRY(h2d(ctx, dS, S, B2 * 8));
+  QK_TRY(h2d(ctx, dT, T, B2 * 8));
+  QK_TRY(h2d(ctx, dV, V, B2 * 8));
+  QK_TRY(h2d(ctx, dHc, Hc, B2 * 8));
+  QK_TRY(h2d(ctx, dX, X, Bn * N * 8));
+  QK_TRY(h2d(ctx, dc, cHF, Bn * N * 8));
+  QK_TRY(h2d(ctx, dP, PHF, B2 * 8));
   QK_TRY(h2d(ctx, de, eHF, N * 8));
   const QsIn in{de, dc, dP, dS, dT, dV, dHc, dX, dERI};
   const QsOut out{de, dc, dP, SigC ? dSig : nullptr, dZ, EqsGW, EcRPA, EcGM, nSCF, Conv};
-  const int st = qsgw_dev(ctx, prm, d, in, out);
+  const int st = qsgw_dev(ctx, prm, nBas, d, in, out);
   if (st != QK_OK && st != QK_ERR_NO_CONV) return end(ctx, st);
   QK_TRY(d2h(ctx, eGW, de, N * 8));
-  if (c) QK_TRY(d2h(ctx, c, dc, N2 * 8));
-  if (P) QK_TRY(d2h(ctx, P, dP, N2 * 8));
+  if (c) QK_TRY(d2h(ctx, c, dc, Bn * N * 8));
+  if (P) QK_TRY(d2h(ctx, P, dP, B2 * 8));
   if (SigC) QK_TRY(d2h(ctx, SigC, dSig, N2 * 8));
   if (Z) QK_TRY(d2h(ctx, Z, dZ, N * 8));
   QK_CK(cudaStreamSynchronize(ctx->stream));

@@ -147,11 +147,16 @@ def hchain_integrals(n_atoms: int, spacing: float = 1.6, exponents=HCHAIN_EXPONE
     return S, T, V, ERI, float(ENuc)
 
 
-def rhf_start(S, Hc, ERI, nO, maxit=500, tol=1e-10):
+def rhf_start(S, Hc, ERI, nO, maxit=500, tol=1e-10, n_drop=0):
     """Closed-shell RHF with DIIS on F (commutator error), the qsGW starting point.
-    Returns (E_elec, eps, C, P, X) with X = S^-1/2 (symmetric orthogonalisation)."""
+    Returns (E_elec, eps, C, P, X) with X = S^-1/2 (symmetric orthogonalisation), or, with
+    n_drop > 0, the canonical orthogonalisation X = U s^-1/2 without the n_drop eigenvectors of
+    the smallest overlap eigenvalues (nOrb = nBas - n_drop)."""
     s, U = np.linalg.eigh(S)
-    X = (U * s ** -0.5) @ U.T
+    if n_drop > 0:
+        X = U[:, n_drop:] * s[n_drop:] ** -0.5
+    else:
+        X = (U * s ** -0.5) @ U.T
     F = Hc.copy()
     P = np.zeros_like(S)
     hist_F, hist_e = [], []
@@ -186,13 +191,15 @@ def rhf_start(S, Hc, ERI, nO, maxit=500, tol=1e-10):
     return E, eps, C, P, X
 
 
-def hchain_system(n_atoms: int, spacing: float = 1.6, exponents=HCHAIN_EXPONENTS) -> dict:
-    """Everything qsRGW reads for an H chain: dict(nBas, nO, S, T, V, Hc, X, ERI_AO, ENuc, ERHF,
-    eHF, cHF, PHF).  n_atoms must be even (closed shell)."""
+def hchain_system(n_atoms: int, spacing: float = 1.6, exponents=HCHAIN_EXPONENTS,
+                  n_drop: int = 0) -> dict:
+    """Everything qsRGW reads for an H chain: dict(nBas, nOrb, nO, S, T, V, Hc, X, ERI_AO, ENuc,
+    ERHF, eHF, cHF, PHF).  n_atoms must be even (closed shell); n_drop > 0 removes that many
+    near-linearly-dependent combinations (nOrb = nBas - n_drop)."""
     assert n_atoms % 2 == 0
     S, T, V, ERI, ENuc = hchain_integrals(n_atoms, spacing, exponents)
     Hc = T + V
     nO = n_atoms // 2
-    E, eps, C, P, X = rhf_start(S, Hc, ERI, nO)
-    return dict(nBas=S.shape[0], nO=nO, S=S, T=T, V=V, Hc=Hc, X=X, ERI_AO=ERI, ENuc=ENuc,
-                ERHF=E, eHF=eps, cHF=C, PHF=P)
+    E, eps, C, P, X = rhf_start(S, Hc, ERI, nO, n_drop=n_drop)
+    return dict(nBas=S.shape[0], nOrb=X.shape[1], nO=nO, S=S, T=T, V=V, Hc=Hc, X=X, ERI_AO=ERI,
+                ENuc=ENuc, ERHF=E, eHF=eps, cHF=C, PHF=P)

@@ -2,7 +2,8 @@
 He/6-31G and linear H chains in s-Gaussian bases (real AO integrals, non-orthogonal basis),
 converged runs with and without DIIS, a fixed number of cycles of a run that does not converge
 (the reference stops there), Tamm-Dancoff screening, the SRG-regularised self-energy, a frozen
-core and virtual, the device-pointer entry, and the mixed precision tier.
+core and virtual, fewer orbitals than basis functions, the device-pointer entry, and the mixed
+precision tier.
 
 Orbital coefficients are defined up to a sign per column, so the comparisons use the quantities
 that do not depend on it: energies, eGW, the density matrix P and the diagonal of SigC."""
@@ -29,18 +30,19 @@ def _he():
 _CACHE = {}
 
 
-def _chain(n_atoms, spacing=1.6):
-    key = (n_atoms, spacing)
+def _chain(n_atoms, spacing=1.6, n_drop=0):
+    key = (n_atoms, spacing, n_drop)
     if key not in _CACHE:
-        _CACHE[key] = synth.hchain_system(n_atoms, spacing)
+        _CACHE[key] = synth.hchain_system(n_atoms, spacing, n_drop=n_drop)
     return _CACHE[key]
 
 
 def _run_both(ctx, sy, maxSCF=64, thresh=1e-5, max_diis=5, eta=0.05, TDA_W=False, doSRG=False,
               nC=0, nR=0, precision=api.QK_PREC_FP64, raise_on_fail=True):
-    n, nO = sy["nBas"], sy["nO"]
+    nb, nO = sy["nBas"], sy["nO"]
+    n = sy.get("nOrb", nb)
     nS = (nO - nC) * (n - nO - nR)
-    args = (n, n, nC, nO, n - nO, nR, nS, sy["eHF"], sy["cHF"], sy["PHF"], sy["S"], sy["T"],
+    args = (nb, n, nC, nO, n - nO, nR, nS, sy["eHF"], sy["cHF"], sy["PHF"], sy["S"], sy["T"],
             sy["V"], sy["Hc"], sy["X"], sy["ERI_AO"])
     ref = O.qsRGW(maxSCF, thresh, max_diis, eta, TDA_W, *args, raise_on_fail=raise_on_fail,
                   doSRG=doSRG)
@@ -92,6 +94,17 @@ def test_qsgw_tda_w_and_srg(ctx):
 
 def test_qsgw_frozen_core_and_virtual(ctx):
     ref, got = _run_both(ctx, _chain(6), eta=0.05, nC=1, nR=2)
+    _compare(ref, got, 1e-8)
+
+
+@pytest.mark.parametrize("n_atoms,n_drop", [(6, 1), (8, 3)])
+def test_qsgw_fewer_orbitals_than_basis_functions(ctx, n_atoms, n_drop):
+    """nOrb < nBas (canonical orthogonalisation without the smallest overlap eigenvalues): F is
+    projected through c and Fp = c^T F c (qsRGW.f90:281-284, 328-333)."""
+    sy = _chain(n_atoms, n_drop=n_drop)
+    assert sy["nOrb"] == sy["nBas"] - n_drop
+    ref, got = _run_both(ctx, sy, eta=0.05)
+    assert not ref["failed"]
     _compare(ref, got, 1e-8)
 
 
