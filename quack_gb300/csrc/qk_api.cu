@@ -1111,10 +1111,6 @@ int qsgw_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, const Dims& d, cons
   TdaScope tda(ctx, prm->TDA_W != 0);
   const int N = d.N, nS = d.nS, B = nBas;
   const bool proj = B != N;  // the reference's nBas /= nOrb branch (qsRGW.f90:281-284,328-333)
-  // mixed tier: the quarter transforms and the full-Sigma GEMM take FP32 products with
-  // compensated sums; ρ is BF16x3 and the eigenvectors are back-transformed with FP32 products
-  // as in G0W0; the eigenvalues, the N x N algebra and the DIIS stay FP64
-  const int mixed = prm->precision == QK_PREC_BF16X3;
   const double flow = 500.0;
   const size_t N1 = N, N2 = N1 * N1, B1 = B, B2 = B1 * B1, B3 = B2 * B1;
   const size_t rw = B3 * d.no > N2 * nS ? B3 * d.no : N2 * nS;
@@ -1167,13 +1163,13 @@ int qsgw_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, const Dims& d, cons
   while (Conv > prm->thresh && nSCF < prm->maxSCF) {  // qsRGW.f90:193
     ++nSCF;
     QK_TRY(qk_qs_jk(ctx, B, in.ERI, out.P, part, J, K));                             // :201-202
-    QK_TRY(qk_qs_mo_slab(ctx, B, N, d.nC, d.nO, d.nR, out.c, in.ERI, W1, W2, slab, Kmat,
-                         mixed));                                                    // :210
+    QK_TRY(qk_qs_mo_slab(ctx, B, N, d.nC, d.nO, d.nR, out.c, in.ERI, W1, W2, slab,
+                         Kmat));                                                     // :210
     QK_TRY(casida_dev(ctx, d, out.eGW, nullptr, Om, XpY, nullptr, sm, 1, Kmat,
                       prm->precision));                                              // :214-217
     QK_TRY(rho_gemm(ctx, prm->precision, N, nS, slab, XpY, rho));                    // :220
     QK_TRY(qk_qs_sigma(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, out.eGW, Om,
-                       rho, W1, Sraw, mixed));                                       // :255-264
+                       rho, W1, Sraw));                                              // :255-264
     QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, out.eGW, Om,
                          rho, sdiag, out.Z, sm + 8));                                // Z, EcGM
     QK_TRY(qk_qs_sym(ctx, N, d.nC, d.nR, Sraw, Smo));                                // :269

@@ -178,16 +178,14 @@ int phrlr_dev(qk_ctx* ctx, int TDA, int nS, double* dA, double* dB, double* dOm,
 //   J = Hartree, K = exchange matrix of P over the AO tensor (N = nBas; part: 2 N^3 scratch);
 //   slab / Kmat from the partial MO transform with c (nBas x N; W1, W2: max(nBas^3 no, N^2 nS));
 //   Sig = full correlation self-energy (unsymmetrised, W: N^2 nS scratch);
-//   fp32: the GEMMs take FP32 products with compensated sums (mixed tier);
 //   out[0..5] = ET, EV, EJ, EK, EqsGW, max|err|.
 int qk_qs_jk(qk_ctx* ctx, int N, const double* ERI, const double* P, double* part, double* J,
              double* K);
 int qk_qs_mo_slab(qk_ctx* ctx, int nBas, int N, int nC, int nO, int nR, const double* c,
-                  const double* ERI, double* W1, double* W2, double* slab, double* Kmat,
-                  int fp32);
+                  const double* ERI, double* W1, double* W2, double* slab, double* Kmat);
 int qk_qs_sigma(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                 int nS, const double* e, const double* Om, const double* rho, double* W,
-                double* Sig, int fp32);
+                double* Sig);
 int qk_qs_sym(qk_ctx* ctx, int N, int nC, int nR, const double* Sig, double* out);
 int qk_qs_fock(qk_ctx* ctx, int N, const double* Hc, const double* J, const double* K,
                const double* SigCp, double* F);
