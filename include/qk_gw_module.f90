@@ -137,6 +137,34 @@ module qk_gw_module
       integer(c_int), intent(out)   :: nSCF
     end function qk_evRGW
 
+    integer(c_int) function qk_RGW_self_energy(ctx, eta, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, &
+        rho, EcGM, SigC, Z) bind(C, name="qk_RGW_self_energy")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      real(c_double), value         :: eta
+      integer(c_int), value         :: nBas, nOrb, nC, nO, nV, nR, nS
+      real(c_double), intent(in)    :: e(nOrb), Om(nS), rho(nOrb,nOrb,nS)
+      real(c_double), intent(out)   :: EcGM, SigC(nOrb,nOrb), Z(nOrb)
+    end function qk_RGW_self_energy
+
+    integer(c_int) function qk_Hartree_matrix_AO_basis(ctx, nBas, P, ERI, H) &
+        bind(C, name="qk_Hartree_matrix_AO_basis")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      integer(c_int), value         :: nBas
+      real(c_double), intent(in)    :: P(nBas,nBas), ERI(nBas,nBas,nBas,nBas)
+      real(c_double), intent(out)   :: H(nBas,nBas)
+    end function qk_Hartree_matrix_AO_basis
+
+    integer(c_int) function qk_exchange_matrix_AO_basis(ctx, nBas, P, ERI, K) &
+        bind(C, name="qk_exchange_matrix_AO_basis")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      integer(c_int), value         :: nBas
+      real(c_double), intent(in)    :: P(nBas,nBas), ERI(nBas,nBas,nBas,nBas)
+      real(c_double), intent(out)   :: K(nBas,nBas)
+    end function qk_exchange_matrix_AO_basis
+
     integer(c_int) function qk_qsRGW(ctx, prm, nBas, nOrb, nC, nO, nV, nR, nS, eHF, cHF, PHF, S, T, &
         V, Hc, X, ERI_AO, eGW, c, P, SigC, Z, EqsGW, EcRPA, EcGM, nSCF, Conv) bind(C, name="qk_qsRGW")
       import c_int, c_ptr, c_double, qk_gw_params

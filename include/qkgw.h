@@ -113,6 +113,20 @@ int qk_RGW_self_energy_diag(qk_ctx* ctx, double eta, int nBas, int nOrb, int nC,
                             int nR, int nS, const double* e, const double* Om, const double* rho,
                             double* EcGM, double* Sig, double* Z);
 /* GW/RGW_SRG_self_energy_diag.f90:1-160 */
+/* GW/RGW_self_energy.f90:1-161 and GW/RGW_SRG_self_energy.f90:1-170: the full (unsymmetrised)
+ * correlation self-energy SigC(nOrb,nOrb) (zero outside the active block), Z and EcGM.  FP64. */
+int qk_RGW_self_energy(qk_ctx* ctx, double eta, int nBas, int nOrb, int nC, int nO, int nV,
+                       int nR, int nS, const double* e, const double* Om, const double* rho,
+                       double* EcGM, double* SigC, double* Z);
+int qk_RGW_SRG_self_energy(qk_ctx* ctx, double flow, int nBas, int nOrb, int nC, int nO, int nV,
+                           int nR, int nS, const double* e, const double* Om, const double* rho,
+                           double* EcGM, double* SigC, double* Z);
+/* AOtoMO/Hartree_matrix_AO_basis.f90:1-34 and AOtoMO/exchange_matrix_AO_basis.f90:1-34:
+ * H(mu,nu) = sum P(la,si) ERI(mu,la,nu,si), K(mu,nu) = -sum P(la,si) ERI(mu,la,si,nu). */
+int qk_Hartree_matrix_AO_basis(qk_ctx* ctx, int nBas, const double* P, const double* ERI,
+                               double* H);
+int qk_exchange_matrix_AO_basis(qk_ctx* ctx, int nBas, const double* P, const double* ERI,
+                                double* K);
 int qk_RGW_SRG_self_energy_diag(qk_ctx* ctx, double flow, int nBas, int nOrb, int nC, int nO,
                                 int nV, int nR, int nS, const double* e, const double* Om,
                                 const double* rho, double* EcGM, double* SigC, double* Z);

@@ -234,6 +234,41 @@ def RGW_self_energy_diag(eta, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho, ctx=No
     return gm.value, Sig, Z
 
 
+def RGW_self_energy(eta, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho, ctx=None, srg_flow=None):
+    """GW/RGW_self_energy.f90 (or, with srg_flow, GW/RGW_SRG_self_energy.f90): the full
+    unsymmetrised SigC(nOrb, nOrb).  Returns (EcGM, SigC, Z)."""
+    c = _ctx(ctx)
+    e, Om, rho = _f(e), _f(Om), _f(rho)
+    Sig = np.empty((nOrb, nOrb), order="F")
+    Z = np.empty(nOrb)
+    gm = C.c_double()
+    if srg_flow is None:
+        fn, x = lib().qk_RGW_self_energy, eta
+    else:
+        fn, x = lib().qk_RGW_SRG_self_energy, srg_flow
+    c.check(fn(c.handle, C.c_double(x), nBas, nOrb, nC, nO, nV, nR, nS, _ptr(e), _ptr(Om),
+               _ptr(rho), C.byref(gm), _ptr(Sig), _ptr(Z)))
+    return gm.value, Sig, Z
+
+
+def Hartree_matrix_AO_basis(nBas, P, ERI, ctx=None):
+    """AOtoMO/Hartree_matrix_AO_basis.f90.  Returns H(nBas, nBas)."""
+    c = _ctx(ctx)
+    P, ERI = _f(P), _f(ERI)
+    H = np.empty((nBas, nBas), order="F")
+    c.check(lib().qk_Hartree_matrix_AO_basis(c.handle, nBas, _ptr(P), _ptr(ERI), _ptr(H)))
+    return H
+
+
+def exchange_matrix_AO_basis(nBas, P, ERI, ctx=None):
+    """AOtoMO/exchange_matrix_AO_basis.f90.  Returns K(nBas, nBas)."""
+    c = _ctx(ctx)
+    P, ERI = _f(P), _f(ERI)
+    K = np.empty((nBas, nBas), order="F")
+    c.check(lib().qk_exchange_matrix_AO_basis(c.handle, nBas, _ptr(P), _ptr(ERI), _ptr(K)))
+    return K
+
+
 def RGW_SRG_self_energy_diag(flow, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, rho, ctx=None):
     """GW/RGW_SRG_self_energy_diag.f90.  Returns (EcGM, SigC, Z)."""
     c = _ctx(ctx)

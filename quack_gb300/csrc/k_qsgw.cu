@@ -146,6 +146,17 @@ __global__ void k_qs_sym(int N, int nC, int nR, const double* __restrict__ Sig,
   }
 }
 
+// zero the rows and columns of inactive orbitals in place (RGW_self_energy.f90:38-84 fills the
+// active block only)
+__global__ void k_qs_mask(int N, int nC, int nR, double* __restrict__ Sig) {
+  const long long N1 = N, total = N1 * N1;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int p = (int)(idx % N1), q = (int)(idx / N1);
+    if (!(p >= nC && p < N - nR && q >= nC && q < N - nR)) Sig[idx] = 0.0;
+  }
+}
+
 // SRG-regularised full self-energy (RGW_SRG_self_energy.f90:40-80), tiled over (p,q):
 //   Sig(p,q) = sum_(x,m) 2 rho(p,x,m) rho(q,x,m) (1 - g_p g_q) (D_p + D_q)/(D_p^2 + D_q^2),
 //   D_p = e_p - e_x +- Om_m, g_p = exp(-s D_p^2).
@@ -319,6 +330,12 @@ int qk_qs_sigma(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, 
 
 int qk_qs_sym(qk_ctx* ctx, int N, int nC, int nR, const double* Sig, double* out) {
   k_qs_sym<<<grid_1d(ctx, (long long)N * N), 256, 0, ctx->stream>>>(N, nC, nR, Sig, out);
+  QK_LAUNCHED();
+  return QK_OK;
+}
+
+int qk_qs_mask(qk_ctx* ctx, int N, int nC, int nR, double* Sig) {
+  k_qs_mask<<<grid_1d(ctx, (long long)N * N), 256, 0, ctx->stream>>>(N, nC, nR, Sig);
   QK_LAUNCHED();
   return QK_OK;
 }

@@ -1009,6 +1009,59 @@ static int sigma_stage(qk_ctx* ctx, int doSRG, double eta, double flow, int nBas
   return end(ctx, QK_OK);
 }
 
+// full (N x N) correlation self-energy, Z and EcGM (RGW_self_energy.f90 / RGW_SRG_self_energy.f90)
+static int sigma_full_stage(qk_ctx* ctx, int doSRG, double eta, double flow, int nOrb, int nC,
+                            int nO, int nR, int nS, const double* e, const double* Om,
+                            const double* rho, double* EcGM, double* Sig, double* Z) {
+  QK_TRY(begin(ctx));
+  const int no = nO - nC, nv = nOrb - nO - nR;
+  if (no <= 0 || nv <= 0 || (long long)no * nv != nS) return qk_fail(ctx, QK_ERR_ARG, "bad sizes");
+  const size_t N = nOrb, N2 = N * N, N2S = N2 * nS;
+  double *dR, *W, *sm;
+  QK_TRY(qk_wst(ctx, W_RHO, N2S, &dR));
+  QK_TRY(qk_wst(ctx, W_QSR1, N2S, &W));
+  QK_TRY(qk_wst(ctx, W_HOST_A, N2 + 3 * N + nS + 16, &sm));
+  double* dSig = sm;
+  double* de = sm + N2;
+  double* dd = de + N;
+  double* dZ = dd + N;
+  double* dOm = dZ + N;
+  double* dGM = dOm + nS;
+  QK_TRY(h2d(ctx, dR, rho, N2S * 8));
+  QK_TRY(h2d(ctx, de, e, N * 8));
+  QK_TRY(h2d(ctx, dOm, Om, nS * 8));
+  QK_TRY(qk_qs_sigma(ctx, doSRG, eta, flow, nOrb, nC, nO, nR, nS, de, dOm, dR, W, dSig));
+  QK_TRY(qk_qs_mask(ctx, nOrb, nC, nR, dSig));
+  QK_TRY(qk_sigma_diag(ctx, doSRG, eta, flow, nOrb, nC, nO, nR, nS, de, dOm, dR, dd, dZ, dGM));
+  QK_TRY(d2h(ctx, Sig, dSig, N2 * 8));
+  QK_TRY(d2h(ctx, Z, dZ, N * 8));
+  QK_TRY(d2h(ctx, EcGM, dGM, 8));
+  QK_CK(cudaStreamSynchronize(ctx->stream));
+  return end(ctx, QK_OK);
+}
+
+// J or K of a density in the AO basis (one pass over the tensor computes both)
+static int jk_stage(qk_ctx* ctx, int nBas, const double* P, const double* ERI, double* J,
+                    double* K) {
+  QK_TRY(begin(ctx));
+  if (nBas <= 0) return qk_fail(ctx, QK_ERR_ARG, "bad sizes");
+  const size_t B = nBas, B2 = B * B, B3 = B2 * B, B4 = B2 * B2;
+  double *dE, *part, *sm;
+  QK_TRY(qk_wst(ctx, W_ERI, B4, &dE));
+  QK_TRY(qk_wst(ctx, W_QSJK, 2 * B3, &part));
+  QK_TRY(qk_wst(ctx, W_HOST_A, 3 * B2 + 16, &sm));
+  double* dP = sm;
+  double* dJ = sm + B2;
+  double* dK = dJ + B2;
+  QK_TRY(h2d(ctx, dE, ERI, B4 * 8));
+  QK_TRY(h2d(ctx, dP, P, B2 * 8));
+  QK_TRY(qk_qs_jk(ctx, nBas, dE, dP, part, dJ, dK));
+  if (J) QK_TRY(d2h(ctx, J, dJ, B2 * 8));
+  if (K) QK_TRY(d2h(ctx, K, dK, B2 * 8));
+  QK_CK(cudaStreamSynchronize(ctx->stream));
+  return end(ctx, QK_OK);
+}
+
 int qk_set_stage_precision(qk_ctx* ctx, int precision) {
   if (!ctx || (precision != QK_PREC_FP64 && precision != QK_PREC_BF16X3)) return QK_ERR_ARG;
   ctx->stage_precision = precision;
@@ -1020,6 +1073,30 @@ int qk_RGW_self_energy_diag(qk_ctx* ctx, double eta, int nBas, int nOrb, int nC,
                             double* EcGM, double* Sig, double* Z) {
   (void)nOrb; (void)nV;
   return sigma_stage(ctx, 0, eta, 500.0, nBas, nC, nO, nR, nS, e, Om, rho, EcGM, Sig, Z);
+}
+
+int qk_RGW_self_energy(qk_ctx* ctx, double eta, int nBas, int nOrb, int nC, int nO, int nV,
+                       int nR, int nS, const double* e, const double* Om, const double* rho,
+                       double* EcGM, double* SigC, double* Z) {
+  (void)nBas; (void)nV;
+  return sigma_full_stage(ctx, 0, eta, 500.0, nOrb, nC, nO, nR, nS, e, Om, rho, EcGM, SigC, Z);
+}
+
+int qk_RGW_SRG_self_energy(qk_ctx* ctx, double flow, int nBas, int nOrb, int nC, int nO, int nV,
+                           int nR, int nS, const double* e, const double* Om, const double* rho,
+                           double* EcGM, double* SigC, double* Z) {
+  (void)nBas; (void)nV;
+  return sigma_full_stage(ctx, 1, 0.0, flow, nOrb, nC, nO, nR, nS, e, Om, rho, EcGM, SigC, Z);
+}
+
+int qk_Hartree_matrix_AO_basis(qk_ctx* ctx, int nBas, const double* P, const double* ERI,
+                               double* H) {
+  return jk_stage(ctx, nBas, P, ERI, H, nullptr);
+}
+
+int qk_exchange_matrix_AO_basis(qk_ctx* ctx, int nBas, const double* P, const double* ERI,
+                                double* K) {
+  return jk_stage(ctx, nBas, P, ERI, nullptr, K);
 }
 
 int qk_RGW_SRG_self_energy_diag(qk_ctx* ctx, double flow, int nBas, int nOrb, int nC, int nO,

@@ -187,6 +187,7 @@ int qk_qs_sigma(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, 
                 int nS, const double* e, const double* Om, const double* rho, double* W,
                 double* Sig);
 int qk_qs_sym(qk_ctx* ctx, int N, int nC, int nR, const double* Sig, double* out);
+int qk_qs_mask(qk_ctx* ctx, int N, int nC, int nR, double* Sig);
 int qk_qs_fock(qk_ctx* ctx, int N, const double* Hc, const double* J, const double* K,
                const double* SigCp, double* F);
 int qk_qs_energy(qk_ctx* ctx, int N, const double* P, const double* T, const double* V,

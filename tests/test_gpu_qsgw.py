@@ -139,3 +139,39 @@ def test_qsgw_mixed_tier_within_1meV(ctx):
     assert not got["failed"]
     assert np.max(np.abs(got["eGW"] - ref["eGW"])) < 3.6749e-5   # 1 meV
     assert abs(got["EqsGW"] - ref["EqsGW"]) < 3.6749e-5
+
+
+@pytest.mark.parametrize("srg", [False, True])
+def test_full_self_energy_stage(ctx, srg):
+    """Stage-level drop-in of RGW_self_energy / RGW_SRG_self_energy (unsymmetrised SigC)."""
+    rng = np.random.default_rng(11)
+    N, nO, nC, nR = 14, 4, 1, 2
+    nS = (nO - nC) * (N - nO - nR)
+    e = np.sort(rng.uniform(-3.0, 2.0, N))
+    Om = np.sort(rng.uniform(0.2, 4.0, nS))
+    rho = rng.standard_normal((N, N, nS)) * 0.3
+    if srg:
+        ref = O.RGW_SRG_self_energy(500.0, N, N, nC, nO, N - nO, nR, nS, e, Om, rho)
+        got = api.RGW_self_energy(0.0, N, N, nC, nO, N - nO, nR, nS, e, Om, rho, ctx=ctx,
+                                  srg_flow=500.0)
+    else:
+        ref = O.RGW_self_energy(0.02, N, N, nC, nO, N - nO, nR, nS, e, Om, rho)
+        got = api.RGW_self_energy(0.02, N, N, nC, nO, N - nO, nR, nS, e, Om, rho, ctx=ctx)
+    scale = max(1.0, np.max(np.abs(ref[1])))
+    assert np.max(np.abs(got[1] - ref[1])) < 1e-11 * scale
+    assert np.max(np.abs(got[2] - ref[2])) < 1e-11
+    assert abs(got[0] - ref[0]) < 1e-11 * max(1.0, abs(ref[0]))
+
+
+def test_hartree_exchange_stage(ctx):
+    """Hartree_matrix_AO_basis / exchange_matrix_AO_basis on an H-chain density and on a
+    tensor without any permutational symmetry (the kernel reads the indices as written)."""
+    sy = _chain(4)
+    n = sy["nBas"]
+    for E, P in ((sy["ERI_AO"], sy["PHF"]),
+                 (np.random.default_rng(5).standard_normal((n,) * 4),
+                  np.random.default_rng(6).standard_normal((n, n)))):
+        H = api.Hartree_matrix_AO_basis(n, P, E, ctx=ctx)
+        K = api.exchange_matrix_AO_basis(n, P, E, ctx=ctx)
+        assert np.max(np.abs(H - O.Hartree_matrix_AO_basis(n, P, E))) < 1e-12 * max(1, np.abs(H).max())
+        assert np.max(np.abs(K - O.exchange_matrix_AO_basis(n, P, E))) < 1e-12 * max(1, np.abs(K).max())
