@@ -359,13 +359,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 // P[p*rows_pad*Kpad + r*Kpad + k], zero padded to rows_pad x Kpad.  X(r, k) = X[r + ld*k]
 // (trans = 0, read through a shared-memory transpose) or X[k + ld*r] (trans = 1, read along k
 // directly); kscale (optional) multiplies X(r, k) by kscale[k] first.
+// The split runs in FP32 after one exact-enough FP64 step: x = h + l with h = fl32(x) and
+// l = fl32(x - h) (48 bits of x, four FP64-pipe operations), then x0 = bf16(h), the remainder
+// r1 = (h - x0) + l (h - x0 is exact in FP32; the addition rounds at 2^-24 |r1| <= 2^-32 |x|),
+// x1 = bf16(r1), r2 = r1 - x1 (exact), x2 = bf16(r2): |x - x0 - x1 - x2| <= ~2^-24 |x|, the
+// accuracy of a three-way BF16 split, at a third of the FP64 work of splitting in FP64 (the
+// kernel is FP64-issue-bound otherwise).
 __device__ __forceinline__ void split_store(double x, __nv_bfloat16* __restrict__ P, size_t o,
                                             size_t plane) {
-  const __nv_bfloat16 x0 = __double2bfloat16(x);
-  const double r1 = x - (double)__bfloat162float(x0);
-  const __nv_bfloat16 x1 = __double2bfloat16(r1);
-  const double r2 = r1 - (double)__bfloat162float(x1);
-  const __nv_bfloat16 x2 = __double2bfloat16(r2);
+  const float h = __double2float_rn(x);
+  const float l = __double2float_rn(x - (double)h);
+  const __nv_bfloat16 x0 = __float2bfloat16_rn(h);
+  const float r1 = (h - __bfloat162float(x0)) + l;
+  const __nv_bfloat16 x1 = __float2bfloat16_rn(r1);
+  const float r2 = r1 - __bfloat162float(x1);
+  const __nv_bfloat16 x2 = __float2bfloat16_rn(r2);
   P[o] = x0;
   P[o + plane] = x1;
   P[o + 2 * plane] = x2;
