@@ -175,3 +175,26 @@ def test_hartree_exchange_stage(ctx):
         K = api.exchange_matrix_AO_basis(n, P, E, ctx=ctx)
         assert np.max(np.abs(H - O.Hartree_matrix_AO_basis(n, P, E))) < 1e-12 * max(1, np.abs(H).max())
         assert np.max(np.abs(K - O.exchange_matrix_AO_basis(n, P, E))) < 1e-12 * max(1, np.abs(K).max())
+
+
+def test_qsgw_argument_errors_and_single_cycle(ctx):
+    """max_diis above the DIIS kernel's 32, nBas < nOrb and negative maxSCF are refused; maxSCF = 0
+    runs exactly one cycle and, as in the reference (nSCF == maxSCF), reports no convergence."""
+    sy = _chain(4)
+    n, nO = sy["nBas"], sy["nO"]
+    args = (n, n, 0, nO, n - nO, 0, nO * (n - nO), sy["eHF"], sy["cHF"], sy["PHF"], sy["S"],
+            sy["T"], sy["V"], sy["Hc"], sy["X"], sy["ERI_AO"])
+    for opts in (api.GWOptions(max_diis=40, eta=0.05), api.GWOptions(maxSCF=-1, eta=0.05)):
+        with pytest.raises(api.QkError):
+            api.qsRGW(opts, *args, ctx=ctx)
+    bad = (n - 1,) + args[1:]
+    with pytest.raises(api.QkError):
+        api.qsRGW(api.GWOptions(eta=0.05), *bad, ctx=ctx)
+    got = api.qsRGW(api.GWOptions(maxSCF=0, eta=0.05, max_diis=5), *args, ctx=ctx,
+                    raise_on_fail=False)
+    ref = O.qsRGW(0, 1e-5, 5, 0.05, False, *args, raise_on_fail=False)
+    assert got["failed"] and ref["failed"] and got["nSCF"] == 0 == ref["nSCF"]
+    _compare(ref, got, 1e-9)
+    # the context stays usable after the refused calls
+    ref, got = _run_both(ctx, sy, eta=0.05)
+    _compare(ref, got, 1e-8)
