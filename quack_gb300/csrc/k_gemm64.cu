@@ -295,6 +295,120 @@ __global__ void __launch_bounds__(256) k_gemm_simt(int M, int N, int K, double a
   }
 }
 
+// DFMA GEMM with tall 128 x 32 tiles for outputs with few columns (the quarter transforms of
+// qsGW contract the AO tensor with the nO occupied columns: a 64-wide tile would run mostly on
+// padding).  Same contract as k_gemm_simt<TA, TB, double> (split-K slices, strided batches, no
+// lower-triangle mode): 256 threads, each a 4 x 4 block of C (rows tx + 32 i, columns ty + 8 j),
+// 16 independent FMA chains, 8 shared loads per 16 FMA.
+constexpr int TM = 128, TN = 32;
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) k_gemm_tall(int M, int N, int K, double alpha,
+                                                     const double* __restrict__ A, long long lda,
+                                                     long long sA, const double* __restrict__ B,
+                                                     long long ldb, long long sB, double beta,
+                                                     double* __restrict__ C, long long ldc,
+                                                     long long sC, int kc) {
+  __shared__ double As[2][BK][TM];
+  __shared__ double Bs[2][BK][TN];
+  const long long bz = blockIdx.z;
+  int kbeg = 0, kend = K;
+  if (kc > 0) {
+    kbeg = (int)bz * kc;
+    kend = min(K, kbeg + kc);
+    C += bz * sC;
+  } else {
+    A += bz * sA;
+    B += bz * sB;
+    C += bz * sC;
+  }
+  const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN;
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+  double ra[8], rb[2];
+  auto ldA = [&](int k0) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int idx = tid + r * 256;
+      int mm, kk;
+      if (!TA) { mm = idx & (TM - 1); kk = idx >> 7; } else { kk = idx & (BK - 1); mm = idx >> 4; }
+      const int gm = m0 + mm, gk = k0 + kk;
+      ra[r] = (gm < M && gk < kend) ? (!TA ? A[gm + lda * gk] : A[gk + lda * gm]) : 0.0;
+    }
+  };
+  auto stA = [&](int st) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int idx = tid + r * 256;
+      int mm, kk;
+      if (!TA) { mm = idx & (TM - 1); kk = idx >> 7; } else { kk = idx & (BK - 1); mm = idx >> 4; }
+      As[st][kk][mm] = ra[r];
+    }
+  };
+  auto ldB = [&](int k0) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int idx = tid + r * 256;
+      int nn, kk;
+      if (!TB) { kk = idx & (BK - 1); nn = idx >> 4; } else { nn = idx & (TN - 1); kk = idx >> 5; }
+      const int gn = n0 + nn, gk = k0 + kk;
+      rb[r] = (gn < N && gk < kend) ? (!TB ? B[gk + ldb * gn] : B[gn + ldb * gk]) : 0.0;
+    }
+  };
+  auto stB = [&](int st) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int idx = tid + r * 256;
+      int nn, kk;
+      if (!TB) { kk = idx & (BK - 1); nn = idx >> 4; } else { nn = idx & (TN - 1); kk = idx >> 5; }
+      Bs[st][kk][nn] = rb[r];
+    }
+  };
+  ldA(kbeg);
+  ldB(kbeg);
+  stA(0);
+  stB(0);
+  __syncthreads();
+  int st = 0;
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    const bool more = (k0 + BK) < kend;
+    if (more) { ldA(k0 + BK); ldB(k0 + BK); }
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double af[4], bf[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) af[i] = As[st][kk][tx + 32 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bf[j] = Bs[st][kk][ty + 8 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(af[i], bf[j], acc[i][j]);
+    }
+    if (more) { stA(st ^ 1); stB(st ^ 1); }
+    __syncthreads();
+    st ^= 1;
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + tx + 32 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gn = n0 + ty + 8 * j;
+      if (gn < N) {
+        double* c = C + gm + ldc * (long long)gn;
+        double v = alpha * acc[i][j];
+        if (beta != 0.0) v += beta * (*c);
+        *c = v;
+      }
+    }
+  }
+}
+
 // C = alpha * sum_s W[s] + beta * C  (split-K reduction, column-major m x n)
 __global__ void k_splitk_reduce(int m, int n, int S, const double* __restrict__ W, double alpha,
                                 double beta, double* __restrict__ C, long long ldc) {
@@ -312,13 +426,16 @@ __global__ void k_splitk_reduce(int m, int n, int S, const double* __restrict__ 
   }
 }
 
-// path: 0 = DMMA, 1 = DFMA, 2 = FP32 products
+// path: 0 = DMMA, 1 = DFMA, 2 = FP32 products, 3 = DFMA with tall 128 x 32 tiles
 template <bool TA, bool TB>
 void launch(int path, dim3 grid, cudaStream_t st, int m, int n, int k, double alpha,
             const double* A, long long lda, long long sA, const double* B, long long ldb,
             long long sB, double beta, double* C, long long ldc, long long sC, int kc,
             const float* kscale, long long sK) {
-  if (path == 1)
+  if (path == 3)
+    k_gemm_tall<TA, TB><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C,
+                                              ldc, sC, kc);
+  else if (path == 1)
     k_gemm_simt<TA, TB, double><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB,
                                                       beta, C, ldc, sC, kc, nullptr, 0);
   else if (path == 2)
@@ -358,8 +475,16 @@ int gemm_impl(qk_ctx* ctx, bool fp32, char ta, char tb, int m, int n, int k, dou
   }
   const bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
   // FP64 path: 1 = DFMA (default), 2 = DMMA tensor path; tunable per size of the product
-  const int path = fp32 ? 2 : (qk_tune_get(ctx, TUNE_DGEMM_PATH, (long long)m * n, 1) != 2 ? 1 : 0);
-  dim3 grid((m + BM - 1) / BM, (n + BN - 1) / BN, batch);
+  int path = fp32 ? 2 : (qk_tune_get(ctx, TUNE_DGEMM_PATH, (long long)m * n, 1) != 2 ? 1 : 0);
+  // DFMA with 128 x 32 tiles where they cover m x n with clearly less padding than 64 x 64
+  // (outputs with few columns)
+  if (path == 1 && !lower && !kscale) {
+    const long long a64 = (long long)((m + 63) / 64) * 64 * ((n + 63) / 64) * 64;
+    const long long a32 = (long long)((m + TM - 1) / TM) * TM * ((n + TN - 1) / TN) * TN;
+    if (8 * a32 < 7 * a64) path = 3;
+  }
+  const int tm = path == 3 ? TM : BM, tn = path == 3 ? TN : BN;
+  dim3 grid((m + tm - 1) / tm, (n + tn - 1) / tn, batch);
   if (grid.y > 65535 || grid.z > 65535) return qk_fail(ctx, QK_ERR_ARG, "qk_dgemm: grid too large");
   const long long tiles = (long long)grid.x * grid.y;
   // fewer output tiles than mult CTAs per SM and a long K: split K and reduce

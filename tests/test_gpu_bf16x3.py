@@ -59,6 +59,32 @@ def test_dgemm_dev_matches_numpy(ctx, path):
         ctx.tune_set("dgemm_path", key, max(v, 0))
 
 
+@pytest.mark.parametrize("ta,tb,m,n,k", [("T", "N", 4000, 20, 150), ("N", "N", 1000, 25, 77),
+                                         ("N", "T", 513, 7, 33), ("T", "T", 1000, 150, 40),
+                                         ("N", "N", 200, 20, 5000), ("T", "N", 300, 31, 4097)])
+def test_dgemm_tall_tiles(ctx, ta, tb, m, n, k):
+    """The DFMA path's 128 x 32 tiles (chosen for outputs with few columns, like the quarter
+    transforms of qsGW): every transpose, ragged sizes, split-K (few tiles, long k)."""
+    import torch
+    rng = np.random.default_rng(m + 5 * n + 11 * k)
+    A = rng.standard_normal((k, m) if ta == "T" else (m, k))
+    B = rng.standard_normal((n, k) if tb == "T" else (k, n))
+    C0 = rng.standard_normal((m, n))
+    old = ctx.tune_query("dgemm_path", m * n)
+    ctx.tune_set("dgemm_path", m * n, 1)
+    dA = torch.from_numpy(np.asfortranarray(A).ravel(order="F")).cuda()
+    dB = torch.from_numpy(np.asfortranarray(B).ravel(order="F")).cuda()
+    dC = torch.from_numpy(np.asfortranarray(C0).ravel(order="F")).cuda()
+    api.dgemm_dev(ta, tb, m, n, k, 0.5, dA.data_ptr(), A.shape[0], dB.data_ptr(), B.shape[0],
+                  -1.5, dC.data_ptr(), m, ctx=ctx)
+    ctx.tune_set("dgemm_path", m * n, max(old, 0))
+    opA = A.T if ta == "T" else A
+    opB = B.T if tb == "T" else B
+    ref = 0.5 * opA @ opB - 1.5 * C0
+    C = dC.cpu().numpy().reshape((m, n), order="F")
+    assert np.allclose(C, ref, rtol=1e-13, atol=1e-12 * max(1.0, np.sqrt(k / 64.0)))
+
+
 @pytest.mark.parametrize("ta,tb,m,n,k", [("N", "N", 70, 33, 45), ("T", "N", 64, 65, 66),
                                          ("N", "T", 129, 17, 3), ("T", "T", 5, 200, 77),
                                          ("N", "N", 300, 128, 3000), ("T", "N", 128, 600, 3600),
