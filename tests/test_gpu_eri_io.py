@@ -79,3 +79,37 @@ def test_ao_to_mo_on_device_then_g0w0(ctx, tmp_path):
                   out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), dOm.data_ptr(), ctx=ctx)
     ref = O.RG0W0(True, 0.0, False, N, N, 0, nO, N - nO, 0, nS, ref_mo, s["eHF"])
     assert np.max(np.abs(out[0].cpu().numpy() - ref["eGW"])) < 1e-8
+
+
+def test_eri_chem_bin_into_qsgw(ctx, tmp_path):
+    """The AO integrals of an H chain written as QuAcK's packed int/ERI_chem.bin, read straight
+    into device memory and handed to the device-pointer qsGW: the same result as the oracle on
+    the in-memory integrals."""
+    import torch
+    sy = synth.hchain_system(4)
+    n, nO = sy["nBas"], sy["nO"]
+    chem = sy["ERI_AO"].transpose(0, 2, 1, 3)          # (pq|rs) = <pr|qs>
+    (tmp_path / "int").mkdir()
+    pack_s8(chem).tofile(tmp_path / "int" / "ERI_chem.bin")
+    dERI = torch.empty(n ** 4, dtype=torch.float64, device="cuda")
+    api.read_eri_chem_bin(tmp_path / "int" / "ERI_chem.bin", n, dERI.data_ptr(), ctx=ctx)
+
+    def dev(a):
+        return torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).cuda()
+
+    d = {k: dev(sy[k]) for k in ("eHF", "cHF", "PHF", "S", "T", "V", "Hc", "X")}
+    eGW = torch.empty(n, dtype=torch.float64, device="cuda")
+    c = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    P = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    Z = torch.empty(n, dtype=torch.float64, device="cuda")
+    opts = api.GWOptions(maxSCF=64, thresh=1e-5, max_diis=5, eta=0.05)
+    r = api.qsRGW_dev(opts, n, 0, nO, 0, *[d[k].data_ptr() for k in ("eHF", "cHF", "PHF", "S", "T",
+                                                                      "V", "Hc", "X")],
+                      dERI.data_ptr(), eGW.data_ptr(), c.data_ptr(), P.data_ptr(), Z.data_ptr(),
+                      ctx=ctx)
+    torch.cuda.synchronize()
+    ref = O.qsRGW(64, 1e-5, 5, 0.05, False, n, n, 0, nO, n - nO, 0, nO * (n - nO), sy["eHF"],
+                  sy["cHF"], sy["PHF"], sy["S"], sy["T"], sy["V"], sy["Hc"], sy["X"], sy["ERI_AO"])
+    assert r["nSCF"] == ref["nSCF"]
+    assert np.max(np.abs(eGW.cpu().numpy() - ref["eGW"])) < 1e-8
+    assert abs(r["EqsGW"] - ref["EqsGW"]) < 1e-8
