@@ -324,6 +324,9 @@ int qk_gauss_legendre(int n, double* x, double* w);
  * qk_dgemm_f32p_dev: the same contract with FP64 operands and result but FP32 products (the
  *   16 products of each k tile summed in FP32, the tiles folded into a compensated FP32 pair);
  *   the mixed tier's eigenvector back-transformation (dsyev's dormtr step).
+ * qk_dgemm_df_dev: the same contract in double-float: operands staged as FP32 pairs, products
+ *   exact by TwoProduct, sums by TwoSum (~1e-13 of sum |a_ik b_kj| whatever the cancellation, on
+ *   the FP32 pipe); the mixed tier's quarter transforms and full self-energy in qsGW.
  * qk_gemm_bf16x3_dev: C = A * B^T with the three-way BF16 split on tcgen05 (FP32 accumulate),
  *   the precision tier of the same excitation-density dgemm.
  * qk_gemm_bf16x3_ex_dev: the qk_dgemm_dev contract (transposes, alpha, beta) on the same tensor-core
@@ -335,6 +338,9 @@ int qk_dgemm_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, dou
 int qk_dgemm_f32p_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, double alpha,
                       const double* d_A, int lda, const double* d_B, int ldb, double beta,
                       double* d_C, int ldc);
+int qk_dgemm_df_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, double alpha,
+                    const double* d_A, int lda, const double* d_B, int ldb, double beta,
+                    double* d_C, int ldc);
 int qk_gemm_bf16x3_dev(qk_ctx* ctx, int m, int n, int k, const double* d_A, int lda,
                        const double* d_B, int ldb, double* d_C, int ldc);
 int qk_gemm_bf16x3_ex_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k,

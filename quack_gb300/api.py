@@ -558,6 +558,14 @@ def dgemm_f32p_dev(transa, transb, m, n, k, alpha, d_A, lda, d_B, ldb, beta, d_C
                                     C.c_void_p(d_B), ldb, C.c_double(beta), C.c_void_p(d_C), ldc))
 
 
+def dgemm_df_dev(transa, transb, m, n, k, alpha, d_A, lda, d_B, ldb, beta, d_C, ldc, ctx=None):
+    """The dgemm_dev contract in double-float (FP32 pairs, exact products, compensated sums)."""
+    c = _ctx(ctx)
+    c.check(lib().qk_dgemm_df_dev(c.handle, C.c_char(transa.encode()), C.c_char(transb.encode()),
+                                  m, n, k, C.c_double(alpha), C.c_void_p(d_A), lda,
+                                  C.c_void_p(d_B), ldb, C.c_double(beta), C.c_void_p(d_C), ldc))
+
+
 def gemm_bf16x3_ex_dev(transa, transb, m, n, k, alpha, d_A, lda, d_B, ldb, beta, d_C, ldc,
                        ctx=None):
     """C = alpha op(A) op(B) + beta C with the BF16x3 split on the tensor cores (FP64 in/out)."""

@@ -409,6 +409,139 @@ __global__ void __launch_bounds__(256) k_gemm_tall(int M, int N, int K, double a
   }
 }
 
+// Double-float GEMM (the mixed tier's accurate substitute for FP64 on the FP32 pipe): each FP64
+// operand is staged as an FP32 pair a = ah + al (al = fl32(a - ah)), each product is formed
+// exactly to 2^-48 by TwoProduct (p = ah bh, e = fma(ah, bh, -p) + ah bl + al bh) and added to a
+// (hi, lo) accumulator by TwoSum, so the result is accurate to ~K 2^-48 of sum |a_ik b_kj|
+// whatever the cancellation -- about twelve FP32 operations per multiply-add, on a pipe with 64x
+// the FP64 issue rate.  Tiles BMt x BNt (64 x 64, or 128 x 32 for outputs with few columns),
+// 256 threads, each a 4 x 4 block of C; split-K slices and strided batches as k_gemm_simt.
+template <bool TA, bool TB, int BMt, int BNt>
+__global__ void __launch_bounds__(256) k_gemm_df(int M, int N, int K, double alpha,
+                                                   const double* __restrict__ A, long long lda,
+                                                   long long sA, const double* __restrict__ B,
+                                                   long long ldb, long long sB, double beta,
+                                                   double* __restrict__ C, long long ldc,
+                                                   long long sC, int kc) {
+  constexpr int RT = BMt / 4, CT = BNt / 4;  // RT * CT = 256
+  constexpr int NA = BMt * BK / 256, NB = BNt * BK / 256;
+  __shared__ float2 As[2][BK][BMt];
+  __shared__ float2 Bs[2][BK][BNt];
+  const long long bz = blockIdx.z;
+  int kbeg = 0, kend = K;
+  if (kc > 0) {
+    kbeg = (int)bz * kc;
+    kend = min(K, kbeg + kc);
+    C += bz * sC;
+  } else {
+    A += bz * sA;
+    B += bz * sB;
+    C += bz * sC;
+  }
+  const int m0 = blockIdx.x * BMt, n0 = blockIdx.y * BNt;
+  const int tid = threadIdx.x, tx = tid % RT, ty = tid / RT;
+  float hi[4][4], lo[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) hi[i][j] = lo[i][j] = 0.0f;
+  auto split = [](double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+  };
+  double ra[NA], rb[NB];
+  auto ldA = [&](int k0) {
+#pragma unroll
+    for (int r = 0; r < NA; ++r) {
+      const int idx = tid + r * 256;
+      int mm, kk;
+      if (!TA) { mm = idx % BMt; kk = idx / BMt; } else { kk = idx % BK; mm = idx / BK; }
+      const int gm = m0 + mm, gk = k0 + kk;
+      ra[r] = (gm < M && gk < kend) ? (!TA ? A[gm + lda * gk] : A[gk + lda * gm]) : 0.0;
+    }
+  };
+  auto stA = [&](int st) {
+#pragma unroll
+    for (int r = 0; r < NA; ++r) {
+      const int idx = tid + r * 256;
+      int mm, kk;
+      if (!TA) { mm = idx % BMt; kk = idx / BMt; } else { kk = idx % BK; mm = idx / BK; }
+      As[st][kk][mm] = split(ra[r]);
+    }
+  };
+  auto ldB = [&](int k0) {
+#pragma unroll
+    for (int r = 0; r < NB; ++r) {
+      const int idx = tid + r * 256;
+      int nn, kk;
+      if (!TB) { kk = idx % BK; nn = idx / BK; } else { nn = idx % BNt; kk = idx / BNt; }
+      const int gn = n0 + nn, gk = k0 + kk;
+      rb[r] = (gn < N && gk < kend) ? (!TB ? B[gk + ldb * gn] : B[gn + ldb * gk]) : 0.0;
+    }
+  };
+  auto stB = [&](int st) {
+#pragma unroll
+    for (int r = 0; r < NB; ++r) {
+      const int idx = tid + r * 256;
+      int nn, kk;
+      if (!TB) { kk = idx % BK; nn = idx / BK; } else { nn = idx % BNt; kk = idx / BNt; }
+      Bs[st][kk][nn] = split(rb[r]);
+    }
+  };
+  ldA(kbeg);
+  ldB(kbeg);
+  stA(0);
+  stB(0);
+  __syncthreads();
+  int st = 0;
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    const bool more = (k0 + BK) < kend;
+    if (more) { ldA(k0 + BK); ldB(k0 + BK); }
+#pragma unroll 4
+    for (int kk = 0; kk < BK; ++kk) {
+      float2 af[4], bf[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) af[i] = As[st][kk][tx + RT * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bf[j] = Bs[st][kk][ty + CT * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          // __fmul_rn / __fadd_rn keep the compiler from contracting hi + ah bh into an FMA,
+          // which would break the error-free transformations
+          const float p = __fmul_rn(af[i].x, bf[j].x);
+          float e = fmaf(af[i].x, bf[j].x, -p);
+          e = fmaf(af[i].x, bf[j].y, e);
+          e = fmaf(af[i].y, bf[j].x, e);
+          const float s = __fadd_rn(hi[i][j], p);
+          const float bb = __fsub_rn(s, hi[i][j]);
+          const float er = __fadd_rn(__fsub_rn(hi[i][j], __fsub_rn(s, bb)), __fsub_rn(p, bb));
+          hi[i][j] = s;
+          lo[i][j] += er + e;
+        }
+    }
+    if (more) { stA(st ^ 1); stB(st ^ 1); }
+    __syncthreads();
+    st ^= 1;
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + tx + RT * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gn = n0 + ty + CT * j;
+      if (gn < N) {
+        double* c = C + gm + ldc * (long long)gn;
+        double v = alpha * ((double)hi[i][j] + (double)lo[i][j]);
+        if (beta != 0.0) v += beta * (*c);
+        *c = v;
+      }
+    }
+  }
+}
+
 // C = alpha * sum_s W[s] + beta * C  (split-K reduction, column-major m x n)
 __global__ void k_splitk_reduce(int m, int n, int S, const double* __restrict__ W, double alpha,
                                 double beta, double* __restrict__ C, long long ldc) {
@@ -426,7 +559,8 @@ __global__ void k_splitk_reduce(int m, int n, int S, const double* __restrict__ 
   }
 }
 
-// path: 0 = DMMA, 1 = DFMA, 2 = FP32 products, 3 = DFMA with tall 128 x 32 tiles
+// path: 0 = DMMA, 1 = DFMA, 2 = FP32 products, 3 = DFMA with tall 128 x 32 tiles,
+// 4 / 5 = double-float products (64 x 64 / 128 x 32 tiles)
 template <bool TA, bool TB>
 void launch(int path, dim3 grid, cudaStream_t st, int m, int n, int k, double alpha,
             const double* A, long long lda, long long sA, const double* B, long long ldb,
@@ -435,6 +569,12 @@ void launch(int path, dim3 grid, cudaStream_t st, int m, int n, int k, double al
   if (path == 3)
     k_gemm_tall<TA, TB><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C,
                                               ldc, sC, kc);
+  else if (path == 4)
+    k_gemm_df<TA, TB, 64, 64><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta,
+                                                    C, ldc, sC, kc);
+  else if (path == 5)
+    k_gemm_df<TA, TB, TM, TN><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta,
+                                                    C, ldc, sC, kc);
   else if (path == 1)
     k_gemm_simt<TA, TB, double><<<grid, 256, 0, st>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB,
                                                       beta, C, ldc, sC, kc, nullptr, 0);
@@ -463,7 +603,8 @@ namespace {
 int gemm_impl(qk_ctx* ctx, bool fp32, char ta, char tb, int m, int n, int k, double alpha,
               const double* A, long long lda, long long strideA, const double* B, long long ldb,
               long long strideB, double beta, double* C, long long ldc, long long strideC,
-              int batch, bool lower = false, const float* kscale = nullptr, long long sK = 0) {
+              int batch, bool lower = false, const float* kscale = nullptr, long long sK = 0,
+              bool df = false) {
   if (m <= 0 || n <= 0 || batch <= 0) return QK_OK;
   if (k <= 0) {
     // C = beta*C: only beta == 0 is needed by callers
@@ -475,15 +616,18 @@ int gemm_impl(qk_ctx* ctx, bool fp32, char ta, char tb, int m, int n, int k, dou
   }
   const bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
   // FP64 path: 1 = DFMA (default), 2 = DMMA tensor path; tunable per size of the product
-  int path = fp32 ? 2 : (qk_tune_get(ctx, TUNE_DGEMM_PATH, (long long)m * n, 1) != 2 ? 1 : 0);
-  // DFMA with 128 x 32 tiles where they cover m x n with clearly less padding than 64 x 64
-  // (outputs with few columns)
-  if (path == 1 && !lower && !kscale) {
+  int path = df ? 4 : fp32 ? 2
+                        : (qk_tune_get(ctx, TUNE_DGEMM_PATH, (long long)m * n, 1) != 2 ? 1 : 0);
+  if (df && (lower || kscale)) return qk_fail(ctx, QK_ERR_ARG, "double-float GEMM: full C only");
+  // 128 x 32 tiles where they cover m x n with clearly less padding than 64 x 64 (outputs with
+  // few columns): DFMA -> path 3, double-float -> path 5
+  if ((path == 1 || path == 4) && !lower && !kscale) {
     const long long a64 = (long long)((m + 63) / 64) * 64 * ((n + 63) / 64) * 64;
     const long long a32 = (long long)((m + TM - 1) / TM) * TM * ((n + TN - 1) / TN) * TN;
-    if (8 * a32 < 7 * a64) path = 3;
+    if (8 * a32 < 7 * a64) path = path == 1 ? 3 : 5;
   }
-  const int tm = path == 3 ? TM : BM, tn = path == 3 ? TN : BN;
+  const bool tall = path == 3 || path == 5;
+  const int tm = tall ? TM : BM, tn = tall ? TN : BN;
   dim3 grid((m + tm - 1) / tm, (n + tn - 1) / tn, batch);
   if (grid.y > 65535 || grid.z > 65535) return qk_fail(ctx, QK_ERR_ARG, "qk_dgemm: grid too large");
   const long long tiles = (long long)grid.x * grid.y;
@@ -524,6 +668,14 @@ int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, c
              double beta, double* C, long long ldc, long long strideC, int batch) {
   return gemm_impl(ctx, false, ta, tb, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C,
                    ldc, strideC, batch);
+}
+
+int qk_gemm_df(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, const double* A,
+               long long lda, long long strideA, const double* B, long long ldb,
+               long long strideB, double beta, double* C, long long ldc, long long strideC,
+               int batch) {
+  return gemm_impl(ctx, false, ta, tb, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C,
+                   ldc, strideC, batch, false, nullptr, 0, true);
 }
 
 int qk_gemm_f32p(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha,

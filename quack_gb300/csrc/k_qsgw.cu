@@ -15,8 +15,9 @@
 //     integral, (ia|jb) = <ji|ba> with real orbitals;
 //   * the full correlation self-energy (RGW_self_energy.f90:40-84):
 //         Sig(p,q) = sum_(x,m) [2 rho(p,x,m) eps_pxm/(eps_pxm^2 + eta^2)] rho(q,x,m)
-//     the weighted factor is formed once (k_qs_weight) and the sum over (x,m) is one FP64 GEMM
-//     of k = nOrb nS (split over k); the SRG form (RGW_SRG_self_energy.f90:40-80), whose weight
+//     the weighted factor is formed once (k_qs_weight) and the sum over (x,m) is one GEMM of
+//     k = nOrb nS (split over k; FP64, or double-float in the mixed tier like the quarter
+//     transforms); the SRG form (RGW_SRG_self_energy.f90:40-80), whose weight
 //     depends on p and q together, is a tiled kernel (k_qs_srg_sigma);
 //   * symmetrisation, the Fock matrix, and the energy traces (qsRGW.f90:269-310).
 #include "qk_internal.cuh"
@@ -279,20 +280,21 @@ int qk_qs_jk(qk_ctx* ctx, int N, const double* ERI, const double* P, double* par
 }
 
 int qk_qs_mo_slab(qk_ctx* ctx, int nBas, int N, int nC, int nO, int nR, const double* c,
-                  const double* ERI, double* W1, double* W2, double* slab, double* Kmat) {
+                  const double* ERI, double* W1, double* W2, double* slab, double* Kmat, int df) {
   const int no = nO - nC, nv = N - nO - nR;
   const long long N1 = N, B = nBas;
   const double* cocc = c + B * nC;
   const double* cvir = c + B * nO;
+  auto gemm = df ? qk_gemm_df : qk_dgemm;
   // <mu la|nu si> -> (la,nu,si,j) -> (nu,si,j,p) -> (si,j,p,b) -> (j,p,b,q); c is nBas x nOrb
-  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)(B * B * B), no, nBas, 1.0, ERI, B, 0, cocc, B, 0, 0.0, W1,
-                  B * B * B, 0, 1));
-  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)(B * B * no), N, nBas, 1.0, W1, B, 0, c, B, 0, 0.0, W2,
-                  B * B * no, 0, 1));
-  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)(B * no * N1), nv, nBas, 1.0, W2, B, 0, cvir, B, 0, 0.0, W1,
-                  B * no * N1, 0, 1));
-  QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)((long long)no * N1 * nv), N, nBas, 1.0, W1, B, 0, c, B, 0,
-                  0.0, W2, (long long)no * N1 * nv, 0, 1));
+  QK_TRY(gemm(ctx, 'T', 'N', (int)(B * B * B), no, nBas, 1.0, ERI, B, 0, cocc, B, 0, 0.0, W1,
+              B * B * B, 0, 1));
+  QK_TRY(gemm(ctx, 'T', 'N', (int)(B * B * no), N, nBas, 1.0, W1, B, 0, c, B, 0, 0.0, W2,
+              B * B * no, 0, 1));
+  QK_TRY(gemm(ctx, 'T', 'N', (int)(B * no * N1), nv, nBas, 1.0, W2, B, 0, cvir, B, 0, 0.0, W1,
+              B * no * N1, 0, 1));
+  QK_TRY(gemm(ctx, 'T', 'N', (int)((long long)no * N1 * nv), N, nBas, 1.0, W1, B, 0, c, B, 0, 0.0,
+              W2, (long long)no * N1 * nv, 0, 1));
   const long long nS = (long long)no * nv;
   k_qs_slab<<<grid_1d(ctx, N1 * N1 * nS), 256, 0, ctx->stream>>>(N, no, nv, W2, slab);
   QK_LAUNCHED();
@@ -303,14 +305,15 @@ int qk_qs_mo_slab(qk_ctx* ctx, int nBas, int N, int nC, int nO, int nR, const do
 
 int qk_qs_sigma(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                 int nS, const double* e, const double* Om, const double* rho, double* W,
-                double* Sig) {
+                double* Sig, int df) {
   const long long N1 = N, N2 = N1 * N1;
   if (!doSRG) {
     k_qs_weight<<<grid_1d(ctx, N2 * nS), 256, 0, ctx->stream>>>(N, nC, nO, nR, nS, eta, e, Om,
                                                                   rho, W);
     QK_LAUNCHED();
-    return qk_dgemm(ctx, 'N', 'T', N, N, (int)(N1 * nS), 1.0, W, N1, 0, rho, N1, 0, 0.0, Sig, N1,
-                    0, 1);
+    auto gemm = df ? qk_gemm_df : qk_dgemm;
+    return gemm(ctx, 'N', 'T', N, N, (int)(N1 * nS), 1.0, W, N1, 0, rho, N1, 0, 0.0, Sig, N1, 0,
+                1);
   }
   const int tiles = (N + SRG_T - 1) / SRG_T;
   const long long K = (long long)(N - nC - nR) * nS;

@@ -1030,7 +1030,7 @@ static int sigma_full_stage(qk_ctx* ctx, int doSRG, double eta, double flow, int
   QK_TRY(h2d(ctx, dR, rho, N2S * 8));
   QK_TRY(h2d(ctx, de, e, N * 8));
   QK_TRY(h2d(ctx, dOm, Om, nS * 8));
-  QK_TRY(qk_qs_sigma(ctx, doSRG, eta, flow, nOrb, nC, nO, nR, nS, de, dOm, dR, W, dSig));
+  QK_TRY(qk_qs_sigma(ctx, doSRG, eta, flow, nOrb, nC, nO, nR, nS, de, dOm, dR, W, dSig, 0));
   QK_TRY(qk_qs_mask(ctx, nOrb, nC, nR, dSig));
   QK_TRY(qk_sigma_diag(ctx, doSRG, eta, flow, nOrb, nC, nO, nR, nS, de, dOm, dR, dd, dZ, dGM));
   QK_TRY(d2h(ctx, Sig, dSig, N2 * 8));
@@ -1188,6 +1188,11 @@ int qsgw_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, const Dims& d, cons
   TdaScope tda(ctx, prm->TDA_W != 0);
   const int N = d.N, nS = d.nS, B = nBas;
   const bool proj = B != N;  // the reference's nBas /= nOrb branch (qsRGW.f90:281-284,328-333)
+  // mixed tier: the quarter transforms and the full-Sigma GEMM in double-float (FP32 pairs with
+  // exact products: ~1e-13 of sum |terms|, where plain FP32 products left ~1e-5 Ha of noise in F
+  // and stalled the SCF); ρ BF16x3 and the eigenvector back-transformation on FP32 products as in
+  // G0W0; eigenvalues, the N x N algebra and the DIIS stay FP64
+  const int mixed = prm->precision == QK_PREC_BF16X3;
   const double flow = 500.0;
   const size_t N1 = N, N2 = N1 * N1, B1 = B, B2 = B1 * B1, B3 = B2 * B1;
   const size_t rw = B3 * d.no > N2 * nS ? B3 * d.no : N2 * nS;
@@ -1240,13 +1245,13 @@ int qsgw_dev(qk_ctx* ctx, const qk_gw_params* prm, int nBas, const Dims& d, cons
   while (Conv > prm->thresh && nSCF < prm->maxSCF) {  // qsRGW.f90:193
     ++nSCF;
     QK_TRY(qk_qs_jk(ctx, B, in.ERI, out.P, part, J, K));                             // :201-202
-    QK_TRY(qk_qs_mo_slab(ctx, B, N, d.nC, d.nO, d.nR, out.c, in.ERI, W1, W2, slab,
-                         Kmat));                                                     // :210
+    QK_TRY(qk_qs_mo_slab(ctx, B, N, d.nC, d.nO, d.nR, out.c, in.ERI, W1, W2, slab, Kmat,
+                         mixed));                                                    // :210
     QK_TRY(casida_dev(ctx, d, out.eGW, nullptr, Om, XpY, nullptr, sm, 1, Kmat,
                       prm->precision));                                              // :214-217
     QK_TRY(rho_gemm(ctx, prm->precision, N, nS, slab, XpY, rho));                    // :220
     QK_TRY(qk_qs_sigma(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, out.eGW, Om,
-                       rho, W1, Sraw));                                              // :255-264
+                       rho, W1, Sraw, mixed));                                       // :255-264
     QK_TRY(qk_sigma_diag(ctx, prm->doSRG, prm->eta, flow, N, d.nC, d.nO, d.nR, nS, out.eGW, Om,
                          rho, sdiag, out.Z, sm + 8));                                // Z, EcGM
     QK_TRY(qk_qs_sym(ctx, N, d.nC, d.nR, Sraw, Smo));                                // :269
@@ -1515,6 +1520,15 @@ int qk_gauss_legendre(int n, double* x, double* w) {
   if (n < 1 || n > 4096 || !x || !w) return QK_ERR_ARG;
   qk_gauss_legendre_host(n, x, w);
   return QK_OK;
+}
+
+int qk_dgemm_df_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, double alpha,
+                    const double* d_A, int lda, const double* d_B, int ldb, double beta,
+                    double* d_C, int ldc) {
+  QK_TRY(begin(ctx));
+  const int st = qk_gemm_df(ctx, transa, transb, m, n, k, alpha, d_A, lda, 0, d_B, ldb, 0, beta,
+                            d_C, ldc, 0, 1);
+  return end(ctx, st);
 }
 
 int qk_dgemm_f32p_dev(qk_ctx* ctx, char transa, char transb, int m, int n, int k, double alpha,

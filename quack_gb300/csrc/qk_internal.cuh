@@ -134,6 +134,12 @@ void qk_timings_collect(qk_ctx* ctx);
 // ------------------------------------------------------------------------------------------
 // kernel-level entry points (all enqueue on ctx->stream; device pointers)
 // ------------------------------------------------------------------------------------------
+// Double-float GEMM (FP32 pairs, exact products, compensated sums; ~1e-13 of sum |a b|): the
+// mixed tier's substitute for FP64 where cancellation rules out FP32 products.
+int qk_gemm_df(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, const double* A,
+               long long lda, long long strideA, const double* B, long long ldb,
+               long long strideB, double beta, double* C, long long ldc, long long strideC,
+               int batch);
 // FP64 GEMM (DFMA or DMMA), column-major: C = alpha*op(A)*op(B) + beta*C, batched by strides.
 int qk_dgemm(qk_ctx* ctx, char ta, char tb, int m, int n, int k, double alpha, const double* A,
              long long lda, long long strideA, const double* B, long long ldb, long long strideB,
@@ -178,14 +184,15 @@ int phrlr_dev(qk_ctx* ctx, int TDA, int nS, double* dA, double* dB, double* dOm,
 //   J = Hartree, K = exchange matrix of P over the AO tensor (N = nBas; part: 2 N^3 scratch);
 //   slab / Kmat from the partial MO transform with c (nBas x N; W1, W2: max(nBas^3 no, N^2 nS));
 //   Sig = full correlation self-energy (unsymmetrised, W: N^2 nS scratch);
+//   df: the GEMMs run in double-float (mixed tier) instead of FP64;
 //   out[0..5] = ET, EV, EJ, EK, EqsGW, max|err|.
 int qk_qs_jk(qk_ctx* ctx, int N, const double* ERI, const double* P, double* part, double* J,
              double* K);
 int qk_qs_mo_slab(qk_ctx* ctx, int nBas, int N, int nC, int nO, int nR, const double* c,
-                  const double* ERI, double* W1, double* W2, double* slab, double* Kmat);
+                  const double* ERI, double* W1, double* W2, double* slab, double* Kmat, int df);
 int qk_qs_sigma(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                 int nS, const double* e, const double* Om, const double* rho, double* W,
-                double* Sig);
+                double* Sig, int df);
 int qk_qs_sym(qk_ctx* ctx, int N, int nC, int nR, const double* Sig, double* out);
 int qk_qs_mask(qk_ctx* ctx, int N, int nC, int nR, double* Sig);
 int qk_qs_fock(qk_ctx* ctx, int N, const double* Hc, const double* J, const double* K,

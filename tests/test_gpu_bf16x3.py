@@ -236,3 +236,29 @@ def test_mixed_g0w0_newton_regular_orbitals(ctx, N, nO, seed):
     assert regular.sum() >= N // 2
     assert np.max(np.abs(r["eGW"][regular] - ref["eGW"][regular])) < MEV
     assert abs(r["EcGM"] - ref["EcGM"]) < 1e-5 * max(1.0, abs(ref["EcGM"]))
+
+
+@pytest.mark.parametrize("ta,tb,m,n,k", [("T", "N", 4000, 20, 150), ("N", "N", 70, 33, 45),
+                                         ("N", "T", 129, 17, 3), ("T", "T", 300, 150, 40),
+                                         ("N", "N", 200, 20, 5000), ("N", "T", 257, 300, 128)])
+def test_dgemm_df_dev_accuracy_under_cancellation(ctx, ta, tb, m, n, k):
+    """Double-float GEMM: every transpose, both tile shapes, split-K; operands with large
+    entries whose products cancel (the qsGW quarter transforms in a near-linearly-dependent
+    basis), where FP32 products fail: the error stays at ~1e-13 of sum |a_ik b_kj|."""
+    import torch
+    rng = np.random.default_rng(m + 7 * n + 13 * k)
+    A = rng.standard_normal((k, m) if ta == "T" else (m, k)) * 30.0
+    B = rng.standard_normal((n, k) if tb == "T" else (k, n))
+    C0 = rng.standard_normal((m, n))
+    opA = A.T if ta == "T" else A
+    opB = B.T if tb == "T" else B
+    dA = torch.from_numpy(np.asfortranarray(A).ravel(order="F")).cuda()
+    dB = torch.from_numpy(np.asfortranarray(B).ravel(order="F")).cuda()
+    dC = torch.from_numpy(np.asfortranarray(C0).ravel(order="F")).cuda()
+    api.dgemm_df_dev(ta, tb, m, n, k, 0.5, dA.data_ptr(), A.shape[0], dB.data_ptr(), B.shape[0],
+                     -1.5, dC.data_ptr(), m, ctx=ctx)
+    ref = 0.5 * opA @ opB - 1.5 * C0
+    scale = 0.5 * np.abs(opA) @ np.abs(opB) + 1.5 * np.abs(C0)
+    C = dC.cpu().numpy().reshape((m, n), order="F")
+    ratio = np.max(np.abs(C - ref) / scale)
+    assert ratio < 1e-12 * max(1.0, k / 64.0), ratio
