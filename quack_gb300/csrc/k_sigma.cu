@@ -482,6 +482,160 @@ __global__ void k_qp_update(int N, int nchunks, const double* __restrict__ part,
   qp_compact(N, s);
 }
 
+// p-major copy of R for the persistent Newton solve: Rt[m + nS (q + N p)] = R[p + N q + N^2 m]
+// (32 x 32 tiles of (p, m) per q through shared memory: both sides coalesced)
+__global__ void k_r_pmajor(int N, int nS, const float* __restrict__ R, float* __restrict__ Rt) {
+  __shared__ float t[32][33];
+  const int p0 = blockIdx.x * 32, m0 = blockIdx.y * 32, q = blockIdx.z;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  const long long N1 = N, N2 = N1 * N1;
+  for (int i = ty; i < 32; i += 8) {
+    const int p = p0 + tx, m = m0 + i;
+    t[i][tx] = (p < N && m < nS) ? R[p + N1 * q + N2 * m] : 0.f;
+  }
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int p = p0 + i, m = m0 + tx;
+    if (p < N && m < nS) Rt[m + (long long)nS * (q + N1 * p)] = t[tx][i];
+  }
+}
+
+// Persistent Newton solve of the mixed tier (RGW_QP_graph.f90:50-92; eta = 0, no SRG): one CTA
+// per orbital, taken from a queue, iterates w <- w - f/(1 - Sigma'(w)) on chip until |f| <= 1e-6
+// or maxit steps, so that a search costs no launches and the chaotic orbitals, which run all 64
+// steps, no longer hold the whole GPU for two launches per step.  A step sweeps the orbital's
+// (q, m) terms: warps over q, lanes over m (Rt is p-major, so the loads are coalesced), the
+// same FP32 far-pole / FP64 window split and float-float accumulation as k_sigma_partial_ff,
+// then one block reduction.  The update and the bookkeeping are k_qp_update's.
+struct NewtFF {
+  int N, nC, nO, nR, nS, maxit;
+  const double* eq;     // energies in the poles
+  const double* eHF;
+  const double* Om;
+  const double* rho;
+  const float* Rt;      // p-major 2 rho^2
+  const float2* OmF;
+  const int* bad;
+  float tau;
+  int* queue;           // next list index to take
+};
+
+__global__ void __launch_bounds__(SIG_WARPS * 32) k_qp_newton_ff(NewtFF a, QPState s) {
+  extern __shared__ double se[];  // e (N doubles) | e as float pairs (N)
+  __shared__ double r_sig[SIG_WARPS], r_ds[SIG_WARPS];
+  __shared__ double s_w;
+  __shared__ int s_p, s_done;
+  const int N = a.N, nS = a.nS;
+  float2* eF = (float2*)(se + N);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double e = a.eq[i];
+    const float h = (float)e;
+    se[i] = e;
+    eF[i] = make_float2(h, (float)(e - (double)h));
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int pend = N - a.nR;
+  const int nl = *s.nact;
+  const bool bad = *a.bad != 0;
+  const long long N1 = N, N2 = N1 * N1;
+  for (;;) {
+    __syncthreads();  // the previous orbital's s_p / s_w / s_done have been read by every thread
+    if (threadIdx.x == 0) {
+      const int idx = atomicAdd(a.queue, 1);
+      s_p = idx < nl ? s.list[idx] : -1;
+      s_w = s_p >= 0 ? s.w[s_p] : 0.0;
+      s_done = 0;
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (p < 0) break;
+    const float* Rp = a.Rt + (long long)nS * N1 * p;
+    const double* rp = a.rho + p;
+    for (;;) {  // at most maxit steps: every step increments nit[p]
+      const double w = s_w;
+      const float w_hi = (float)w;
+      const float w_lo = (float)(w - (double)w_hi);
+      float so_h = 0.f, so_l = 0.f, sv_h = 0.f, sv_l = 0.f, d_h = 0.f, d_l = 0.f;
+      double Sn = 0.0, Dn = 0.0;  // window (FP64) parts, per lane
+      for (int q = a.nC + warp; q < pend; q += SIG_WARPS) {
+        const bool occ = q < a.nO;
+        const float2 eq = eF[q];
+        const float chi = w_hi - eq.x;
+        const float bb = chi - w_hi;
+        const float clo = ((w_hi - (chi - bb)) + (-eq.x - bb)) + (w_lo - eq.y);
+        const float sg = occ ? 1.f : -1.f;
+        int lo = 0, hi = nS;
+        if (!bad) {
+          const float ctr = -sg * chi;
+          lo = om_lower_bound(a.OmF, 0, 0, nS, ctr - a.tau);
+          hi = om_lower_bound(a.OmF, 0, lo, nS, ctr + a.tau);
+        }
+        const float* Rq = Rp + (long long)nS * q;
+        float sl = 0.f, dl = 0.f;
+        for (int m = lane; m < nS; m += 32) {
+          const float2 o = __ldg(a.OmF + m);
+          const float e = fmaf(sg, o.x, chi) + fmaf(sg, o.y, clo);
+          float r = rcp32(e);
+          r = (m >= lo && m < hi) ? 0.f : r;
+          const float t = __ldg(Rq + m) * r;
+          sl += t;
+          dl = fmaf(t, r, dl);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          sl += __shfl_xor_sync(0xffffffffu, sl, o);
+          dl += __shfl_xor_sync(0xffffffffu, dl, o);
+        }
+        if (occ) ff_add(so_h, so_l, sl);
+        else ff_add(sv_h, sv_l, sl);
+        ff_add(d_h, d_l, dl);
+        // the window, in FP64 (RGW_Re_SigC.f90:30-50 / RGW_Re_dSigC.f90:30-50 with eta = 0)
+        for (int m = lo + lane; m < hi; m += 32) {
+          const double om = __ldg(a.Om + m);
+          const double x = __ldg(rp + N1 * q + N2 * m);
+          const double ir = rcp_nr(occ ? (w - se[q] + om) : (w - se[q] - om));
+          const double t = (2.0 * (x * x)) * ir;
+          Sn += t;
+          Dn = fma(t, ir, Dn);
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        Sn += __shfl_xor_sync(0xffffffffu, Sn, o);
+        Dn += __shfl_xor_sync(0xffffffffu, Dn, o);
+      }
+      // lanes hold identical float-float accumulators (the shuffles gave every lane the sums)
+      if (lane == 0) {
+        r_sig[warp] = (((double)so_h + (double)so_l) + ((double)sv_h + (double)sv_l)) + Sn;
+        r_ds[warp] = -(((double)d_h + (double)d_l) + Dn);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double sig = 0.0, dsig = 0.0;
+        for (int k = 0; k < SIG_WARPS; ++k) {
+          sig += r_sig[k];
+          dsig += r_ds[k];
+        }
+        const int nIt = s.nit[p] + 1;
+        s.nit[p] = nIt;
+        s.evals[p] += 1;
+        const double f = w - a.eHF[p] - sig;
+        const double df = 1.0 / (1.0 - dsig);
+        const double wn = w - df * f;
+        s.w[p] = wn;
+        s.df[p] = df;
+        const bool ok = !(fabs(f) > QP_THRESH);
+        if (ok || nIt >= a.maxit) {
+          s.active[p] = 0;
+          s.conv[p] = ok;
+          s_done = 1;
+        }
+        s_w = wn;
+      }
+      __syncthreads();
+      if (s_done) break;
+    }
+  }
+}
+
 __global__ void k_qp_finish(int N, int nC, int nR, const double* __restrict__ eGWlin, QPState s,
                             double* __restrict__ eGW, double* __restrict__ Z, int* status) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
@@ -722,11 +876,35 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
   // reference search (RGW_QP_graph.f90:50-92) from eGWlin for every orbital not yet converged
   k_qp_init<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, w_guess ? w_guess : eGWlin, s);
   QK_LAUNCHED();
+  // mixed tier: the persistent on-chip search over a p-major copy of R
+  const bool persistent = ff && !doSRG && eta == 0.0 && (size_t)N * 16 <= 40 * 1024 &&
+                          qk_tune_get(ctx, TUNE_QP_PERSIST, (long long)nS, 1) != 0;
+  float* Rt = nullptr;
+  int* queue = nullptr;
+  if (persistent) {
+    QK_TRY(qk_wst(ctx, W_RHO32T, (size_t)N * N * nS + 32, &Rt));
+    QK_TRY(qk_wst(ctx, W_QPQUEUE, 16, &queue));
+    dim3 tg((N + 31) / 32, (nS + 31) / 32, N);
+    if (tg.y > 65535 || tg.z > 65535) return qk_fail(ctx, QK_ERR_ARG, "k_r_pmajor grid");
+    k_r_pmajor<<<tg, dim3(32, 8), 0, ctx->stream>>>(N, nS, ff->R, Rt);
+    QK_LAUNCHED();
+  }
   for (int phase = w_guess ? 1 : 2; phase <= 2; ++phase) {
     const int maxit = phase == 1 ? guess_maxit : QP_MAXIT;
     if (phase == 2 && w_guess) {
       k_qp_restart<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, eGWlin, eHF, s);
       QK_LAUNCHED();
+    }
+    if (persistent) {
+      QK_CK(cudaMemsetAsync(queue, 0, sizeof(int), ctx->stream));
+      NewtFF a{N, nC, nO, nR, nS, maxit, eOld, eHF, Om, rho, Rt, ff->OmF, ff->bad, ff->tau, queue};
+      const int nq = N - nC - nR;
+      int grid = 2 * ctx->num_sms;
+      if (grid > nq) grid = nq;
+      if (grid < 1) grid = 1;
+      k_qp_newton_ff<<<grid, SIG_WARPS * 32, (size_t)N * 16, ctx->stream>>>(a, s);
+      QK_LAUNCHED();
+      continue;
     }
     int hact = N;  // upper bound on the active count, refreshed by the polls
     for (int it = 0; it < maxit; ++it) {

@@ -20,7 +20,8 @@
 #include "qk_internal.cuh"
 
 static const char* k_tune_names[TUNE_NUM] = {"bf16x3_chunk", "splitk_mult", "sigma_chunks",
-                                             "sytrd_grid", "dgemm_path", "stebz_k"};
+                                             "sytrd_grid", "dgemm_path", "stebz_k",
+                                             "qp_persist"};
 
 static int bucket_of(long long size) {
   int b = 0;

@@ -26,7 +26,7 @@ enum {
 };
 
 // runtime-tunable launch parameters (chosen by qk_autotune, looked up by size bucket)
-enum { TUNE_BF16X3_CHUNK = 0, TUNE_SPLITK_MULT, TUNE_SIGMA_CHUNKS, TUNE_SYTRD_GRID, TUNE_DGEMM_PATH, TUNE_STEBZ_K, TUNE_NUM };
+enum { TUNE_BF16X3_CHUNK = 0, TUNE_SPLITK_MULT, TUNE_SIGMA_CHUNKS, TUNE_SYTRD_GRID, TUNE_DGEMM_PATH, TUNE_STEBZ_K, TUNE_QP_PERSIST, TUNE_NUM };
 constexpr int TUNE_BUCKETS = 40;
 
 struct DevBuf {
@@ -38,7 +38,7 @@ enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
   W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_TMAT2, W_RHO32, W_OMF, W_TFAC, W_STEBZ,
   W_QUAD, W_QLT, W_QPV, W_QL, W_QX, W_QQ, W_QD, W_BSE, W_BSEU, W_BSER, W_BSEK, W_ERIPACK,
-  W_QSR1, W_QSR2, W_QSJK, W_QSMAT, W_QSDIIS, W_QSIN, W_NUMBUF
+  W_QSR1, W_QSR2, W_QSJK, W_QSMAT, W_QSDIIS, W_QSIN, W_RHO32T, W_QPQUEUE, W_NUMBUF
 };
 
 struct qk_ctx {
