@@ -13,6 +13,7 @@
 // so EcGM comes out of the same sweep: EcGM = -2 * sum_{a} SigOcc_a.
 #include <cmath>
 #include <cfloat>
+#include <mutex>
 #include "qk_internal.cuh"
 
 namespace {
@@ -507,6 +508,7 @@ __global__ void k_r_pmajor(int N, int nS, const float* __restrict__ R, float* __
 // (q, m) terms: warps over q, lanes over m (Rt is p-major, so the loads are coalesced), the
 // same FP32 far-pole / FP64 window split and float-float accumulation as k_sigma_partial_ff,
 // then one block reduction.  The update and the bookkeeping are k_qp_update's.
+constexpr size_t NEWT_SMEM_MAX = 200 * 1024;
 struct NewtFF {
   int N, nC, nO, nR, nS, maxit;
   const double* eq;     // energies in the poles
@@ -521,18 +523,22 @@ struct NewtFF {
 };
 
 __global__ void __launch_bounds__(SIG_WARPS * 32) k_qp_newton_ff(NewtFF a, QPState s) {
-  extern __shared__ double se[];  // e (N doubles) | e as float pairs (N)
+  // dynamic shared memory: e (N doubles) | e as float pairs (N) | Om as float pairs (nS), so
+  // that the two window bisections per (step, q) probe shared memory
+  extern __shared__ double se[];
   __shared__ double r_sig[SIG_WARPS], r_ds[SIG_WARPS];
   __shared__ double s_w;
   __shared__ int s_p, s_done;
   const int N = a.N, nS = a.nS;
   float2* eF = (float2*)(se + N);
+  float2* oS = eF + N;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const double e = a.eq[i];
     const float h = (float)e;
     se[i] = e;
     eF[i] = make_float2(h, (float)(e - (double)h));
   }
+  for (int i = threadIdx.x; i < nS; i += blockDim.x) oS[i] = a.OmF[i];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int pend = N - a.nR;
   const int nl = *s.nact;
@@ -567,13 +573,13 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_qp_newton_ff(NewtFF a, QPSta
         int lo = 0, hi = nS;
         if (!bad) {
           const float ctr = -sg * chi;
-          lo = om_lower_bound(a.OmF, 0, 0, nS, ctr - a.tau);
-          hi = om_lower_bound(a.OmF, 0, lo, nS, ctr + a.tau);
+          lo = om_lower_bound(oS, 0, 0, nS, ctr - a.tau);
+          hi = om_lower_bound(oS, 0, lo, nS, ctr + a.tau);
         }
         const float* Rq = Rp + (long long)nS * q;
         float sl = 0.f, dl = 0.f;
         for (int m = lane; m < nS; m += 32) {
-          const float2 o = __ldg(a.OmF + m);
+          const float2 o = oS[m];
           const float e = fmaf(sg, o.x, chi) + fmaf(sg, o.y, clo);
           float r = rcp32(e);
           r = (m >= lo && m < hi) ? 0.f : r;
@@ -877,13 +883,21 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
   k_qp_init<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, w_guess ? w_guess : eGWlin, s);
   QK_LAUNCHED();
   // mixed tier: the persistent on-chip search over a p-major copy of R
-  const bool persistent = ff && !doSRG && eta == 0.0 && (size_t)N * 16 <= 40 * 1024 &&
+  const size_t newt_smem = (size_t)N * 16 + (size_t)nS * 8;
+  const bool persistent = ff && !doSRG && eta == 0.0 && newt_smem <= NEWT_SMEM_MAX &&
                           qk_tune_get(ctx, TUNE_QP_PERSIST, (long long)nS, 1) != 0;
   float* Rt = nullptr;
   int* queue = nullptr;
   if (persistent) {
     QK_TRY(qk_wst(ctx, W_RHO32T, (size_t)N * N * nS + 32, &Rt));
     QK_TRY(qk_wst(ctx, W_QPQUEUE, 16, &queue));
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+      attr_err = cudaFuncSetAttribute(k_qp_newton_ff, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)NEWT_SMEM_MAX);
+    });
+    QK_CK(attr_err);
     dim3 tg((N + 31) / 32, (nS + 31) / 32, N);
     if (tg.y > 65535 || tg.z > 65535) return qk_fail(ctx, QK_ERR_ARG, "k_r_pmajor grid");
     k_r_pmajor<<<tg, dim3(32, 8), 0, ctx->stream>>>(N, nS, ff->R, Rt);
@@ -902,7 +916,7 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
       int grid = 2 * ctx->num_sms;
       if (grid > nq) grid = nq;
       if (grid < 1) grid = 1;
-      k_qp_newton_ff<<<grid, SIG_WARPS * 32, (size_t)N * 16, ctx->stream>>>(a, s);
+      k_qp_newton_ff<<<grid, SIG_WARPS * 32, newt_smem, ctx->stream>>>(a, s);
       QK_LAUNCHED();
       continue;
     }
