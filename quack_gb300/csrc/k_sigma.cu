@@ -522,11 +522,13 @@ struct NewtFF {
   int* queue;           // next list index to take
 };
 
-__global__ void __launch_bounds__(SIG_WARPS * 32) k_qp_newton_ff(NewtFF a, QPState s) {
+constexpr int NEWT_WARPS = 32;  // one CTA per SM: its loads must fill the memory pipeline alone
+constexpr int NEWT_U = 8;       // R loads per lane issued together
+__global__ void __launch_bounds__(NEWT_WARPS * 32) k_qp_newton_ff(NewtFF a, QPState s) {
   // dynamic shared memory: e (N doubles) | e as float pairs (N) | Om as float pairs (nS), so
   // that the two window bisections per (step, q) probe shared memory
   extern __shared__ double se[];
-  __shared__ double r_sig[SIG_WARPS], r_ds[SIG_WARPS];
+  __shared__ double r_sig[NEWT_WARPS], r_ds[NEWT_WARPS];
   __shared__ double s_w;
   __shared__ int s_p, s_done;
   const int N = a.N, nS = a.nS;
@@ -563,7 +565,7 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_qp_newton_ff(NewtFF a, QPSta
       const float w_lo = (float)(w - (double)w_hi);
       float so_h = 0.f, so_l = 0.f, sv_h = 0.f, sv_l = 0.f, d_h = 0.f, d_l = 0.f;
       double Sn = 0.0, Dn = 0.0;  // window (FP64) parts, per lane
-      for (int q = a.nC + warp; q < pend; q += SIG_WARPS) {
+      for (int q = a.nC + warp; q < pend; q += NEWT_WARPS) {
         const bool occ = q < a.nO;
         const float2 eq = eF[q];
         const float chi = w_hi - eq.x;
@@ -578,7 +580,25 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_qp_newton_ff(NewtFF a, QPSta
         }
         const float* Rq = Rp + (long long)nS * q;
         float sl = 0.f, dl = 0.f;
-        for (int m = lane; m < nS; m += 32) {
+        int m0 = 0;
+        // batches of NEWT_U coalesced warp loads issued before their arithmetic
+        for (; m0 + 32 * NEWT_U <= nS; m0 += 32 * NEWT_U) {
+          float rv[NEWT_U];
+#pragma unroll
+          for (int u = 0; u < NEWT_U; ++u) rv[u] = __ldg(Rq + m0 + 32 * u + lane);
+#pragma unroll
+          for (int u = 0; u < NEWT_U; ++u) {
+            const int m = m0 + 32 * u + lane;
+            const float2 o = oS[m];
+            const float e = fmaf(sg, o.x, chi) + fmaf(sg, o.y, clo);
+            float r = rcp32(e);
+            r = (m >= lo && m < hi) ? 0.f : r;
+            const float t = rv[u] * r;
+            sl += t;
+            dl = fmaf(t, r, dl);
+          }
+        }
+        for (int m = m0 + lane; m < nS; m += 32) {
           const float2 o = oS[m];
           const float e = fmaf(sg, o.x, chi) + fmaf(sg, o.y, clo);
           float r = rcp32(e);
@@ -616,7 +636,7 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_qp_newton_ff(NewtFF a, QPSta
       __syncthreads();
       if (threadIdx.x == 0) {
         double sig = 0.0, dsig = 0.0;
-        for (int k = 0; k < SIG_WARPS; ++k) {
+        for (int k = 0; k < NEWT_WARPS; ++k) {
           sig += r_sig[k];
           dsig += r_ds[k];
         }
@@ -884,8 +904,9 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
   QK_LAUNCHED();
   // mixed tier: the persistent on-chip search over a p-major copy of R
   const size_t newt_smem = (size_t)N * 16 + (size_t)nS * 8;
+  // tunable per nS bucket: 1 (default) = persistent kernel, 2 = per-step sweeps
   const bool persistent = ff && !doSRG && eta == 0.0 && newt_smem <= NEWT_SMEM_MAX &&
-                          qk_tune_get(ctx, TUNE_QP_PERSIST, (long long)nS, 1) != 0;
+                          qk_tune_get(ctx, TUNE_QP_PERSIST, (long long)nS, 1) != 2;
   float* Rt = nullptr;
   int* queue = nullptr;
   if (persistent) {
@@ -913,10 +934,10 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
       QK_CK(cudaMemsetAsync(queue, 0, sizeof(int), ctx->stream));
       NewtFF a{N, nC, nO, nR, nS, maxit, eOld, eHF, Om, rho, Rt, ff->OmF, ff->bad, ff->tau, queue};
       const int nq = N - nC - nR;
-      int grid = 2 * ctx->num_sms;
+      int grid = ctx->num_sms;
       if (grid > nq) grid = nq;
       if (grid < 1) grid = 1;
-      k_qp_newton_ff<<<grid, SIG_WARPS * 32, newt_smem, ctx->stream>>>(a, s);
+      k_qp_newton_ff<<<grid, NEWT_WARPS * 32, newt_smem, ctx->stream>>>(a, s);
       QK_LAUNCHED();
       continue;
     }
