@@ -935,6 +935,8 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
       NewtFF a{N, nC, nO, nR, nS, maxit, eOld, eHF, Om, rho, Rt, ff->OmF, ff->bad, ff->tau, queue};
       const int nq = N - nC - nR;
       int grid = ctx->num_sms;
+      // batch workers run several systems at once: each takes its share of the SMs
+      if (ctx->sytrd_max_ctas > 0 && grid > ctx->sytrd_max_ctas) grid = ctx->sytrd_max_ctas;
       if (grid > nq) grid = nq;
       if (grid < 1) grid = 1;
       k_qp_newton_ff<<<grid, NEWT_WARPS * 32, newt_smem, ctx->stream>>>(a, s);
