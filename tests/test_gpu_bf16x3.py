@@ -238,6 +238,32 @@ def test_mixed_g0w0_newton_regular_orbitals(ctx, N, nO, seed):
     assert abs(r["EcGM"] - ref["EcGM"]) < 1e-5 * max(1.0, abs(ref["EcGM"]))
 
 
+def test_persistent_newton_matches_per_step_sweeps(ctx):
+    """The mixed tier's persistent Newton kernel (one CTA per orbital, on-chip iterations) and
+    the per-step sweeps (qp_persist = 2) follow the same search: regular orbitals agree to
+    roundoff, step counts match, and both are within 1 meV of the FP64 oracle."""
+    N, nO, seed = 48, 6, 23
+    s = synth.small_system(N, nO, 3 * N, seed)
+    E = synth.eri_phys_numpy(s["L"])
+    nS = nO * (N - nO)
+    opts = api.GWOptions(precision=api.QK_PREC_BF16X3)
+    old = ctx.tune_query("qp_persist", nS)
+    res = {}
+    try:
+        for mode in (1, 2):
+            ctx.tune_set("qp_persist", nS, mode)
+            r = api.RG0W0(opts, N, N, 0, nO, N - nO, 0, nS, E, s["eHF"], ctx=ctx)
+            res[mode] = (r["eGW"], np.array(ctx.qp_iters(N)))
+    finally:
+        ctx.tune_set("qp_persist", nS, max(old, 0))
+    ref = O.RG0W0(False, 0.0, False, N, N, 0, nO, N - nO, 0, nS, E, s["eHF"])
+    regular = (np.asarray(ref["qp_iters"]) <= 6) & (res[1][1] <= 6) & (res[2][1] <= 6)
+    assert regular.sum() >= N // 2
+    assert np.max(np.abs(res[1][0][regular] - res[2][0][regular])) < 1e-9
+    assert np.array_equal(res[1][1][regular], res[2][1][regular])
+    assert np.max(np.abs(res[1][0][regular] - ref["eGW"][regular])) < MEV
+
+
 @pytest.mark.parametrize("ta,tb,m,n,k", [("T", "N", 4000, 20, 150), ("N", "N", 70, 33, 45),
                                          ("N", "T", 129, 17, 3), ("T", "T", 300, 150, 40),
                                          ("N", "N", 200, 20, 5000), ("N", "T", 257, 300, 128)])
