@@ -368,7 +368,9 @@ int qk_RGW_self_energy_diag_noalloc_dev(double eta, int nBas, int nOrb, int nC, 
  * per size bucket floor(log2(size)): "bf16x3_chunk" (k blocks per TMEM chunk of the BF16x3 GEMM,
  * size = K), "splitk_mult" (split-K target CTAs per SM of the DMMA GEMM, size = K),
  * "sigma_chunks" (m chunks of the pole sweeps per SM, size = nS), "sytrd_grid" (quarters of the
- * SMs in the cooperative tridiagonalisation, size = n).  qk_autotune times all candidates on
+ * SMs in the cooperative tridiagonalisation, size = n), "dgemm_path" (1 DFMA, 2 DMMA, size = m n),
+ * "stebz_k" (lanes per eigenvalue in the bisection, size = n), "qp_persist" (mixed-tier Newton:
+ * 1 persistent kernel, 2 per-step sweeps, size = nS).  qk_autotune times all candidates on
  * problems of the given sizes (allocates temporary buffers) and keeps the fastest; the table
  * can be saved to / loaded from a JSON file. */
 int qk_autotune(qk_ctx* ctx, int nOrb, int nS, int flags);
