@@ -807,7 +807,7 @@ def run_profile_case(args):
     ctx = api.Context(0)
     out = {"case": args.profile_case}
     if args.profile_case == "c4":
-        # configuration 4: N=400, nO=40, naux=1200, seed 2 (nS=14400), factorised drivers;
+        # the N=400, nO=40, naux=1200, seed 2 system (nS=14400), factorised drivers;
         # both tiers, Newton and linearised QP, per-stage times and the tier difference
         N, nO, naux = 400, 40, 1200
         nS = nO * (N - nO)

@@ -21,10 +21,10 @@ import math
 
 import numpy as np
 
-CONFIGS = {
+SYSTEMS = {
     # name: (N, nO, naux, seed)
-    "c2_g0w0_n200": (200, 20, 600, 0),
-    "c4_large_n400": (400, 40, 1200, 2),
+    "g0w0_n200_o20_aux600": (200, 20, 600, 0),
+    "g0w0_n400_o40_aux1200": (400, 40, 1200, 2),
 }
 
 
@@ -46,8 +46,8 @@ def gen_system(N: int, nO: int, naux: int, rng: np.random.Generator) -> dict:
     return dict(N=N, nO=nO, naux=naux, L=L, eHF=eHF)
 
 
-def config_system(name: str) -> dict:
-    N, nO, naux, seed = CONFIGS[name]
+def named_system(name: str) -> dict:
+    N, nO, naux, seed = SYSTEMS[name]
     return gen_system(N, nO, naux, np.random.default_rng(seed))
 
 
