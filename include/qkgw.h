@@ -293,6 +293,16 @@ typedef struct {
   double eta;           /* the GW broadening of the static kernels */
 } qk_bse_params;
 
+/* GW/RGW_phACFDT.f90:1-219 (the doACFDT branch of RG0W0.f90:259-261): adiabatic-connection
+ * correlation energy of phBSE@GW, EcAC[2] = (singlet, triplet), by the 21-point Gauss-Legendre
+ * lambda quadrature of RPA/phACFDT_correlation_energy.f90; doXBS rebuilds the screening at
+ * every lambda.  prm: TDA_W, TDA, singlet, triplet, exchange_kernel, eta. */
+int qk_RGW_phACFDT(qk_ctx* ctx, const qk_bse_params* prm, int doXBS, int nBas, int nOrb, int nC,
+                   int nO, int nV, int nR, int nS, const double* ERI, const double* eW,
+                   const double* eGW, double* EcAC);
+int qk_RGW_phACFDT_dev(qk_ctx* ctx, const qk_bse_params* prm, int doXBS, int nOrb, int nC, int nO,
+                       int nR, const double* d_ERI, const double* d_eW, const double* d_eGW,
+                       double* EcAC);
 int qk_RGW_phBSE(qk_ctx* ctx, const qk_bse_params* prm, int nBas, int nOrb, int nC, int nO,
                  int nV, int nR, int nS, const double* ERI, const double* eW, const double* eGW,
                  double* EcBSE, double* OmBSE_singlet, double* OmBSE_triplet);

@@ -420,6 +420,64 @@ def RGW_phBSE(TDA_W, TDA, singlet, triplet, exchange_kernel, eta, nOrb, nC, nO, 
     return out
 
 
+def phACFDT_correlation_energy(ispin, exchange_kernel, nBas, nC, nO, nV, nR, nS, ERI, XpY, XmY):
+    """RPA/phACFDT_correlation_energy.f90:56-80: Ec = tr(X Bp Y^T + Y Bp X^T)
+    + tr(X Ap X^T + Y Ap Y^T) - tr(Ap), Ap(ia,jb) = (1+ds) ERI(i,b,a,j) - dK ERI(i,b,j,a),
+    Bp(ia,jb) = (1+ds) ERI(i,j,a,b) - dK ERI(i,j,b,a), X = (XpY+XmY)/2, Y = (XpY-XmY)/2."""
+    o, v = _ov(nBas, nC, nO, nR)
+    ds = 1.0 if ispin == 1 else -1.0
+    dK = 1.0 if exchange_kernel else 0.0
+    E_ibaj = ERI[np.ix_(o, v, v, o)]                      # [i,b,a,j]
+    E_ibja = ERI[np.ix_(o, v, o, v)]                      # [i,b,j,a]
+    E_ijab = ERI[np.ix_(o, o, v, v)]                      # [i,j,a,b] (also [i,j,b,a] swapped)
+    Ap = ((1.0 + ds) * E_ibaj.transpose(0, 2, 3, 1) - dK * E_ibja.transpose(0, 3, 2, 1)).reshape(nS, nS)
+    Bp = ((1.0 + ds) * E_ijab.transpose(0, 2, 1, 3) - dK * E_ijab.transpose(0, 3, 1, 2)).reshape(nS, nS)
+    X = 0.5 * (XpY + XmY)
+    Y = 0.5 * (XpY - XmY)
+    return (trace_matrix(X @ Bp @ Y.T + Y @ Bp @ X.T) + trace_matrix(X @ Ap @ X.T + Y @ Ap @ Y.T)
+            - trace_matrix(Ap))
+
+
+def RGW_phACFDT(exchange_kernel, doXBS, TDA_W, TDA, singlet, triplet, eta, nBas, nC, nO, nV, nR,
+                nS, ERI, eW, eGW):
+    """Adiabatic-connection correlation energy of phBSE@GW -- GW/RGW_phACFDT.f90:94-210.
+    The 21 Gauss-Legendre nodes/weights on [0, 1] of include/quadrature.h, computed here
+    (r = (1+x)/2, w/2).  Returns [EcAC singlet, EcAC triplet]."""
+    x, wq = np.polynomial.legendre.leggauss(21)
+    rAC, wAC = 0.5 * (1.0 + x), 0.5 * wq
+
+    def kernels(lam):
+        Aw = phRLR_A(1, True, nBas, nC, nO, nV, nR, nS, lam, eW, ERI)
+        Bw = np.zeros((nS, nS)) if TDA_W else phRLR_B(1, True, nBas, nC, nO, nV, nR, nS, lam, ERI)
+        _, OmRPA, XpY, _ = phRLR(TDA_W, nS, Aw, Bw)
+        rho = RGW_excitation_density(nBas, nC, nO, nR, nS, ERI, XpY)
+        KA = RGW_phBSE_static_kernel_A(eta, nBas, nC, nO, nV, nR, nS, lam, OmRPA, rho)
+        KB = np.zeros((nS, nS)) if TDA else RGW_phBSE_static_kernel_B(eta, nBas, nC, nO, nV, nR,
+                                                                        nS, lam, OmRPA, rho)
+        return KA, KB
+
+    KA, KB = kernels(1.0)                                              # :96-103
+    EcAC = [0.0, 0.0]
+    for ispin, on in ((1, singlet), (2, triplet)):
+        if not on:
+            continue
+        Ec = np.zeros(21)
+        for k, lam in enumerate(rAC):                                  # :120, :177
+            if doXBS:
+                KA, KB = kernels(lam)
+            A = phRLR_A(ispin, False, nBas, nC, nO, nV, nR, nS, lam, eGW, ERI) + KA
+            B = (np.zeros((nS, nS)) if TDA
+                 else phRLR_B(ispin, False, nBas, nC, nO, nV, nR, nS, lam, ERI) + KB)
+            _, _, XpY, XmY = phRLR(TDA, nS, A, B)
+            Ec[k] = phACFDT_correlation_energy(ispin, exchange_kernel, nBas, nC, nO, nV, nR, nS,
+                                               ERI, XpY, XmY)
+        e = 0.5 * float(np.dot(wAC, Ec))                               # :151, :208
+        if exchange_kernel:
+            e *= 0.5 if ispin == 1 else 1.5                            # :153, :210
+        EcAC[ispin - 1] = e
+    return EcAC
+
+
 # ---------------------------------------------------------------------------
 # Drivers (src/GW/RG0W0.f90, src/GW/evRGW.f90)
 # ---------------------------------------------------------------------------

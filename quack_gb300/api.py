@@ -355,6 +355,18 @@ class BSEOptions:
                              int(self.exchange_kernel), self.eta)
 
 
+def RGW_phACFDT(opts: BSEOptions, doXBS, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eW, eGW, ctx=None):
+    """GW/RGW_phACFDT.f90: adiabatic-connection correlation energy of phBSE@GW.
+    Returns [EcAC singlet, EcAC triplet]."""
+    c = _ctx(ctx)
+    ERI, eW, eGW = _f(ERI), _f(eW), _f(eGW)
+    ec = (C.c_double * 2)()
+    prm = opts.c()
+    c.check(lib().qk_RGW_phACFDT(c.handle, C.byref(prm), int(bool(doXBS)), nBas, nOrb, nC, nO, nV,
+                                 nR, nS, _ptr(ERI), _ptr(eW), _ptr(eGW), ec))
+    return [ec[0], ec[1]]
+
+
 def RGW_phBSE(opts: BSEOptions, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eW, eGW, ctx=None):
     """GW/RGW_phBSE.f90 (static kernel).  Returns dict(EcBSE=[singlet, triplet], Om_singlet,
     Om_triplet) -- the excitation energies of the manifolds asked for (else None)."""

@@ -1464,6 +1464,41 @@ int qk_RGW_phBSE_dev(qk_ctx* ctx, const qk_bse_params* prm, int nOrb, int nC, in
   return end(ctx, st);
 }
 
+int qk_RGW_phACFDT_dev(qk_ctx* ctx, const qk_bse_params* prm, int doXBS, int nOrb, int nC, int nO,
+                       int nR, const double* d_ERI, const double* d_eW, const double* d_eGW,
+                       double* EcAC) {
+  QK_TRY(begin(ctx));
+  if (!prm || !d_ERI || !d_eW || !d_eGW || !EcAC)
+    return qk_fail(ctx, QK_ERR_ARG, "inputs and EcAC required");
+  Dims d;
+  const int nS = (nO - nC) * (nOrb - nO - nR);
+  QK_TRY(check_dims(ctx, nOrb, nOrb, nC, nO, nOrb - nO, nR, nS, &d));
+  const int st = qk_bse_acfdt_dev(ctx, prm->exchange_kernel, doXBS, prm->TDA_W, prm->TDA,
+                                  prm->singlet, prm->triplet, prm->eta, nOrb, nC, nO, nR, d_ERI,
+                                  d_eW, d_eGW, EcAC);
+  return end(ctx, st);
+}
+
+int qk_RGW_phACFDT(qk_ctx* ctx, const qk_bse_params* prm, int doXBS, int nBas, int nOrb, int nC,
+                   int nO, int nV, int nR, int nS, const double* ERI, const double* eW,
+                   const double* eGW, double* EcAC) {
+  QK_TRY(begin(ctx));
+  if (!prm || !ERI || !eW || !eGW || !EcAC) return qk_fail(ctx, QK_ERR_ARG, "inputs required");
+  Dims d;
+  QK_TRY(check_dims(ctx, nBas, nOrb, nC, nO, nV, nR, nS, &d));
+  const size_t N = nOrb, N4 = N * N * N * N;
+  double *dERI, *io;
+  QK_TRY(qk_wst(ctx, W_ERI, N4, &dERI));
+  QK_TRY(qk_wst(ctx, W_HOST_B, 2 * N + 16, &io));
+  QK_TRY(h2d(ctx, dERI, ERI, N4 * 8));
+  QK_TRY(h2d(ctx, io, eW, N * 8));
+  QK_TRY(h2d(ctx, io + N, eGW, N * 8));
+  const int st = qk_bse_acfdt_dev(ctx, prm->exchange_kernel, doXBS, prm->TDA_W, prm->TDA,
+                                  prm->singlet, prm->triplet, prm->eta, nOrb, nC, nO, nR, dERI,
+                                  io, io + N, EcAC);
+  return end(ctx, st);
+}
+
 int qk_RGW_phBSE(qk_ctx* ctx, const qk_bse_params* prm, int nBas, int nOrb, int nC, int nO,
                  int nV, int nR, int nS, const double* ERI, const double* eW, const double* eGW,
                  double* EcBSE, double* OmBSE_singlet, double* OmBSE_triplet) {

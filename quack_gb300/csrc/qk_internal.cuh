@@ -38,7 +38,7 @@ enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
   W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_TMAT2, W_RHO32, W_OMF, W_TFAC, W_STEBZ,
   W_QUAD, W_QLT, W_QPV, W_QL, W_QX, W_QQ, W_QD, W_BSE, W_BSEU, W_BSER, W_BSEK, W_ERIPACK,
-  W_QSR1, W_QSR2, W_QSJK, W_QSMAT, W_QSDIIS, W_QSIN, W_RHO32T, W_QPQUEUE, W_NUMBUF
+  W_QSR1, W_QSR2, W_QSJK, W_QSMAT, W_QSDIIS, W_QSIN, W_RHO32T, W_QPQUEUE, W_ACF, W_NUMBUF
 };
 
 struct qk_ctx {
@@ -202,6 +202,11 @@ int qk_qs_energy(qk_ctx* ctx, int N, const double* P, const double* T, const dou
 
 // static phBSE@GW excitation energies (k_bse.cu; GW/RGW_phBSE.f90:83-190): device ERI (full
 // N^4), eW (screening energies), eGW; EcBSE[2] on the host; OmS / OmT (device, nS) optional.
+// adiabatic-connection (ACFDT) correlation energy of phBSE@GW (k_bse.cu; GW/RGW_phACFDT.f90:1-219):
+// EcAC[2] (singlet, triplet) on the host
+int qk_bse_acfdt_dev(qk_ctx* ctx, int exchange_kernel, int doXBS, int TDA_W, int TDA, int singlet,
+                     int triplet, double eta, int N, int nC, int nO, int nR, const double* ERI,
+                     const double* eW, const double* eGW, double* hEcAC);
 int qk_bse_dev(qk_ctx* ctx, int TDA_W, int TDA, int singlet, int triplet, int exchange_kernel,
                double eta, int N, int nC, int nO, int nR, const double* ERI, const double* eW,
                const double* eGW, double* hEcBSE, double* OmS, double* OmT);

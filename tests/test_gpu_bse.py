@@ -64,3 +64,25 @@ def test_phrlr_tda_matches_oracle(ctx, ispin):
     ov = np.abs(np.sum(XpY * XpY0, axis=1))
     assert np.all(np.abs(ov - 1.0) < 1e-8)
     assert np.array_equal(XpY, XmY)
+
+
+@pytest.mark.parametrize("TDA_W,TDA,xk,doXBS,eta", [(False, False, False, False, 0.0),
+                                                    (False, True, True, False, 0.0),
+                                                    (True, False, True, False, 0.05),
+                                                    (False, False, False, True, 0.0)])
+def test_phacfdt_matches_oracle(ctx, TDA_W, TDA, xk, doXBS, eta):
+    """Adiabatic-connection correlation energy of phBSE@GW (GW/RGW_phACFDT.f90): singlet and
+    triplet, full and Tamm-Dancoff BSE, TDA screening, the exchange kernel and the scaled
+    screening (doXBS), against the oracle's 21-node quadrature."""
+    N, nO, nC, nR, naux, seed = 16, 3, 0, 0, 32, 47
+    s = synth.small_system(N, nO, naux, seed)
+    E = synth.eri_phys_numpy(s["L"])
+    nS = (nO - nC) * (N - nO - nR)
+    rng = np.random.default_rng(seed)
+    eGW = s["eHF"] + 0.02 * rng.standard_normal(N)
+    ref = O.RGW_phACFDT(xk, doXBS, TDA_W, TDA, True, True, eta, N, nC, nO, N - nO, nR, nS, E,
+                        s["eHF"], eGW)
+    got = api.RGW_phACFDT(api.BSEOptions(TDA_W=TDA_W, TDA=TDA, exchange_kernel=xk, eta=eta),
+                          doXBS, N, N, nC, nO, N - nO, nR, nS, E, s["eHF"], eGW, ctx=ctx)
+    for k in range(2):
+        assert abs(got[k] - ref[k]) < 1e-8 * max(1.0, abs(ref[k])), (k, got, ref)

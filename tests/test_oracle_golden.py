@@ -249,3 +249,36 @@ def test_qsgw_oracle_converges_on_h4():
     assert abs(r["EqsGW"] - sy["ERHF"]) < 1e-2
     c = r["c"]
     assert np.max(np.abs(c.T @ sy["S"] @ c - np.eye(n))) < 1e-10
+
+
+def test_acfdt_correlation_energy_matrices_follow_the_loops():
+    """The vectorised Ap/Bp of phACFDT_correlation_energy against the reference's index loops
+    (RPA/phACFDT_correlation_energy.f90:56-70) on a tensor without symmetry."""
+    rng = np.random.default_rng(3)
+    N, nC, nO, nR = 7, 1, 3, 1
+    nV = N - nO
+    nS = (nO - nC) * (N - nO - nR)
+    E = rng.standard_normal((N,) * 4)
+    XpY = rng.standard_normal((nS, nS))
+    XmY = rng.standard_normal((nS, nS))
+    for ispin in (1, 2):
+        for xk in (False, True):
+            ds = 1.0 if ispin == 1 else -1.0
+            dK = 1.0 if xk else 0.0
+            Ap = np.zeros((nS, nS))
+            Bp = np.zeros((nS, nS))
+            ia = 0
+            for i in range(nC, nO):
+                for a in range(nO, N - nR):
+                    jb = 0
+                    for j in range(nC, nO):
+                        for b in range(nO, N - nR):
+                            Ap[ia, jb] = (1 + ds) * E[i, b, a, j] - dK * E[i, b, j, a]
+                            Bp[ia, jb] = (1 + ds) * E[i, j, a, b] - dK * E[i, j, b, a]
+                            jb += 1
+                    ia += 1
+            X, Y = 0.5 * (XpY + XmY), 0.5 * (XpY - XmY)
+            ref = (np.trace(X @ Bp @ Y.T + Y @ Bp @ X.T) + np.trace(X @ Ap @ X.T + Y @ Ap @ Y.T)
+                   - np.trace(Ap))
+            got = O.phACFDT_correlation_energy(ispin, xk, N, nC, nO, nV, nR, nS, E, XpY, XmY)
+            assert abs(got - ref) < 1e-10 * max(1.0, abs(ref))
