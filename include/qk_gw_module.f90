@@ -25,6 +25,15 @@ module qk_gw_module
     integer(c_int)    :: qp_guess
   end type qk_gw_params
 
+  type, bind(C) :: qk_bse_params
+    integer(c_int)    :: TDA_W
+    integer(c_int)    :: TDA
+    integer(c_int)    :: singlet
+    integer(c_int)    :: triplet
+    integer(c_int)    :: exchange_kernel
+    real(c_double)    :: eta
+  end type qk_bse_params
+
   integer(c_int), parameter :: QK_OK = 0, QK_ERR_NO_CONV = 5
   integer(c_int), parameter :: QK_PREC_FP64 = 0, QK_PREC_BF16X3 = 1
 
@@ -136,6 +145,26 @@ module qk_gw_module
       real(c_double), intent(out)   :: eGW(nOrb), SigC(nOrb), Z(nOrb), EcRPA, EcGM, Conv
       integer(c_int), intent(out)   :: nSCF
     end function qk_evRGW
+
+    integer(c_int) function qk_RGW_phBSE(ctx, prm, nBas, nOrb, nC, nO, nV, nR, nS, ERI, eW, eGW, &
+        EcBSE, OmS, OmT) bind(C, name="qk_RGW_phBSE")
+      import c_int, c_ptr, c_double, qk_bse_params
+      type(c_ptr), value            :: ctx
+      type(qk_bse_params), intent(in) :: prm
+      integer(c_int), value         :: nBas, nOrb, nC, nO, nV, nR, nS
+      real(c_double), intent(in)    :: ERI(nOrb,nOrb,nOrb,nOrb), eW(nOrb), eGW(nOrb)
+      real(c_double), intent(out)   :: EcBSE(2), OmS(nS), OmT(nS)
+    end function qk_RGW_phBSE
+
+    integer(c_int) function qk_RGW_phACFDT(ctx, prm, doXBS, nBas, nOrb, nC, nO, nV, nR, nS, ERI, &
+        eW, eGW, EcAC) bind(C, name="qk_RGW_phACFDT")
+      import c_int, c_ptr, c_double, qk_bse_params
+      type(c_ptr), value            :: ctx
+      type(qk_bse_params), intent(in) :: prm
+      integer(c_int), value         :: doXBS, nBas, nOrb, nC, nO, nV, nR, nS
+      real(c_double), intent(in)    :: ERI(nOrb,nOrb,nOrb,nOrb), eW(nOrb), eGW(nOrb)
+      real(c_double), intent(out)   :: EcAC(2)
+    end function qk_RGW_phACFDT
 
     integer(c_int) function qk_RGW_self_energy(ctx, eta, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, &
         rho, EcGM, SigC, Z) bind(C, name="qk_RGW_self_energy")
