@@ -282,3 +282,30 @@ def test_acfdt_correlation_energy_matrices_follow_the_loops():
                    - np.trace(Ap))
             got = O.phACFDT_correlation_energy(ispin, xk, N, nC, nO, nV, nR, nS, E, XpY, XmY)
             assert abs(got - ref) < 1e-10 * max(1.0, abs(ref))
+
+
+def test_hchain_integrals_are_those_of_real_gaussians():
+    """The closed-form s-Gaussian integrals of the H-chain inputs: normalised primitives
+    (S_ii = 1), symmetric positive-definite S, T, the 8-fold permutational symmetry of the
+    physicist ERI tensor, the positive-semidefinite (pq|rs) supermatrix, the nuclear repulsion,
+    and the one-centre closed forms."""
+    from quack_gb300 import synth
+    S, T, V, E, ENuc = synth.hchain_integrals(4, 1.6)
+    n = S.shape[0]
+    assert np.allclose(np.diag(S), 1.0, atol=1e-14)
+    for M in (S, T, V):
+        assert np.max(np.abs(M - M.T)) < 1e-14
+    assert np.linalg.eigvalsh(S).min() > 0 and np.linalg.eigvalsh(T).min() > 0
+    for perm in ((1, 0, 3, 2), (2, 1, 0, 3), (0, 3, 2, 1), (2, 3, 0, 1)):
+        assert np.max(np.abs(E - E.transpose(perm))) < 1e-13
+    chem = E.transpose(0, 2, 1, 3).reshape(n * n, n * n)
+    assert np.linalg.eigvalsh(chem).min() > -1e-12
+    assert abs(ENuc - sum(1.0 / (1.6 * abs(i - j)) for i in range(4) for j in range(i))) < 1e-14
+    # one normalised primitive (the partner atom 50 bohr away): <aa|aa> by the one-centre
+    # formula 2 pi^2.5 / (p q sqrt(p + q)) N^4 with p = q = 2a, and <a|T|a> = 3a/2
+    a = synth.HCHAIN_EXPONENTS[0]
+    S1, T1, V1, E1, _ = synth.hchain_integrals(2, 50.0, exponents=(a,))
+    nrm = (2 * a / np.pi) ** 0.75
+    p = 2 * a
+    assert abs(E1[0, 0, 0, 0] - 2 * np.pi ** 2.5 / (p * p * np.sqrt(2 * p)) * nrm ** 4) < 1e-12
+    assert abs(T1[0, 0] - 1.5 * a) < 1e-12
