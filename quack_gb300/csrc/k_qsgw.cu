@@ -10,7 +10,8 @@
 //     (ia|jb) too), so the driver runs the four quarter transformations with the occupied and
 //     virtual coefficient blocks in the positions that shrink the tensor first:
 //         <j p|b q> = sum c(mu,j) c(la,p) c(nu,b) c(si,q) <mu la|nu si>
-//     (4 N^4 no + 4 N^3 no nv flop), and the kernels below permute it into the slab layout and
+//     (4 N^4 no + 4 N^3 no nv flop; FP64 GEMMs, double-float ones in the mixed tier), and the
+//     kernels below permute it into the slab layout and
 //     the Casida K -- <pj|qb> = <jp|bq> is the particle-exchange symmetry of any two-electron
 //     integral, (ia|jb) = <ji|ba> with real orbitals;
 //   * the full correlation self-energy (RGW_self_energy.f90:40-84):
