@@ -44,6 +44,25 @@ def test_python_api_binds_every_symbol(libpath):
         getattr(L, s)
 
 
+def test_fortran_module_binds_declared_symbols_with_their_arity(libpath):
+    """Every bind(C, name=...) interface of include/qk_gw_module.f90 names a symbol that the C
+    header declares and the library exports, with the same number of arguments."""
+    f90 = open(os.path.join(ROOT, "include", "qk_gw_module.f90")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", open(HDR).read(), flags=re.S)
+    lib = ctypes.CDLL(libpath)
+    found = re.findall(r"function\s+(\w+)\s*\(([^)]*)\)\s*(?:&\s*)?bind\(C,\s*name=\"(\w+)\"\)",
+                       f90.replace("&\n", " "))
+    assert len(found) >= 10
+    for fname, args, cname in found:
+        assert fname == cname
+        assert hasattr(lib, cname), cname
+        m = re.search(r"\b" + cname + r"\s*\(([^;]*)\);", hdr)
+        assert m, cname
+        n_c = len([x for x in m.group(1).split(",") if x.strip()])
+        n_f = len([x for x in args.split(",") if x.strip()])
+        assert n_c == n_f, (cname, n_c, n_f)
+
+
 def test_init_without_gpu_reports_no_device(libpath):
     import torch
     if torch.cuda.is_available():
