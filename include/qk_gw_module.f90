@@ -102,6 +102,36 @@ module qk_gw_module
       real(c_double), intent(out)   :: EcGM, Sig(nBas), Z(nBas)
     end function qk_RGW_self_energy_diag
 
+    integer(c_int) function qk_RGW_SRG_self_energy_diag(ctx, flow, nBas, nOrb, nC, nO, nV, nR, nS, e, &
+        Om, rho, EcGM, Sig, Z) bind(C, name="qk_RGW_SRG_self_energy_diag")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      real(c_double), value         :: flow
+      integer(c_int), value         :: nBas, nOrb, nC, nO, nV, nR, nS
+      real(c_double), intent(in)    :: e(nBas), Om(nS), rho(nBas,nBas,nS)
+      real(c_double), intent(out)   :: EcGM, Sig(nBas), Z(nBas)
+    end function qk_RGW_SRG_self_energy_diag
+
+    ! utils/DIIS_extrapolation.f90 (error and e histories updated in place)
+    integer(c_int) function qk_DIIS_extrapolation(ctx, rcond, n_err, n_e, n_diis, error, e, &
+        error_in, e_inout) bind(C, name="qk_DIIS_extrapolation")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      real(c_double), intent(out)   :: rcond
+      integer(c_int), value         :: n_err, n_e, n_diis
+      real(c_double), intent(inout) :: error(n_err,*), e(n_e,*)
+      real(c_double), intent(in)    :: error_in(n_err)
+      real(c_double), intent(inout) :: e_inout(n_e)
+    end function qk_DIIS_extrapolation
+
+    ! precision tier of the stage-level drop-ins (QK_PREC_FP64 or QK_PREC_BF16X3)
+    integer(c_int) function qk_set_stage_precision(ctx, precision) &
+        bind(C, name="qk_set_stage_precision")
+      import c_int, c_ptr
+      type(c_ptr), value            :: ctx
+      integer(c_int), value         :: precision
+    end function qk_set_stage_precision
+
     ! GW/RGW_QP_graph.f90 (Z is in/out, as in the reference)
     integer(c_int) function qk_RGW_QP_graph(ctx, doSRG, eta, flow, nBas, nC, nO, nV, nR, nS, eHF, Om, rho, &
         eGWlin, eOld, eGW, Z) bind(C, name="qk_RGW_QP_graph")
@@ -175,6 +205,16 @@ module qk_gw_module
       real(c_double), intent(in)    :: e(nOrb), Om(nS), rho(nOrb,nOrb,nS)
       real(c_double), intent(out)   :: EcGM, SigC(nOrb,nOrb), Z(nOrb)
     end function qk_RGW_self_energy
+
+    integer(c_int) function qk_RGW_SRG_self_energy(ctx, flow, nBas, nOrb, nC, nO, nV, nR, nS, e, Om, &
+        rho, EcGM, SigC, Z) bind(C, name="qk_RGW_SRG_self_energy")
+      import c_int, c_ptr, c_double
+      type(c_ptr), value            :: ctx
+      real(c_double), value         :: flow
+      integer(c_int), value         :: nBas, nOrb, nC, nO, nV, nR, nS
+      real(c_double), intent(in)    :: e(nOrb), Om(nS), rho(nOrb,nOrb,nS)
+      real(c_double), intent(out)   :: EcGM, SigC(nOrb,nOrb), Z(nOrb)
+    end function qk_RGW_SRG_self_energy
 
     integer(c_int) function qk_Hartree_matrix_AO_basis(ctx, nBas, P, ERI, H) &
         bind(C, name="qk_Hartree_matrix_AO_basis")
