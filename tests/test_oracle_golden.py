@@ -309,3 +309,28 @@ def test_hchain_integrals_are_those_of_real_gaussians():
     p = 2 * a
     assert abs(E1[0, 0, 0, 0] - 2 * np.pi ** 2.5 / (p * p * np.sqrt(2 * p)) * nrm ** 4) < 1e-12
     assert abs(T1[0, 0] - 1.5 * a) < 1e-12
+
+
+def test_qsgw_oracle_invariances():
+    """Properties of the qsGW restatement: the result does not depend on the signs of the
+    starting orbitals, nor on which orthogonaliser X spans the basis (symmetric S^-1/2 or
+    canonical U s^-1/2), and the converged Fock matrix commutes with P S to the threshold."""
+    from quack_gb300 import synth
+    sy = synth.hchain_system(4)
+    n, nO = sy["nBas"], sy["nO"]
+    args = (n, n, 0, nO, n - nO, 0, nO * (n - nO))
+
+    def run(c, X):
+        return O.qsRGW(64, 1e-7, 5, 0.05, False, *args, sy["eHF"], c, sy["PHF"], sy["S"], sy["T"],
+                       sy["V"], sy["Hc"], X, sy["ERI_AO"])
+
+    ref = run(sy["cHF"], sy["X"])
+    signs = np.where(np.arange(n) % 2 == 0, 1.0, -1.0)
+    flipped = run(sy["cHF"] * signs[None, :], sy["X"])
+    s, U = np.linalg.eigh(sy["S"])
+    canon = run(sy["cHF"], U * s ** -0.5)
+    for r in (flipped, canon):
+        assert np.max(np.abs(r["eGW"] - ref["eGW"])) < 1e-7
+        assert np.max(np.abs(r["P"] - ref["P"])) < 1e-6
+        assert abs(r["EqsGW"] - ref["EqsGW"]) < 1e-8
+    assert not ref["failed"] and ref["Conv"] <= 1e-7
