@@ -256,7 +256,8 @@ int qk_get_features(const qk_ctx* ctx, float* host, int n);
  * 1 = evGW.  The systems are spread over n_workers CUDA streams (one host thread each), largest
  * first.  Per-system results: status[i] (QK_OK, QK_ERR_NO_CONV, ...), EcRPA[i], nSCF[i] (host
  * arrays); a failing system does not stop the others.  Returns the worst status other than
- * QK_ERR_NO_CONV. */
+ * QK_ERR_NO_CONV.  The context's tuned launch parameters and attached QP model (qk_set_qp_model,
+ * for prm->qp_guess = 1) apply to every system. */
 typedef struct qk_sys_desc {
   int nOrb, nC, nO, nR, naux;
   long long offset_L;

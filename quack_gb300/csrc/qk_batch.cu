@@ -8,6 +8,7 @@
 // A failing or non-converged system is recorded in its status word and does not stop the batch.
 #include <algorithm>
 #include <atomic>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -50,8 +51,13 @@ extern "C" int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int metho
   // starts after the caller's default-stream work (the packed inputs)
   const int share = ctx->num_sms / n_workers > 16 ? ctx->num_sms / n_workers : 16;
   for (int wi = 0; wi < n_workers; ++wi) {
-    ctx->workers[wi]->sytrd_max_ctas = share;
-    QK_TRY(qk_order_after_default(ctx->workers[wi]));
+    qk_ctx* w = ctx->workers[wi];
+    w->sytrd_max_ctas = share;
+    // the caller's tuned launch parameters and learned QP model apply to every worker (the
+    // model is only read: its inference writes the worker's own workspace)
+    std::memcpy(w->tune, ctx->tune, sizeof(ctx->tune));
+    w->mlp = ctx->mlp;
+    QK_TRY(qk_order_after_default(w));
   }
   std::vector<Item> order(nsys);
   for (int i = 0; i < nsys; ++i) {
