@@ -91,3 +91,34 @@ def test_learned_guess_saves_newton_evaluations(ctx):
     assert ev_g < ev_hf
     assert ev_g < ev_ref
     assert n_same >= 0.95 * n_conv
+
+
+def test_batched_driver_uses_the_attached_model(ctx):
+    """The batched driver's worker contexts take the caller's learned model: a batched G0W0 with
+    qp_guess = 1 succeeds for every system and gives the per-system guess-path energies."""
+    import torch
+    from quack_gb300 import api
+    rng = np.random.default_rng(31)
+    train_sys = [synth.gen_system(N, synth.n_occ(N), 3 * N, rng) for N in (24, 28, 32, 30)]
+    test_sys = [synth.gen_system(N, synth.n_occ(N), 3 * N, rng) for N in (26, 34, 29)]
+    X, T = learned.collect(ctx, train_sys)
+    m = learned.QPModel(ctx, seed=9)
+    learned.train(m, X, T, epochs=60, batch=128, lr=3e-3)
+    ctx.set_qp_model(m)
+    try:
+        desc, Lf, Ef = api.pack_systems(test_sys)
+        dL = torch.from_numpy(np.ascontiguousarray(Lf)).cuda()
+        dE = torch.from_numpy(np.ascontiguousarray(Ef)).cuda()
+        dG = torch.zeros_like(dE)
+        opts = api.GWOptions(qp_guess=1)
+        r = api.gw_batch_L_dev(opts, 0, desc, dL.data_ptr(), dE.data_ptr(), dG.data_ptr(),
+                               n_workers=2, ctx=ctx)
+        assert r["rc"] == api.QK_OK, (r["error"], r["status"])
+        eG = dG.cpu().numpy()
+        for i, s in enumerate(test_sys):
+            one = learned.run_g0w0_L(ctx, s, opts)
+            got = eG[desc[i].offset_e:desc[i].offset_e + s["N"]]
+            conv = np.asarray(one["iters"]) < 16
+            assert np.max(np.abs(got[conv] - one["eGW"][conv])) < 1e-8, i
+    finally:
+        ctx.set_qp_model(None)
