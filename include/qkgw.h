@@ -366,9 +366,11 @@ int qk_gemm_bf16x3_ex_dev(qk_ctx* ctx, char transa, char transb, int m, int n, i
  * e(nBas), Om(nS), rho(nBas,nBas,nS) into Sig(nBas), Z(nBas), EcGM(1), enqueued on `stream`
  * (a cudaStream_t, 0 = default stream) and synchronised before returning.  It needs no qk_ctx and
  * calls no cudaMalloc/cudaFree.  Scratch is a static 3 MiB device array, so nBas <= 1024
- * (QK_ERR_ARG beyond that).  The first call on each device (made current) resolves the array's
- * device address; make it before any stream capture.  Calls share the array: calls that overlap
- * on the GPU race and must be serialised by the caller. */
+ * (QK_ERR_ARG beyond that).  QuAcK's counts are checked: nV = nBas - nO (frozen virtuals
+ * included) and nO <= nOrb <= nBas, else QK_ERR_ARG.  Each call resolves the array's device
+ * address on the current device (no allocation), so it stays valid across cudaDeviceReset.
+ * Calls share the array: calls that overlap on the GPU race and must be serialised by the
+ * caller. */
 int qk_RGW_self_energy_diag_noalloc_dev(double eta, int nBas, int nOrb, int nC, int nO, int nV,
                                         int nR, int nS, const double* d_e, const double* d_Om,
                                         const double* d_rho, double* d_EcGM, double* d_Sig,
@@ -396,6 +398,9 @@ void* qk_stream(const qk_ctx* ctx);
 /* Measured FP64 peak of this GPU: back-to-back DMMA (mma.sync.m8n8k4.f64) and DFMA in registers,
  * TFLOP/s. */
 int qk_probe_fp64_peak(qk_ctx* ctx, double* tflops_dmma, double* tflops_dfma);
+/* Measured FP32 FMA peak of this GPU (back-to-back FFMA in registers), TFLOP/s: the roofline of
+ * the mixed tier's FP32-product stages. */
+int qk_probe_fp32_peak(qk_ctx* ctx, double* tflops_ffma);
 
 #ifdef __cplusplus
 }

@@ -12,12 +12,11 @@
 // library until the process exits.  Limits that follow from it: nBas <= 1024 orbitals, and
 // at most 128 excitation chunks (chosen internally).
 //
-// Set-up: the first call on each device (with that device current) looks up the array's
-// device address with cudaGetSymbolAddress and caches it; make that first call before any
-// stream capture.  All calls share the one array and it keeps the last call's contents, so
-// calls whose kernels overlap on the GPU (different streams or host threads on one device)
-// race with each other; serialise them.
-#include <mutex>
+// Set-up: every call looks up the array's device address with cudaGetSymbolAddress on the
+// device that is current at the call (a host-side lookup that allocates nothing), so the address
+// stays right after cudaDeviceReset or a context change.  All calls share the one array and it
+// keeps the last call's contents, so calls whose kernels overlap on the GPU (different streams
+// or host threads on one device) race with each other; serialise them.
 #include "qk_internal.cuh"
 
 #define QK_NOALLOC_MAX_N 1024
@@ -29,10 +28,6 @@ static __device__ __align__(256) double qk_noalloc_scratch[QK_NOALLOC_SCRATCH_DO
 namespace {
 
 constexpr int NA_WARPS = 8;
-constexpr int NA_MAX_DEV = 64;
-
-std::mutex g_mu;
-double* g_scratch[NA_MAX_DEV] = {};
 
 // same pole sums as RGW_self_energy_diag.f90:44-84 (one thread per orbital p, warps split m),
 // partials per (m chunk, p) written to part[chunk*N + p] (+ stride for dSig and the occupied part)
@@ -107,17 +102,12 @@ __global__ void k_sigma_final_noalloc(int N, int nC, int nO, int nR, int nchunks
   if (threadIdx.x == 0) *EcGM = -2.0 * gm;
 }
 
-// once per device: device address of the scratch array (the host-side symbol is only a stand-in)
+// device address of the scratch array on the current device (the host-side symbol is only a
+// stand-in); resolved on every call, since a reset or a new context may move the module
 int scratch_for_current_device(double** out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEV) return QK_ERR_CUDA;
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch[dev]) {
-    void* ptr = nullptr;
-    if (cudaGetSymbolAddress(&ptr, qk_noalloc_scratch) != cudaSuccess || !ptr) return QK_ERR_CUDA;
-    g_scratch[dev] = (double*)ptr;
-  }
-  *out = g_scratch[dev];
+  void* ptr = nullptr;
+  if (cudaGetSymbolAddress(&ptr, qk_noalloc_scratch) != cudaSuccess || !ptr) return QK_ERR_CUDA;
+  *out = (double*)ptr;
   return QK_OK;
 }
 
@@ -128,19 +118,19 @@ extern "C" int qk_RGW_self_energy_diag_noalloc_dev(double eta, int nBas, int nOr
                                                    const double* d_Om, const double* d_rho,
                                                    double* d_EcGM, double* d_Sig, double* d_Z,
                                                    void* stream) {
-  (void)nOrb;
-  (void)nV;
   const int N = nBas;
   const int no = nO - nC, nv = N - nO - nR;
   if (N <= 0 || nC < 0 || nR < 0 || no <= 0 || nv <= 0 || (long long)no * nv != nS)
     return QK_ERR_ARG;
+  // QuAcK's counts: nV = nBas - nO (frozen virtuals included), nO <= nOrb <= nBas
+  if (nV != N - nO || nOrb < nO || nOrb > N) return QK_ERR_ARG;
   if (N > QK_NOALLOC_MAX_N) return QK_ERR_ARG;  // beyond the static scratch (nBas <= 1024)
   if (!d_e || !d_Om || !d_rho || !d_EcGM || !d_Sig || !d_Z) return QK_ERR_ARG;
   double* part = nullptr;
   int st = scratch_for_current_device(&part);
   if (st != QK_OK) return st;
   int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
+  if (cudaGetDevice(&dev) != cudaSuccess) return QK_ERR_CUDA;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return QK_ERR_CUDA;
   const int nact = N - nR - nC;
@@ -156,11 +146,27 @@ extern "C" int qk_RGW_self_energy_diag_noalloc_dev(double eta, int nBas, int nOr
   // the array keeps the previous call's partial sums: clear the part this call reads
   if (cudaMemsetAsync(part, 0, sizeof(double) * 3 * (size_t)nchunks * N, s) != cudaSuccess)
     return QK_ERR_CUDA;
-  k_sigma_partial_noalloc<<<dim3(ptiles, nchunks), NA_WARPS * 32, N * sizeof(double), s>>>(
-      N, nC, nO, nR, nS, nchunks, mper, eta, d_e, d_Om, d_rho, part);
-  if (cudaGetLastError() != cudaSuccess) return QK_ERR_CUDA;
-  k_sigma_final_noalloc<<<1, 1024, 0, s>>>(N, nC, nO, nR, nchunks, part, d_Sig, d_Z, d_EcGM);
-  if (cudaGetLastError() != cudaSuccess) return QK_ERR_CUDA;
+  // launch statuses are taken from the launches themselves, so an earlier error left by the
+  // caller's own work is neither reported as this call's nor cleared
+  {
+    int a0 = N, a1 = nC, a2 = nO, a3 = nR, a4 = nS, a5 = nchunks, a6 = mper;
+    double a7 = eta;
+    const double *p8 = d_e, *p9 = d_Om, *p10 = d_rho;
+    double* p11 = part;
+    void* args[] = {&a0, &a1, &a2, &a3, &a4, &a5, &a6, &a7, &p8, &p9, &p10, &p11};
+    if (cudaLaunchKernel((const void*)k_sigma_partial_noalloc, dim3(ptiles, nchunks),
+                         dim3(NA_WARPS * 32), args, N * sizeof(double), s) != cudaSuccess)
+      return QK_ERR_CUDA;
+  }
+  {
+    int a0 = N, a1 = nC, a2 = nO, a3 = nR, a4 = nchunks;
+    const double* p5 = part;
+    double *p6 = d_Sig, *p7 = d_Z, *p8 = d_EcGM;
+    void* args[] = {&a0, &a1, &a2, &a3, &a4, &p5, &p6, &p7, &p8};
+    if (cudaLaunchKernel((const void*)k_sigma_final_noalloc, dim3(1), dim3(1024), args, 0, s) !=
+        cudaSuccess)
+      return QK_ERR_CUDA;
+  }
   if (cudaStreamSynchronize(s) != cudaSuccess) return QK_ERR_CUDA;
   return QK_OK;
 }
