@@ -7,7 +7,8 @@
 //      step k+1 on the lower triangle only, so the trailing triangle is streamed once per column
 //      (read+write) and every element costs 4 FMAs (LAPACK's 4/3 n^3 flops); every CTA
 //      recomputes the O(n) vector work redundantly (bitwise identical in all CTAs), leaving
-//      one bounded grid barrier per column.
+//      one bounded grid barrier per column.  The mat-vec's partial sums from different CTAs
+//      meet in exact (order-independent) accumulators, so the result is the same in every run.
 //   2. k_stebz: Sturm-count k-section (K lanes per eigenvalue), full FP64 precision.
 //   3. k_stein: inverse iteration on T - lambda I (tridiagonal GEPP), one thread per cluster of
 //      close eigenvalues, modified Gram-Schmidt inside clusters; eigenvectors written as rows.
@@ -61,6 +62,24 @@ __device__ __forceinline__ void tri_block_sum(double v, double* scratch, int cnt
   __syncthreads();
 }
 
+// Order-independent accumulation of the mat-vec partial sums.  Several warps of several CTAs
+// add into each element of p, so plain FP64 atomics would make the result depend on their
+// order.  Each contribution x is instead split into two parts aligned to fixed binary grids
+// (the error-free extraction q = (x + C) - C), and each grid has its own accumulator: every
+// part is a multiple of its grid's spacing and every running sum stays below 2^53 spacings, so
+// all additions are exact and the sums are the same in any order.  The grids come from a bound
+// B >= sum of |x| over all contributions to an element (B = 2 ||A||_F ||u||_2): the first has
+// spacing 2^(E-51) (2^E > B), the second 2^(E-92); the dropped remainder is below 2^(E-93) per
+// contribution, i.e. 2^-80 B for up to 2^13 contributions per element (n <= 2^18).
+__device__ __forceinline__ void tri_exact_add(double* b1, double* b2, double x, double c1,
+                                              double c2) {
+  const double q1 = __dsub_rn(__dadd_rn(x, c1), c1);
+  const double r1 = __dsub_rn(x, q1);
+  const double q2 = __dsub_rn(__dadd_rn(r1, c2), c2);
+  atomicAdd(b1, q1);
+  atomicAdd(b2, q2);
+}
+
 struct TriArgs {
   double* A;
   long long lda;
@@ -70,7 +89,8 @@ struct TriArgs {
   double* tau;
   double* V;
   long long ldv;
-  double* pbuf;  // 3*n
+  double* pbuf;  // 6*n: three rotating p vectors, each as two exact accumulators (n + n)
+  double* fslot; // gridDim.x per-CTA partial sums of ||A||_F^2
   double* gvec;  // gridDim.x * 3 * n when vectors do not fit in shared memory
   unsigned* bar;
   int* status;
@@ -79,7 +99,7 @@ struct TriArgs {
 
 __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
   extern __shared__ double sm[];
-  __shared__ double s_pj, s_dj, s_alpha, s_sc[7];
+  __shared__ double s_pj, s_dj, s_alpha, s_sc[9], s_fro;
   const int n = a.n;
   double* ytile = sm;  // one TRI_TC x TRI_TLD tile per warp
   double *vk, *wk, *vk1;
@@ -100,11 +120,37 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
   const int gthread = blockIdx.x * nt + tid, totthreads = gridDim.x * nt;
   double tau_k = 0.0, scal_k = 1.0;
 
+  // ---- ||A||_F (bounds every p element's partial sums): fixed per-thread order, per-CTA slot,
+  // then every CTA adds the slots in the same order, so all CTAs hold the same value ----
+  {
+    double fs = 0.0;
+    for (int c = blockIdx.x; c < n; c += gridDim.x) {
+      const double* col = a.A + a.lda * c;
+      for (int i = c + tid; i < n; i += nt) {
+        const double x = __ldcg(col + i);
+        fs = fma(i == c ? x : x + x, x, fs);
+      }
+    }
+    tri_block_sum(fs, ytile, nt, [&](double t) { __stcg(a.fslot + blockIdx.x, t); });
+    if (!qk_grid_barrier(a.bar, gridDim.x, epoch, a.status)) return;
+    if (tid == 0) {
+      double t = 0.0;
+      for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(a.fslot + b);
+      s_fro = sqrt(t);
+    }
+    __syncthreads();
+  }
+  const double fro = s_fro;
+
   for (int k = -1; k <= n - 2; ++k) {
     // ---- zero the p accumulator used two iterations ahead (triple buffering) ----
     {
       double* pz = a.pbuf + (size_t)((k + 2) % 3) * n;
-      for (int i = gthread; i < n; i += totthreads) __stcg(pz + i, 0.0);
+      double* pz2 = pz + 3 * (size_t)n;
+      for (int i = gthread; i < n; i += totthreads) {
+        __stcg(pz + i, 0.0);
+        __stcg(pz2 + i, 0.0);
+      }
     }
     // ---- small phase (redundant in every CTA): step k's scalars, then v_{k+1} from column j ----
     // FP64 is the scarce resource (one warp instruction per 64 cycles per SM sub-partition), so
@@ -129,7 +175,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
         for (int r = 0; r < 4; ++r) {
           const int i = i0 + r * nt;
           xv[r] = i < n ? __ldcg(a.A + i + a.lda * j) : 0.0;
-          pv[r] = (k >= 0 && i < n) ? __ldcg(p + i) : 0.0;
+          pv[r] = (k >= 0 && i < n) ? __ldcg(p + i) + __ldcg(p + 3 * (size_t)n + i) : 0.0;
           uv[r] = (k >= 0 && i < n) ? vk[i] : 0.0;
         }
 #pragma unroll
@@ -179,7 +225,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       }
       // Householder reflector of the updated column (dlarfg), computed once by thread 0
       tri_block_sum(ss, ytile, cnt, [&](double sigma) {
-        double beta = 0.0, t1 = 0.0, scal = 1.0, inv = 1.0;
+        double beta = 0.0, t1 = 0.0, scal = 1.0, inv = 1.0, unrm = 1.0;
         if (j <= n - 2) {
           const double alpha = s_alpha;
           if (sigma == 0.0) {
@@ -191,12 +237,21 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
             t1 = (beta - alpha) * qk_rcp(beta);
             inv = alpha - beta;
             scal = qk_rcp(inv);
+            unrm = sqrt(fma(inv, inv, sigma));
           }
           vk1[j + 1] = inv;  // u_{j+1} = 1/scal, so that scal * u_{j+1} = 1
         }
         s_sc[3] = beta;
         s_sc[4] = t1;
         s_sc[5] = scal;
+        // grids of the exact accumulators for p~ = A' u: |A'_ic| <= ||A||_F, so the partial
+        // sums of every element are bounded by ||A||_F ||u||_2; twice that absorbs rounding
+        int ex = 0;
+        const double bnd = 2.0 * fro * unrm;
+        if (bnd > 0.0 && bnd <= DBL_MAX) frexp(bnd, &ex);
+        ex = ex < -960 ? -960 : (ex > 1000 ? 1000 : ex);
+        s_sc[7] = ldexp(3.0, ex);
+        s_sc[8] = ldexp(3.0, ex - 41);
       });
       const double dj = s_dj;
       tau1 = s_sc[4];
@@ -220,6 +275,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
     const int mm = n - r0;
     if (mm > 0) {
       double* pnext = a.pbuf + (size_t)((k + 1) % 3) * n;
+      double* pnext2 = pnext + 3 * (size_t)n;
       const bool upd = (k >= 0);
       const bool wantp = (j <= n - 2);
       const int nb = (mm + 31) >> 5;
@@ -244,7 +300,8 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
             ++bi;
           }
           if (bi != cur) {
-            if (cur >= 0 && wantp && rowok) atomicAdd(pnext + i, rowacc);
+            if (cur >= 0 && wantp && rowok)
+              tri_exact_add(pnext + i, pnext2 + i, rowacc, s_sc[7], s_sc[8]);
             cur = bi;
             i = r0 + 32 * bi + lane;
             rowok = i < n;
@@ -289,11 +346,12 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
             for (int r = 0; r < 16; ++r) cs += tp[r] * (rb + r < n ? vk1[rb + r] : 0.0);
             cs += __shfl_xor_sync(0xffffffffu, cs, 16);
             const int c = c0 + u;
-            if (hh == 0 && c < n && c <= r0 + 32 * bi + 31) atomicAdd(pnext + c, cs);
+            if (hh == 0 && c < n && c <= r0 + 32 * bi + 31)
+              tri_exact_add(pnext + c, pnext2 + c, cs, s_sc[7], s_sc[8]);
           }
           __syncwarp();
         }
-        if (wantp && rowok) atomicAdd(pnext + i, rowacc);
+        if (wantp && rowok) tri_exact_add(pnext + i, pnext2 + i, rowacc, s_sc[7], s_sc[8]);
       }
     }
     if (!qk_grid_barrier(a.bar, gridDim.x, epoch, a.status)) return;
@@ -737,18 +795,20 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
                int backtransform) {
   if (n <= 0) return QK_OK;
   const size_t N = (size_t)n;
-  // workspace: V (n*n), small vectors (d, e, tau, e2, pbuf(3n), prep(8))
+  // workspace: V (n*n), small vectors (d, e, tau, e2, pbuf(6n), prep(64), per-CTA slots)
   double *V = nullptr, *tri = nullptr;
+  const size_t tri_len = 10 * N + 64 + 1024;
   QK_TRY(qk_wst(ctx, W_V, N * N, &V));
-  QK_TRY(qk_wst(ctx, W_TRI, 8 * N + 64, &tri));
+  QK_TRY(qk_wst(ctx, W_TRI, tri_len, &tri));
   double* d = tri;
   double* e = tri + N;
   double* tau = tri + 2 * N;
   double* e2 = tri + 3 * N;
   double* pbuf = tri + 4 * N;
-  double* prep = tri + 7 * N;
+  double* prep = tri + 10 * N;
+  double* fslot = tri + 10 * N + 64;
   QK_CK(cudaMemsetAsync(V, 0, N * N * sizeof(double), ctx->stream));
-  QK_CK(cudaMemsetAsync(tri, 0, (8 * N + 64) * sizeof(double), ctx->stream));
+  QK_CK(cudaMemsetAsync(tri, 0, tri_len * sizeof(double), ctx->stream));
   QK_CK(cudaMemsetAsync(ctx->d_bar, 0, 16 * sizeof(unsigned), ctx->stream));
 
   // ---- 1. tridiagonalisation ----
@@ -795,6 +855,7 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
     ta.V = V;
     ta.ldv = n;
     ta.pbuf = pbuf;
+    ta.fslot = fslot;
     ta.gvec = gvec;
     ta.bar = ctx->d_bar;
     ta.status = ctx->d_status;
