@@ -610,6 +610,14 @@ def probe_fp64_peak(ctx=None):
     return a.value, b.value
 
 
+def probe_fp32_peak(ctx=None):
+    """FFMA TFLOP/s measured on this GPU."""
+    c = _ctx(ctx)
+    a = C.c_double()
+    c.check(lib().qk_probe_fp32_peak(c.handle, C.byref(a)))
+    return a.value
+
+
 def RGW_self_energy_diag_noalloc_dev(eta, nBas, nOrb, nC, nO, nV, nR, nS, d_e, d_Om, d_rho,
                                      d_EcGM, d_Sig, d_Z, stream=0):
     """Allocation-free self-energy on caller-owned device buffers (integer device addresses).

@@ -1,5 +1,5 @@
-// k_probe.cu -- FP64 peak probes (register-only DMMA / DFMA loops) used to state the FP64
-// roofline of this GPU, which the HBM/BF16 peak table does not cover.
+// k_probe.cu -- FP64 and FP32 peak probes (register-only DMMA / DFMA / FFMA loops) used to state
+// the FP64 and FP32 rooflines of this GPU, which the HBM/BF16 peak table does not cover.
 #include "qk_internal.cuh"
 
 namespace {
@@ -39,6 +39,21 @@ __global__ void k_probe_dfma(double* out) {
   if (s == 12345.678) out[0] = s;
 }
 
+__global__ void k_probe_ffma(float* out) {
+  float x[16];
+  const float a = 1.0f + 1e-7f * threadIdx.x, b = 1e-7f;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) x[i] = (float)i;
+  for (int it = 0; it < PROBE_ITERS; ++it) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) x[i] = fmaf(x[i], a, b);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) s += x[i];
+  if (s == 12345.678f) out[0] = s;
+}
+
 }  // namespace
 
 extern "C" {
@@ -74,6 +89,30 @@ int qk_probe_fp64_peak(qk_ctx* ctx, double* tflops_dmma, double* tflops_dfma) {
   ctx->launches += 4;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return QK_OK;
+}
+
+int qk_probe_fp32_peak(qk_ctx* ctx, double* tflops_ffma) {
+  if (!ctx || !tflops_ffma) return QK_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  double* dummy = nullptr;
+  QK_TRY(qk_wst(ctx, W_MISC, 16, &dummy));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = ctx->num_sms * 8, threads = 256;
+  float ms = 0.f;
+  k_probe_ffma<<<blocks, threads, 0, ctx->stream>>>((float*)dummy);
+  cudaEventRecord(e0, ctx->stream);
+  k_probe_ffma<<<blocks, threads, 0, ctx->stream>>>((float*)dummy);
+  cudaEventRecord(e1, ctx->stream);
+  const cudaError_t st = cudaEventSynchronize(e1);
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  QK_CK(st);
+  *tflops_ffma = (double)blocks * threads * PROBE_ITERS * 16 * 2.0 / (ms * 1e-3) / 1e12;
+  ctx->launches += 2;
   return QK_OK;
 }
 
