@@ -334,3 +334,57 @@ def test_qsgw_oracle_invariances():
         assert np.max(np.abs(r["P"] - ref["P"])) < 1e-6
         assert abs(r["EqsGW"] - ref["EqsGW"]) < 1e-8
     assert not ref["failed"] and ref["Conv"] <= 1e-7
+
+
+def test_qp_graph_maxit_fallback():
+    """RGW_QP_graph.f90:78-81: a search that reaches maxIt keeps eGWlin and Z; the test is
+    nIt == maxIt after the loop, so it applies even when the last step met the threshold."""
+    from oracle import qkgw_oracle as O
+    f = np.load(os.path.join(GOLD, "synth_n24.npz"))
+    N, nO = int(f["N"]), int(f["nO"])
+    nS = nO * (N - nO)
+    E = synth.eri_phys_numpy(f["L"])
+    ref = O.RG0W0(True, 0.0, False, N, N, 0, nO, N - nO, 0, nS, E, f["eHF"])
+    Z0 = ref["Z"]
+    full = O.RGW_QP_graph(False, 0.0, 500.0, N, 0, nO, N - nO, 0, nS, f["eHF"], ref["Om"],
+                          ref["rho"], ref["eGWlin"], f["eHF"], Z0, return_iters=True)
+    assert np.max(np.abs(full[0] - f["g0w0_eGW"])) < 1e-12
+    for mi in (1, int(full[2].max())):
+        eGW, Z, it = O.RGW_QP_graph(False, 0.0, 500.0, N, 0, nO, N - nO, 0, nS, f["eHF"],
+                                    ref["Om"], ref["rho"], ref["eGWlin"], f["eHF"], Z0,
+                                    return_iters=True, maxit=mi)
+        hit = it == mi
+        assert hit.any()
+        assert np.array_equal(eGW[hit], ref["eGWlin"][hit])
+        assert np.array_equal(Z[hit], Z0[hit])
+        assert np.array_equal(eGW[~hit], full[0][~hit])
+
+
+def test_qp_root_certificate_implies_reference_root():
+    """Whenever the root certificate holds for a root r reached from another start, the
+    reference Newton search from eGWlin (RGW_QP_graph.f90:56-76) ends on r."""
+    from oracle import qkgw_oracle as O
+    n_cert = 0
+    for N, nO, seed in ((24, 3, 41), (32, 4, 42), (40, 5, 43)):
+        s = synth.small_system(N, nO, 3 * N, seed)
+        E = synth.eri_phys_numpy(s["L"])
+        nS = nO * (N - nO)
+        g = O.RG0W0(True, 0.0, False, N, N, 0, nO, N - nO, 0, nS, E, s["eHF"])
+        e, Om, rho, lin = s["eHF"], g["Om"], g["rho"], g["eGWlin"]
+        rng = np.random.default_rng(seed)
+        for p in range(N):
+            for shift in rng.normal(0.0, 0.05, 3):
+                # a root reached from a perturbed start
+                w, f, it = lin[p] + shift, 1.0, 0
+                while abs(f) > O.QP_THRESH and it < O.QP_MAXIT:
+                    it += 1
+                    f = w - e[p] - O.RGW_Re_SigC(p, w, 0.0, N, 0, nO, N - nO, 0, nS, e, Om, rho)
+                    w -= f / (1.0 - O.RGW_Re_dSigC(p, w, 0.0, N, 0, nO, N - nO, 0, nS, e, Om, rho))
+                if it == O.QP_MAXIT or not O.qp_root_certificate(p, w, lin[p], N, 0, nO, 0, e,
+                                                                   Om, rho):
+                    continue
+                n_cert += 1
+                ref, _ = O.RGW_QP_graph(False, 0.0, 500.0, N, 0, nO, N - nO, 0, nS, e, Om, rho,
+                                        lin, e, g["Z"])
+                assert abs(ref[p] - w) < 1e-8, (N, p, ref[p], w)
+    assert n_cert > 50
