@@ -248,6 +248,13 @@ module qk_gw_module
       integer(c_int), intent(out)   :: nSCF
     end function qk_qsRGW
 
+    ! QKD_* bits recorded on the device during the context's last call (warnings such as a
+    ! negative A-B eigenvalue or a Newton search that used all maxIt steps)
+    integer(c_int) function qk_last_device_status(ctx) bind(C, name="qk_last_device_status")
+      import c_int, c_ptr
+      type(c_ptr), value            :: ctx
+    end function qk_last_device_status
+
   end interface
 
 end module qk_gw_module

@@ -76,6 +76,21 @@ const char* qk_last_error_string(const qk_ctx* ctx);
 int qk_get_timings(const qk_ctx* ctx, double* ms, int n);
 const char* qk_timing_name(int i);
 int qk_num_timings(void);
+/* Device-side status bits of the context's last call (kernels record them instead of trapping;
+ * the call returns QK_ERR_DEVICE when a fatal one is set, the others mirror the reference's
+ * printed warnings). */
+enum {
+  QKD_BARRIER_TIMEOUT = 1, /* a bounded grid/group barrier wait expired (fatal) */
+  QKD_BAD_INDEX = 2,       /* an index check failed (fatal) */
+  QKD_NEG_AMB = 4,         /* A-B had a negative eigenvalue (phRLR.f90:56-58 warns) */
+  QKD_NEG_OMEGA = 8,       /* Casida produced a negative Omega^2 (phRLR.f90:70-74 warns) */
+  QKD_QP_NOCONV = 16,      /* a Newton QP search used all maxIt steps (RGW_QP_graph.f90:78-81) */
+  QKD_MBAR_TIMEOUT = 32    /* an mbarrier wait expired in a tensor-core kernel (fatal) */
+};
+int qk_last_device_status(const qk_ctx* ctx);
+/* Grouped tridiagonalisation launches of the context's last batched call and the matrices they
+ * covered (diagnostics: each launch tridiagonalises every worker's current matrix at once). */
+int qk_batch_group_stats(const qk_ctx* ctx, long long* launches, long long* matrices);
 /* Count of this library's kernel launches since qk_init (diagnostics). */
 long long qk_launch_count(const qk_ctx* ctx);
 /* Newton steps per orbital of the context's last graphical QP solve (64 = not converged). */
@@ -385,7 +400,14 @@ int qk_RGW_self_energy_diag_noalloc_dev(double eta, int nBas, int nOrb, int nC, 
  * "stebz_k" (lanes per eigenvalue in the bisection, size = n), "qp_persist" (mixed-tier Newton:
  * 1 persistent kernel, 2 per-step sweeps, size = nS).  qk_autotune times all candidates on
  * problems of the given sizes (allocates temporary buffers) and keeps the fastest; the table
- * can be saved to / loaded from a JSON file. */
+ * can be saved to / loaded from a JSON file.
+ * Two context-wide settings share qk_tune_set (size ignored): "newton_maxit" (steps of the
+ * graphical QP solve, 1..4096, default 64 = maxIt of RGW_QP_graph.f90:38; a search that uses all
+ * of them keeps eGWlin, :78-81) and "spin_limit" (polls of every bounded grid-barrier wait before
+ * it gives up and reports QKD_BARRIER_TIMEOUT, QK_ERR_DEVICE from the call; 0 = the built-in
+ * limit of about a second) and "fail_alloc" (n > 0: the n-th next workspace allocation that
+ * would call cudaMalloc fails instead, with QK_ERR_NOMEM; 0 disarms) -- hooks for the
+ * failure-path tests. */
 int qk_autotune(qk_ctx* ctx, int nOrb, int nS, int flags);
 int qk_tune_set(qk_ctx* ctx, const char* name, long long size, int value);
 int qk_tune_query(const qk_ctx* ctx, const char* name, long long size);

@@ -21,6 +21,9 @@ _lib = None
 
 QK_OK, QK_ERR_ARG, QK_ERR_CUDA, QK_ERR_NOMEM, QK_ERR_NOT_PD, QK_ERR_NO_CONV = 0, 1, 2, 3, 4, 5
 QK_ERR_UNSUPPORTED, QK_ERR_DEVICE, QK_ERR_NO_DEVICE = 6, 7, 8
+# device-side status bits of the last call (qk_last_device_status)
+QKD_BARRIER_TIMEOUT, QKD_BAD_INDEX, QKD_NEG_AMB, QKD_NEG_OMEGA, QKD_QP_NOCONV, QKD_MBAR_TIMEOUT = \
+    1, 2, 4, 8, 16, 32
 QK_PREC_FP64, QK_PREC_BF16X3 = 0, 1
 
 _dp = C.POINTER(C.c_double)
@@ -96,6 +99,16 @@ class Context:
         buf = (C.c_double * n)()
         L.qk_get_timings(self._h, buf, n)
         return {L.qk_timing_name(i).decode(): buf[i] for i in range(n)}
+
+    def batch_group_stats(self):
+        """(grouped tridiagonalisation launches, matrices) of the last batched call."""
+        a, b = C.c_longlong(), C.c_longlong()
+        self.check(lib().qk_batch_group_stats(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def last_device_status(self) -> int:
+        """QKD_* bits recorded on the device during the last call."""
+        return int(lib().qk_last_device_status(self._h))
 
     def launches(self) -> int:
         return int(lib().qk_launch_count(self._h))

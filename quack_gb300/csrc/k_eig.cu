@@ -19,7 +19,9 @@
 // degenerate subspaces, which every downstream GW quantity is invariant to.
 #include <cmath>
 #include <cfloat>
+#include <condition_variable>
 #include <mutex>
+#include <vector>
 #include "qk_internal.cuh"
 
 namespace {
@@ -90,14 +92,28 @@ struct TriArgs {
   double* V;
   long long ldv;
   double* pbuf;  // 6*n: three rotating p vectors, each as two exact accumulators (n + n)
-  double* fslot; // gridDim.x per-CTA partial sums of ||A||_F^2
-  double* gvec;  // gridDim.x * 3 * n when vectors do not fit in shared memory
+  double* fslot; // one partial sum of ||A||_F^2 per CTA of the group
+  double* gvec;  // (CTAs of the group) * 3 * n when vectors do not fit in shared memory
   unsigned* bar;
   int* status;
   int use_smem;
 };
 
-__global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
+// CTA group of a tridiagonalisation: the whole grid (k_sytrd; the sizes stay in special
+// registers) or a slice of it (k_sytrd_grouped; the sizes live in shared memory)
+struct TriGridWhole {
+  __device__ __forceinline__ int size() const { return (int)gridDim.x; }
+  __device__ __forceinline__ int rank() const { return (int)blockIdx.x; }
+};
+struct TriGridSlice {
+  const int* s;  // shared memory: {size, rank}
+  __device__ __forceinline__ int size() const { return *(const volatile int*)s; }
+  __device__ __forceinline__ int rank() const { return *(const volatile int*)(s + 1); }
+};
+
+// The tridiagonalisation of one matrix by a group of co-resident CTAs.
+template <class Grp>
+__device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
   extern __shared__ double sm[];
   __shared__ double s_pj, s_dj, s_alpha, s_sc[9], s_fro;
   const int n = a.n;
@@ -108,7 +124,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
     wk = vk + n;
     vk1 = vk + 2 * n;
   } else {
-    double* base = a.gvec + (size_t)blockIdx.x * 3 * n;
+    double* base = a.gvec + (size_t)grp.rank() * 3 * n;
     vk = base;
     wk = base + n;
     vk1 = base + 2 * n;
@@ -116,26 +132,26 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
   unsigned epoch = 0;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
-  const int totwarps = gridDim.x * nwarps;
-  const int gthread = blockIdx.x * nt + tid, totthreads = gridDim.x * nt;
+  const int totwarps = grp.size() * nwarps;
+  const int gthread = grp.rank() * nt + tid, totthreads = grp.size() * nt;
   double tau_k = 0.0, scal_k = 1.0;
 
   // ---- ||A||_F (bounds every p element's partial sums): fixed per-thread order, per-CTA slot,
   // then every CTA adds the slots in the same order, so all CTAs hold the same value ----
   {
     double fs = 0.0;
-    for (int c = blockIdx.x; c < n; c += gridDim.x) {
+    for (int c = grp.rank(); c < n; c += grp.size()) {
       const double* col = a.A + a.lda * c;
       for (int i = c + tid; i < n; i += nt) {
         const double x = __ldcg(col + i);
         fs = fma(i == c ? x : x + x, x, fs);
       }
     }
-    tri_block_sum(fs, ytile, nt, [&](double t) { __stcg(a.fslot + blockIdx.x, t); });
-    if (!qk_grid_barrier(a.bar, gridDim.x, epoch, a.status)) return;
+    tri_block_sum(fs, ytile, nt, [&](double t) { __stcg(a.fslot + grp.rank(), t); });
+    if (!qk_grid_barrier(a.bar, grp.size(), epoch, a.status)) return;
     if (tid == 0) {
       double t = 0.0;
-      for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(a.fslot + b);
+      for (int b = 0; b < grp.size(); ++b) t += __ldcg(a.fslot + b);
       s_fro = sqrt(t);
     }
     __syncthreads();
@@ -258,11 +274,11 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       scal1 = s_sc[5];
       if (j <= n - 2) {
         // every CTA holds the reflector: the V column is written by all of them, a slice each
-        if (blockIdx.x == 0 && tid == 0) { a.e[j] = s_sc[3]; a.tau[j] = tau1; }
+        if (grp.rank() == 0 && tid == 0) { a.e[j] = s_sc[3]; a.tau[j] = tau1; }
         for (int i = j + 1 + gthread; i < n; i += totthreads)
           a.V[i + a.ldv * j] = (i == j + 1) ? 1.0 : vk1[i] * scal1;
       }
-      if (blockIdx.x == 0 && tid == 0) a.d[j] = dj;
+      if (grp.rank() == 0 && tid == 0) a.d[j] = dj;
     }
     // ---- big pass: rank-2 update of step k fused with p_{k+1} = A' v_{k+1}, lower triangle ----
     // The trailing lower triangle is cut into tiles of 32 rows x TRI_TC columns (row block bi
@@ -282,7 +298,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
       const int items = nb * (nb + 1);  // < 2^31 for every n this kernel can hold
       const int per = (items + totwarps - 1) / totwarps;
       // warps numbered across CTAs first, so that a short tile list still spreads over all SMs
-      const int it0 = (warp * (int)gridDim.x + (int)blockIdx.x) * per;
+      const int it0 = (warp * grp.size() + grp.rank()) * per;
       const int it1 = it0 + per < items ? it0 + per : items;
       double* tile = ytile + (size_t)warp * (TRI_TC * TRI_TLD);
       if (it0 < it1) {
@@ -354,7 +370,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
         if (wantp && rowok) tri_exact_add(pnext + i, pnext2 + i, rowacc, s_sc[7], s_sc[8]);
       }
     }
-    if (!qk_grid_barrier(a.bar, gridDim.x, epoch, a.status)) return;
+    if (!qk_grid_barrier(a.bar, grp.size(), epoch, a.status)) return;
     // rotate vectors: v_{k+1} becomes v_k
     double* t = vk;
     vk = vk1;
@@ -362,6 +378,33 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
     tau_k = tau1;
     scal_k = scal1;
   }
+}
+
+__global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
+  sytrd_body(a, TriGridWhole{});
+}
+
+// Many tridiagonalisations in one cooperative launch: request r owns the CTAs
+// [cta0[r], cta0[r+1]) and synchronises them with its own bounded group barrier (its own counter),
+// so the per-column latency of small systems overlaps instead of queueing for the whole GPU.
+constexpr int TRI_GROUP_MAX = 32;
+struct TriGroup {
+  int nreq;
+  int cta0[TRI_GROUP_MAX + 1];
+  TriArgs req[TRI_GROUP_MAX];
+};
+
+__global__ void __launch_bounds__(TRI_THREADS) k_sytrd_grouped(const __grid_constant__ TriGroup g) {
+  __shared__ int s_grp[2];
+  int r = 0;
+  while (r + 1 < g.nreq && (int)blockIdx.x >= g.cta0[r + 1]) ++r;
+  if ((int)blockIdx.x >= g.cta0[g.nreq]) return;
+  if (threadIdx.x == 0) {
+    s_grp[0] = g.cta0[r + 1] - g.cta0[r];
+    s_grp[1] = (int)blockIdx.x - g.cta0[r];
+  }
+  __syncthreads();
+  sytrd_body(g.req[r], TriGridSlice{s_grp});
 }
 
 // Gershgorin bounds, pivmin, ||T||_1 and e^2 (single block).
@@ -548,9 +591,13 @@ __device__ __forceinline__ double pivot_rcp(double u, double tiny) {
 // The iterate lives directly in the output row Zt[jj + n*i].
 __global__ void k_stein(int n, const double* __restrict__ d, const double* __restrict__ e,
                         const double* __restrict__ w, const double* __restrict__ prep,
-                        double* __restrict__ W, double* __restrict__ Zt) {
+                        double* __restrict__ W, double* __restrict__ Zt,
+                        const int* __restrict__ status) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
+  // after a failed tridiagonalisation (barrier expired) T is meaningless -- possibly one cluster
+  // of n equal eigenvalues, whose Gram-Schmidt would take seconds: the call fails anyway
+  if (*(const volatile int*)status & QKD_BARRIER_TIMEOUT) return;
   const double tnrm = prep[3];
   const double ortol = CLUSTER_REL * tnrm;
   if (j > 0 && w[j] - w[j - 1] <= ortol) return;  // not a cluster leader
@@ -791,6 +838,166 @@ int eig_tfactors(qk_ctx* ctx, int n, const double* V, const double* tau, const d
 }  // namespace
 
 // ------------------------------------------------------------------------------------------
+// grouped tridiagonalisation of the batch workers
+// ------------------------------------------------------------------------------------------
+struct qk_tri_service {
+  struct Req {
+    TriArgs ta;
+    cudaStream_t stream;
+    cudaEvent_t ready;
+  };
+  qk_ctx* parent = nullptr;
+  std::mutex mu;
+  std::condition_variable cv;
+  int n_active = 0;
+  unsigned long long gen = 0;
+  int last_status = QK_OK;
+  std::vector<Req> pending;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  long long launches = 0;
+  long long matrices = 0;
+};
+
+namespace {
+
+// CTAs per request: proportional to the n^3 work, at least one, at most what the matrix can use
+// (one 32 x 128 trailing block per CTA, as in the single-matrix launch), all within one CTA per SM
+void tri_split(const std::vector<qk_tri_service::Req>& rq, int sms, int* cta0) {
+  const int R = (int)rq.size();
+  std::vector<double> wgt(R);
+  std::vector<int> g(R), cap(R);
+  double tot = 0.0;
+  for (int r = 0; r < R; ++r) {
+    const double n = rq[r].ta.n;
+    wgt[r] = n * n * n;
+    tot += wgt[r];
+    const long long want = (long long)rq[r].ta.n * rq[r].ta.n / (32 * 128) + 1;
+    cap[r] = (int)(want < sms ? want : sms);
+  }
+  int used = 0;
+  for (int r = 0; r < R; ++r) {
+    int v = (int)((double)sms * wgt[r] / (tot > 0.0 ? tot : 1.0));
+    v = v < 1 ? 1 : (v > cap[r] ? cap[r] : v);
+    g[r] = v;
+    used += v;
+  }
+  // hand the SMs left over to the largest requests still below their cap
+  while (used < sms) {
+    int best = -1;
+    for (int r = 0; r < R; ++r)
+      if (g[r] < cap[r] && (best < 0 || wgt[r] / g[r] > wgt[best] / g[best])) best = r;
+    if (best < 0) break;
+    ++g[best];
+    ++used;
+  }
+  while (used > sms) {  // R > sms cannot happen (R <= TRI_GROUP_MAX < SMs); keep it safe anyway
+    int best = 0;
+    for (int r = 1; r < R; ++r)
+      if (g[r] > g[best]) best = r;
+    if (g[best] <= 1) break;
+    --g[best];
+    --used;
+  }
+  cta0[0] = 0;
+  for (int r = 0; r < R; ++r) cta0[r + 1] = cta0[r] + g[r];
+}
+
+// one cooperative launch for all pending requests (called with the lock held)
+void tri_launch_locked(qk_tri_service* sv) {
+  int st = QK_OK;
+  const int R = (int)sv->pending.size();
+  TriGroup g;
+  g.nreq = R;
+  size_t smem = 0;
+  for (int r = 0; r < R; ++r) {
+    g.req[r] = sv->pending[r].ta;
+    const size_t need = TRI_TILE_BYTES + 3 * (size_t)g.req[r].n * sizeof(double);
+    smem = need > smem ? need : smem;
+    if (cudaStreamWaitEvent(sv->stream, sv->pending[r].ready, 0) != cudaSuccess) st = QK_ERR_CUDA;
+  }
+  tri_split(sv->pending, sv->parent->num_sms, g.cta0);
+  if (st == QK_OK) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g.cta0[R]);
+    cfg.blockDim = dim3(TRI_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = sv->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, k_sytrd_grouped, g) != cudaSuccess) st = QK_ERR_CUDA;
+    sv->launches++;
+    sv->matrices += R;
+  }
+  if (cudaEventRecord(sv->done, sv->stream) != cudaSuccess) st = QK_ERR_CUDA;
+  // every requester's stream continues after the group (enqueued before they wake up)
+  for (int r = 0; r < R; ++r)
+    if (cudaStreamWaitEvent(sv->pending[r].stream, sv->done, 0) != cudaSuccess) st = QK_ERR_CUDA;
+  sv->last_status = st;
+  sv->pending.clear();
+  sv->gen++;
+  sv->cv.notify_all();
+}
+
+int tri_submit(qk_tri_service* sv, qk_ctx* ctx, const TriArgs& ta) {
+  if (!ctx->ev_tri) QK_CK(cudaEventCreateWithFlags(&ctx->ev_tri, cudaEventDisableTiming));
+  QK_CK(cudaEventRecord(ctx->ev_tri, ctx->stream));
+  std::unique_lock<std::mutex> lk(sv->mu);
+  sv->pending.push_back({ta, ctx->stream, ctx->ev_tri});
+  const unsigned long long my = sv->gen;
+  if ((int)sv->pending.size() >= sv->n_active || (int)sv->pending.size() >= TRI_GROUP_MAX)
+    tri_launch_locked(sv);
+  else
+    sv->cv.wait(lk, [&] { return sv->gen != my; });
+  ctx->launches++;
+  if (sv->last_status != QK_OK)
+    return qk_fail(ctx, QK_ERR_CUDA, "grouped tridiagonalisation launch failed");
+  return QK_OK;
+}
+
+}  // namespace
+
+qk_tri_service* qk_tri_service_new(qk_ctx* parent, int n_workers) {
+  auto* sv = new qk_tri_service();
+  sv->parent = parent;
+  sv->n_active = n_workers;
+  if (cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&sv->done, cudaEventDisableTiming) != cudaSuccess) {
+    qk_tri_service_free(sv);
+    return nullptr;
+  }
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_sytrd_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TRI_SMEM_MAX);
+  });
+  return sv;
+}
+
+void qk_tri_service_worker_done(qk_tri_service* sv) {
+  std::unique_lock<std::mutex> lk(sv->mu);
+  sv->n_active--;
+  if (!sv->pending.empty() && (int)sv->pending.size() >= sv->n_active) tri_launch_locked(sv);
+}
+
+void qk_tri_service_free(qk_tri_service* sv) {
+  if (!sv) return;
+  if (sv->parent) {
+    sv->parent->tri_groups = sv->launches;
+    sv->parent->tri_grouped = sv->matrices;
+  }
+  if (sv->stream) {
+    cudaStreamSynchronize(sv->stream);
+    cudaStreamDestroy(sv->stream);
+  }
+  if (sv->done) cudaEventDestroy(sv->done);
+  delete sv;
+}
+
+// ------------------------------------------------------------------------------------------
 int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, int want_vectors,
                int backtransform) {
   if (n <= 0) return QK_OK;
@@ -860,19 +1067,24 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
     ta.bar = ctx->d_bar;
     ta.status = ctx->d_status;
     ta.use_smem = use_smem;
-    // cooperative launch (all CTAs co-resident for the grid barrier); also valid under capture
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(TRI_THREADS);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = ctx->stream;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeCooperative;
-    at[0].val.cooperative = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    QK_CK(cudaLaunchKernelEx(&cfg, k_sytrd, ta));
-    ctx->launches++;
+    if (ctx->tri_service && use_smem && !ctx->capturing) {
+      // batch worker: the matrix joins the other workers' in one grouped launch
+      QK_TRY(tri_submit(ctx->tri_service, ctx, ta));
+    } else {
+      // cooperative launch (all CTAs co-resident for the grid barrier); also valid under capture
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(grid);
+      cfg.blockDim = dim3(TRI_THREADS);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = ctx->stream;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeCooperative;
+      at[0].val.cooperative = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      QK_CK(cudaLaunchKernelEx(&cfg, k_sytrd, ta));
+      ctx->launches++;
+    }
   }
   if (tm) qk_toc(ctx, T_TRIDIAG);
 
@@ -895,7 +1107,7 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   double* Wst = nullptr;
   QK_TRY(qk_wst(ctx, W_EIGWORK, 5 * N * N, &Wst));
   if (tm) qk_tic(ctx, T_STEIN);
-  k_stein<<<(n + 63) / 64, 64, 0, ctx->stream>>>(n, d, e, w, prep, Wst, Zt);
+  k_stein<<<(n + 63) / 64, 64, 0, ctx->stream>>>(n, d, e, w, prep, Wst, Zt, ctx->d_status);
   QK_LAUNCHED();
   if (tm) qk_toc(ctx, T_STEIN);
 

@@ -127,11 +127,12 @@ __global__ void __launch_bounds__(1024) k_pchol(PcArgs a) {
       s_key = 0ull;
       epoch++;
       const unsigned target = epoch * gridDim.x;
+      const unsigned limit = qk_spin_limit(a.status);
       __threadfence();
       atomicAdd(a.bar, 1u);
       unsigned spins = 0;
       while (qk_ld_acquire(a.bar) < target) {
-        if (++spins > QK_MAX_SPIN) { atomicOr(a.status, QKD_BARRIER_TIMEOUT); ok = 0; break; }
+        if (++spins > limit) { atomicOr(a.status, QKD_BARRIER_TIMEOUT); ok = 0; break; }
         if (spins > 64) __nanosleep(32);
       }
       if (ok && (*((volatile int*)a.status) & QKD_BARRIER_TIMEOUT)) ok = 0;

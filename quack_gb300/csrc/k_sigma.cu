@@ -33,7 +33,6 @@ __device__ __forceinline__ double rcp_nr(double x) {
 }
 
 constexpr int SIG_WARPS = 8;
-constexpr int QP_MAXIT = 64;        // RGW_QP_graph.f90:38
 constexpr double QP_THRESH = 1e-6;  // RGW_QP_graph.f90:39
 
 struct SigArgs {
@@ -196,140 +195,136 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float x) {
   hi = t;
 }
 
-constexpr int FF_B = 12;  // terms per batch of independent loads
-
 struct SigFF {
-  const float* R;
+  const float* Rt;  // R = 2 rho^2 (FP32), p-major: Rt[m + nS (q + N p)]
   const float2* OmF;
   const int* bad;
   float tau;
-  int om_smem;  // stage the chunk's Om pairs in shared memory
 };
 
-__global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial_ff(SigArgs a, SigFF f) {
-  // dynamic shared memory: e (N doubles) | e as float pairs (N) | Om pairs of this m chunk
+// Mixed-tier sweep over the p-major R: one CTA per (orbital, q group); its warps take the q of
+// the group, the lanes the excitations m (contiguous in Rt, so each warp streams 128-byte lines,
+// FFT_U loads per lane in flight).  Per (p, q): c = w - e_q as a float pair (TwoSum in FP32) and
+// the window of m with |w - e_q +- Om_m| < tau by two bisections on the ascending Om (pairs in
+// shared memory); outside the window eps = (c_hi +- Om_hi) + (c_lo +- Om_lo) and R/eps on the FP32
+// pipe, the warp's per-(p,q) sums added into float-float (TwoSum) accumulators; inside it the
+// FP64 terms of k_sigma_partial.  Same partial-sum layout as k_sigma_partial (chunk = q group).
+constexpr int FFT_WARPS = 8;
+constexpr int FFT_U = 8;
+
+__global__ void __launch_bounds__(FFT_WARPS * 32) k_sigma_partial_ffT(SigArgs a, SigFF f) {
+  // dynamic shared memory: e (N doubles) | e as float pairs (N) | Om pairs (nS)
   extern __shared__ double se[];
-  __shared__ double ssig[SIG_WARPS][32], sds[SIG_WARPS][32], socc[SIG_WARPS][32];
-  const int nl = a.nact ? *a.nact : 0;
-  if (a.list && (int)blockIdx.x * 32 >= nl) return;
-  const int N = a.N;
+  __shared__ double r_sig[FFT_WARPS], r_ds[FFT_WARPS], r_so[FFT_WARPS];
+  const int N = a.N, nS = a.nS;
+  int p;
+  if (a.list) {
+    if ((int)blockIdx.x >= *a.nact) return;
+    p = a.list[blockIdx.x];
+  } else {
+    p = a.nC + blockIdx.x;
+  }
   float2* eF = (float2*)(se + N);
-  const int mc = blockIdx.y % a.mchunks, qg = blockIdx.y / a.mchunks;
-  const int m0 = mc * a.mper;
-  const int m1 = min(a.nS, m0 + a.mper);
+  float2* oS = eF + N;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const double e = a.eq[i];
     const float h = (float)e;
     se[i] = e;
     eF[i] = make_float2(h, (float)(e - (double)h));
   }
-  // Om pairs of the chunk: omp[m - mb] for m0 <= m < m1 (shared copy when it fits)
-  const float2* omp = f.OmF;
-  int mb = 0;
-  if (f.om_smem) {
-    float2* oms = eF + N;
-    for (int i = threadIdx.x; i < m1 - m0; i += blockDim.x) oms[i] = f.OmF[m0 + i];
-    omp = oms;
-    mb = m0;
-  }
+  for (int i = threadIdx.x; i < nS; i += blockDim.x) oS[i] = f.OmF[i];
+  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int pend = N - a.nR;
-  int p;
-  bool pok;
-  if (a.list) {
-    const int idx = blockIdx.x * 32 + lane;
-    pok = idx < nl;
-    p = pok ? a.list[idx] : pend;
-  } else {
-    p = a.nC + blockIdx.x * 32 + lane;
-    pok = p < pend;
-  }
-  __syncthreads();
-  double sig = 0.0, ds = 0.0, so = 0.0;
-  if (pok) {
-    const double w = a.wp ? a.wp[p] : se[p];
-    const float w_hi = (float)w;
-    const float w_lo = (float)(w - (double)w_hi);
-    const long long N1 = N, N2 = N1 * N1;
-    const bool bad = *f.bad != 0;
-    const float* Rp = f.R + p;
-    const double* rp = a.rho + p;
-    float so_h = 0.f, so_l = 0.f, sv_h = 0.f, sv_l = 0.f, d_h = 0.f, d_l = 0.f;
-    double Sn_o = 0.0, Sn_v = 0.0, Dn = 0.0;  // near-pole (FP64) parts
-    const int qend = min(pend, a.nC + (qg + 1) * a.qper);
-    for (int q = a.nC + qg * a.qper + warp; q < qend; q += SIG_WARPS) {
-      const bool occ = q < a.nO;
-      // c = w - e_q as a float pair, FP32 only: TwoSum of the high parts plus the low parts
-      const float2 eq = eF[q];
-      const float chi = w_hi - eq.x;
-      const float bb = chi - w_hi;
-      const float clo = ((w_hi - (chi - bb)) + (-eq.x - bb)) + (w_lo - eq.y);
-      const float sg = occ ? 1.f : -1.f;
-      int lo = m0, hi = m1;
-      if (!bad) {
-        const float ctr = -sg * chi;  // the pole sits at Om = -c (occupied) or Om = c (virtual)
-        lo = om_lower_bound(omp, mb, m0, m1, ctr - f.tau);
-        hi = om_lower_bound(omp, mb, lo, m1, ctr + f.tau);
-      }
-      const float* Rq = Rp + N1 * q + N2 * m0;
-      float s = 0.f, d = 0.f;
-      int m = m0;
-      // batches of FF_B terms: all loads first (independent), then the arithmetic
-      for (; m + FF_B <= m1; m += FF_B, Rq += FF_B * N2) {
-        float rv[FF_B];
-        float2 ov[FF_B];
+  const long long N1 = N, N2 = N1 * N1;
+  const bool bad = *f.bad != 0;
+  const double w = a.wp ? a.wp[p] : se[p];
+  const float w_hi = (float)w;
+  const float w_lo = (float)(w - (double)w_hi);
+  const float* Rp = f.Rt + (long long)nS * N1 * p;
+  const double* rp = a.rho + p;
+  float so_h = 0.f, so_l = 0.f, sv_h = 0.f, sv_l = 0.f, d_h = 0.f, d_l = 0.f;
+  double Sn_o = 0.0, Sn_v = 0.0, Dn = 0.0;  // window (FP64) parts, per lane
+  const int q0 = a.nC + (int)blockIdx.y * a.qper;
+  const int q1 = min(pend, q0 + a.qper);
+  for (int q = q0 + warp; q < q1; q += FFT_WARPS) {
+    const bool occ = q < a.nO;
+    const float2 eq = eF[q];
+    const float chi = w_hi - eq.x;
+    const float bb = chi - w_hi;
+    const float clo = ((w_hi - (chi - bb)) + (-eq.x - bb)) + (w_lo - eq.y);
+    const float sg = occ ? 1.f : -1.f;
+    int lo = 0, hi = nS;
+    if (!bad) {
+      const float ctr = -sg * chi;  // the pole sits at Om = -c (occupied) or Om = c (virtual)
+      lo = om_lower_bound(oS, 0, 0, nS, ctr - f.tau);
+      hi = om_lower_bound(oS, 0, lo, nS, ctr + f.tau);
+    }
+    const float* Rq = Rp + (long long)nS * q;
+    float sl = 0.f, dl = 0.f;
+    int m0 = 0;
+    for (; m0 + 32 * FFT_U <= nS; m0 += 32 * FFT_U) {
+      float rv[FFT_U];
 #pragma unroll
-        for (int u = 0; u < FF_B; ++u) {
-          rv[u] = __ldg(Rq + u * N2);
-          ov[u] = omp[m + u - mb];
-        }
+      for (int u = 0; u < FFT_U; ++u) rv[u] = __ldg(Rq + m0 + 32 * u + lane);
 #pragma unroll
-        for (int u = 0; u < FF_B; ++u) {
-          const float e = fmaf(sg, ov[u].x, chi) + fmaf(sg, ov[u].y, clo);
-          float r = rcp32(e);
-          r = (m + u >= lo && m + u < hi) ? 0.f : r;
-          const float t = rv[u] * r;
-          s += t;
-          d = fmaf(t, r, d);
-        }
-      }
-      for (; m < m1; ++m, Rq += N2) {
-        const float2 o = omp[m - mb];
+      for (int u = 0; u < FFT_U; ++u) {
+        const int m = m0 + 32 * u + lane;
+        const float2 o = oS[m];
         const float e = fmaf(sg, o.x, chi) + fmaf(sg, o.y, clo);
         float r = rcp32(e);
         r = (m >= lo && m < hi) ? 0.f : r;
-        const float t = __ldg(Rq) * r;
-        s += t;
-        d = fmaf(t, r, d);
-      }
-      if (occ) ff_add(so_h, so_l, s);
-      else ff_add(sv_h, sv_l, s);
-      ff_add(d_h, d_l, d);
-      // the window, in FP64 (RGW_Re_SigC.f90:30-50 / RGW_Re_dSigC.f90:30-50 with eta = 0)
-      for (int m = lo; m < hi; ++m) {
-        const double om = __ldg(a.Om + m);
-        const double x = __ldg(rp + N1 * q + N2 * m);
-        const double ir = rcp_nr(occ ? (w - se[q] + om) : (w - se[q] - om));
-        const double t = (2.0 * (x * x)) * ir;
-        if (occ) Sn_o += t;
-        else Sn_v += t;
-        Dn = fma(t, ir, Dn);
+        const float t = rv[u] * r;
+        sl += t;
+        dl = fmaf(t, r, dl);
       }
     }
-    so = ((double)so_h + (double)so_l) + Sn_o;
-    sig = ((double)sv_h + (double)sv_l) + Sn_v + so;
-    ds = -(((double)d_h + (double)d_l) + Dn);
+    for (int m = m0 + lane; m < nS; m += 32) {
+      const float2 o = oS[m];
+      const float e = fmaf(sg, o.x, chi) + fmaf(sg, o.y, clo);
+      float r = rcp32(e);
+      r = (m >= lo && m < hi) ? 0.f : r;
+      const float t = __ldg(Rq + m) * r;
+      sl += t;
+      dl = fmaf(t, r, dl);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      sl += __shfl_xor_sync(0xffffffffu, sl, o);
+      dl += __shfl_xor_sync(0xffffffffu, dl, o);
+    }
+    if (occ) ff_add(so_h, so_l, sl);
+    else ff_add(sv_h, sv_l, sl);
+    ff_add(d_h, d_l, dl);
+    // the window, in FP64 (RGW_Re_SigC.f90:30-50 / RGW_Re_dSigC.f90:30-50 with eta = 0)
+    for (int m = lo + lane; m < hi; m += 32) {
+      const double om = __ldg(a.Om + m);
+      const double x = __ldg(rp + N1 * q + N2 * m);
+      const double ir = rcp_nr(occ ? (w - se[q] + om) : (w - se[q] - om));
+      const double t = (2.0 * (x * x)) * ir;
+      if (occ) Sn_o += t;
+      else Sn_v += t;
+      Dn = fma(t, ir, Dn);
+    }
   }
-  ssig[warp][lane] = sig;
-  sds[warp][lane] = ds;
-  socc[warp][lane] = so;
+  for (int o = 16; o > 0; o >>= 1) {
+    Sn_o += __shfl_xor_sync(0xffffffffu, Sn_o, o);
+    Sn_v += __shfl_xor_sync(0xffffffffu, Sn_v, o);
+    Dn += __shfl_xor_sync(0xffffffffu, Dn, o);
+  }
+  // lanes hold identical float-float accumulators (the shuffles gave every lane the sums)
+  if (lane == 0) {
+    const double so = ((double)so_h + (double)so_l) + Sn_o;
+    r_so[warp] = so;
+    r_sig[warp] = ((double)sv_h + (double)sv_l) + Sn_v + so;
+    r_ds[warp] = -(((double)d_h + (double)d_l) + Dn);
+  }
   __syncthreads();
-  if (warp == 0 && p < pend) {
+  if (threadIdx.x == 0) {
     double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-    for (int w = 0; w < SIG_WARPS; ++w) {
-      s0 += ssig[w][lane];
-      s1 += sds[w][lane];
-      s2 += socc[w][lane];
+    for (int k = 0; k < FFT_WARPS; ++k) {
+      s0 += r_sig[k];
+      s1 += r_ds[k];
+      s2 += r_so[k];
     }
     const size_t o = (size_t)blockIdx.y * N + p;
     const size_t stride = (size_t)a.nchunks * N;
@@ -339,17 +334,34 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial_ff(SigArgs a, 
   }
 }
 
-// R = 2 rho^2 in FP32; Om split into float pairs; flag Om that is not ascending (or NaN)
-__global__ void k_sigma_ff_prep(long long n, const double* __restrict__ rho, float* __restrict__ R,
-                                int nS, const double* __restrict__ Om, float2* __restrict__ OmF,
-                                int* __restrict__ bad) {
-  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long nth = (long long)gridDim.x * blockDim.x;
-  for (long long i = tid; i < n; i += nth) {
-    const double x = rho[i];
-    R[i] = (float)(2.0 * (x * x));
+// Rt = 2 rho^2 in FP32, p-major: Rt[m + nS (q + N p)] from rho[p + N q + N^2 m], through 32 x 32
+// shared-memory tiles of (p, m) per q, both sides coalesced
+__global__ void k_sigma_ff_prepT(int N, int nS, const double* __restrict__ rho,
+                                 float* __restrict__ Rt) {
+  __shared__ float t[32][33];
+  const int p0 = blockIdx.x * 32, m0 = blockIdx.y * 32, q = blockIdx.z;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  const long long N1 = N, N2 = N1 * N1;
+  for (int i = ty; i < 32; i += 8) {
+    const int p = p0 + tx, m = m0 + i;
+    float v = 0.f;
+    if (p < N && m < nS) {
+      const double x = rho[p + N1 * q + N2 * m];
+      v = (float)(2.0 * (x * x));
+    }
+    t[i][tx] = v;
   }
-  for (long long m = tid; m < nS; m += nth) {
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int p = p0 + i, m = m0 + tx;
+    if (p < N && m < nS) Rt[m + (long long)nS * (q + N1 * p)] = t[tx][i];
+  }
+}
+
+// Om split into float pairs; flag Om that is not ascending (or NaN)
+__global__ void k_om_pairs(int nS, const double* __restrict__ Om, float2* __restrict__ OmF,
+                           int* __restrict__ bad) {
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nS; m += gridDim.x * blockDim.x) {
     const double om = Om[m];
     const float hi = (float)om;
     OmF[m] = make_float2(hi, (float)(om - (double)hi));
@@ -422,20 +434,18 @@ __global__ void k_qp_init(int N, int nC, int nR, const double* __restrict__ w0, 
   qp_compact(N, s);
 }
 
-// Orbitals whose guess-started search did not converge, or converged outside the trust region
-// |w - eGWlin| <= |eGWlin - eHF| + 0.02 Ha around the reference start, restart from the
-// reference start (the root must stay the one the linearised solution points at).  Orbitals that
-// started at the reference start are already on the reference trajectory and just continue.
+// Orbitals whose guess-started search did not converge, or converged to a root that the root
+// certificate (k_cert_partial) does not prove to be the reference search's, restart from the
+// reference start.  Orbitals that started at the reference start are already on the reference
+// trajectory and just continue.
 __global__ void k_qp_restart(int N, int nC, int nR, const double* __restrict__ eGWlin,
-                             const double* __restrict__ eHF, QPState s) {
+                             const int* __restrict__ cert, QPState s, int maxit) {
   for (int p = threadIdx.x; p < N; p += blockDim.x) {
     if (s.fromref && s.fromref[p]) {
-      s.active[p] = (p >= nC && p < N - nR) && !s.conv[p] && s.nit[p] < QP_MAXIT;
+      s.active[p] = (p >= nC && p < N - nR) && !s.conv[p] && s.nit[p] < maxit;
       continue;
     }
-    const double trust = fabs(eGWlin[p] - eHF[p]) + 0.02;
-    const double wnew = s.w[p];
-    const bool keep = s.conv[p] && fabs(wnew - eGWlin[p]) <= trust;
+    const bool keep = s.conv[p] && cert[p];
     const bool act = (p >= nC && p < N - nR) && !keep;
     if (act) {
       s.w[p] = eGWlin[p];
@@ -483,30 +493,12 @@ __global__ void k_qp_update(int N, int nchunks, const double* __restrict__ part,
   qp_compact(N, s);
 }
 
-// p-major copy of R for the persistent Newton solve: Rt[m + nS (q + N p)] = R[p + N q + N^2 m]
-// (32 x 32 tiles of (p, m) per q through shared memory: both sides coalesced)
-__global__ void k_r_pmajor(int N, int nS, const float* __restrict__ R, float* __restrict__ Rt) {
-  __shared__ float t[32][33];
-  const int p0 = blockIdx.x * 32, m0 = blockIdx.y * 32, q = blockIdx.z;
-  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
-  const long long N1 = N, N2 = N1 * N1;
-  for (int i = ty; i < 32; i += 8) {
-    const int p = p0 + tx, m = m0 + i;
-    t[i][tx] = (p < N && m < nS) ? R[p + N1 * q + N2 * m] : 0.f;
-  }
-  __syncthreads();
-  for (int i = ty; i < 32; i += 8) {
-    const int p = p0 + i, m = m0 + tx;
-    if (p < N && m < nS) Rt[m + (long long)nS * (q + N1 * p)] = t[tx][i];
-  }
-}
-
 // Persistent Newton solve of the mixed tier (RGW_QP_graph.f90:50-92; eta = 0, no SRG): one CTA
 // per orbital, taken from a queue, iterates w <- w - f/(1 - Sigma'(w)) on chip until |f| <= 1e-6
 // or maxit steps, so that a search costs no launches and the chaotic orbitals, which run all 64
 // steps, no longer hold the whole GPU for two launches per step.  A step sweeps the orbital's
 // (q, m) terms: warps over q, lanes over m (Rt is p-major, so the loads are coalesced), the
-// same FP32 far-pole / FP64 window split and float-float accumulation as k_sigma_partial_ff,
+// same FP32 far-pole / FP64 window split and float-float accumulation as k_sigma_partial_ffT,
 // then one block reduction.  The update and the bookkeeping are k_qp_update's.
 constexpr size_t NEWT_SMEM_MAX = 200 * 1024;
 struct NewtFF {
@@ -662,11 +654,14 @@ __global__ void __launch_bounds__(NEWT_WARPS * 32) k_qp_newton_ff(NewtFF a, QPSt
   }
 }
 
+// RGW_QP_graph.f90:78-86: a search that used all maxIt steps keeps eGWlin (and Z) -- also when
+// its last step met the threshold, as the reference tests nIt == maxIt after the loop
 __global__ void k_qp_finish(int N, int nC, int nR, const double* __restrict__ eGWlin, QPState s,
-                            double* __restrict__ eGW, double* __restrict__ Z, int* status) {
+                            double* __restrict__ eGW, double* __restrict__ Z, int* status,
+                            int maxit) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
     if (p < nC || p >= N - nR) continue;
-    if (s.nit[p] == QP_MAXIT) {
+    if (s.nit[p] == maxit) {
       eGW[p] = eGWlin[p];
       atomicOr(status, QKD_QP_NOCONV);
     } else {
@@ -786,6 +781,97 @@ __global__ void k_diis(int n_err, int n_e, int nd_host, double* __restrict__ err
   }
 }
 
+// Root certificate of a guess-started Newton search (eta = 0, no SRG).  Between consecutive poles
+// p_k = e_q -+ Om_m the QP function f(w) = w - eHF - sum_k R_k/(w - p_k) is increasing (f' >= 1)
+// and f''(w) = 2 [A(w) - B(w)] with A = sum_{p_k > w} R_k/(p_k - w)^3 (increasing in w) and
+// B = sum_{p_k < w} R_k/(w - p_k)^3 (decreasing), so f'' is increasing on any pole-free interval.
+// Let r be the root the guess-started search converged to and w0 = eGWlin the reference start.
+// If no pole lies between w0 and r, and f''(r) has the sign of w0 - r (then f'' keeps that sign
+// on the whole interval between them, f'' being monotone), Newton from w0 converges monotonically
+// to r (the classical convex-case theorem): the reference search from eGWlin ends on the same
+// root, and the guess-started result is kept.  Otherwise the orbital restarts from eGWlin.  One
+// FP64 sweep at r per guess-started orbital that converged: A, B and the count of poles strictly
+// between w0 and r (or at either end).
+constexpr int CERT_ACC = 3;
+
+__global__ void __launch_bounds__(SIG_WARPS * 32)
+    k_cert_partial(int N, int nC, int nO, int nR, int nS, int nchunks, int mper,
+                   const double* __restrict__ e, const double* __restrict__ w0s, QPState st,
+                   const double* __restrict__ Om, const double* __restrict__ rho,
+                   double* __restrict__ part) {
+  extern __shared__ double se[];
+  __shared__ double acc[CERT_ACC][SIG_WARPS][32];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) se[i] = e[i];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p = nC + blockIdx.x * 32 + lane;
+  const int pend = N - nR;
+  __syncthreads();
+  double sa = 0.0, sb = 0.0, cross = 0.0;
+  const bool need = p < pend && st.conv[p] && !(st.fromref && st.fromref[p]);
+  if (need) {
+    const double w = st.w[p], d0 = w0s[p] - w;
+    const long long N1 = N, N2 = N1 * N1;
+    const int m0 = blockIdx.y * mper, m1 = min(nS, m0 + mper);
+    for (int mm = m0 + warp; mm < m1; mm += SIG_WARPS) {
+      const double om = Om[mm];
+      const double* r = rho + p + N2 * mm;
+      for (int q = nC; q < pend; ++q) {
+        const double x = r[N1 * q];
+        const double R = 2.0 * (x * x);
+        const double eps = q < nO ? (w - se[q] + om) : (w - se[q] - om);  // r - p_k
+        const double eps0 = eps + d0;                                      // w0 - p_k (approx.)
+        const double ie = rcp_nr(eps);
+        const double t = R * ie * ie * ie;
+        if (eps > 0.0) sb += t;
+        else sa -= t;
+        // a pole between w0 and r, or within rounding of either end, voids the certificate
+        if (!(eps * eps0 > 0.0) || fabs(eps0) <= 1e-12 * (1.0 + fabs(w))) cross += 1.0;
+      }
+    }
+  }
+  acc[0][warp][lane] = sa;
+  acc[1][warp][lane] = sb;
+  acc[2][warp][lane] = cross;
+  __syncthreads();
+  if (warp == 0 && p < pend) {
+    const size_t stride = (size_t)nchunks * N;
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int w = 0; w < SIG_WARPS; ++w) {
+      a += acc[0][w][lane];
+      b += acc[1][w][lane];
+      c += acc[2][w][lane];
+    }
+    const size_t o = (size_t)blockIdx.y * N + p;
+    part[o] = a;
+    part[o + stride] = b;
+    part[o + 2 * stride] = c;
+  }
+}
+
+__global__ void k_cert_final(int N, int nC, int nR, int nchunks, const double* __restrict__ part,
+                             const double* __restrict__ w0s, QPState st, int* __restrict__ cert) {
+  const size_t stride = (size_t)nchunks * N;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+    const bool need = p >= nC && p < N - nR && st.conv[p] && !(st.fromref && st.fromref[p]);
+    int ok = 0;
+    if (need) {
+      double a = 0.0, b = 0.0, c = 0.0;
+      for (int k = 0; k < nchunks; ++k) {
+        const size_t o = (size_t)k * N + p;
+        a += part[o];
+        b += part[o + stride];
+        c += part[o + 2 * stride];
+      }
+      const double r = st.w[p], w0 = w0s[p], margin = 1e-9 * (a + b);
+      // f''(r)/2 = a - b must have the sign of w0 - r (with a margin for rounding)
+      const bool convex_ok = (w0 > r && a - b > margin) || (w0 < r && b - a > margin) || w0 == r;
+      ok = c == 0.0 && convex_ok && a == a && b == b;
+      st.evals[p] += 1;
+    }
+    cert[p] = ok;
+  }
+}
+
 }  // namespace
 
 static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
@@ -795,52 +881,63 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
   // p tiles: all orbitals, or (with a compacted list) an upper bound on the active count
   int nact_p = N - nR - nC;
   if (list && nact_max >= 0 && nact_max < nact_p) nact_p = nact_max;
-  const int ptiles = (nact_p + 31) / 32;
   const int cm = qk_tune_get(ctx, TUNE_SIGMA_CHUNKS, (long long)nS, 4);
-  const int target = (cm * ctx->num_sms + (ptiles > 0 ? ptiles : 1) - 1) / (ptiles > 0 ? ptiles : 1);
-  const size_t base = (size_t)N * (sizeof(double) + sizeof(float2));
-  // the mixed sweep keeps e in shared memory twice; very large N takes the FP64 sweep
-  const bool use_ff = ff && !doSRG && eta == 0.0 && base <= 40 * 1024;
-  int mchunks = target;
-  int maxch = (nS + SIG_WARPS - 1) / SIG_WARPS;
-  if (use_ff) maxch = (nS + 2 * FF_B - 1) / (2 * FF_B);  // at least two load batches per q
-  if (mchunks > maxch) mchunks = maxch;
-  if (mchunks < 1) mchunks = 1;
-  const int mper = (nS + mchunks - 1) / mchunks;
-  mchunks = (nS + mper - 1) / mper;
-  // mixed sweep: when few orbitals are active, the q range is split over CTAs too
   const int nq = N - nR - nC;
-  int qgroups = 1;
-  if (use_ff) {
-    const int gmax = nq / (2 * SIG_WARPS) > 1 ? nq / (2 * SIG_WARPS) : 1;
-    qgroups = target / mchunks;
-    if (qgroups > gmax) qgroups = gmax;
-    if (qgroups < 1) qgroups = 1;
-  }
-  int qper = (nq + qgroups - 1) / qgroups;
-  qper = (qper + SIG_WARPS - 1) / SIG_WARPS * SIG_WARPS;
-  qgroups = (nq + qper - 1) / qper;
-  if (qgroups < 1) qgroups = 1;
-  const int nchunks = mchunks * qgroups;
-  double* part = nullptr;
-  // every (chunk, p) entry the consumers read is written by the sweep: no clearing needed
-  QK_TRY(qk_wst(ctx, W_MISC, (size_t)3 * nchunks * N + 64, &part));
+  // the mixed sweep keeps e and Om in shared memory; beyond that it takes the FP64 sweep
+  const size_t ff_smem = (size_t)N * 16 + (size_t)nS * 8;
+  const bool use_ff = ff && !doSRG && eta == 0.0 && ff_smem <= NEWT_SMEM_MAX;
   SigArgs a;
   a.N = N; a.nC = nC; a.nO = nO; a.nR = nR; a.nS = nS;
-  a.nchunks = nchunks; a.mper = mper; a.mchunks = mchunks; a.qper = qper;
   a.doSRG = doSRG; a.eta = eta; a.flow = flow;
-  a.eq = eq; a.wp = wp; a.Om = Om; a.rho = rho; a.list = list; a.nact = nact; a.part = part;
-  if (ptiles > 0 && nS > 0) {
-    if (use_ff) {
-      const size_t with_om = base + (size_t)mper * sizeof(float2);
-      const int om_smem = with_om <= 40 * 1024;
-      SigFF f{ff->R, ff->OmF, ff->bad, ff->tau, om_smem};
-      k_sigma_partial_ff<<<dim3(ptiles, nchunks), SIG_WARPS * 32, om_smem ? with_om : base,
-                           ctx->stream>>>(a, f);
-    } else {
-      k_sigma_partial<<<dim3(ptiles, nchunks), SIG_WARPS * 32, N * sizeof(double), ctx->stream>>>(a);
+  a.eq = eq; a.wp = wp; a.Om = Om; a.rho = rho; a.list = list; a.nact = nact;
+  double* part = nullptr;
+  int nchunks = 1;
+  if (use_ff) {
+    // a CTA per (orbital, q group): groups so that about cm CTAs per SM are in flight
+    const int items = nact_p > 0 ? nact_p : 1;
+    int qgroups = (cm * ctx->num_sms + items - 1) / items;
+    const int gmax = nq / FFT_WARPS > 1 ? nq / FFT_WARPS : 1;
+    if (qgroups > gmax) qgroups = gmax;
+    if (qgroups < 1) qgroups = 1;
+    const int qper = (nq + qgroups - 1) / qgroups;
+    qgroups = (nq + qper - 1) / qper;
+    if (qgroups < 1) qgroups = 1;
+    nchunks = qgroups;
+    a.nchunks = nchunks; a.mper = nS; a.mchunks = 1; a.qper = qper;
+    // every (chunk, p) entry the consumers read is written by the sweep: no clearing needed
+    QK_TRY(qk_wst(ctx, W_MISC, (size_t)3 * nchunks * N + 64, &part));
+    a.part = part;
+    if (nact_p > 0 && nS > 0) {
+      static std::once_flag once;
+      static cudaError_t attr_err = cudaSuccess;
+      std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(k_sigma_partial_ffT,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)NEWT_SMEM_MAX);
+      });
+      QK_CK(attr_err);
+      SigFF f{ff->R, ff->OmF, ff->bad, ff->tau};
+      k_sigma_partial_ffT<<<dim3(nact_p, nchunks), FFT_WARPS * 32, ff_smem, ctx->stream>>>(a, f);
+      QK_LAUNCHED();
     }
-    QK_LAUNCHED();
+  } else {
+    const int ptiles = (nact_p + 31) / 32;
+    const int target =
+        (cm * ctx->num_sms + (ptiles > 0 ? ptiles : 1) - 1) / (ptiles > 0 ? ptiles : 1);
+    int mchunks = target;
+    const int maxch = (nS + SIG_WARPS - 1) / SIG_WARPS;
+    if (mchunks > maxch) mchunks = maxch;
+    if (mchunks < 1) mchunks = 1;
+    const int mper = (nS + mchunks - 1) / mchunks;
+    mchunks = (nS + mper - 1) / mper;
+    nchunks = mchunks;
+    a.nchunks = nchunks; a.mper = mper; a.mchunks = mchunks; a.qper = nq;
+    QK_TRY(qk_wst(ctx, W_MISC, (size_t)3 * nchunks * N + 64, &part));
+    a.part = part;
+    if (ptiles > 0 && nS > 0) {
+      k_sigma_partial<<<dim3(ptiles, nchunks), SIG_WARPS * 32, N * sizeof(double), ctx->stream>>>(a);
+      QK_LAUNCHED();
+    }
   }
   *part_out = part;
   *nchunks_out = nchunks;
@@ -856,11 +953,11 @@ int qk_sigma_ff_prep(qk_ctx* ctx, int N, int nS, const double* rho, const double
   float2* OmF = (float2*)of;
   int* bad = (int*)(of + 2 * (size_t)nS);
   QK_CK(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
-  long long blocks = (n + 255) / 256;
-  const long long cap = 16LL * ctx->num_sms;
-  if (blocks > cap) blocks = cap;
-  if (blocks < 1) blocks = 1;
-  k_sigma_ff_prep<<<(int)blocks, 256, 0, ctx->stream>>>(n, rho, R, nS, Om, OmF, bad);
+  const dim3 tg((N + 31) / 32, (nS + 31) / 32, N);
+  if (tg.y > 65535 || tg.z > 65535) return qk_fail(ctx, QK_ERR_ARG, "k_sigma_ff_prepT grid");
+  k_sigma_ff_prepT<<<tg, dim3(32, 8), 0, ctx->stream>>>(N, nS, rho, R);
+  QK_LAUNCHED();
+  k_om_pairs<<<(nS + 255) / 256, 256, 0, ctx->stream>>>(nS, Om, OmF, bad);
   QK_LAUNCHED();
   ff->R = R;
   ff->OmF = OmF;
@@ -881,13 +978,43 @@ int qk_sigma_diag(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC
   return QK_OK;
 }
 
+// certificates of the guess-started roots (all 0 where the pole structure of the certificate
+// does not hold: eta != 0 or SRG, whose searches then all restart from the reference start)
+static int qp_certify(qk_ctx* ctx, int doSRG, double eta, int N, int nC, int nO, int nR, int nS,
+                      const double* e, const double* w0, const QPState& s, const double* Om,
+                      const double* rho, int* cert) {
+  if (doSRG || eta != 0.0) {
+    QK_CK(cudaMemsetAsync(cert, 0, sizeof(int) * N, ctx->stream));
+    return QK_OK;
+  }
+  const int nact = N - nR - nC;
+  const int ptiles = (nact + 31) / 32;
+  int nchunks = (4 * ctx->num_sms + ptiles - 1) / (ptiles > 0 ? ptiles : 1);
+  const int maxch = (nS + SIG_WARPS - 1) / SIG_WARPS;
+  if (nchunks > maxch) nchunks = maxch;
+  if (nchunks < 1) nchunks = 1;
+  const int mper = (nS + nchunks - 1) / nchunks;
+  nchunks = (nS + mper - 1) / mper;
+  double* part = nullptr;
+  QK_TRY(qk_wst(ctx, W_MISC, (size_t)CERT_ACC * nchunks * N + 64, &part));
+  QK_CK(cudaMemsetAsync(part, 0, sizeof(double) * CERT_ACC * (size_t)nchunks * N, ctx->stream));
+  if (ptiles > 0) {
+    k_cert_partial<<<dim3(ptiles, nchunks), SIG_WARPS * 32, N * sizeof(double), ctx->stream>>>(
+        N, nC, nO, nR, nS, nchunks, mper, e, w0, s, Om, rho, part);
+    QK_LAUNCHED();
+  }
+  k_cert_final<<<(N + 127) / 128, 128, 0, ctx->stream>>>(N, nC, nR, nchunks, part, w0, s, cert);
+  QK_LAUNCHED();
+  return QK_OK;
+}
+
 int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC, int nO, int nR,
                  int nS, const double* eHF, const double* Om, const double* rho,
                  const double* eGWlin, const double* eOld, double* eGW, double* Z,
                  const double* w_guess, int guess_maxit, const qk_sigma_ff* ff,
                  const int* guess_fromref) {
   double* st = nullptr;
-  QK_TRY(qk_wst(ctx, W_M2, (size_t)8 * N + 64, &st));
+  QK_TRY(qk_wst(ctx, W_M2, (size_t)9 * N + 64, &st));
   QPState s;
   s.w = st;
   s.df = st + N;
@@ -907,10 +1034,9 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
   // tunable per nS bucket: 1 (default) = persistent kernel, 2 = per-step sweeps
   const bool persistent = ff && !doSRG && eta == 0.0 && newt_smem <= NEWT_SMEM_MAX &&
                           qk_tune_get(ctx, TUNE_QP_PERSIST, (long long)nS, 1) != 2;
-  float* Rt = nullptr;
+  const float* Rt = ff ? ff->R : nullptr;  // p-major R of qk_sigma_ff_prep
   int* queue = nullptr;
   if (persistent) {
-    QK_TRY(qk_wst(ctx, W_RHO32T, (size_t)N * N * nS + 32, &Rt));
     QK_TRY(qk_wst(ctx, W_QPQUEUE, 16, &queue));
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
@@ -919,15 +1045,13 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
                                       (int)NEWT_SMEM_MAX);
     });
     QK_CK(attr_err);
-    dim3 tg((N + 31) / 32, (nS + 31) / 32, N);
-    if (tg.y > 65535 || tg.z > 65535) return qk_fail(ctx, QK_ERR_ARG, "k_r_pmajor grid");
-    k_r_pmajor<<<tg, dim3(32, 8), 0, ctx->stream>>>(N, nS, ff->R, Rt);
-    QK_LAUNCHED();
   }
   for (int phase = w_guess ? 1 : 2; phase <= 2; ++phase) {
-    const int maxit = phase == 1 ? guess_maxit : QP_MAXIT;
+    const int maxit = phase == 1 ? guess_maxit : ctx->newton_maxit;
     if (phase == 2 && w_guess) {
-      k_qp_restart<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, eGWlin, eHF, s);
+      int* cert = (int*)(st + 8 * N);
+      QK_TRY(qp_certify(ctx, doSRG, eta, N, nC, nO, nR, nS, eOld, eGWlin, s, Om, rho, cert));
+      k_qp_restart<<<1, 1024, 0, ctx->stream>>>(N, nC, nR, eGWlin, cert, s, ctx->newton_maxit);
       QK_LAUNCHED();
     }
     if (persistent) {
@@ -958,7 +1082,8 @@ int qk_qp_newton(qk_ctx* ctx, int doSRG, double eta, double flow, int N, int nC,
       }
     }
   }
-  k_qp_finish<<<(N + 255) / 256, 256, 0, ctx->stream>>>(N, nC, nR, eGWlin, s, eGW, Z, ctx->d_status);
+  k_qp_finish<<<(N + 255) / 256, 256, 0, ctx->stream>>>(N, nC, nR, eGWlin, s, eGW, Z, ctx->d_status,
+                                                        ctx->newton_maxit);
   QK_LAUNCHED();
   if (ctx->capturing) return QK_OK;  // no host readback inside a graph
   // per-orbital Newton step counts and Sigma evaluations for diagnostics (qk_get_qp_iters)

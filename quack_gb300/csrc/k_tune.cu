@@ -85,6 +85,25 @@ extern "C" {
 
 int qk_tune_set(qk_ctx* ctx, const char* name, long long size, int value) {
   if (!ctx || !name) return QK_ERR_ARG;
+  // context-wide settings (size ignored)
+  if (!strcmp(name, "newton_maxit")) {
+    if (value < 1 || value > 4096) return QK_ERR_ARG;
+    ctx->newton_maxit = value;
+    return QK_OK;
+  }
+  if (!strcmp(name, "fail_alloc")) {
+    if (value < 0) return QK_ERR_ARG;
+    ctx->fail_alloc_in = value;
+    return QK_OK;
+  }
+  if (!strcmp(name, "spin_limit")) {
+    if (value < 0) return QK_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    QK_CK(cudaMemcpyAsync(ctx->d_status + 1, &value, sizeof(int), cudaMemcpyHostToDevice,
+                          ctx->stream));
+    QK_CK(cudaStreamSynchronize(ctx->stream));
+    return QK_OK;
+  }
   for (int p = 0; p < TUNE_NUM; ++p)
     if (!strcmp(name, k_tune_names[p])) {
       ctx->tune[p][bucket_of(size)] = value;
@@ -95,6 +114,7 @@ int qk_tune_set(qk_ctx* ctx, const char* name, long long size, int value) {
 
 int qk_tune_query(const qk_ctx* ctx, const char* name, long long size) {
   if (!ctx || !name) return -1;
+  if (!strcmp(name, "newton_maxit")) return ctx->newton_maxit;
   for (int p = 0; p < TUNE_NUM; ++p)
     if (!strcmp(name, k_tune_names[p])) return ctx->tune[p][bucket_of(size)];
   return -1;

@@ -5,6 +5,11 @@
 // Workers pull systems from a shared queue ordered by decreasing cost (nS^3), so the large
 // systems start first and the small ones fill the gaps; the GPU runs the workers' kernels
 // concurrently (the cooperative tridiagonalisation of a small system occupies only a few SMs).
+// The tridiagonalisations, the dominant cost, do not run one system at a time: the workers hand
+// their matrices to a grouped launch (qk_tri_service, k_eig.cu) that tridiagonalises all the
+// workers' current matrices at once, a CTA group per matrix sized by its n^3 work, each group with
+// its own bounded barrier -- one persistent cooperative launch per round instead of a whole-GPU
+// launch per system.
 // A failing or non-converged system is recorded in its status word and does not stop the batch.
 #include <algorithm>
 #include <atomic>
@@ -56,9 +61,13 @@ extern "C" int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int metho
     // the caller's tuned launch parameters and learned QP model apply to every worker (the
     // model is only read: its inference writes the worker's own workspace)
     std::memcpy(w->tune, ctx->tune, sizeof(ctx->tune));
+    w->newton_maxit = ctx->newton_maxit;
     w->mlp = ctx->mlp;
     QK_TRY(qk_order_after_default(w));
   }
+  qk_tri_service* svc = qk_tri_service_new(ctx, n_workers);
+  if (!svc) return qk_fail(ctx, QK_ERR_CUDA, "could not create the grouped tridiagonalisation");
+  for (int wi = 0; wi < n_workers; ++wi) ctx->workers[wi]->tri_service = svc;
   std::vector<Item> order(nsys);
   for (int i = 0; i < nsys; ++i) {
     const double nS = (double)(desc[i].nO - desc[i].nC) * (desc[i].nOrb - desc[i].nO - desc[i].nR);
@@ -109,12 +118,15 @@ extern "C" int qk_gw_batch_L_dev(qk_ctx* ctx, const qk_gw_params* prm, int metho
       if (EcRPA) EcRPA[i] = ec;
       if (nSCF) nSCF[i] = method == 1 ? ns : 1;
     }
+    qk_tri_service_worker_done(svc);
     cudaStreamSynchronize(w->stream);
   };
   std::vector<std::thread> th;
   for (int wi = 1; wi < n_workers; ++wi) th.emplace_back(run, wi);
   run(0);
   for (auto& t : th) t.join();
+  for (int wi = 0; wi < n_workers; ++wi) ctx->workers[wi]->tri_service = nullptr;
+  qk_tri_service_free(svc);
   long long launches = 0;
   for (auto* w : ctx->workers) launches += w->launches;
   ctx->launches = launches;  // for diagnostics: the batch's own launch total

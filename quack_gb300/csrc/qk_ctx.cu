@@ -29,6 +29,10 @@ int qk_ws(qk_ctx* ctx, int slot, size_t bytes, void** out) {
   DevBuf& b = ctx->buf[slot];
   if (bytes == 0) bytes = 16;
   if (b.bytes < bytes) {
+    // failure-path hook: the armed n-th growing allocation fails as cudaMalloc would
+    if (ctx->fail_alloc_in > 0 && --ctx->fail_alloc_in == 0)
+      return qk_fail(ctx, QK_ERR_NOMEM, "cudaMalloc(workspace) failed (simulated by the "
+                                        "fail_alloc hook)");
     if (b.p) {
       cudaError_t e = cudaStreamSynchronize(ctx->stream);
       if (e != cudaSuccess) return qk_cuda_fail(ctx, e, "cudaStreamSynchronize", __FILE__, __LINE__);
@@ -140,6 +144,7 @@ int qk_finalize(qk_ctx* ctx) {
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
+  if (ctx->ev_tri) cudaEventDestroy(ctx->ev_tri);
   if (ctx->copy_stream) {
     cudaStreamSynchronize(ctx->copy_stream);
     cudaStreamDestroy(ctx->copy_stream);
@@ -169,6 +174,13 @@ int qk_get_timings(const qk_ctx* ctx, double* ms, int n) {
   return QK_OK;
 }
 
+int qk_last_device_status(const qk_ctx* ctx) { return ctx ? ctx->last_dev_status : 0; }
+int qk_batch_group_stats(const qk_ctx* ctx, long long* launches, long long* matrices) {
+  if (!ctx) return QK_ERR_ARG;
+  if (launches) *launches = ctx->tri_groups;
+  if (matrices) *matrices = ctx->tri_grouped;
+  return QK_OK;
+}
 const char* qk_timing_name(int i) { return (i >= 0 && i < T_NUM) ? k_timing_names[i] : ""; }
 int qk_num_timings(void) { return T_NUM; }
 long long qk_launch_count(const qk_ctx* ctx) { return ctx ? ctx->launches : 0; }

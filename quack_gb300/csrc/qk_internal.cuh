@@ -7,17 +7,7 @@
 #include <vector>
 #include "../../include/qkgw.h"
 
-// ------------------------------------------------------------------------------------------
-// device status bits (written by kernels instead of trapping; read back by the host)
-// ------------------------------------------------------------------------------------------
-enum : int {
-  QKD_BARRIER_TIMEOUT = 1,   // a bounded grid/group barrier wait expired
-  QKD_BAD_INDEX = 2,         // an index check failed
-  QKD_NEG_AMB = 4,           // A-B had a negative eigenvalue (reference prints a warning)
-  QKD_NEG_OMEGA = 8,         // Casida produced a negative Omega^2 (reference prints a warning)
-  QKD_QP_NOCONV = 16,        // a Newton QP search hit 64 iterations (reference prints "Cvg Failed!")
-  QKD_MBAR_TIMEOUT = 32      // an mbarrier wait expired in a tensor-core kernel
-};
+// device status bits (QKD_*, written by kernels instead of trapping) are in qkgw.h
 
 // stage timers (device time via cudaEvents on the context stream)
 enum {
@@ -38,8 +28,10 @@ enum {
   W_ERI = 0, W_E, W_M, W_V, W_ZT, W_EIGWORK, W_TRI, W_SLAB, W_RHO, W_XPY, W_XMY, W_VEC, W_PART,
   W_MISC, W_HOST_A, W_HOST_B, W_SPLIT_A, W_SPLIT_B, W_M2, W_SPLITK, W_QPLIST, W_VEC2, W_KMAT, W_BATCHIO, W_MLPIO, W_FEAT, W_GUESS, W_TUNE, W_TMAT, W_TMAT2, W_RHO32, W_OMF, W_TFAC, W_STEBZ,
   W_QUAD, W_QLT, W_QPV, W_QL, W_QX, W_QQ, W_QD, W_BSE, W_BSEU, W_BSER, W_BSEK, W_ERIPACK,
-  W_QSR1, W_QSR2, W_QSJK, W_QSMAT, W_QSDIIS, W_QSIN, W_RHO32T, W_QPQUEUE, W_ACF, W_NUMBUF
+  W_QSR1, W_QSR2, W_QSJK, W_QSMAT, W_QSDIIS, W_QSIN, W_QPQUEUE, W_ACF, W_NUMBUF
 };
+
+struct qk_tri_service;  // grouped tridiagonalisation for the batch workers (k_eig.cu)
 
 struct qk_ctx {
   int device = 0;
@@ -58,7 +50,13 @@ struct qk_ctx {
   DevBuf buf[W_NUMBUF];
   long long launches = 0;
   int stage_precision = QK_PREC_FP64;
-  int sytrd_max_ctas = 0;  // cap on the tridiagonalisation grid (batch workers share the GPU)  // tier of the stage-level drop-ins (qk_set_stage_precision)
+  int sytrd_max_ctas = 0;  // cap on the tridiagonalisation grid (batch workers share the GPU)
+  int newton_maxit = 64;   // Newton steps of the graphical QP solve (RGW_QP_graph.f90:38)
+  int fail_alloc_in = 0;   // > 0: the n-th next growing workspace allocation fails (test hook)
+  qk_tri_service* tri_service = nullptr;  // batch worker: tridiagonalise through the group launch
+  cudaEvent_t ev_tri = nullptr;           // end of this context's work before a group launch
+  long long tri_groups = 0;               // grouped tridiagonalisation launches of the last batch
+  long long tri_grouped = 0;              // matrices they tridiagonalised
   int last_dev_status = 0;
   bool time_eig = true;  // stage timers inside the eigensolver (off for the eigenvalue-only pass)
   std::vector<int> qp_iters;  // Newton steps per orbital of the last QP solve
@@ -213,6 +211,12 @@ int qk_bse_dev(qk_ctx* ctx, int TDA_W, int TDA, int singlet, int triplet, int ex
 
 // dense symmetric eigensolver pieces.  backtransform: 0 = leave Zt as the eigenvectors of the
 // tridiagonal matrix, 1 = back-transform in FP64, 2 = back-transform with FP32 products.
+// Grouped tridiagonalisation service of the batched driver: workers' tridiagonalisations are
+// collected until every active worker has submitted one (or finished), then run as ONE
+// cooperative launch of k_sytrd_grouped with a CTA group per matrix.
+qk_tri_service* qk_tri_service_new(qk_ctx* parent, int n_workers);
+void qk_tri_service_worker_done(qk_tri_service* svc);
+void qk_tri_service_free(qk_tri_service* svc);
 int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, int want_vectors,
                int backtransform = 1);
 int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols, int fp32 = 0);
@@ -239,7 +243,8 @@ int qk_launch_slab_gather(qk_ctx* ctx, int N, int nC, int nO, int nR, const doub
 
 // self-energy / QP pieces (k_sigma.cu)
 // Mixed-tier pole sums (eta = 0, no SRG): terms with |eps| >= tau in FP32 from R = 2 rho^2
-// (FP32) and Om as (hi, lo) float pairs, the terms within tau of a pole in FP64 from rho.
+// (FP32, p-major: R[m + nS (q + N p)]) and Om as (hi, lo) float pairs, the terms within tau of a
+// pole in FP64 from rho.
 struct qk_sigma_ff {
   const float* R = nullptr;
   const float2* OmF = nullptr;
@@ -293,6 +298,14 @@ int qk_gemm_bf16x3_nt(qk_ctx* ctx, int m, int n, int k, const double* A, long lo
 // ------------------------------------------------------------------------------------------
 #define QK_MAX_SPIN (1u << 25)
 
+// Poll limit of the bounded grid barriers: the context's status block holds an optional
+// override in its second word (set by qk_tune_set(ctx, "spin_limit", ., n); 0 = QK_MAX_SPIN),
+// so that a test can make a barrier wait run out and check the reported status.
+__device__ __forceinline__ unsigned qk_spin_limit(const int* status) {
+  const unsigned v = (unsigned)((const volatile int*)status)[1];
+  return v ? v : QK_MAX_SPIN;
+}
+
 __device__ __forceinline__ unsigned qk_ld_acquire(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -300,8 +313,8 @@ __device__ __forceinline__ unsigned qk_ld_acquire(const unsigned* p) {
 }
 
 // Monotone-counter barrier over `nblocks` co-resident CTAs (cooperative launch guarantees
-// co-residency).  Bounded: after QK_MAX_SPIN polls it records QKD_BARRIER_TIMEOUT and returns
-// false; callers then leave the kernel.  `epoch` counts barriers passed by this CTA.
+// co-residency).  Bounded: after qk_spin_limit(status) polls it records QKD_BARRIER_TIMEOUT and
+// returns false; callers then leave the kernel.  `epoch` counts barriers passed by this CTA.
 __device__ __forceinline__ bool qk_grid_barrier(unsigned* counter, unsigned nblocks,
                                                 unsigned& epoch, int* status) {
   __shared__ int s_ok;
@@ -310,11 +323,12 @@ __device__ __forceinline__ bool qk_grid_barrier(unsigned* counter, unsigned nblo
     int ok = 1;
     epoch++;
     unsigned target = epoch * nblocks;
+    const unsigned limit = qk_spin_limit(status);
     __threadfence();
     atomicAdd(counter, 1u);
     unsigned spins = 0;
     while (qk_ld_acquire(counter) < target) {
-      if (++spins > QK_MAX_SPIN) { atomicOr(status, QKD_BARRIER_TIMEOUT); ok = 0; break; }
+      if (++spins > limit) { atomicOr(status, QKD_BARRIER_TIMEOUT); ok = 0; break; }
       if (spins > 64) __nanosleep(64);
     }
     if (ok && (*((volatile int*)status) & QKD_BARRIER_TIMEOUT)) ok = 0;

@@ -484,6 +484,9 @@ def test_batched_driver_vs_oracle(ctx, method):
         assert np.max(np.abs(got - ref["eGW"]) / scale) < 1e-7, i
         if method == 1:
             assert r["nSCF"][i] == ref["nSCF"]
+    # the tridiagonalisations ran as grouped launches, several matrices per launch
+    launches, matrices = ctx.batch_group_stats()
+    assert launches > 0 and matrices > launches
 
 
 def test_batched_driver_isolates_bad_system(ctx):
