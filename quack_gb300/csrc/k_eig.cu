@@ -861,65 +861,46 @@ struct qk_tri_service {
 
 namespace {
 
-// CTAs per request: proportional to the n^3 work, at least one, at most what the matrix can use
-// (one 32 x 128 trailing block per CTA, as in the single-matrix launch), all within one CTA per SM
-void tri_split(const std::vector<qk_tri_service::Req>& rq, int sms, int* cta0) {
-  const int R = (int)rq.size();
-  std::vector<double> wgt(R);
-  std::vector<int> g(R), cap(R);
-  double tot = 0.0;
-  for (int r = 0; r < R; ++r) {
-    const double n = rq[r].ta.n;
-    wgt[r] = n * n * n;
-    tot += wgt[r];
-    const long long want = (long long)rq[r].ta.n * rq[r].ta.n / (32 * 128) + 1;
-    cap[r] = (int)(want < sms ? want : sms);
-  }
-  int used = 0;
-  for (int r = 0; r < R; ++r) {
-    int v = (int)((double)sms * wgt[r] / (tot > 0.0 ? tot : 1.0));
-    v = v < 1 ? 1 : (v > cap[r] ? cap[r] : v);
-    g[r] = v;
-    used += v;
-  }
-  // hand the SMs left over to the largest requests still below their cap
-  while (used < sms) {
-    int best = -1;
-    for (int r = 0; r < R; ++r)
-      if (g[r] < cap[r] && (best < 0 || wgt[r] / g[r] > wgt[best] / g[best])) best = r;
-    if (best < 0) break;
-    ++g[best];
-    ++used;
-  }
-  while (used > sms) {  // R > sms cannot happen (R <= TRI_GROUP_MAX < SMs); keep it safe anyway
-    int best = 0;
-    for (int r = 1; r < R; ++r)
-      if (g[r] > g[best]) best = r;
-    if (g[best] <= 1) break;
-    --g[best];
-    --used;
-  }
-  cta0[0] = 0;
-  for (int r = 0; r < R; ++r) cta0[r + 1] = cta0[r] + g[r];
+// CTAs of one matrix in a grouped launch: a fixed function of n alone, so that a matrix is
+// tridiagonalised the same way (the same tile assignment, hence the same rounding) whatever the
+// other matrices of its group -- the batched results repeat bitwise.  About one CTA per 49152
+// trailing elements balances the FP64 work per CTA against the per-column latency (~8 us); at
+// most one 32 x 128 trailing block per CTA, as in the single-matrix launch, and the whole GPU.
+int tri_group_ctas(int n, int sms) {
+  const long long n2 = (long long)n * n;
+  long long g = (n2 + 49151) / 49152;
+  const long long want = n2 / (32 * 128) + 1;
+  if (g > want) g = want;
+  if (g > sms) g = sms;
+  return g < 1 ? 1 : (int)g;
 }
 
-// one cooperative launch for all pending requests (called with the lock held)
+// cooperative launches for all pending requests, packed in submission order so that each launch
+// holds at most one CTA per SM (called with the lock held)
 void tri_launch_locked(qk_tri_service* sv) {
   int st = QK_OK;
   const int R = (int)sv->pending.size();
-  TriGroup g;
-  g.nreq = R;
-  size_t smem = 0;
-  for (int r = 0; r < R; ++r) {
-    g.req[r] = sv->pending[r].ta;
-    const size_t need = TRI_TILE_BYTES + 3 * (size_t)g.req[r].n * sizeof(double);
-    smem = need > smem ? need : smem;
+  const int sms = sv->parent->num_sms;
+  for (int r = 0; r < R; ++r)
     if (cudaStreamWaitEvent(sv->stream, sv->pending[r].ready, 0) != cudaSuccess) st = QK_ERR_CUDA;
-  }
-  tri_split(sv->pending, sv->parent->num_sms, g.cta0);
-  if (st == QK_OK) {
+  int r0 = 0;
+  while (st == QK_OK && r0 < R) {
+    TriGroup g;
+    g.nreq = 0;
+    g.cta0[0] = 0;
+    size_t smem = 0;
+    while (r0 + g.nreq < R && g.nreq < TRI_GROUP_MAX) {
+      const TriArgs& ta = sv->pending[r0 + g.nreq].ta;
+      const int c = tri_group_ctas(ta.n, sms);
+      if (g.nreq > 0 && g.cta0[g.nreq] + c > sms) break;
+      g.req[g.nreq] = ta;
+      g.cta0[g.nreq + 1] = g.cta0[g.nreq] + c;
+      const size_t need = TRI_TILE_BYTES + 3 * (size_t)ta.n * sizeof(double);
+      smem = need > smem ? need : smem;
+      g.nreq++;
+    }
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(g.cta0[R]);
+    cfg.gridDim = dim3(g.cta0[g.nreq]);
     cfg.blockDim = dim3(TRI_THREADS);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = sv->stream;
@@ -930,7 +911,8 @@ void tri_launch_locked(qk_tri_service* sv) {
     cfg.numAttrs = 1;
     if (cudaLaunchKernelEx(&cfg, k_sytrd_grouped, g) != cudaSuccess) st = QK_ERR_CUDA;
     sv->launches++;
-    sv->matrices += R;
+    sv->matrices += g.nreq;
+    r0 += g.nreq;
   }
   if (cudaEventRecord(sv->done, sv->stream) != cudaSuccess) st = QK_ERR_CUDA;
   // every requester's stream continues after the group (enqueued before they wake up)

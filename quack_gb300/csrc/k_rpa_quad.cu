@@ -110,7 +110,7 @@ __device__ __forceinline__ unsigned long long pc_key(double v, int i) {
 // factor does not depend on the order of the atomics: every CTA reads the same final maximum.
 // The pivot row is staged in shared memory and each row's entries are loaded 4 per lane at once,
 // so a step costs a few L2 round trips plus the barrier (~12 us per pivot at nS = 3600).
-__global__ void __launch_bounds__(1024) k_pchol(PcArgs a) {
+__global__ void __launch_bounds__(1024, 1) k_pchol(PcArgs a) {
   extern __shared__ double lp[];  // the pivot row of L (a.rmax doubles)
   __shared__ unsigned long long s_key;
   __shared__ double s_rp, s_inv, s_tol;
@@ -308,35 +308,39 @@ __global__ void __launch_bounds__(256) k_chol_blk(int r, int kb, int nb, double*
 
 // Panel below the diagonal block: P = S(rows, kb:kb+nb) L11^-T, one row per thread, held in
 // registers; column-oriented so that the updates of one step are independent.
-__global__ void __launch_bounds__(128) k_chol_trsm(int r, int kb, int nb, double* __restrict__ S) {
-  __shared__ double L[CB][CB + 1];
-  __shared__ double rinv[CB];
+constexpr int TRSM_THREADS = 128;
+constexpr size_t TRSM_SMEM = sizeof(double) * ((size_t)CB * (CB + 1) + CB + (size_t)CB * TRSM_THREADS);
+
+// Rows below the diagonal block: S_row <- S_row L^-T (forward substitution over the block's
+// columns, one thread per row).  The row being solved lives in shared memory (column c of all
+// the CTA's rows contiguous, so the accesses are conflict-free): a CB-long row in registers
+// spilled, as the compiler keeps the unrolled loop's operands live.
+__global__ void __launch_bounds__(TRSM_THREADS) k_chol_trsm(int r, int kb, int nb,
+                                                            double* __restrict__ S) {
+  extern __shared__ double sm_trsm[];
+  double* L = sm_trsm;                      // CB x (CB + 1)
+  double* rinv = L + CB * (CB + 1);         // CB
+  double* xs = rinv + CB;                   // CB x TRSM_THREADS
   const int q = blockIdx.y, tid = threadIdx.x;
   double* Sq = S + (long long)q * r * r;
   for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
     const int j = idx % nb, k = idx / nb;
-    L[j][k] = (j >= k) ? Sq[(kb + j) + (long long)r * (kb + k)] : 0.0;
+    L[j * (CB + 1) + k] = (j >= k) ? Sq[(kb + j) + (long long)r * (kb + k)] : 0.0;
   }
   __syncthreads();
-  for (int c = tid; c < nb; c += blockDim.x) rinv[c] = 1.0 / L[c][c];
+  for (int c = tid; c < nb; c += blockDim.x) rinv[c] = 1.0 / L[c * (CB + 1) + c];
   __syncthreads();
   const int row = kb + nb + blockIdx.x * blockDim.x + tid;
   if (row >= r) return;
-  double x[CB];
-#pragma unroll
-  for (int c = 0; c < CB; ++c) x[c] = c < nb ? Sq[row + (long long)r * (kb + c)] : 0.0;
-#pragma unroll
-  for (int c = 0; c < CB; ++c) {
-    if (c < nb) {
-      x[c] *= rinv[c];
-#pragma unroll
-      for (int k = c + 1; k < CB; ++k)
-        if (k < nb) x[k] = fma(-x[c], L[k][c], x[k]);
-    }
+  double* x = xs + tid;
+  for (int c = 0; c < nb; ++c) x[c * TRSM_THREADS] = Sq[row + (long long)r * (kb + c)];
+  for (int c = 0; c < nb; ++c) {
+    const double xc = x[c * TRSM_THREADS] * rinv[c];
+    x[c * TRSM_THREADS] = xc;
+    for (int k = c + 1; k < nb; ++k)
+      x[k * TRSM_THREADS] = fma(-xc, L[k * (CB + 1) + c], x[k * TRSM_THREADS]);
   }
-#pragma unroll
-  for (int c = 0; c < CB; ++c)
-    if (c < nb) Sq[row + (long long)r * (kb + c)] = x[c];
+  for (int c = 0; c < nb; ++c) Sq[row + (long long)r * (kb + c)] = x[c * TRSM_THREADS];
 }
 
 __global__ void k_quad_final(int nq, const double* __restrict__ wt, const double* __restrict__ acc,
@@ -529,6 +533,15 @@ int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, 
   if (nch < 1) nch = 1;
   if (nch > nq) nch = nq;
   double *Q = nullptr, *qd = nullptr;
+  {
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+      attr_err = cudaFuncSetAttribute(k_chol_trsm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)TRSM_SMEM);
+    });
+    QK_CK(attr_err);
+  }
   QK_TRY(qk_wst(ctx, W_QQ, (size_t)r2 * nch, &Q));
   QK_TRY(qk_wst(ctx, W_QD, (size_t)r * nch, &qd));
   for (int q0 = 0; q0 < nq; q0 += nch) {
@@ -547,7 +560,8 @@ int qk_rpa_ec_quad(qk_ctx* ctx, int N, int nC, int nO, int nR, const double* e, 
       QK_LAUNCHED();
       const int m = r - kb - nb;
       if (m <= 0) break;
-      k_chol_trsm<<<dim3((m + 127) / 128, nc), 128, 0, ctx->stream>>>(r, kb, nb, Q);
+      k_chol_trsm<<<dim3((m + TRSM_THREADS - 1) / TRSM_THREADS, nc), TRSM_THREADS, TRSM_SMEM,
+                    ctx->stream>>>(r, kb, nb, Q);
       QK_LAUNCHED();
       double* P = Q + (kb + nb) + (long long)r * kb;
       double* S22 = Q + (kb + nb) + (long long)r * (kb + nb);

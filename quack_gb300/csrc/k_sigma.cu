@@ -75,8 +75,12 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial(SigArgs a) {
     const double w = a.wp ? a.wp[p] : se[p];
     const double eta2 = a.eta * a.eta;
     const long long N1 = N, N2 = N1 * N1;
-    const int m0 = blockIdx.y * a.mper;
+    // chunk = (m range, q range)
+    const int mc = blockIdx.y % a.mchunks, qg = blockIdx.y / a.mchunks;
+    const int m0 = mc * a.mper;
     const int m1 = min(a.nS, m0 + a.mper);
+    const int qa = a.nC + qg * a.qper, qb = min(pend, qa + a.qper);
+    const int qo0 = qa, qo1 = min(a.nO, qb), qv0 = max(a.nO, qa), qv1 = qb;
     for (int m = m0 + warp; m < m1; m += SIG_WARPS) {
       const double om = __ldg(a.Om + m);
       const double* r = a.rho + p + N2 * m;
@@ -85,14 +89,14 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial(SigArgs a) {
       if (!a.doSRG && a.eta == 0.0) {
         // eta = 0: num*eps/(eps^2) = num/eps and num*eps^2/(eps^2)^2 = num/eps^2
         double s1 = 0.0, s2 = 0.0, d1 = 0.0;
-        for (int q = a.nC; q < a.nO; ++q) {
+        for (int q = qo0; q < qo1; ++q) {
           const double x = __ldg(r + N1 * q);
           const double ir = rcp_nr(w - se[q] + om);
           const double t = (x * x) * ir;
           s1 += t;
           d1 = fma(t, ir, d1);
         }
-        for (int q = a.nO; q < pend; ++q) {
+        for (int q = qv0; q < qv1; ++q) {
           const double x = __ldg(r + N1 * q);
           const double ir = rcp_nr(w - se[q] - om);
           const double t = (x * x) * ir;
@@ -104,7 +108,7 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial(SigArgs a) {
         ds -= 2.0 * d1;
         continue;
       }
-      for (int q = a.nC; q < a.nO; ++q) {
+      for (int q = qo0; q < qo1; ++q) {
         const double x = __ldg(r + N1 * q);
         const double num = 2.0 * x * x;
         const double eps = w - se[q] + om;
@@ -122,7 +126,7 @@ __global__ void __launch_bounds__(SIG_WARPS * 32) k_sigma_partial(SigArgs a) {
       }
       socc_acc += so;
       // virtual part: eps = w - e_a - Om_m
-      for (int q = a.nO; q < pend; ++q) {
+      for (int q = qv0; q < qv1; ++q) {
         const double x = __ldg(r + N1 * q);
         const double num = 2.0 * x * x;
         const double eps = w - se[q] - om;
@@ -878,11 +882,16 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
                        int nS, const double* eq, const double* wp, const double* Om,
                        const double* rho, const int* list, const int* nact, double** part_out,
                        int* nchunks_out, const qk_sigma_ff* ff = nullptr, int nact_max = -1) {
-  // p tiles: all orbitals, or (with a compacted list) an upper bound on the active count
+  // p tiles: all orbitals, or (with a compacted list) an upper bound on the active count.  The
+  // partition of every orbital's terms into chunks (the summation order) is fixed by N and nS
+  // alone -- never by how many orbitals are still searching -- so an orbital's Sigma(w) is the
+  // same bits whatever the other orbitals do (a Newton search started elsewhere for some
+  // orbitals must not perturb the chaotic searches of the others)
   int nact_p = N - nR - nC;
   if (list && nact_max >= 0 && nact_max < nact_p) nact_p = nact_max;
   const int cm = qk_tune_get(ctx, TUNE_SIGMA_CHUNKS, (long long)nS, 4);
   const int nq = N - nR - nC;
+  const int nall = nq;  // the orbital count the partition is chosen for
   // the mixed sweep keeps e and Om in shared memory; beyond that it takes the FP64 sweep
   const size_t ff_smem = (size_t)N * 16 + (size_t)nS * 8;
   const bool use_ff = ff && !doSRG && eta == 0.0 && ff_smem <= NEWT_SMEM_MAX;
@@ -893,8 +902,9 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
   double* part = nullptr;
   int nchunks = 1;
   if (use_ff) {
-    // a CTA per (orbital, q group): groups so that about cm CTAs per SM are in flight
-    const int items = nact_p > 0 ? nact_p : 1;
+    // a CTA per (orbital, q group): groups so that about cm CTAs per SM are in flight when
+    // every orbital is active
+    const int items = nall > 0 ? nall : 1;
     int qgroups = (cm * ctx->num_sms + items - 1) / items;
     const int gmax = nq / FFT_WARPS > 1 ? nq / FFT_WARPS : 1;
     if (qgroups > gmax) qgroups = gmax;
@@ -921,17 +931,21 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
       QK_LAUNCHED();
     }
   } else {
-    const int ptiles = (nact_p + 31) / 32;
-    const int target =
-        (cm * ctx->num_sms + (ptiles > 0 ? ptiles : 1) - 1) / (ptiles > 0 ? ptiles : 1);
-    int mchunks = target;
+    const int ptiles = (nact_p + 31) / 32;                // launched
+    const int ptiles_all = (nall + 31) / 32 > 0 ? (nall + 31) / 32 : 1;
+    int mchunks = (cm * ctx->num_sms + ptiles_all - 1) / ptiles_all;
     const int maxch = (nS + SIG_WARPS - 1) / SIG_WARPS;
     if (mchunks > maxch) mchunks = maxch;
     if (mchunks < 1) mchunks = 1;
     const int mper = (nS + mchunks - 1) / mchunks;
     mchunks = (nS + mper - 1) / mper;
-    nchunks = mchunks;
-    a.nchunks = nchunks; a.mper = mper; a.mchunks = mchunks; a.qper = nq;
+    // q groups as well, so that a single tile of still-searching orbitals fills the GPU
+    int qgroups = nq / 16 < ptiles_all ? nq / 16 : ptiles_all;
+    if (qgroups < 1) qgroups = 1;
+    const int qper = (nq + qgroups - 1) / qgroups;
+    qgroups = (nq + qper - 1) / qper;
+    nchunks = mchunks * qgroups;
+    a.nchunks = nchunks; a.mper = mper; a.mchunks = mchunks; a.qper = qper;
     QK_TRY(qk_wst(ctx, W_MISC, (size_t)3 * nchunks * N + 64, &part));
     a.part = part;
     if (ptiles > 0 && nS > 0) {

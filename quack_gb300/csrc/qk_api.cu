@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstring>
 #include <vector>
+#include <climits>
 #include "qk_internal.cuh"
 
 namespace {
@@ -1155,9 +1156,18 @@ int aotomo_dev(qk_ctx* ctx, int nBas, int nOrb, const double* dc, double* X, dou
                     (long long)(O * O * O)};
   double* src = X;
   double* dst = Y;
+  // stage precision BF16X3: the quarter transforms in double-float (FP32 pairs, exact products;
+  // ~1e-13 of sum |a b|) -- the MO coefficients of near-linearly-dependent bases cancel too much
+  // for the BF16x3 / FP32-product tiers (the reason qsGW's mixed tier uses it as well)
+  const bool df = ctx->stage_precision == QK_PREC_BF16X3;
   for (int s = 0; s < 4; ++s) {
-    QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)R[s], nOrb, nBas, 1.0, src, nBas, 0, dc, nBas, 0, 0.0, dst,
-                    R[s], 0, 1));
+    if (R[s] > INT_MAX) return qk_fail(ctx, QK_ERR_ARG, "AO->MO quarter transform too large");
+    if (df)
+      QK_TRY(qk_gemm_df(ctx, 'T', 'N', (int)R[s], nOrb, nBas, 1.0, src, nBas, 0, dc, nBas, 0, 0.0,
+                        dst, R[s], 0, 1));
+    else
+      QK_TRY(qk_dgemm(ctx, 'T', 'N', (int)R[s], nOrb, nBas, 1.0, src, nBas, 0, dc, nBas, 0, 0.0,
+                      dst, R[s], 0, 1));
     double* t = src;
     src = dst;
     dst = t;

@@ -155,8 +155,11 @@ def train(model: QPModel, X, T, epochs=200, batch=256, lr=2e-3):
     return model.train_dev(len(T), dX.data_ptr(), dT.data_ptr(), epochs, min(batch, len(T)), lr)
 
 
-def evaluate(ctx, model, systems, tol=1e-8):
-    """Newton from the reference start vs from the learned guess on held-out systems."""
+def evaluate(ctx, model, systems, tol=1e-6):
+    """Newton from the reference start vs from the learned guess on held-out systems.  A QP
+    energy counts as the same root when the two agree within tol * max(1, |Sigma|): the Newton
+    threshold |f| <= 1e-6 of RGW_QP_graph.f90:59 (two searches that end on one root stop at
+    different iterates)."""
     ctx.set_qp_model(model)
     rows = []
     for s in systems:

@@ -123,3 +123,20 @@ def test_batched_driver_uses_the_attached_model(ctx):
             assert np.max(np.abs(got[conv] - one["eGW"][conv])) < 1e-8, i
     finally:
         ctx.set_qp_model(None)
+
+
+@pytest.mark.parametrize("N,nO,seed", [(57, 7, 22), (96, 12, 23), (150, 19, 24)])
+def test_started_elsewhere_keeps_reference_roots(ctx, N, nO, seed):
+    """The restart protocol alone (qp_guess = 2: searches started at eHF, kept only where the
+    root certificate proves the reference search ends there, the others restarted from eGWlin)
+    gives the reference-start roots for every orbital whose reference search converged -- also
+    the chaotic ones, which need each orbital's Sigma(w) to be independent of which other
+    orbitals are still searching."""
+    s = synth.small_system(N, nO, 3 * N, seed)
+    a = learned.run_g0w0_L(ctx, s, api.GWOptions())
+    b = learned.run_g0w0_L(ctx, s, api.GWOptions(qp_guess=2))
+    ok = (a["iters"] < 64) & np.isfinite(a["eGW"])
+    d = np.abs(a["eGW"] - b["eGW"])
+    assert ok.sum() > N // 2
+    # same root: within the Newton threshold (the two searches stop at different iterates)
+    assert np.all(d[ok] < 1e-6 * np.maximum(1.0, np.abs(a["SigC"][ok]))), np.where(ok & (d > 1e-6))

@@ -189,6 +189,24 @@ def test_aotomo(ctx):
     assert np.allclose(out, ref, rtol=1e-12, atol=1e-11)
 
 
+def test_aotomo_mixed_stage_precision(ctx):
+    """The mixed tier's quarter transforms run in double-float (FP32 pairs, exact products):
+    ~1e-13 of sum |a b| even with coefficients that cancel (x30 here)."""
+    rng = np.random.default_rng(19)
+    nB, nOrb = 24, 20
+    ERI = rng.standard_normal((nB,) * 4)
+    c = 30.0 * rng.standard_normal((nB, nOrb))
+    ref = O.AOtoMO_ERI_RHF(nB, nOrb, c, ERI)
+    bound = np.einsum("pqrs,pi,qj,rk,sl->ijkl", np.abs(ERI), np.abs(c), np.abs(c), np.abs(c),
+                      np.abs(c), optimize=True)
+    ctx.set_stage_precision(api.QK_PREC_BF16X3)
+    try:
+        out = api.AOtoMO_ERI_RHF(nB, nOrb, c, ERI, ctx=ctx)
+    finally:
+        ctx.set_stage_precision(api.QK_PREC_FP64)
+    assert np.max(np.abs(out - ref) / bound) < 1e-12
+
+
 def test_diis(ctx):
     rng = np.random.default_rng(4)
     n, md = 10, 4

@@ -52,3 +52,24 @@ def test_g0w0_newton_bitwise_repeatable(ctx):
             assert np.array_equal(r[k], runs[0][k], equal_nan=True), k
         assert np.array_equal(np.float64(r["EcRPA"]), np.float64(runs[0]["EcRPA"]),
                               equal_nan=True)
+
+
+def test_batched_driver_bitwise_repeatable(ctx):
+    """The batched driver groups the workers' tridiagonalisations into shared launches whose
+    composition depends on timing; each matrix's CTA group is fixed by its size, so the results
+    do not change between runs."""
+    import torch
+    rng = np.random.default_rng(77)
+    systems = [synth.gen_system(N, synth.n_occ(N), 3 * N, rng) for N in (40, 57, 24, 66, 31, 48)]
+    desc, Lf, Ef = api.pack_systems(systems)
+    dL = torch.from_numpy(Lf).cuda()
+    dE = torch.from_numpy(Ef).cuda()
+    outs = []
+    for nw in (3, 3, 2):
+        dG = torch.zeros_like(dE)
+        r = api.gw_batch_L_dev(api.GWOptions(), 0, desc, dL.data_ptr(), dE.data_ptr(),
+                               dG.data_ptr(), n_workers=nw, ctx=ctx)
+        assert r["rc"] == api.QK_OK, (r["error"], r["status"])
+        outs.append(dG.cpu().numpy())
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0], equal_nan=True)
