@@ -407,7 +407,9 @@ int qk_RGW_self_energy_diag_noalloc_dev(double eta, int nBas, int nOrb, int nC, 
  * it gives up and reports QKD_BARRIER_TIMEOUT, QK_ERR_DEVICE from the call; 0 = the built-in
  * limit of about a second) and "fail_alloc" (n > 0: the n-th next workspace allocation that
  * would call cudaMalloc fails instead, with QK_ERR_NOMEM; 0 disarms) -- hooks for the
- * failure-path tests. */
+ * failure-path tests -- and "guess_gate" (learned-guess start rule: 0 where the model agrees with
+ * the Halley step from eGWlin, 1 the model's prediction everywhere, 2 the Halley step
+ * everywhere; results are the reference start's in every case). */
 int qk_autotune(qk_ctx* ctx, int nOrb, int nS, int flags);
 int qk_tune_set(qk_ctx* ctx, const char* name, long long size, int value);
 int qk_tune_query(const qk_ctx* ctx, const char* name, long long size);

@@ -111,8 +111,12 @@ struct TriGridSlice {
   __device__ __forceinline__ int rank() const { return *(const volatile int*)(s + 1); }
 };
 
-// The tridiagonalisation of one matrix by a group of co-resident CTAs.
-template <class Grp>
+// The tridiagonalisation of one matrix by a group of co-resident CTAs.  With kFixed, every
+// rounded quantity is independent of the group size: ||A||_F is summed over fixed column chunks
+// and each tile's row partial sum is split into the exact accumulators on its own (not summed
+// over a warp's run of tiles, whose extent depends on the group size), so the result is the same
+// bits for any number of CTAs -- the grouped launch then sizes the groups freely.
+template <class Grp, bool kFixed>
 __device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
   extern __shared__ double sm[];
   __shared__ double s_pj, s_dj, s_alpha, s_sc[9], s_fro;
@@ -138,7 +142,7 @@ __device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
 
   // ---- ||A||_F (bounds every p element's partial sums): fixed per-thread order, per-CTA slot,
   // then every CTA adds the slots in the same order, so all CTAs hold the same value ----
-  {
+  if (!kFixed) {
     double fs = 0.0;
     for (int c = grp.rank(); c < n; c += grp.size()) {
       const double* col = a.A + a.lda * c;
@@ -152,6 +156,28 @@ __device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
     if (tid == 0) {
       double t = 0.0;
       for (int b = 0; b < grp.size(); ++b) t += __ldcg(a.fslot + b);
+      s_fro = sqrt(t);
+    }
+    __syncthreads();
+  } else {
+    // chunks of 32 columns, one slot each (n <= 32768), summed in chunk order
+    const int nch = (n + 31) / 32;
+    for (int ch = grp.rank(); ch < nch; ch += grp.size()) {
+      double fs = 0.0;
+      const int c1 = 32 * ch + 32 < n ? 32 * ch + 32 : n;
+      for (int c = 32 * ch; c < c1; ++c) {
+        const double* col = a.A + a.lda * c;
+        for (int i = c + tid; i < n; i += nt) {
+          const double x = __ldcg(col + i);
+          fs = fma(i == c ? x : x + x, x, fs);
+        }
+      }
+      tri_block_sum(fs, ytile, nt, [&](double t) { __stcg(a.fslot + ch, t); });
+    }
+    if (!qk_grid_barrier(a.bar, grp.size(), epoch, a.status)) return;
+    if (tid == 0) {
+      double t = 0.0;
+      for (int b = 0; b < nch; ++b) t += __ldcg(a.fslot + b);
       s_fro = sqrt(t);
     }
     __syncthreads();
@@ -310,14 +336,22 @@ __device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
         int i = 0;
         bool rowok = false;
         double ri = 0.0, si = 0.0, rowacc = 0.0;
+        double rb1 = 0.0, rb2 = 0.0;  // kFixed: the row's tile sums, already split (exact)
         for (int it = it0; it < it1; ++it) {
           while (it >= off + 2 * bi + 2) {
             off += 2 * bi + 2;
             ++bi;
           }
           if (bi != cur) {
-            if (cur >= 0 && wantp && rowok)
+            if (kFixed) {
+              if (cur >= 0 && wantp && rowok) {
+                atomicAdd(pnext + i, rb1);
+                atomicAdd(pnext2 + i, rb2);
+              }
+              rb1 = rb2 = 0.0;
+            } else if (cur >= 0 && wantp && rowok) {
               tri_exact_add(pnext + i, pnext2 + i, rowacc, s_sc[7], s_sc[8]);
+            }
             cur = bi;
             i = r0 + 32 * bi + lane;
             rowok = i < n;
@@ -364,10 +398,26 @@ __device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
             const int c = c0 + u;
             if (hh == 0 && c < n && c <= r0 + 32 * bi + 31)
               tri_exact_add(pnext + c, pnext2 + c, cs, s_sc[7], s_sc[8]);
+            if (kFixed) {
+              // this tile's row sum into the row's exact register accumulators
+              const double c1 = s_sc[7], c2 = s_sc[8];
+              const double q1 = __dsub_rn(__dadd_rn(rowacc, c1), c1);
+              const double r1 = __dsub_rn(rowacc, q1);
+              rb1 = __dadd_rn(rb1, q1);
+              rb2 = __dadd_rn(rb2, __dsub_rn(__dadd_rn(r1, c2), c2));
+              rowacc = 0.0;
+            }
           }
           __syncwarp();
         }
-        if (wantp && rowok) tri_exact_add(pnext + i, pnext2 + i, rowacc, s_sc[7], s_sc[8]);
+        if (kFixed) {
+          if (wantp && rowok) {
+            atomicAdd(pnext + i, rb1);
+            atomicAdd(pnext2 + i, rb2);
+          }
+        } else if (wantp && rowok) {
+          tri_exact_add(pnext + i, pnext2 + i, rowacc, s_sc[7], s_sc[8]);
+        }
       }
     }
     if (!qk_grid_barrier(a.bar, grp.size(), epoch, a.status)) return;
@@ -381,7 +431,7 @@ __device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
 }
 
 __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
-  sytrd_body(a, TriGridWhole{});
+  sytrd_body<TriGridWhole, false>(a, TriGridWhole{});
 }
 
 // Many tridiagonalisations in one cooperative launch: request r owns the CTAs
@@ -404,7 +454,7 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd_grouped(const __grid_cons
     s_grp[1] = (int)blockIdx.x - g.cta0[r];
   }
   __syncthreads();
-  sytrd_body(g.req[r], TriGridSlice{s_grp});
+  sytrd_body<TriGridSlice, true>(g.req[r], TriGridSlice{s_grp});
 }
 
 // Gershgorin bounds, pivmin, ||T||_1 and e^2 (single block).
@@ -861,46 +911,67 @@ struct qk_tri_service {
 
 namespace {
 
-// CTAs of one matrix in a grouped launch: a fixed function of n alone, so that a matrix is
-// tridiagonalised the same way (the same tile assignment, hence the same rounding) whatever the
-// other matrices of its group -- the batched results repeat bitwise.  About one CTA per 49152
-// trailing elements balances the FP64 work per CTA against the per-column latency (~8 us); at
-// most one 32 x 128 trailing block per CTA, as in the single-matrix launch, and the whole GPU.
-int tri_group_ctas(int n, int sms) {
-  const long long n2 = (long long)n * n;
-  long long g = (n2 + 49151) / 49152;
-  const long long want = n2 / (32 * 128) + 1;
-  if (g > want) g = want;
-  if (g > sms) g = sms;
-  return g < 1 ? 1 : (int)g;
+// CTAs per request: proportional to the n^3 work, at least one, at most what the matrix can use
+// (one 32 x 128 trailing block per CTA, as in the single-matrix launch), all within one CTA per
+// SM.  The grouped kernel's arithmetic does not depend on a group's size (sytrd_body<., true>),
+// so this split, which changes with the launch's other matrices, never changes a result.
+void tri_split(const std::vector<qk_tri_service::Req>& rq, int sms, int* cta0) {
+  const int R = (int)rq.size();
+  std::vector<double> wgt(R);
+  std::vector<int> g(R), cap(R);
+  double tot = 0.0;
+  for (int r = 0; r < R; ++r) {
+    const double n = rq[r].ta.n;
+    wgt[r] = n * n * n;
+    tot += wgt[r];
+    const long long want = (long long)rq[r].ta.n * rq[r].ta.n / (32 * 128) + 1;
+    cap[r] = (int)(want < sms ? want : sms);
+  }
+  int used = 0;
+  for (int r = 0; r < R; ++r) {
+    int v = (int)((double)sms * wgt[r] / (tot > 0.0 ? tot : 1.0));
+    v = v < 1 ? 1 : (v > cap[r] ? cap[r] : v);
+    g[r] = v;
+    used += v;
+  }
+  // hand the SMs left over to the requests with the most work per CTA, below their cap
+  while (used < sms) {
+    int best = -1;
+    for (int r = 0; r < R; ++r)
+      if (g[r] < cap[r] && (best < 0 || wgt[r] / g[r] > wgt[best] / g[best])) best = r;
+    if (best < 0) break;
+    ++g[best];
+    ++used;
+  }
+  while (used > sms) {  // R <= TRI_GROUP_MAX < SMs, so at least one request has g > 1
+    int best = 0;
+    for (int r = 1; r < R; ++r)
+      if (g[r] > g[best]) best = r;
+    if (g[best] <= 1) break;
+    --g[best];
+    --used;
+  }
+  cta0[0] = 0;
+  for (int r = 0; r < R; ++r) cta0[r + 1] = cta0[r] + g[r];
 }
 
-// cooperative launches for all pending requests, packed in submission order so that each launch
-// holds at most one CTA per SM (called with the lock held)
+// one cooperative launch for all pending requests (called with the lock held)
 void tri_launch_locked(qk_tri_service* sv) {
   int st = QK_OK;
   const int R = (int)sv->pending.size();
-  const int sms = sv->parent->num_sms;
-  for (int r = 0; r < R; ++r)
+  TriGroup g;
+  g.nreq = R;
+  size_t smem = 0;
+  for (int r = 0; r < R; ++r) {
+    g.req[r] = sv->pending[r].ta;
+    const size_t need = TRI_TILE_BYTES + 3 * (size_t)g.req[r].n * sizeof(double);
+    smem = need > smem ? need : smem;
     if (cudaStreamWaitEvent(sv->stream, sv->pending[r].ready, 0) != cudaSuccess) st = QK_ERR_CUDA;
-  int r0 = 0;
-  while (st == QK_OK && r0 < R) {
-    TriGroup g;
-    g.nreq = 0;
-    g.cta0[0] = 0;
-    size_t smem = 0;
-    while (r0 + g.nreq < R && g.nreq < TRI_GROUP_MAX) {
-      const TriArgs& ta = sv->pending[r0 + g.nreq].ta;
-      const int c = tri_group_ctas(ta.n, sms);
-      if (g.nreq > 0 && g.cta0[g.nreq] + c > sms) break;
-      g.req[g.nreq] = ta;
-      g.cta0[g.nreq + 1] = g.cta0[g.nreq] + c;
-      const size_t need = TRI_TILE_BYTES + 3 * (size_t)ta.n * sizeof(double);
-      smem = need > smem ? need : smem;
-      g.nreq++;
-    }
+  }
+  tri_split(sv->pending, sv->parent->num_sms, g.cta0);
+  if (st == QK_OK) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(g.cta0[g.nreq]);
+    cfg.gridDim = dim3(g.cta0[R]);
     cfg.blockDim = dim3(TRI_THREADS);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = sv->stream;
@@ -911,8 +982,7 @@ void tri_launch_locked(qk_tri_service* sv) {
     cfg.numAttrs = 1;
     if (cudaLaunchKernelEx(&cfg, k_sytrd_grouped, g) != cudaSuccess) st = QK_ERR_CUDA;
     sv->launches++;
-    sv->matrices += g.nreq;
-    r0 += g.nreq;
+    sv->matrices += R;
   }
   if (cudaEventRecord(sv->done, sv->stream) != cudaSuccess) st = QK_ERR_CUDA;
   // every requester's stream continues after the group (enqueued before they wake up)

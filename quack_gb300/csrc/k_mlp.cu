@@ -189,17 +189,26 @@ __global__ void k_normalise(int n, const float* __restrict__ F, const float* __r
 // equation from eGWlin (FP64, from the feature sweep) is exact to far below the network's
 // resolution where the search is regular; where the two agree to QK_GUESS_AGREE the search starts
 // at eGWlin + h, elsewhere it starts at the reference start and follows the reference trajectory.
+// Gate 1 (the context setting "guess_gate" = 1) starts every search at eGWlin + y instead, and
+// gate 2 at eGWlin + h wherever h exists; the root certificate keeps the results either way.
 constexpr double QK_GUESS_AGREE = 3e-3;  // Ha
 __global__ void k_guess(int n, const float* __restrict__ Y, float ymean, float ystd,
                         const double* __restrict__ base, const double* __restrict__ hal,
-                        double* __restrict__ w0, int* __restrict__ fromref) {
+                        double* __restrict__ w0, int* __restrict__ fromref, int gate) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double y = (double)(Y[i] * ystd + ymean);
   const double h = hal[i];
-  const bool agree = (h == h) && fabs(y - h) <= QK_GUESS_AGREE;
-  w0[i] = agree ? base[i] + h : base[i];
-  fromref[i] = agree ? 0 : 1;
+  bool use = (h == h) && fabs(y - h) <= QK_GUESS_AGREE;
+  double start = base[i] + h;
+  if (gate == 1) {
+    use = y == y;
+    start = base[i] + y;
+  } else if (gate == 2) {
+    use = h == h;
+  }
+  w0[i] = use ? start : base[i];
+  fromref[i] = use ? 0 : 1;
 }
 
 }  // namespace
@@ -244,7 +253,8 @@ int qk_guess_from_model(qk_ctx* ctx, int N, const float* F, const double* base, 
   k_mlp_infer_bf16<<<(N + 127) / 128, 128, 0, ctx->stream>>>(N, X, m->P, Y);
   QK_LAUNCHED();
   k_guess<<<(N + 127) / 128, 128, 0, ctx->stream>>>(N, Y, m->ymean, m->ystd, base, hal, w0,
-                                                   fromref);
+                                                   fromref,
+                                                   ctx->guess_gate);
   QK_LAUNCHED();
   return QK_OK;
 }

@@ -214,7 +214,7 @@ struct SigFF {
 // pipe, the warp's per-(p,q) sums added into float-float (TwoSum) accumulators; inside it the
 // FP64 terms of k_sigma_partial.  Same partial-sum layout as k_sigma_partial (chunk = q group).
 constexpr int FFT_WARPS = 8;
-constexpr int FFT_U = 8;
+constexpr int FFT_U = 16;
 
 __global__ void __launch_bounds__(FFT_WARPS * 32) k_sigma_partial_ffT(SigArgs a, SigFF f) {
   // dynamic shared memory: e (N doubles) | e as float pairs (N) | Om pairs (nS)
@@ -902,10 +902,24 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
   double* part = nullptr;
   int nchunks = 1;
   if (use_ff) {
-    // a CTA per (orbital, q group): groups so that about cm CTAs per SM are in flight when
-    // every orbital is active
+    // a CTA per (orbital, q group): as many groups as fill the resident CTA slots in one wave
+    // when every orbital is active (a second, partial wave left SMs idle)
     const int items = nall > 0 ? nall : 1;
-    int qgroups = (cm * ctx->num_sms + items - 1) / items;
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+      attr_err = cudaFuncSetAttribute(k_sigma_partial_ffT,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)NEWT_SMEM_MAX);
+    });
+    QK_CK(attr_err);
+    int ffT_per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ffT_per_sm, k_sigma_partial_ffT,
+                                                      FFT_WARPS * 32, ff_smem) != cudaSuccess ||
+        ffT_per_sm < 1)
+      ffT_per_sm = 1;
+    (void)cm;
+    int qgroups = ffT_per_sm * ctx->num_sms / items;
     const int gmax = nq / FFT_WARPS > 1 ? nq / FFT_WARPS : 1;
     if (qgroups > gmax) qgroups = gmax;
     if (qgroups < 1) qgroups = 1;
@@ -918,14 +932,6 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
     QK_TRY(qk_wst(ctx, W_MISC, (size_t)3 * nchunks * N + 64, &part));
     a.part = part;
     if (nact_p > 0 && nS > 0) {
-      static std::once_flag once;
-      static cudaError_t attr_err = cudaSuccess;
-      std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(k_sigma_partial_ffT,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)NEWT_SMEM_MAX);
-      });
-      QK_CK(attr_err);
       SigFF f{ff->R, ff->OmF, ff->bad, ff->tau};
       k_sigma_partial_ffT<<<dim3(nact_p, nchunks), FFT_WARPS * 32, ff_smem, ctx->stream>>>(a, f);
       QK_LAUNCHED();
@@ -939,9 +945,9 @@ static int sigma_sweep(qk_ctx* ctx, int doSRG, double eta, double flow, int N, i
     if (mchunks < 1) mchunks = 1;
     const int mper = (nS + mchunks - 1) / mchunks;
     mchunks = (nS + mper - 1) / mper;
-    // q groups as well, so that a single tile of still-searching orbitals fills the GPU
-    int qgroups = nq / 16 < ptiles_all ? nq / 16 : ptiles_all;
-    if (qgroups < 1) qgroups = 1;
+    // two q groups as well, so that the last few still-searching orbitals keep more SMs busy
+    // (more groups cost staging overhead when all orbitals are active)
+    int qgroups = nq >= 32 ? 2 : 1;
     const int qper = (nq + qgroups - 1) / qgroups;
     qgroups = (nq + qper - 1) / qper;
     nchunks = mchunks * qgroups;

@@ -91,6 +91,11 @@ int qk_tune_set(qk_ctx* ctx, const char* name, long long size, int value) {
     ctx->newton_maxit = value;
     return QK_OK;
   }
+  if (!strcmp(name, "guess_gate")) {
+    if (value < 0 || value > 2) return QK_ERR_ARG;
+    ctx->guess_gate = value;
+    return QK_OK;
+  }
   if (!strcmp(name, "fail_alloc")) {
     if (value < 0) return QK_ERR_ARG;
     ctx->fail_alloc_in = value;

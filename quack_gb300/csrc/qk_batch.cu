@@ -7,9 +7,10 @@
 // concurrently (the cooperative tridiagonalisation of a small system occupies only a few SMs).
 // The tridiagonalisations, the dominant cost, do not run one system at a time: the workers hand
 // their matrices to a grouped launch (qk_tri_service, k_eig.cu) that tridiagonalises all the
-// workers' current matrices at once, a CTA group per matrix sized by its n alone (so results do
-// not depend on which matrices share a launch), each group with its own bounded barrier -- one
-// persistent cooperative launch per round instead of a whole-GPU launch per system.
+// workers' current matrices at once, a CTA group per matrix sized by its share of the work, each
+// group with its own bounded barrier -- one persistent cooperative launch per round instead of a
+// whole-GPU launch per system.  The grouped kernel's arithmetic does not depend on the group's
+// size, so results do not depend on which matrices share a launch.
 // A failing or non-converged system is recorded in its status word and does not stop the batch.
 #include <algorithm>
 #include <atomic>

@@ -2,6 +2,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <nvtx3/nvToolsExt.h>
 #include "qk_internal.cuh"
 
 static const char* k_timing_names[T_NUM] = {"casida_build", "tridiag", "bisect",  "stein",
@@ -73,10 +74,18 @@ int qk_order_after_default(qk_ctx* ctx) {
   return QK_OK;
 }
 
+// Each stage is also an NVTX range (host-side span of the enqueueing, named like the timer), so
+// that a profiler timeline shows the library's stages; start/end pairs by id, not a stack, so
+// nested stages (the eigensolver inside the second Casida) stay well formed.
 void qk_tic(qk_ctx* ctx, int stage) {
+  ctx->nvtx[stage] = nvtxRangeStartA(k_timing_names[stage]);
   if (ctx->timing && !ctx->capturing) cudaEventRecord(ctx->ev[2 * stage], ctx->stream);
 }
 void qk_toc(qk_ctx* ctx, int stage) {
+  if (ctx->nvtx[stage]) {
+    nvtxRangeEnd(ctx->nvtx[stage]);
+    ctx->nvtx[stage] = 0;
+  }
   if (!ctx->timing || ctx->capturing) return;
   cudaEventRecord(ctx->ev[2 * stage + 1], ctx->stream);
   ctx->timings[stage] = -1.0;  // mark pending

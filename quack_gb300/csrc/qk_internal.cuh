@@ -44,6 +44,7 @@ struct qk_ctx {
   bool eri_pending = false;            // the slab gather must wait for ev_copy first
   bool tda_w = false;                  // the drivers' screening Casida in the Tamm-Dancoff form
   double timings[T_NUM] = {};
+  unsigned long long nvtx[T_NUM] = {};  // open NVTX range per stage (0 = none)
   std::string err;
   int* d_status = nullptr;      // device status word
   unsigned* d_bar = nullptr;    // grid-barrier counters (zeroed before each cooperative launch)
@@ -52,6 +53,7 @@ struct qk_ctx {
   int stage_precision = QK_PREC_FP64;
   int sytrd_max_ctas = 0;  // cap on the tridiagonalisation grid (batch workers share the GPU)
   int newton_maxit = 64;   // Newton steps of the graphical QP solve (RGW_QP_graph.f90:38)
+  int guess_gate = 0;      // learned-guess start rule (k_guess: 0 Halley agreement, 1, 2)
   int fail_alloc_in = 0;   // > 0: the n-th next growing workspace allocation fails (test hook)
   qk_tri_service* tri_service = nullptr;  // batch worker: tridiagonalise through the group launch
   cudaEvent_t ev_tri = nullptr;           // end of this context's work before a group launch
