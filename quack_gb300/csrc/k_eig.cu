@@ -66,18 +66,26 @@ __device__ __forceinline__ void tri_block_sum(double v, double* scratch, int cnt
 
 // Order-independent accumulation of the mat-vec partial sums.  Several warps of several CTAs
 // add into each element of p, so plain FP64 atomics would make the result depend on their
-// order.  Each contribution x is instead split into two parts aligned to fixed binary grids
-// (the error-free extraction q = (x + C) - C), and each grid has its own accumulator: every
-// part is a multiple of its grid's spacing and every running sum stays below 2^53 spacings, so
-// all additions are exact and the sums are the same in any order.  The grids come from a bound
-// B >= sum of |x| over all contributions to an element (B = 2 ||A||_F ||u||_2): the first has
-// spacing 2^(E-51) (2^E > B), the second 2^(E-92); the dropped remainder is below 2^(E-93) per
-// contribution, i.e. 2^-80 B for up to 2^13 contributions per element (n <= 2^18).
-__device__ __forceinline__ void tri_exact_add(double* b1, double* b2, double x, double c1,
-                                              double c2) {
-  const double q1 = __dsub_rn(__dadd_rn(x, c1), c1);
-  const double r1 = __dsub_rn(x, q1);
-  const double q2 = __dsub_rn(__dadd_rn(r1, c2), c2);
+// order.  Each contribution x is instead split into two parts aligned to fixed binary grids,
+// and each grid has its own accumulator: every part is a multiple of its grid's spacing and every
+// running sum stays below 2^53 spacings, so all additions are exact and the sums are the same in
+// any order.  The grids come from a bound B >= sum of |x| over all contributions to an element
+// (B = 2 ||A||_F ||u||_2): the first has spacing 2^g1, g1 = E - 51 (2^E > B), the second 2^g2,
+// g2 = E - 92.  A part is its input truncated toward zero to the grid, by clearing low
+// significand bits on the integer pipe (FP64 issue is the scarce resource here), and the
+// remainder is exact: x = q1 + r1, |r1| < 2^g1; r1 = q2 + (dropped, < 2^g2 = 2^-92 2^E).  Up to
+// 2^12 contributions per element keep the second sum exact (n <= 2^16).
+__device__ __forceinline__ double tri_trunc(double x, int g) {
+  const long long b = __double_as_longlong(x);
+  const int k = g - ((int)((b >> 52) & 0x7FF) - 1075);  // low significand bits below 2^g
+  const long long keep = k >= 53 ? (long long)0x8000000000000000ULL   // +-0
+                                 : (k <= 0 ? -1LL : ~((1LL << k) - 1));
+  return __longlong_as_double(b & keep);
+}
+
+__device__ __forceinline__ void tri_exact_add(double* b1, double* b2, double x, int g1) {
+  const double q1 = tri_trunc(x, g1);
+  const double q2 = tri_trunc(__dsub_rn(x, q1), g1 - 41);
   atomicAdd(b1, q1);
   atomicAdd(b2, q2);
 }
@@ -119,7 +127,8 @@ struct TriGridSlice {
 template <class Grp, bool kFixed>
 __device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
   extern __shared__ double sm[];
-  __shared__ double s_pj, s_dj, s_alpha, s_sc[9], s_fro;
+  __shared__ double s_pj, s_dj, s_alpha, s_sc[7], s_fro;
+  __shared__ int s_g1;  // exponent of the first accumulator grid
   const int n = a.n;
   double* ytile = sm;  // one TRI_TC x TRI_TLD tile per warp
   double *vk, *wk, *vk1;
@@ -292,8 +301,7 @@ __device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
         const double bnd = 2.0 * fro * unrm;
         if (bnd > 0.0 && bnd <= DBL_MAX) frexp(bnd, &ex);
         ex = ex < -960 ? -960 : (ex > 1000 ? 1000 : ex);
-        s_sc[7] = ldexp(3.0, ex);
-        s_sc[8] = ldexp(3.0, ex - 41);
+        s_g1 = ex - 51;
       });
       const double dj = s_dj;
       tau1 = s_sc[4];
@@ -350,7 +358,7 @@ __device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
               }
               rb1 = rb2 = 0.0;
             } else if (cur >= 0 && wantp && rowok) {
-              tri_exact_add(pnext + i, pnext2 + i, rowacc, s_sc[7], s_sc[8]);
+              tri_exact_add(pnext + i, pnext2 + i, rowacc, s_g1);
             }
             cur = bi;
             i = r0 + 32 * bi + lane;
@@ -397,14 +405,13 @@ __device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
             cs += __shfl_xor_sync(0xffffffffu, cs, 16);
             const int c = c0 + u;
             if (hh == 0 && c < n && c <= r0 + 32 * bi + 31)
-              tri_exact_add(pnext + c, pnext2 + c, cs, s_sc[7], s_sc[8]);
+              tri_exact_add(pnext + c, pnext2 + c, cs, s_g1);
             if (kFixed) {
               // this tile's row sum into the row's exact register accumulators
-              const double c1 = s_sc[7], c2 = s_sc[8];
-              const double q1 = __dsub_rn(__dadd_rn(rowacc, c1), c1);
-              const double r1 = __dsub_rn(rowacc, q1);
+              const int g1 = s_g1;
+              const double q1 = tri_trunc(rowacc, g1);
               rb1 = __dadd_rn(rb1, q1);
-              rb2 = __dadd_rn(rb2, __dsub_rn(__dadd_rn(r1, c2), c2));
+              rb2 = __dadd_rn(rb2, tri_trunc(__dsub_rn(rowacc, q1), g1 - 41));
               rowacc = 0.0;
             }
           }
@@ -416,7 +423,7 @@ __device__ __forceinline__ void sytrd_body(const TriArgs a, const Grp grp) {
             atomicAdd(pnext2 + i, rb2);
           }
         } else if (wantp && rowok) {
-          tri_exact_add(pnext + i, pnext2 + i, rowacc, s_sc[7], s_sc[8]);
+          tri_exact_add(pnext + i, pnext2 + i, rowacc, s_g1);
         }
       }
     }
