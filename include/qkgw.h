@@ -409,7 +409,9 @@ int qk_RGW_self_energy_diag_noalloc_dev(double eta, int nBas, int nOrb, int nC, 
  * would call cudaMalloc fails instead, with QK_ERR_NOMEM; 0 disarms) -- hooks for the
  * failure-path tests -- and "guess_gate" (learned-guess start rule: 0 where the model agrees with
  * the Halley step from eGWlin, 1 the model's prediction everywhere, 2 the Halley step
- * everywhere; results are the reference start's in every case). */
+ * everywhere; results are the reference start's in every case) and "dsyev_df" (1: qk_dsyev_dev
+ * tridiagonalises in double-float arithmetic on the FP32 pipe, as the mixed tier's Casida solve
+ * does; 0, the default, in FP64). */
 int qk_autotune(qk_ctx* ctx, int nOrb, int nS, int flags);
 int qk_tune_set(qk_ctx* ctx, const char* name, long long size, int value);
 int qk_tune_query(const qk_ctx* ctx, const char* name, long long size);

@@ -99,6 +99,9 @@ struct TriArgs {
   double* tau;
   double* V;
   long long ldv;
+  int df;        // 1: double-float arithmetic on the FP32 pipe (sytrd_df_body)
+  double* vscal;   // df: n slots for the reflectors' scale factors (consumed by k_tri_df_finish)
+  double* dfscale; // df: one slot, the power of two that undoes the matrix scaling
   double* pbuf;  // 6*n: three rotating p vectors, each as two exact accumulators (n + n)
   double* fslot; // one partial sum of ||A||_F^2 per CTA of the group
   double* gvec;  // (CTAs of the group) * 3 * n when vectors do not fit in shared memory
@@ -441,6 +444,552 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd(TriArgs a) {
   sytrd_body<TriGridWhole, false>(a, TriGridWhole{});
 }
 
+// ---------------------------------------------------------------------------------------------
+// Double-float tridiagonalisation (the mixed tier).  GB300 issues one FP64 warp instruction per
+// 64 cycles per SM sub-partition but one FP32 instruction per cycle, so the O(n^3) passes run in
+// double-float arithmetic instead: a value is an unevaluated sum hi + lo of two floats (about 47
+// significant bits), kept in the 8 bytes of the double it replaces.  Products use the exact FP32
+// product error from an FMA (Dekker's two-product), sums use Knuth's two-sum; the lo x lo term
+// and the rounding of the lo parts are dropped ("sloppy" double-float, relative error of each
+// operation about 2^-46 of its operands), so the factorisation stays backward stable with unit
+// roundoff about 2^-46 instead of 2^-53.  The scalar work of each column (reflector, dot
+// products, grid exponents) and every quantity that leaves the kernel (d, e, tau, V) stay FP64;
+// the mat-vec partial sums go into the same exact accumulators as in the FP64 kernel, so the
+// results repeat bitwise too.  Explicit __f*_rn intrinsics keep nvcc from contracting the
+// error-free transformations into FMAs.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 df_fma(float2 acc, float2 a, float2 b) {  // acc + a b
+  const float p = __fmul_rn(a.x, b.x);
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  const float s = __fadd_rn(acc.x, p);
+  const float bb = __fsub_rn(s, acc.x);
+  float t = __fadd_rn(__fsub_rn(acc.x, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  t = __fadd_rn(t, __fadd_rn(acc.y, e));
+  const float h = __fadd_rn(s, t);
+  return make_float2(h, __fsub_rn(t, __fsub_rn(h, s)));
+}
+
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  const float s = __fadd_rn(a.x, b.x);
+  const float bb = __fsub_rn(s, a.x);
+  float t = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+  t = __fadd_rn(t, __fadd_rn(a.y, b.y));
+  const float h = __fadd_rn(s, t);
+  return make_float2(h, __fsub_rn(t, __fsub_rn(h, s)));
+}
+
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  const float h = __fadd_rn(p, e);
+  return make_float2(h, __fsub_rn(e, __fsub_rn(h, p)));
+}
+
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, df_neg(b)); }
+// times a power of two (exact)
+__device__ __forceinline__ float2 df_scale(float2 a, float s) {
+  return make_float2(__fmul_rn(a.x, s), __fmul_rn(a.y, s));
+}
+
+// 1/b: the float reciprocal refined by one Newton step whose residual 1 - b r is formed exactly
+// enough in double-float (1 - fl(b.x r) is exact near 1), relative error about 2^-46
+__device__ __forceinline__ float2 df_rcp(float2 b) {
+  const float r = __frcp_rn(b.x);
+  const float p = __fmul_rn(b.x, r);
+  const float pe = fmaf(b.x, r, -p);
+  const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p), pe), __fmul_rn(b.y, r));
+  const float c = __fmul_rn(r, e);
+  const float h = __fadd_rn(r, c);
+  return make_float2(h, __fsub_rn(c, __fsub_rn(h, r)));
+}
+
+// sqrt(a), a >= 0: the float square root refined by one Newton step on the exact residual
+// a - s^2 (Dekker's product), relative error about 2^-46
+__device__ __forceinline__ float2 df_sqrt(float2 a) {
+  if (!(a.x > 0.f)) return make_float2(a.x == 0.f ? 0.f : __fsqrt_rn(a.x), 0.f);
+  const float s = __fsqrt_rn(a.x);
+  const float p = __fmul_rn(s, s);
+  const float pe = fmaf(s, s, -p);
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.x, p), pe), a.y);
+  const float c = __fdiv_rn(r, __fadd_rn(s, s));
+  const float h = __fadd_rn(s, c);
+  return make_float2(h, __fsub_rn(c, __fsub_rn(h, s)));
+}
+
+// Sum over the CTA in double-float, in a fixed order (butterflies within each warp, then warp 0
+// over the warp sums; df_add is commutative to the bit, so every lane of a butterfly holds the
+// same value); fin(total) runs on thread 0 before the closing barrier publishes its results.
+template <class Fin>
+__device__ __forceinline__ void df_block_sum(float2 v, float2* red, Fin fin) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float2 w;
+    w.x = __shfl_xor_sync(0xffffffffu, v.x, o);
+    w.y = __shfl_xor_sync(0xffffffffu, v.y, o);
+    v = df_add(v, w);
+  }
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? red[lane] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      float2 w;
+      w.x = __shfl_xor_sync(0xffffffffu, v.x, o);
+      w.y = __shfl_xor_sync(0xffffffffu, v.y, o);
+      v = df_add(v, w);
+    }
+    if (lane == 0) fin(v);
+  }
+  __syncthreads();
+}
+
+// FP64 -> double-float by bit operations on the integer pipe (no FP64 issue): hi = x truncated
+// to 24 significant bits, lo = the next 23 bits of x.  |x| < 2^-126 gives 0 (and lo = 0 below
+// 2^-80); infinities and NaN come through in hi.  Callers keep magnitudes inside float's range
+// (the kernel checks ||A||_F first).
+__device__ __forceinline__ float2 df_from_double(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hw = (unsigned)(b >> 32);
+  const unsigned sgn = hw & 0x80000000u;
+  const int e = (int)((hw >> 20) & 0x7FFu);
+  const unsigned m = (unsigned)(b >> 29) & 0x7FFFFFu;
+  if (e == 0x7FF) return make_float2(__uint_as_float(sgn | 0x7F800000u | (m ? 0x400000u : 0u)), 0.f);
+  const int fe = e - 896;  // float's biased exponent
+  if (fe <= 0) return make_float2(0.f, 0.f);
+  if (fe >= 255) return make_float2(__uint_as_float(sgn | 0x7F800000u), 0.f);
+  const float h = __uint_as_float(sgn | ((unsigned)fe << 23) | m);
+  float l = 0.f;
+  if (e >= 943) {
+    // the 23 bits below hi's last one: r * 2^(e - 1069), r < 2^23 converted exactly through
+    // the 2^23 exponent pattern
+    const unsigned r = ((unsigned)b & 0x1FFFFFFFu) >> 6;
+    const float rf = __fsub_rn(__uint_as_float(0x4B000000u | r), 8388608.0f);
+    l = __fmul_rn(rf, __uint_as_float((unsigned)(e - 942) << 23));
+    l = __uint_as_float(__float_as_uint(l) | sgn);
+  }
+  return make_float2(h, l);
+}
+
+// float -> double by bit operations (exact; zeros and subnormals give 0, which only drops
+// magnitudes below 2^-126)
+__device__ __forceinline__ double df_f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xFFu;
+  if (e == 0xFFu) return (double)f;
+  const unsigned long long d =
+      e == 0u ? ((unsigned long long)(u & 0x80000000u) << 32)
+              : ((unsigned long long)(u & 0x80000000u) << 32) |
+                    ((unsigned long long)(e + 896u) << 52) |
+                    ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)d);
+}
+
+// hi + lo as a double: exact (|lo| < ulp(hi), 48 bits in all), one FP64 addition
+__device__ __forceinline__ double df_to_double(float2 a) { return __dadd_rn(df_f2d(a.x), df_f2d(a.y)); }
+
+// The same factorisation as sytrd_body (the same fused rank-2 update and symmetric mat-vec over
+// the same tiles, the same reflector formulas and exact accumulators), with the matrix and the
+// vectors u_k, p~_k, u_{k+1} in double-float.  The lower triangle of A is converted in place
+// (float2 in each double's slot) after the Frobenius norm has been found, scaled by the power of
+// two 2^-ex that brings ||A||_F into [1/2, 1): every double-float intermediate (entries, mat-vec
+// products up to ||A||^2, dot products up to n ||A||^3) then stays far inside float's range, and
+// the scaling is exact.  The per-column scalars (dot products, reflector, update coefficients)
+// are double-float as well, so that no FP64 latency sits on the per-column critical path: the
+// outputs d, e, tau, the reflector scale factors and the unscaled reflectors are stored as
+// double-floats in the slots of their doubles, and k_tri_df_finish converts them afterwards (d and
+// e scaled back by 2^ex; the reflectors do not depend on the scaling).
+template <class Grp, bool kFixed>
+__device__ __forceinline__ void sytrd_df_body(const TriArgs a, const Grp grp) {
+  extern __shared__ double sm[];
+  __shared__ double s_fro;
+  __shared__ float2 s_df[4];  // a1, a2x2, cu, cp of the current step
+  __shared__ float2 s_pj, s_dj, s_alpha, s_beta, s_t1, s_scal;
+  __shared__ float2 s_red[32];
+  __shared__ int s_g1;
+  const int n = a.n;
+  float2* ytile = reinterpret_cast<float2*>(sm);  // one TRI_TC x TRI_TLD tile per warp
+  float2 *vk, *wk, *vk1;
+  if (a.use_smem) {
+    vk = reinterpret_cast<float2*>(sm) + (blockDim.x >> 5) * (TRI_TC * TRI_TLD);
+    wk = vk + n;
+    vk1 = vk + 2 * n;
+  } else {
+    float2* base = reinterpret_cast<float2*>(a.gvec + (size_t)grp.rank() * 3 * n);
+    vk = base;
+    wk = base + n;
+    vk1 = base + 2 * n;
+  }
+  float2* A2 = reinterpret_cast<float2*>(a.A);
+  unsigned epoch = 0;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+  const int totwarps = grp.size() * nwarps;
+  const int gthread = grp.rank() * nt + tid, totthreads = grp.size() * nt;
+  const float2 zero2 = make_float2(0.f, 0.f), one2 = make_float2(1.f, 0.f);
+  float2* V2 = reinterpret_cast<float2*>(a.V);
+  float2 tau_k = zero2, scal_k = one2;
+
+  // ---- ||A||_F exactly as the FP64 body computes it (fixed orders) ----
+  const int nch = kFixed ? (n + 31) / 32 : 0;
+  if (!kFixed) {
+    double fs = 0.0;
+    for (int c = grp.rank(); c < n; c += grp.size()) {
+      const double* col = a.A + a.lda * c;
+      for (int i = c + tid; i < n; i += nt) {
+        const double x = __ldcg(col + i);
+        fs = fma(i == c ? x : x + x, x, fs);
+      }
+    }
+    tri_block_sum(fs, sm, nt, [&](double t) { __stcg(a.fslot + grp.rank(), t); });
+  } else {
+    for (int ch = grp.rank(); ch < nch; ch += grp.size()) {
+      double fs = 0.0;
+      const int c1 = 32 * ch + 32 < n ? 32 * ch + 32 : n;
+      for (int c = 32 * ch; c < c1; ++c) {
+        const double* col = a.A + a.lda * c;
+        for (int i = c + tid; i < n; i += nt) {
+          const double x = __ldcg(col + i);
+          fs = fma(i == c ? x : x + x, x, fs);
+        }
+      }
+      tri_block_sum(fs, sm, nt, [&](double t) { __stcg(a.fslot + ch, t); });
+    }
+  }
+  if (!qk_grid_barrier(a.bar, grp.size(), epoch, a.status)) return;
+  if (tid == 0) {
+    double t = 0.0;
+    const int ns = kFixed ? nch : grp.size();
+    for (int b = 0; b < ns; ++b) t += __ldcg(a.fslot + b);
+    s_fro = sqrt(t);
+  }
+  __syncthreads();
+  // power-of-two scaling (1 for a zero, infinite or NaN norm: those propagate as in FP64)
+  int ex = 0;
+  if (s_fro > 0.0 && s_fro <= DBL_MAX) frexp(s_fro, &ex);
+  const double sc = ldexp(1.0, -ex);
+  const float fro = (float)(s_fro * sc);  // only bounds the accumulator grids
+  if (grp.rank() == 0 && tid == 0) *a.dfscale = ldexp(1.0, ex);
+  // ---- the lower triangle to double-float, in place (each CTA its own columns) ----
+  for (int c = grp.rank(); c < n; c += grp.size()) {
+    double* col = a.A + a.lda * c;
+    for (int i = c + tid; i < n; i += nt)
+      __stcg(A2 + a.lda * c + i, df_from_double(__ldcg(col + i) * sc));
+  }
+  if (!qk_grid_barrier(a.bar, grp.size(), epoch, a.status)) return;
+
+  for (int k = -1; k <= n - 2; ++k) {
+    {
+      double* pz = a.pbuf + (size_t)((k + 2) % 3) * n;
+      double* pz2 = pz + 3 * (size_t)n;
+      for (int i = gthread; i < n; i += totthreads) {
+        __stcg(pz + i, 0.0);
+        __stcg(pz2 + i, 0.0);
+      }
+    }
+    // ---- small phase (redundant in every CTA), as in sytrd_body, on the FP32 pipe ----
+    const int j = k + 1;
+    float2 tau1, scal1;
+    {
+      const double* p = a.pbuf + (size_t)((k + 3) % 3) * n;
+      float2 dot = zero2;
+      for (int i0 = j + tid; i0 < n; i0 += 4 * nt) {
+        float2 xv[4], uv[4];
+        double pv[4], pv2[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int i = i0 + r * nt;
+          xv[r] = i < n ? __ldcg(A2 + i + a.lda * j) : zero2;
+          pv[r] = (k >= 0 && i < n) ? __ldcg(p + i) : 0.0;
+          pv2[r] = (k >= 0 && i < n) ? __ldcg(p + 3 * (size_t)n + i) : 0.0;
+          uv[r] = (k >= 0 && i < n) ? vk[i] : zero2;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int i = i0 + r * nt;
+          if (i < n) {
+            vk1[i] = xv[r];
+            if (k >= 0) {
+              // the two exact accumulators, each split on the integer pipe, added in double-float
+              const float2 pf = df_add(df_from_double(pv[r]), df_from_double(pv2[r]));
+              wk[i] = pf;
+              if (i == j) s_pj = pf;
+              dot = df_fma(dot, pf, uv[r]);
+            }
+          }
+        }
+      }
+      if (k >= 0) {
+        df_block_sum(dot, s_red, [&](float2 t) {
+          // true dot p.v = scal^2 p~.u;  c = tau^2 dot / 2;  w = scal^2 (tau p~ - c u)
+          const float2 s2 = df_mul(scal_k, scal_k);
+          const float2 cc = df_scale(df_mul(df_mul(tau_k, tau_k), df_mul(s2, t)), 0.5f);
+          const float2 b1 = df_mul(tau_k, s2), b2 = df_mul(cc, s2);
+          const float2 u = vk[j];
+          const float2 wj = df_sub(df_mul(b1, s_pj), df_mul(b2, u));
+          s_df[0] = b1;
+          s_df[1] = df_scale(b2, 2.0f);
+          s_df[2] = df_sub(df_mul(b2, u), wj);  // coefficient of u_i in column j
+          s_df[3] = df_neg(df_mul(b1, u));      // coefficient of p~_i in column j
+        });
+      } else {
+        if (tid < 4) s_df[tid] = zero2;
+        __syncthreads();
+      }
+      const float2 cu = s_df[2], cp = s_df[3];
+      float2 ss = zero2;
+      for (int i = j + tid; i < n; i += nt) {
+        float2 x = vk1[i];
+        if (k >= 0) {
+          x = df_fma(df_fma(x, cu, vk[i]), cp, wk[i]);
+          vk1[i] = x;
+        }
+        if (i == j) s_dj = x;
+        else if (i == j + 1) s_alpha = x;
+        else ss = df_fma(ss, x, x);
+      }
+      // Householder reflector of the updated column (dlarfg) in double-float, by thread 0
+      df_block_sum(ss, s_red, [&](float2 sigma) {
+        float2 beta = zero2, t1 = zero2, scal = one2, inv = one2;
+        float unrm = 1.0f;
+        if (j <= n - 2) {
+          const float2 alpha = s_alpha;
+          if (sigma.x == 0.f) {
+            beta = alpha;
+          } else {
+            const float2 r = df_sqrt(df_fma(sigma, alpha, alpha));
+            beta = (__float_as_uint(alpha.x) >> 31) ? r : df_neg(r);  // -copysign(r, alpha)
+            t1 = df_mul(df_sub(beta, alpha), df_rcp(beta));
+            inv = df_sub(alpha, beta);
+            scal = df_rcp(inv);
+            // ||u||_2 from the leading parts, rounded up well past float's rounding
+            unrm = __fmul_ru(__fsqrt_ru(fmaf(inv.x, inv.x, sigma.x)), 1.0001f);
+          }
+          vk1[j + 1] = inv;  // u_{j+1} = 1/scal, so that scal * u_{j+1} = 1
+        }
+        s_beta = beta;
+        s_t1 = t1;
+        s_scal = scal;
+        // grids of the exact accumulators for p~ = A' u (bound 2 ||A||_F ||u||_2, as in FP64)
+        int e2x = 0;
+        const float bnd = __fmul_ru(__fmul_ru(2.0f, fro), unrm);
+        if (bnd > 0.f && bnd <= FLT_MAX) frexpf(bnd, &e2x);
+        s_g1 = e2x - 51;
+      });
+      tau1 = s_t1;
+      scal1 = s_scal;
+      // outputs as double-floats (k_tri_df_finish converts them); the reflector unscaled, its
+      // scale factor beside tau
+      if (grp.rank() == 0 && tid == 0) {
+        reinterpret_cast<float2*>(a.d)[j] = s_dj;
+        if (j <= n - 2) {
+          reinterpret_cast<float2*>(a.e)[j] = s_beta;
+          reinterpret_cast<float2*>(a.tau)[j] = tau1;
+          reinterpret_cast<float2*>(a.vscal)[j] = scal1;
+        }
+      }
+      if (j <= n - 2)
+        for (int i = j + 2 + gthread; i < n; i += totthreads) V2[i + a.ldv * j] = vk1[i];
+    }
+    // ---- big pass: the FP64 body's tiles and order, double-float arithmetic ----
+    const int r0 = k + 2;
+    const int mm = n - r0;
+    if (mm > 0) {
+      double* pnext = a.pbuf + (size_t)((k + 1) % 3) * n;
+      double* pnext2 = pnext + 3 * (size_t)n;
+      const bool upd = (k >= 0);
+      const bool wantp = (j <= n - 2);
+      const float2 a1 = s_df[0], a2x2 = s_df[1];
+      const int nb = (mm + 31) >> 5;
+      const int items = nb * (nb + 1);
+      const int per = (items + totwarps - 1) / totwarps;
+      const int it0 = (warp * grp.size() + grp.rank()) * per;
+      const int it1 = it0 + per < items ? it0 + per : items;
+      float2* tile = ytile + (size_t)warp * (TRI_TC * TRI_TLD);
+      if (it0 < it1) {
+        int bi = (int)((sqrtf(4.0f * (float)it0 + 1.0f) - 1.0f) * 0.5f);
+        while (bi > 0 && bi * (bi + 1) > it0) --bi;
+        while ((bi + 1) * (bi + 2) <= it0) ++bi;
+        int off = bi * (bi + 1);
+        int cur = -1;
+        int i = 0;
+        bool rowok = false;
+        float2 nri = zero2, nsi = zero2, rowacc = zero2;  // -(a1 u_i), -(a1 p~_i - a2x2 u_i)
+        double rb1 = 0.0, rb2 = 0.0;
+        for (int it = it0; it < it1; ++it) {
+          while (it >= off + 2 * bi + 2) {
+            off += 2 * bi + 2;
+            ++bi;
+          }
+          if (bi != cur) {
+            if (kFixed) {
+              if (cur >= 0 && wantp && rowok) {
+                atomicAdd(pnext + i, rb1);
+                atomicAdd(pnext2 + i, rb2);
+              }
+              rb1 = rb2 = 0.0;
+            } else if (cur >= 0 && wantp && rowok) {
+              tri_exact_add(pnext + i, pnext2 + i, df_to_double(rowacc), s_g1);
+            }
+            cur = bi;
+            i = r0 + 32 * bi + lane;
+            rowok = i < n;
+            const float2 ui = (upd && rowok) ? vk[i] : zero2;
+            const float2 pi = (upd && rowok) ? wk[i] : zero2;
+            nri = df_neg(df_mul(a1, ui));
+            nsi = df_neg(df_fma(df_mul(a1, pi), df_neg(a2x2), ui));
+            rowacc = zero2;
+          }
+          const int c0 = r0 + TRI_TC * (it - off);
+          float2* col = A2 + i;
+          if (upd && wantp && it - off < 2 * bi && r0 + 32 * bi + 32 <= n) {
+            // interior tile (the common case): every element strictly below the diagonal and
+            // inside the matrix, so no per-element predicates or index tests
+            const float2* wc = wk + c0;
+            const float2* vc = vk + c0;
+            const float2* v1c = vk1 + c0;
+            float2* q = col + a.lda * c0;
+#pragma unroll 1
+            for (int h = 0; h < TRI_TC; h += 8) {
+              float2 x[8];
+              float2* qq = q;
+#pragma unroll
+              for (int u = 0; u < 8; ++u) {
+                x[u] = __ldcg(qq);
+                qq += a.lda;
+              }
+#pragma unroll
+              for (int u = 0; u < 8; ++u) {
+                const float2 y = df_fma(df_fma(x[u], nri, wc[h + u]), nsi, vc[h + u]);
+                __stcg(q, y);
+                q += a.lda;
+                rowacc = df_fma(rowacc, y, v1c[h + u]);
+                tile[(h + u) * TRI_TLD + lane] = y;
+              }
+            }
+            __syncwarp();
+            const int u = lane & (TRI_TC - 1), hh = lane >> 4;
+            const float2* tp = tile + u * TRI_TLD + 16 * hh;
+            const float2* vr = vk1 + r0 + 32 * bi + 16 * hh;
+            float2 cs = zero2;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) cs = df_fma(cs, tp[r], vr[r]);
+            float2 o;
+            o.x = __shfl_xor_sync(0xffffffffu, cs.x, 16);
+            o.y = __shfl_xor_sync(0xffffffffu, cs.y, 16);
+            cs = df_add(cs, o);
+            if (hh == 0) tri_exact_add(pnext + c0 + u, pnext2 + c0 + u, df_to_double(cs), s_g1);
+            if (kFixed) {
+              const int g1 = s_g1;
+              const double ra = df_to_double(rowacc);
+              const double q1 = tri_trunc(ra, g1);
+              rb1 = __dadd_rn(rb1, q1);
+              rb2 = __dadd_rn(rb2, tri_trunc(__dsub_rn(ra, q1), g1 - 41));
+              rowacc = zero2;
+            }
+            __syncwarp();
+            continue;
+          }
+#pragma unroll 1
+          for (int h = 0; h < TRI_TC; h += 8) {
+            float2 x[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int c = c0 + h + u;
+              x[u] = (rowok && c <= i) ? __ldcg(col + a.lda * c) : zero2;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int c = c0 + h + u;
+              const bool ok = rowok && c <= i;
+              float2 y = zero2;
+              if (ok) {
+                y = upd ? df_fma(df_fma(x[u], nri, wk[c]), nsi, vk[c]) : x[u];
+                __stcg(col + a.lda * c, y);
+                rowacc = df_fma(rowacc, y, vk1[c]);
+              }
+              tile[(h + u) * TRI_TLD + lane] = (ok && c < i) ? y : zero2;
+            }
+          }
+          __syncwarp();
+          if (wantp) {
+            const int u = lane & (TRI_TC - 1), hh = lane >> 4;
+            const int rb = r0 + 32 * bi + 16 * hh;
+            const float2* tp = tile + u * TRI_TLD + 16 * hh;
+            float2 cs = zero2;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) cs = df_fma(cs, tp[r], rb + r < n ? vk1[rb + r] : zero2);
+            float2 o;
+            o.x = __shfl_xor_sync(0xffffffffu, cs.x, 16);
+            o.y = __shfl_xor_sync(0xffffffffu, cs.y, 16);
+            cs = df_add(cs, o);
+            const int c = c0 + u;
+            if (hh == 0 && c < n && c <= r0 + 32 * bi + 31)
+              tri_exact_add(pnext + c, pnext2 + c, df_to_double(cs), s_g1);
+            if (kFixed) {
+              const int g1 = s_g1;
+              const double ra = df_to_double(rowacc);
+              const double q1 = tri_trunc(ra, g1);
+              rb1 = __dadd_rn(rb1, q1);
+              rb2 = __dadd_rn(rb2, tri_trunc(__dsub_rn(ra, q1), g1 - 41));
+              rowacc = zero2;
+            }
+          }
+          __syncwarp();
+        }
+        if (kFixed) {
+          if (wantp && rowok) {
+            atomicAdd(pnext + i, rb1);
+            atomicAdd(pnext2 + i, rb2);
+          }
+        } else if (wantp && rowok) {
+          tri_exact_add(pnext + i, pnext2 + i, df_to_double(rowacc), s_g1);
+        }
+      }
+    }
+    if (!qk_grid_barrier(a.bar, grp.size(), epoch, a.status)) return;
+    float2* t = vk;
+    vk = vk1;
+    vk1 = t;
+    tau_k = tau1;
+    scal_k = scal1;
+  }
+}
+
+// NT threads per CTA: 1024 (64 registers a thread) or 512 (up to 128)
+template <int NT>
+__global__ void __launch_bounds__(NT) k_sytrd_df(TriArgs a) {
+  sytrd_df_body<TriGridWhole, false>(a, TriGridWhole{});
+}
+
+// FP64 outputs of the double-float tridiagonalisation, in place: block j converts column j of V
+// (V(j+1, j) = 1, V(i, j) = u_i * scal_j below) and d_j, e_j, tau_j (d and e scaled back).
+__global__ void k_tri_df_finish(int n, double* __restrict__ d, double* __restrict__ e,
+                                double* __restrict__ tau, double* __restrict__ V, long long ldv,
+                                const double* __restrict__ vscal,
+                                const double* __restrict__ dfscale) {
+  const int j = blockIdx.x;
+  const double unsc = *dfscale;
+  if (threadIdx.x == 0) {
+    d[j] = df_to_double(reinterpret_cast<const float2*>(d)[j]) * unsc;
+    if (j <= n - 2) {
+      e[j] = df_to_double(reinterpret_cast<const float2*>(e)[j]) * unsc;
+      tau[j] = df_to_double(reinterpret_cast<const float2*>(tau)[j]);
+    }
+  }
+  if (j > n - 2) return;
+  const double sj = df_to_double(reinterpret_cast<const float2*>(vscal)[j]);
+  double* col = V + ldv * j;
+  for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x)
+    col[i] = i == j + 1 ? 1.0 : df_to_double(reinterpret_cast<const float2*>(col)[i]) * sj;
+}
+
 // Many tridiagonalisations in one cooperative launch: request r owns the CTAs
 // [cta0[r], cta0[r+1]) and synchronises them with its own bounded group barrier (its own counter),
 // so the per-column latency of small systems overlaps instead of queueing for the whole GPU.
@@ -464,10 +1013,54 @@ __global__ void __launch_bounds__(TRI_THREADS) k_sytrd_grouped(const __grid_cons
   sytrd_body<TriGridSlice, true>(g.req[r], TriGridSlice{s_grp});
 }
 
-// Gershgorin bounds, pivmin, ||T||_1 and e^2 (single block).
-__global__ void k_tri_prep(int n, const double* __restrict__ d, const double* __restrict__ e,
-                           double* __restrict__ e2, double* __restrict__ out /* gl, gu, pivmin, tnrm */) {
+// the same for double-float requests (the mixed tier), DF_THREADS per CTA
+constexpr int DF_THREADS = 512;
+__global__ void __launch_bounds__(DF_THREADS)
+    k_sytrd_df_grouped(const __grid_constant__ TriGroup g) {
+  __shared__ int s_grp[2];
+  int r = 0;
+  while (r + 1 < g.nreq && (int)blockIdx.x >= g.cta0[r + 1]) ++r;
+  if ((int)blockIdx.x >= g.cta0[g.nreq]) return;
+  if (threadIdx.x == 0) {
+    s_grp[0] = g.cta0[r + 1] - g.cta0[r];
+    s_grp[1] = (int)blockIdx.x - g.cta0[r];
+  }
+  __syncthreads();
+  sytrd_df_body<TriGridSlice, true>(g.req[r], TriGridSlice{s_grp});
+}
+
+// Gershgorin bounds, pivmin, ||T||_1 and e^2 (single block).  T is first scaled in place by the
+// power of two that brings max(|d_i|, |e_i|) into [1/2, 1), so that the Sturm recurrence's
+// rescaling (every 4 steps, 2^+-400) never meets overflow or underflow whatever the matrix's
+// magnitude; out[4] = the inverse factor, which k_tri_unscale applies to the eigenvalues.
+__global__ void k_tri_prep(int n, double* __restrict__ d, double* __restrict__ e,
+                           double* __restrict__ e2,
+                           double* __restrict__ out /* gl, gu, pivmin, tnrm, unscale */) {
   __shared__ double red[32];
+  __shared__ double s_sc;
+  {
+    double m = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      m = fmax(m, fmax(fabs(d[i]), i < n - 1 ? fabs(e[i]) : 0.0));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+      int ex = 0;
+      if (m > 0.0 && m <= DBL_MAX) frexp(m, &ex);
+      s_sc = ldexp(1.0, -ex);
+      out[4] = ldexp(1.0, ex);
+    }
+    __syncthreads();
+    const double sc = s_sc;
+    if (sc != 1.0)
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        d[i] *= sc;
+        if (i < n - 1) e[i] *= sc;
+      }
+    __syncthreads();
+  }
   double gl = INFINITY, gu = -INFINITY, emax = 0.0, tn = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const double el = i > 0 ? fabs(e[i - 1]) : 0.0;
@@ -507,7 +1100,13 @@ __global__ void k_tri_prep(int n, const double* __restrict__ d, const double* __
     out[2] = pivmin;
     out[3] = tn > 0.0 ? tn : 1.0;
   }
-  (void)red;
+}
+
+// eigenvalues of the scaled T back to the matrix's scale (exact: a power of two)
+__global__ void k_tri_unscale(int n, const double* __restrict__ prep, double* __restrict__ w) {
+  const double f = prep[4];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    w[i] *= f;
 }
 
 // Number of eigenvalues of T below x: sign changes of the leading principal minors
@@ -962,35 +1561,48 @@ void tri_split(const std::vector<qk_tri_service::Req>& rq, int sms, int* cta0) {
   for (int r = 0; r < R; ++r) cta0[r + 1] = cta0[r] + g[r];
 }
 
-// one cooperative launch for all pending requests (called with the lock held)
-void tri_launch_locked(qk_tri_service* sv) {
-  int st = QK_OK;
-  const int R = (int)sv->pending.size();
+// one cooperative launch for the pending requests of one arithmetic (FP64 or double-float)
+int tri_launch_part(qk_tri_service* sv, const std::vector<qk_tri_service::Req>& rq, bool df) {
+  const int R = (int)rq.size();
+  if (R == 0) return QK_OK;
   TriGroup g;
   g.nreq = R;
   size_t smem = 0;
+  const int nt = df ? DF_THREADS : TRI_THREADS;
   for (int r = 0; r < R; ++r) {
-    g.req[r] = sv->pending[r].ta;
-    const size_t need = TRI_TILE_BYTES + 3 * (size_t)g.req[r].n * sizeof(double);
+    g.req[r] = rq[r].ta;
+    const size_t need = (size_t)(nt / 32) * TRI_TC * TRI_TLD * 8 + 3 * (size_t)g.req[r].n * 8;
     smem = need > smem ? need : smem;
+  }
+  tri_split(rq, sv->parent->num_sms, g.cta0);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(g.cta0[R]);
+  cfg.blockDim = dim3(nt);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = sv->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, df ? k_sytrd_df_grouped : k_sytrd_grouped, g) != cudaSuccess)
+    return QK_ERR_CUDA;
+  sv->launches++;
+  sv->matrices += R;
+  return QK_OK;
+}
+
+// cooperative launches for all pending requests (called with the lock held): one per arithmetic
+// present, one after the other on the service stream, each over all SMs
+void tri_launch_locked(qk_tri_service* sv) {
+  int st = QK_OK;
+  const int R = (int)sv->pending.size();
+  std::vector<qk_tri_service::Req> part[2];
+  for (int r = 0; r < R; ++r) {
+    part[sv->pending[r].ta.df ? 1 : 0].push_back(sv->pending[r]);
     if (cudaStreamWaitEvent(sv->stream, sv->pending[r].ready, 0) != cudaSuccess) st = QK_ERR_CUDA;
   }
-  tri_split(sv->pending, sv->parent->num_sms, g.cta0);
-  if (st == QK_OK) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(g.cta0[R]);
-    cfg.blockDim = dim3(TRI_THREADS);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = sv->stream;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeCooperative;
-    at[0].val.cooperative = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    if (cudaLaunchKernelEx(&cfg, k_sytrd_grouped, g) != cudaSuccess) st = QK_ERR_CUDA;
-    sv->launches++;
-    sv->matrices += R;
-  }
+  for (int k = 0; k < 2 && st == QK_OK; ++k) st = tri_launch_part(sv, part[k], k == 1);
   if (cudaEventRecord(sv->done, sv->stream) != cudaSuccess) st = QK_ERR_CUDA;
   // every requester's stream continues after the group (enqueued before they wake up)
   for (int r = 0; r < R; ++r)
@@ -1032,6 +1644,8 @@ qk_tri_service* qk_tri_service_new(qk_ctx* parent, int n_workers) {
   std::call_once(once, [] {
     cudaFuncSetAttribute(k_sytrd_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          TRI_SMEM_MAX);
+    cudaFuncSetAttribute(k_sytrd_df_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TRI_SMEM_MAX);
   });
   return sv;
 }
@@ -1058,7 +1672,7 @@ void qk_tri_service_free(qk_tri_service* sv) {
 
 // ------------------------------------------------------------------------------------------
 int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, int want_vectors,
-               int backtransform) {
+               int backtransform, int tri_df) {
   if (n <= 0) return QK_OK;
   const size_t N = (size_t)n;
   // workspace: V (n*n), small vectors (d, e, tau, e2, pbuf(6n), prep(64), per-CTA slots)
@@ -1081,9 +1695,13 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   const bool tm = ctx->time_eig;
   if (tm) qk_tic(ctx, T_TRIDIAG);
   {
-    const size_t smem_need = TRI_TILE_BYTES + 3 * N * sizeof(double);
+    // threads per CTA: the FP64 kernel 1024; the double-float kernel 512 (its arithmetic needs
+    // the registers) unless the context asks for 1024
+    const int nt = tri_df ? (ctx->sytrd_df_threads == 1024 ? 1024 : DF_THREADS) : TRI_THREADS;
+    const size_t tile_bytes = (size_t)(nt / 32) * TRI_TC * TRI_TLD * 8;
+    const size_t smem_need = tile_bytes + 3 * N * sizeof(double);
     const int use_smem = smem_need <= (size_t)TRI_SMEM_MAX;
-    const size_t smem = use_smem ? smem_need : (size_t)TRI_TILE_BYTES;
+    const size_t smem = use_smem ? smem_need : tile_bytes;
     // the attribute is global to the kernel: set it once, at its maximum, so that concurrent
     // callers on other streams/threads never see a smaller limit than their launch needs
     static std::once_flag once;
@@ -1091,10 +1709,18 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
     std::call_once(once, [] {
       attr_err = cudaFuncSetAttribute(k_sytrd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       TRI_SMEM_MAX);
+      if (attr_err == cudaSuccess)
+        attr_err = cudaFuncSetAttribute(k_sytrd_df<512>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, TRI_SMEM_MAX);
+      if (attr_err == cudaSuccess)
+        attr_err = cudaFuncSetAttribute(k_sytrd_df<1024>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, TRI_SMEM_MAX);
     });
     QK_CK(attr_err);
+    void (*kern)(TriArgs) =
+        tri_df ? (nt == 1024 ? k_sytrd_df<1024> : k_sytrd_df<512>) : k_sytrd;
     int per_sm = 0;
-    QK_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sytrd, TRI_THREADS, smem));
+    QK_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem));
     if (per_sm < 1) return qk_fail(ctx, QK_ERR_CUDA, "k_sytrd cannot be resident");
     // one CTA per SM: the O(n) vector work of each column is repeated by every CTA, so fewer,
     // wider CTAs waste less FP64 issue
@@ -1120,6 +1746,9 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
     ta.tau = tau;
     ta.V = V;
     ta.ldv = n;
+    ta.df = tri_df != 0;
+    ta.vscal = e2;           // free until k_tri_prep fills e^2
+    ta.dfscale = prep + 8;   // k_tri_prep writes prep[0..4]
     ta.pbuf = pbuf;
     ta.fslot = fslot;
     ta.gvec = gvec;
@@ -1133,7 +1762,7 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
       // cooperative launch (all CTAs co-resident for the grid barrier); also valid under capture
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(grid);
-      cfg.blockDim = dim3(TRI_THREADS);
+      cfg.blockDim = dim3(nt);
       cfg.dynamicSmemBytes = smem;
       cfg.stream = ctx->stream;
       cudaLaunchAttribute at[1];
@@ -1141,9 +1770,13 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
       at[0].val.cooperative = 1;
       cfg.attrs = at;
       cfg.numAttrs = 1;
-      QK_CK(cudaLaunchKernelEx(&cfg, k_sytrd, ta));
+      QK_CK(cudaLaunchKernelEx(&cfg, kern, ta));
       ctx->launches++;
     }
+  }
+  if (tri_df) {
+    k_tri_df_finish<<<n, 256, 0, ctx->stream>>>(n, d, e, tau, V, n, e2, prep + 8);
+    QK_LAUNCHED();
   }
   if (tm) qk_toc(ctx, T_TRIDIAG);
 
@@ -1160,6 +1793,10 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   }
   launch_stebz(ctx, n, d, e2, prep, cnt, STEBZ_GRID, w);
   QK_LAUNCHED();
+  if (!want_vectors) {
+    k_tri_unscale<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, prep, w);
+    QK_LAUNCHED();
+  }
   if (tm) qk_toc(ctx, T_BISECT);
   if (!want_vectors) return QK_OK;
   // ---- 3. eigenvectors of T by inverse iteration ----
@@ -1167,6 +1804,8 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   QK_TRY(qk_wst(ctx, W_EIGWORK, 5 * N * N, &Wst));
   if (tm) qk_tic(ctx, T_STEIN);
   k_stein<<<(n + 63) / 64, 64, 0, ctx->stream>>>(n, d, e, w, prep, Wst, Zt, ctx->d_status);
+  QK_LAUNCHED();
+  k_tri_unscale<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, prep, w);
   QK_LAUNCHED();
   if (tm) qk_toc(ctx, T_STEIN);
 
@@ -1242,6 +1881,6 @@ extern "C" int qk_dsyev_dev(qk_ctx* ctx, int n, double* d_A, int lda, double* d_
   cudaSetDevice(ctx->device);
   QK_TRY(qk_order_after_default(ctx));
   QK_TRY(qk_status_reset(ctx));
-  QK_TRY(qk_eig_sym(ctx, n, d_A, lda, d_w, d_Zt, want_vectors, 1));
+  QK_TRY(qk_eig_sym(ctx, n, d_A, lda, d_w, d_Zt, want_vectors, 1, ctx->dsyev_df));
   return qk_status_check(ctx, QKD_BARRIER_TIMEOUT | QKD_BAD_INDEX);
 }

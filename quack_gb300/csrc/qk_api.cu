@@ -242,7 +242,7 @@ int casida_factored(qk_ctx* ctx, int prec, const Dims& d, const double* e, const
     k_trace<<<1, 1024, 0, ctx->stream>>>(nS, M, scal + 0);
     QK_LAUNCHED();
     qk_toc(ctx, T_BUILD);
-    QK_TRY(qk_eig_sym(ctx, nS, M, nS, w, Zt, 1, 0));
+    QK_TRY(qk_eig_sym(ctx, nS, M, nS, w, Zt, 1, 0, f32));
     qk_tic(ctx, T_BACKTRANS);
     QK_CK(cudaMemcpyAsync(X, Lov, (size_t)nS * naux * sizeof(double), cudaMemcpyDeviceToDevice,
                           ctx->stream));
@@ -259,7 +259,7 @@ int casida_factored(qk_ctx* ctx, int prec, const Dims& d, const double* e, const
   qk_tic(ctx, T_BUILD);
   QK_TRY(qk_launch_casida_M_K(ctx, d.N, d.nC, d.nO, d.nR, e, K, M, sq, scal + 0));
   qk_toc(ctx, T_BUILD);
-  QK_TRY(qk_eig_sym(ctx, nS, M, nS, w, Zt, 1, 0));
+  QK_TRY(qk_eig_sym(ctx, nS, M, nS, w, Zt, 1, 0, f32));
   QK_TRY(qk_launch_omega(ctx, nS, w, Om));
   qk_tic(ctx, T_BACKTRANS);
   QK_TRY(qk_launch_rowscale(ctx, nS, naux, sq, 0, Lov, nS, X, nS));           // D_s Lov
@@ -309,7 +309,7 @@ int casida_dev(qk_ctx* ctx, const Dims& d, const double* e, const double* ERI, d
     qk_toc(ctx, T_BUILD);
     ctx->time_eig = want_vectors != 0;
     const int est = qk_eig_sym(ctx, d.nS, M, d.nS, w, want_vectors ? XpY : nullptr, want_vectors,
-                               prec == QK_PREC_BF16X3 ? 2 : 1);
+                               prec == QK_PREC_BF16X3 ? 2 : 1, prec == QK_PREC_BF16X3);
     ctx->time_eig = true;
     QK_TRY(est);
     if (want_vectors && XmY)
@@ -328,10 +328,11 @@ int casida_dev(qk_ctx* ctx, const Dims& d, const double* e, const double* ERI, d
   qk_toc(ctx, T_BUILD);
   if (want_vectors) QK_TRY(qk_wst(ctx, W_ZT, S2, &Zt));
   ctx->time_eig = want_vectors != 0;
-  // the mixed tier back-transforms the eigenvectors with FP32 products (they feed the BF16x3
-  // excitation densities); eigenvalues, and so Om and EcRPA, are FP64 in every tier
+  // the mixed tier tridiagonalises in double-float on the FP32 pipe and back-transforms the
+  // eigenvectors with FP32 products (they feed the BF16x3 excitation densities); the tridiagonal
+  // eigenproblem, and so Om and EcRPA, is FP64 in every tier
   const int est = qk_eig_sym(ctx, d.nS, M, d.nS, w, Zt, want_vectors,
-                             prec == QK_PREC_BF16X3 ? 2 : 1);
+                             prec == QK_PREC_BF16X3 ? 2 : 1, prec == QK_PREC_BF16X3);
   ctx->time_eig = true;
   QK_TRY(est);
   if (want_vectors) QK_TRY(qk_launch_xpy(ctx, d.nS, w, Zt, sq, Om, XpY, XmY, XmY != nullptr));

@@ -55,6 +55,8 @@ struct qk_ctx {
   int newton_maxit = 64;   // Newton steps of the graphical QP solve (RGW_QP_graph.f90:38)
   int guess_gate = 0;      // learned-guess start rule (k_guess: 0 Halley agreement, 1, 2)
   int fail_alloc_in = 0;   // > 0: the n-th next growing workspace allocation fails (test hook)
+  int dsyev_df = 0;        // qk_dsyev_dev tridiagonalises in double-float (the mixed tier's way)
+  int sytrd_df_threads = 0;  // threads per CTA of the double-float tridiagonalisation (0 = 512)
   qk_tri_service* tri_service = nullptr;  // batch worker: tridiagonalise through the group launch
   cudaEvent_t ev_tri = nullptr;           // end of this context's work before a group launch
   long long tri_groups = 0;               // grouped tridiagonalisation launches of the last batch
@@ -213,6 +215,9 @@ int qk_bse_dev(qk_ctx* ctx, int TDA_W, int TDA, int singlet, int triplet, int ex
 
 // dense symmetric eigensolver pieces.  backtransform: 0 = leave Zt as the eigenvectors of the
 // tridiagonal matrix, 1 = back-transform in FP64, 2 = back-transform with FP32 products.
+// tri_df: tridiagonalise in double-float arithmetic on the FP32 pipe (the mixed tier; the
+// tridiagonal matrix, reflectors, eigenvalues and eigenvectors stay FP64); the lower triangle of
+// A is overwritten either way.
 // Grouped tridiagonalisation service of the batched driver: workers' tridiagonalisations are
 // collected until every active worker has submitted one (or finished), then run as ONE
 // cooperative launch of k_sytrd_grouped with a CTA group per matrix.
@@ -220,7 +225,7 @@ qk_tri_service* qk_tri_service_new(qk_ctx* parent, int n_workers);
 void qk_tri_service_worker_done(qk_tri_service* svc);
 void qk_tri_service_free(qk_tri_service* svc);
 int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, int want_vectors,
-               int backtransform = 1);
+               int backtransform = 1, int tri_df = 0);
 int qk_eig_apply_qt(qk_ctx* ctx, int n, double* X, long long ldx, int ncols, int fp32 = 0);
 
 // Casida pieces (k_casida.cu)
