@@ -490,6 +490,52 @@ __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
 }
 
 __device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+// acc += a b for a dot product, compensated (Ogita, Rump and Oishi's Dot2): acc.x is the running
+// float sum, acc.y collects the exact errors of its additions and the products' error terms,
+// unnormalised -- the dependency chain per term is one addition on each part instead of a full
+// double-float renormalisation, and the result is as accurate as double-float accumulation.
+__device__ __forceinline__ void dot2_acc(float2& acc, float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  const float t = __fadd_rn(acc.x, p);
+  const float bb = __fsub_rn(t, acc.x);
+  const float err = __fadd_rn(__fsub_rn(acc.x, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+  acc.x = t;
+  acc.y = __fadd_rn(acc.y, __fadd_rn(err, e));
+}
+
+// two Dot2 partial sums into one (same unnormalised form)
+__device__ __forceinline__ float2 dot2_merge(float2 a, float2 b) {
+  const float t = __fadd_rn(a.x, b.x);
+  const float bb = __fsub_rn(t, a.x);
+  const float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(t, bb)), __fsub_rn(b.x, bb));
+  return make_float2(t, __fadd_rn(__fadd_rn(a.y, b.y), err));
+}
+
+// x + n1 w + n2 v in one pass: the two exact products, two two-sums on the leading parts, all
+// low-order terms added once, one renormalisation
+__device__ __forceinline__ float2 df_upd2(float2 x, float2 n1, float2 w, float2 n2, float2 v) {
+  const float p1 = __fmul_rn(n1.x, w.x);
+  float e1 = fmaf(n1.x, w.x, -p1);
+  e1 = fmaf(n1.x, w.y, e1);
+  e1 = fmaf(n1.y, w.x, e1);
+  const float p2 = __fmul_rn(n2.x, v.x);
+  float e2 = fmaf(n2.x, v.x, -p2);
+  e2 = fmaf(n2.x, v.y, e2);
+  e2 = fmaf(n2.y, v.x, e2);
+  const float s1 = __fadd_rn(x.x, p1);
+  const float b1 = __fsub_rn(s1, x.x);
+  const float t1 = __fadd_rn(__fsub_rn(x.x, __fsub_rn(s1, b1)), __fsub_rn(p1, b1));
+  const float s2 = __fadd_rn(s1, p2);
+  const float b2 = __fsub_rn(s2, s1);
+  const float t2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, b2)), __fsub_rn(p2, b2));
+  const float lo = __fadd_rn(__fadd_rn(__fadd_rn(x.y, e1), __fadd_rn(e2, t1)), t2);
+  const float h = __fadd_rn(s2, lo);
+  return make_float2(h, __fsub_rn(lo, __fsub_rn(h, s2)));
+}
 __device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, df_neg(b)); }
 // times a power of two (exact)
 __device__ __forceinline__ float2 df_scale(float2 a, float s) {
@@ -699,6 +745,7 @@ __device__ __forceinline__ void sytrd_df_body(const TriArgs a, const Grp grp) {
     {
       const double* p = a.pbuf + (size_t)((k + 3) % 3) * n;
       float2 dot = zero2;
+      // four elements per thread per round, loads issued together
       for (int i0 = j + tid; i0 < n; i0 += 4 * nt) {
         float2 xv[4], uv[4];
         double pv[4], pv2[4];
@@ -820,8 +867,13 @@ __device__ __forceinline__ void sytrd_df_body(const TriArgs a, const Grp grp) {
         int cur = -1;
         int i = 0;
         bool rowok = false;
-        float2 nri = zero2, nsi = zero2, rowacc = zero2;  // -(a1 u_i), -(a1 p~_i - a2x2 u_i)
+        // -(a1 u_i), -(a1 p~_i - a2x2 u_i); the row's mat-vec sum as a Dot2 pair
+        float2 nri = zero2, nsi = zero2, rowacc = zero2;
         double rb1 = 0.0, rb2 = 0.0;
+        // interior tiles prefetch the next interior tile's 16 elements into x while they finish
+        // their column sums, so that its L2 latency overlaps them
+        float2 x[TRI_TC];
+        bool have_next = false;
         for (int it = it0; it < it1; ++it) {
           while (it >= off + 2 * bi + 2) {
             off += 2 * bi + 2;
@@ -850,27 +902,44 @@ __device__ __forceinline__ void sytrd_df_body(const TriArgs a, const Grp grp) {
           float2* col = A2 + i;
           if (upd && wantp && it - off < 2 * bi && r0 + 32 * bi + 32 <= n) {
             // interior tile (the common case): every element strictly below the diagonal and
-            // inside the matrix, so no per-element predicates or index tests
+            // inside the matrix, so no per-element predicates or index tests; all 16 loads are
+            // issued before the first use
             const float2* wc = wk + c0;
             const float2* vc = vk + c0;
             const float2* v1c = vk1 + c0;
             float2* q = col + a.lda * c0;
-#pragma unroll 1
-            for (int h = 0; h < TRI_TC; h += 8) {
-              float2 x[8];
-              float2* qq = q;
+            if (!have_next) {
+              const float2* qq = q;
 #pragma unroll
-              for (int u = 0; u < 8; ++u) {
+              for (int u = 0; u < TRI_TC; ++u) {
                 x[u] = __ldcg(qq);
                 qq += a.lda;
               }
+            }
 #pragma unroll
-              for (int u = 0; u < 8; ++u) {
-                const float2 y = df_fma(df_fma(x[u], nri, wc[h + u]), nsi, vc[h + u]);
-                __stcg(q, y);
-                q += a.lda;
-                rowacc = df_fma(rowacc, y, v1c[h + u]);
-                tile[(h + u) * TRI_TLD + lane] = y;
+            for (int u = 0; u < TRI_TC; ++u) {
+              const float2 y = df_upd2(x[u], nri, wc[u], nsi, vc[u]);
+              __stcg(q, y);
+              q += a.lda;
+              dot2_acc(rowacc, y, v1c[u]);
+              tile[u * TRI_TLD + lane] = y;
+            }
+            // the next item: the same row block or the next one (rows blocks grow by 2 tiles)
+            have_next = false;
+            if (it + 1 < it1) {
+              int bn = bi, on = off;
+              if (it + 1 >= off + 2 * bi + 2) {
+                on = off + 2 * bi + 2;
+                ++bn;
+              }
+              if (it + 1 - on < 2 * bn && r0 + 32 * bn + 32 <= n) {
+                const float2* qq = A2 + (r0 + 32 * bn + lane) + a.lda * (r0 + TRI_TC * (it + 1 - on));
+#pragma unroll
+                for (int u = 0; u < TRI_TC; ++u) {
+                  x[u] = __ldcg(qq);
+                  qq += a.lda;
+                }
+                have_next = true;
               }
             }
             __syncwarp();
@@ -879,11 +948,11 @@ __device__ __forceinline__ void sytrd_df_body(const TriArgs a, const Grp grp) {
             const float2* vr = vk1 + r0 + 32 * bi + 16 * hh;
             float2 cs = zero2;
 #pragma unroll
-            for (int r = 0; r < 16; ++r) cs = df_fma(cs, tp[r], vr[r]);
+            for (int r = 0; r < 16; ++r) dot2_acc(cs, tp[r], vr[r]);
             float2 o;
             o.x = __shfl_xor_sync(0xffffffffu, cs.x, 16);
             o.y = __shfl_xor_sync(0xffffffffu, cs.y, 16);
-            cs = df_add(cs, o);
+            cs = dot2_merge(cs, o);
             if (hh == 0) tri_exact_add(pnext + c0 + u, pnext2 + c0 + u, df_to_double(cs), s_g1);
             if (kFixed) {
               const int g1 = s_g1;
@@ -896,25 +965,29 @@ __device__ __forceinline__ void sytrd_df_body(const TriArgs a, const Grp grp) {
             __syncwarp();
             continue;
           }
-#pragma unroll 1
-          for (int h = 0; h < TRI_TC; h += 8) {
-            float2 x[8];
+          // edge tile (the diagonal ones, the last, partial row block, the first and the last
+          // column): the same loads-first schedule and arithmetic with per-element masks, without
+          // branches: masked elements load A(0,0) and read clamped vector entries (both in
+          // bounds), and their results are discarded by selects and a predicated store
+          {
+            const float2* qq = col + a.lda * c0;
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-              const int c = c0 + h + u;
-              x[u] = (rowok && c <= i) ? __ldcg(col + a.lda * c) : zero2;
+            for (int u = 0; u < TRI_TC; ++u) {
+              x[u] = __ldcg((rowok && c0 + u <= i) ? qq : A2);
+              qq += a.lda;
             }
+            float2* q = col + a.lda * c0;
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-              const int c = c0 + h + u;
+            for (int u = 0; u < TRI_TC; ++u) {
+              const int c = c0 + u;
+              const int cc = c < n ? c : n - 1;
               const bool ok = rowok && c <= i;
-              float2 y = zero2;
-              if (ok) {
-                y = upd ? df_fma(df_fma(x[u], nri, wk[c]), nsi, vk[c]) : x[u];
-                __stcg(col + a.lda * c, y);
-                rowacc = df_fma(rowacc, y, vk1[c]);
-              }
-              tile[(h + u) * TRI_TLD + lane] = (ok && c < i) ? y : zero2;
+              float2 y = upd ? df_upd2(x[u], nri, wk[cc], nsi, vk[cc]) : x[u];
+              y = ok ? y : zero2;
+              if (ok) __stcg(q, y);
+              dot2_acc(rowacc, y, vk1[cc]);
+              q += a.lda;
+              tile[u * TRI_TLD + lane] = c < i ? y : zero2;
             }
           }
           __syncwarp();
@@ -924,11 +997,11 @@ __device__ __forceinline__ void sytrd_df_body(const TriArgs a, const Grp grp) {
             const float2* tp = tile + u * TRI_TLD + 16 * hh;
             float2 cs = zero2;
 #pragma unroll
-            for (int r = 0; r < 16; ++r) cs = df_fma(cs, tp[r], rb + r < n ? vk1[rb + r] : zero2);
+            for (int r = 0; r < 16; ++r) dot2_acc(cs, tp[r], vk1[rb + r < n ? rb + r : n - 1]);
             float2 o;
             o.x = __shfl_xor_sync(0xffffffffu, cs.x, 16);
             o.y = __shfl_xor_sync(0xffffffffu, cs.y, 16);
-            cs = df_add(cs, o);
+            cs = dot2_merge(cs, o);
             const int c = c0 + u;
             if (hh == 0 && c < n && c <= r0 + 32 * bi + 31)
               tri_exact_add(pnext + c, pnext2 + c, df_to_double(cs), s_g1);
@@ -962,9 +1035,8 @@ __device__ __forceinline__ void sytrd_df_body(const TriArgs a, const Grp grp) {
   }
 }
 
-// NT threads per CTA: 1024 (64 registers a thread) or 512 (up to 128)
-template <int NT>
-__global__ void __launch_bounds__(NT) k_sytrd_df(TriArgs a) {
+// 512 threads per CTA (DF_THREADS): the double-float arithmetic needs up to 128 registers a thread
+__global__ void __launch_bounds__(512) k_sytrd_df(TriArgs a) {
   sytrd_df_body<TriGridWhole, false>(a, TriGridWhole{});
 }
 
@@ -1695,9 +1767,8 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   const bool tm = ctx->time_eig;
   if (tm) qk_tic(ctx, T_TRIDIAG);
   {
-    // threads per CTA: the FP64 kernel 1024; the double-float kernel 512 (its arithmetic needs
-    // the registers) unless the context asks for 1024
-    const int nt = tri_df ? (ctx->sytrd_df_threads == 1024 ? 1024 : DF_THREADS) : TRI_THREADS;
+    // threads per CTA: the FP64 kernel 1024, the double-float kernel 512 (its registers)
+    const int nt = tri_df ? DF_THREADS : TRI_THREADS;
     const size_t tile_bytes = (size_t)(nt / 32) * TRI_TC * TRI_TLD * 8;
     const size_t smem_need = tile_bytes + 3 * N * sizeof(double);
     const int use_smem = smem_need <= (size_t)TRI_SMEM_MAX;
@@ -1710,15 +1781,11 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
       attr_err = cudaFuncSetAttribute(k_sytrd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       TRI_SMEM_MAX);
       if (attr_err == cudaSuccess)
-        attr_err = cudaFuncSetAttribute(k_sytrd_df<512>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, TRI_SMEM_MAX);
-      if (attr_err == cudaSuccess)
-        attr_err = cudaFuncSetAttribute(k_sytrd_df<1024>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, TRI_SMEM_MAX);
+        attr_err = cudaFuncSetAttribute(k_sytrd_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        TRI_SMEM_MAX);
     });
     QK_CK(attr_err);
-    void (*kern)(TriArgs) =
-        tri_df ? (nt == 1024 ? k_sytrd_df<1024> : k_sytrd_df<512>) : k_sytrd;
+    void (*kern)(TriArgs) = tri_df ? k_sytrd_df : k_sytrd;
     int per_sm = 0;
     QK_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem));
     if (per_sm < 1) return qk_fail(ctx, QK_ERR_CUDA, "k_sytrd cannot be resident");

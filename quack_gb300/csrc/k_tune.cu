@@ -106,11 +106,6 @@ int qk_tune_set(qk_ctx* ctx, const char* name, long long size, int value) {
     ctx->dsyev_df = value;
     return QK_OK;
   }
-  if (!strcmp(name, "sytrd_df_threads")) {
-    if (value != 0 && value != 512 && value != 1024) return QK_ERR_ARG;
-    ctx->sytrd_df_threads = value;
-    return QK_OK;
-  }
   if (!strcmp(name, "spin_limit")) {
     if (value < 0) return QK_ERR_ARG;
     cudaSetDevice(ctx->device);
@@ -131,7 +126,6 @@ int qk_tune_query(const qk_ctx* ctx, const char* name, long long size) {
   if (!ctx || !name) return -1;
   if (!strcmp(name, "newton_maxit")) return ctx->newton_maxit;
   if (!strcmp(name, "dsyev_df")) return ctx->dsyev_df;
-  if (!strcmp(name, "sytrd_df_threads")) return ctx->sytrd_df_threads;
   for (int p = 0; p < TUNE_NUM; ++p)
     if (!strcmp(name, k_tune_names[p])) return ctx->tune[p][bucket_of(size)];
   return -1;

@@ -56,7 +56,6 @@ struct qk_ctx {
   int guess_gate = 0;      // learned-guess start rule (k_guess: 0 Halley agreement, 1, 2)
   int fail_alloc_in = 0;   // > 0: the n-th next growing workspace allocation fails (test hook)
   int dsyev_df = 0;        // qk_dsyev_dev tridiagonalises in double-float (the mixed tier's way)
-  int sytrd_df_threads = 0;  // threads per CTA of the double-float tridiagonalisation (0 = 512)
   qk_tri_service* tri_service = nullptr;  // batch worker: tridiagonalise through the group launch
   cudaEvent_t ev_tri = nullptr;           // end of this context's work before a group launch
   long long tri_groups = 0;               // grouped tridiagonalisation launches of the last batch
