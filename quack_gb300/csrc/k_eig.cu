@@ -1221,6 +1221,64 @@ __device__ __forceinline__ int sturm_count(int n, const double* __restrict__ d,
   return c;
 }
 
+// The same Sturm count in double-float on the FP32 pipe (the mixed tier), with d and e^2 as
+// double-float pairs.  A step is d_i - x (a two-sum) and the fused two-product difference
+// (d_i - x) p_i - e^2 p_{i-1} with one renormalisation; float's exponent range is narrow, so the
+// pair is brought back towards 1 by an exact power of two whenever its larger member leaves
+// [2^-30, 2^30] (checked every step: one step changes magnitudes by at most a few units for the
+// scaled T, or by the size of a tiny e^2 or d_i - x).
+__device__ __forceinline__ float2 df_dif2(float2 a, float2 b, float2 c, float2 d) {  // ab - cd
+  const float p1 = __fmul_rn(a.x, b.x);
+  float e1 = fmaf(a.x, b.x, -p1);
+  e1 = fmaf(a.x, b.y, e1);
+  e1 = fmaf(a.y, b.x, e1);
+  const float p2 = __fmul_rn(c.x, d.x);
+  float e2 = fmaf(c.x, d.x, -p2);
+  e2 = fmaf(c.x, d.y, e2);
+  e2 = fmaf(c.y, d.x, e2);
+  const float s = __fsub_rn(p1, p2);
+  const float bb = __fsub_rn(s, p1);
+  const float t = __fsub_rn(__fsub_rn(p1, __fsub_rn(s, bb)), __fadd_rn(p2, bb));
+  const float lo = __fadd_rn(t, __fsub_rn(e1, e2));
+  const float h = __fadd_rn(s, lo);
+  return make_float2(h, __fsub_rn(lo, __fsub_rn(h, s)));
+}
+
+__device__ __forceinline__ int sturm_count_df(int n, const float2* __restrict__ d,
+                                              const float2* __restrict__ e2, float2 x) {
+  float2 p0 = make_float2(1.f, 0.f), p1 = df_sub(__ldg(d), x);
+  int neg = p1.x == 0.f ? 1 : (int)(__float_as_uint(p1.x) >> 31);
+  int c = neg;
+  for (int i = 1; i < n; ++i) {
+    const float2 p2 = df_dif2(df_sub(__ldg(d + i), x), p1, __ldg(e2 + i - 1), p0);
+    const int n2 = p2.x == 0.f ? !neg : (int)(__float_as_uint(p2.x) >> 31);
+    c += (n2 != neg);
+    neg = n2;
+    p0 = p1;
+    p1 = p2;
+    const int e1x = (int)((__float_as_uint(p1.x) >> 23) & 0xFF);
+    const int e0x = (int)((__float_as_uint(p0.x) >> 23) & 0xFF);
+    const int ex = e1x > e0x ? e1x : e0x;
+    if (ex > 127 + 30) {
+      p0 = df_scale(p0, 0x1p-60f);
+      p1 = df_scale(p1, 0x1p-60f);
+    } else if (ex < 127 - 30) {
+      p0 = df_scale(p0, 0x1p+60f);
+      p1 = df_scale(p1, 0x1p+60f);
+    }
+  }
+  return c;
+}
+
+// d and e^2 of the scaled T as double-float pairs, for the double-float bisection
+__global__ void k_tri_df_copy(int n, const double* __restrict__ d, const double* __restrict__ e2,
+                              float2* __restrict__ dd, float2* __restrict__ ee) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    dd[i] = df_from_double(d[i]);
+    ee[i] = i < n - 1 ? df_from_double(e2[i]) : make_float2(0.f, 0.f);
+  }
+}
+
 // k-section on the Sturm count: K consecutive lanes share eigenvalue j and test K interior points
 // of the bracket per step (log2(K+1) bits per step), to full FP64 precision.  Sturm counts are
 // monotone in x in IEEE arithmetic, so the points with count <= j form a prefix and the new
@@ -1230,19 +1288,29 @@ __device__ __forceinline__ int sturm_count(int n, const double* __restrict__ d,
 // Sturm counts at G+1 equally spaced points of the Gershgorin interval (one thread per point):
 // every eigenvalue then starts its k-section from the grid cell that holds it, log2(G) halvings
 // below the full interval.
+// DF: the counts in double-float (dd, ee), the bracket closed to double-float's precision
+// (2^-45 relative, or 2^-47 ||T||_1 near zero) instead of FP64's.
 constexpr int STEBZ_GRID = 16384;
+template <bool DF>
 __global__ void k_stebz_grid(int n, const double* __restrict__ d, const double* __restrict__ e2,
+                             const float2* __restrict__ dd, const float2* __restrict__ ee,
                              const double* __restrict__ prep, int G, int* __restrict__ cnt) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g > G) return;
   const double lo = prep[0], hi = prep[1];
   const double h = (hi - lo) / G;
-  cnt[g] = g == 0 ? 0 : (g == G ? n : sturm_count(n, d, e2, lo + h * g));
+  const double x = lo + h * g;
+  cnt[g] = g == 0 ? 0
+                  : (g == G ? n
+                            : (DF ? sturm_count_df(n, dd, ee, df_from_double(x))
+                                  : sturm_count(n, d, e2, x)));
 }
 
-template <int K>
+template <int K, bool DF>
 __global__ void __launch_bounds__(128) k_stebz(int n, const double* __restrict__ d,
                                                const double* __restrict__ e2,
+                                               const float2* __restrict__ dd,
+                                               const float2* __restrict__ ee,
                                                const double* __restrict__ prep,
                                                const int* __restrict__ cnt, int G,
                                                double* __restrict__ w) {
@@ -1267,11 +1335,15 @@ __global__ void __launch_bounds__(128) k_stebz(int n, const double* __restrict__
     lo = x0;
     hi = x1;
   }
+  const double rtol = DF ? 0x1p-45 : 2.0 * DBL_EPSILON;
+  const double atol = DF ? 0x1p-47 * prep[3] : 2.0 * pivmin;
   for (int it = 0; it < 128; ++it) {
-    if (hi - lo <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + 2.0 * pivmin) break;
+    if (hi - lo <= rtol * fmax(fabs(lo), fabs(hi)) + atol) break;
     const double h = (hi - lo) / (K + 1);
     const double x = lo + h * (t + 1);
-    const int c = valid ? sturm_count(n, d, e2, x) : 0;
+    const int c = !valid ? 0
+                         : (DF ? sturm_count_df(n, dd, ee, df_from_double(x))
+                               : sturm_count(n, d, e2, x));
     const unsigned le = __ballot_sync(gmask, c <= j) & gmask;
     const int k = __popc(le);
     const double nlo = k > 0 ? lo + h * k : lo;
@@ -1283,18 +1355,34 @@ __global__ void __launch_bounds__(128) k_stebz(int n, const double* __restrict__
   if (valid && t == 0) w[j] = 0.5 * (lo + hi);
 }
 
-void launch_stebz(qk_ctx* ctx, int n, const double* d, const double* e2, const double* prep,
-                  const int* cnt, int G, double* w) {
+void launch_stebz(qk_ctx* ctx, int n, const double* d, const double* e2, const float2* dd,
+                  const float2* ee, const double* prep, const int* cnt, int G, double* w) {
+  const int blocks8 = (int)((8 * (long long)n + 127) / 128);
+  if (dd) {
+    // double-float counts: the FP32 pipe has issue to spare, so 16 lanes per eigenvalue (4.1
+    // bits per sweep) while the warps fit eight per SM sub-partition, else 8
+    const long long slots = 8LL * 4 * 32 * ctx->num_sms;
+    if (slots >= 16LL * n)
+      k_stebz<16, true><<<(int)((16 * (long long)n + 127) / 128), 128, 0, ctx->stream>>>(
+          n, d, e2, dd, ee, prep, cnt, G, w);
+    else
+      k_stebz<8, true><<<blocks8, 128, 0, ctx->stream>>>(n, d, e2, dd, ee, prep, cnt, G, w);
+    return;
+  }
   const long long slots = 4LL * 32 * ctx->num_sms;  // one warp per SM sub-partition
   int K = slots >= 8LL * n ? 8 : slots >= 4LL * n ? 4 : slots >= 2LL * n ? 2 : 1;
   const int tk = qk_tune_get(ctx, TUNE_STEBZ_K, n, 0);  // tuned width, if any
   if (tk == 1 || tk == 2 || tk == 4 || tk == 8) K = tk;
   const int blocks = (int)((K * (long long)n + 127) / 128);
   switch (K) {
-    case 8: k_stebz<8><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, cnt, G, w); break;
-    case 4: k_stebz<4><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, cnt, G, w); break;
-    case 2: k_stebz<2><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, cnt, G, w); break;
-    default: k_stebz<1><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, prep, cnt, G, w); break;
+    case 8: k_stebz<8, false><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, nullptr, nullptr, prep,
+                                                              cnt, G, w); break;
+    case 4: k_stebz<4, false><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, nullptr, nullptr, prep,
+                                                              cnt, G, w); break;
+    case 2: k_stebz<2, false><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, nullptr, nullptr, prep,
+                                                              cnt, G, w); break;
+    default: k_stebz<1, false><<<blocks, 128, 0, ctx->stream>>>(n, d, e2, nullptr, nullptr, prep,
+                                                               cnt, G, w); break;
   }
 }
 
@@ -1851,14 +1939,27 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   if (tm) qk_tic(ctx, T_BISECT);
   k_tri_prep<<<1, 1024, 0, ctx->stream>>>(n, d, e, e2, prep);
   QK_LAUNCHED();
+  // the mixed tier bisects in double-float: d and e^2 as pairs in the (now free) pbuf area
+  float2* dd = nullptr;
+  float2* ee = nullptr;
+  if (tri_df) {
+    dd = reinterpret_cast<float2*>(pbuf);
+    ee = dd + n;
+    k_tri_df_copy<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, d, e2, dd, ee);
+    QK_LAUNCHED();
+  }
   int* cnt = nullptr;
   if (n >= 256) {
     QK_TRY(qk_wst(ctx, W_STEBZ, (size_t)STEBZ_GRID + 64, &cnt));
-    k_stebz_grid<<<(STEBZ_GRID + 128) / 128, 128, 0, ctx->stream>>>(n, d, e2, prep, STEBZ_GRID,
-                                                                     cnt);
+    if (tri_df)
+      k_stebz_grid<true><<<(STEBZ_GRID + 128) / 128, 128, 0, ctx->stream>>>(
+          n, d, e2, dd, ee, prep, STEBZ_GRID, cnt);
+    else
+      k_stebz_grid<false><<<(STEBZ_GRID + 128) / 128, 128, 0, ctx->stream>>>(
+          n, d, e2, nullptr, nullptr, prep, STEBZ_GRID, cnt);
     QK_LAUNCHED();
   }
-  launch_stebz(ctx, n, d, e2, prep, cnt, STEBZ_GRID, w);
+  launch_stebz(ctx, n, d, e2, dd, ee, prep, cnt, STEBZ_GRID, w);
   QK_LAUNCHED();
   if (!want_vectors) {
     k_tri_unscale<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, prep, w);
