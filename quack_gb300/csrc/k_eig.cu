@@ -33,7 +33,7 @@ constexpr int TRI_TLD = 33;         // padded leading dimension of a warp's shar
 constexpr int TRI_TILE_BYTES = (TRI_THREADS / 32) * TRI_TC * TRI_TLD * 8;
 constexpr int BT_NB = 128;          // reflectors per compact-WY block
 constexpr double CLUSTER_REL = 1e-7;  // eigenvalues closer than this * ||T||_1 share a cluster
-constexpr int SB = 8;                 // inverse iteration: steps per batch of prefetched loads
+constexpr int SB = 16;                // inverse iteration: steps per batch of prefetched loads
 
 // Sum over the CTA with few FP64 operations (the FP64 pipe is the scarce resource here): the
 // per-thread partials go to shared memory and warps 0-3 (one per SM sub-partition, so their
@@ -1971,7 +1971,9 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   double* Wst = nullptr;
   QK_TRY(qk_wst(ctx, W_EIGWORK, 5 * N * N, &Wst));
   if (tm) qk_tic(ctx, T_STEIN);
-  k_stein<<<(n + 63) / 64, 64, 0, ctx->stream>>>(n, d, e, w, prep, Wst, Zt, ctx->d_status);
+  // one warp per block: the threads' sweeps are latency-bound chains, so the warps go to as
+  // many SMs as there are (each with its own load/store and FP64 units)
+  k_stein<<<(n + 31) / 32, 32, 0, ctx->stream>>>(n, d, e, w, prep, Wst, Zt, ctx->d_status);
   QK_LAUNCHED();
   k_tri_unscale<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, prep, w);
   QK_LAUNCHED();
