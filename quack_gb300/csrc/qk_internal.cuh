@@ -321,6 +321,11 @@ __device__ __forceinline__ unsigned qk_ld_acquire(const unsigned* p) {
 // Monotone-counter barrier over `nblocks` co-resident CTAs (cooperative launch guarantees
 // co-residency).  Bounded: after qk_spin_limit(status) polls it records QKD_BARRIER_TIMEOUT and
 // returns false; callers then leave the kernel.  `epoch` counts barriers passed by this CTA.
+// Ordering without separate fences: the CTA's writes before the barrier are ordered before
+// thread 0's arrival by the first __syncthreads, the arrival is a release RMW at GPU scope (so
+// those writes become visible with it), the poll is an acquire load, and the arrivals of all CTAs
+// form one release sequence on the counter, so the load that sees the full count synchronises
+// with every CTA's arrival; the second __syncthreads passes that on to the whole CTA.
 __device__ __forceinline__ bool qk_grid_barrier(unsigned* counter, unsigned nblocks,
                                                 unsigned& epoch, int* status) {
   __shared__ int s_ok;
@@ -330,15 +335,13 @@ __device__ __forceinline__ bool qk_grid_barrier(unsigned* counter, unsigned nblo
     epoch++;
     unsigned target = epoch * nblocks;
     const unsigned limit = qk_spin_limit(status);
-    __threadfence();
-    atomicAdd(counter, 1u);
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(counter) : "memory");
     unsigned spins = 0;
     while (qk_ld_acquire(counter) < target) {
       if (++spins > limit) { atomicOr(status, QKD_BARRIER_TIMEOUT); ok = 0; break; }
       if (spins > 64) __nanosleep(64);
     }
     if (ok && (*((volatile int*)status) & QKD_BARRIER_TIMEOUT)) ok = 0;
-    __threadfence();
     s_ok = ok;
   }
   __syncthreads();
