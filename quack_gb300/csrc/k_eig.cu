@@ -1394,7 +1394,7 @@ __device__ __forceinline__ double rand_pm1(unsigned long long i, unsigned long l
   return ((double)(z >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;
 }
 
-// reciprocal of a U pivot, tiny pivots perturbed to +-tiny first (stored once, so that the three
+// reciprocal of a U pivot, tiny pivots perturbed to +-tiny first (stored once, so that the
 // back substitutions multiply instead of divide on their dependency chain)
 __device__ __forceinline__ double pivot_rcp(double u, double tiny) {
   if (fabs(u) < tiny) u = (u < 0.0) ? -tiny : tiny;
@@ -1408,7 +1408,7 @@ __device__ __forceinline__ double pivot_rcp(double u, double tiny) {
 __global__ void k_stein(int n, const double* __restrict__ d, const double* __restrict__ e,
                         const double* __restrict__ w, const double* __restrict__ prep,
                         double* __restrict__ W, double* __restrict__ Zt,
-                        const int* __restrict__ status) {
+                        const int* __restrict__ status, int iters) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   // after a failed tridiagonalisation (barrier expired) T is meaningless -- possibly one cluster
@@ -1464,7 +1464,7 @@ __global__ void k_stein(int n, const double* __restrict__ d, const double* __res
     at(U0, n - 1) = pivot_rcp(r0, tiny); at(U1, n - 1) = 0.0; at(U2, n - 1) = 0.0;
     // ---- start vector ----
     for (int i = 0; i < n; ++i) Zt[(size_t)jj + N * i] = rand_pm1(i, jj);
-    for (int it = 0; it < 3; ++it) {
+    for (int it = 0; it < iters; ++it) {
       // scale to unit inf-norm
       double mx = 0.0;
       for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(Zt[(size_t)jj + N * i]));
@@ -1973,7 +1973,11 @@ int qk_eig_sym(qk_ctx* ctx, int n, double* A, int lda, double* w, double* Zt, in
   if (tm) qk_tic(ctx, T_STEIN);
   // one warp per block: the threads' sweeps are latency-bound chains, so the warps go to as
   // many SMs as there are (each with its own load/store and FP64 units)
-  k_stein<<<(n + 31) / 32, 32, 0, ctx->stream>>>(n, d, e, w, prep, Wst, Zt, ctx->d_status);
+  // iterations from the random start: three in FP64 (as dstein's convergence plus its two
+  // extra steps), two in the mixed tier, whose eigenvalues come from the double-float bisection
+  // and whose vectors feed FP32 products
+  k_stein<<<(n + 31) / 32, 32, 0, ctx->stream>>>(n, d, e, w, prep, Wst, Zt, ctx->d_status,
+                                                 tri_df ? 2 : 3);
   QK_LAUNCHED();
   k_tri_unscale<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, prep, w);
   QK_LAUNCHED();
