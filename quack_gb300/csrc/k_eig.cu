@@ -12,6 +12,8 @@
 //   2. k_stebz: Sturm-count k-section (K lanes per eigenvalue), full FP64 precision.
 //   3. k_stein: inverse iteration on T - lambda I (tridiagonal GEPP), one thread per cluster of
 //      close eigenvalues, modified Gram-Schmidt inside clusters; eigenvectors written as rows.
+//   The mixed tier runs steps 1 and 2 in double-float arithmetic on the FP32 pipe (k_sytrd_df,
+//   sturm_count_df; GB300 issues FP32 at 64x its FP64 rate) and two inverse-iteration steps.
 //   4. Blocked back-transformation E <- E * Q^T with compact-WY blocks of 128 reflectors on the
 //      FP64 GEMM, or with compensated FP32 products in the mixed tier (all T factors from one
 //      batched GEMM and one launch).
