@@ -379,7 +379,8 @@ int qk_gemm_bf16x3_ex_dev(qk_ctx* ctx, char transa, char transb, int m, int n, i
  * evGW cycle) and therefore cannot let the library call cudaMalloc: computes the same Sig, Z and
  * EcGM as qk_RGW_self_energy_diag (GW/RGW_self_energy_diag.f90) from caller-owned device buffers
  * e(nBas), Om(nS), rho(nBas,nBas,nS) into Sig(nBas), Z(nBas), EcGM(1), enqueued on `stream`
- * (a cudaStream_t, 0 = default stream) and synchronised before returning.  It needs no qk_ctx and
+ * (a cudaStream_t, 0 = default stream) and synchronised before returning (so the call cannot be
+ * captured into a CUDA graph).  It needs no qk_ctx and
  * calls no cudaMalloc/cudaFree.  Scratch is a static 3 MiB device array, so nBas <= 1024
  * (QK_ERR_ARG beyond that).  QuAcK's counts are checked: nV = nBas - nO (frozen virtuals
  * included) and nO <= nOrb <= nBas, else QK_ERR_ARG.  Each call resolves the array's device
