@@ -46,7 +46,8 @@ def _casida_like(n, seed):
     return np.diag(dia**2) + 2.0 * (sd[:, None] * (L @ L.T) * sd[None, :])
 
 
-@pytest.mark.parametrize("n,kind", [(300, "random"), (1500, "random"), (2000, "casida")])
+@pytest.mark.parametrize("n,kind", [(300, "random"), (301, "random"), (1500, "random"),
+                                    (2000, "casida")])
 def test_df_eigenpairs_match_lapack(ctx, n, kind):
     if kind == "random":
         rng = np.random.default_rng(11 + n)
