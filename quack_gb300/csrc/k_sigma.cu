@@ -214,7 +214,7 @@ struct SigFF {
 // pipe, the warp's per-(p,q) sums added into float-float (TwoSum) accumulators; inside it the
 // FP64 terms of k_sigma_partial.  Same partial-sum layout as k_sigma_partial (chunk = q group).
 constexpr int FFT_WARPS = 8;
-constexpr int FFT_U = 16;
+constexpr int FFT_U = 8;
 
 __global__ void __launch_bounds__(FFT_WARPS * 32) k_sigma_partial_ffT(SigArgs a, SigFF f) {
   // dynamic shared memory: e (N doubles) | e as float pairs (N) | Om pairs (nS)
@@ -267,10 +267,22 @@ __global__ void __launch_bounds__(FFT_WARPS * 32) k_sigma_partial_ffT(SigArgs a,
     const float* Rq = Rp + (long long)nS * q;
     float sl = 0.f, dl = 0.f;
     int m0 = 0;
-    for (; m0 + 32 * FFT_U <= nS; m0 += 32 * FFT_U) {
-      float rv[FFT_U];
+    // batches of FFT_U loads per lane, the next batch's loads issued before the current one is
+    // used, so that a lane always has loads in flight; each lane still takes its m in increasing
+    // order (the sums are the same bits as with one batch at a time)
+    const int nfull = nS / (32 * FFT_U);
+    float rv[FFT_U];
+    if (nfull > 0) {
 #pragma unroll
-      for (int u = 0; u < FFT_U; ++u) rv[u] = __ldg(Rq + m0 + 32 * u + lane);
+      for (int u = 0; u < FFT_U; ++u) rv[u] = __ldg(Rq + 32 * u + lane);
+    }
+    for (int b = 0; b < nfull; ++b, m0 += 32 * FFT_U) {
+      float rn[FFT_U];
+      const bool more = b + 1 < nfull;
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < FFT_U; ++u) rn[u] = __ldg(Rq + m0 + 32 * FFT_U + 32 * u + lane);
+      }
 #pragma unroll
       for (int u = 0; u < FFT_U; ++u) {
         const int m = m0 + 32 * u + lane;
@@ -281,6 +293,10 @@ __global__ void __launch_bounds__(FFT_WARPS * 32) k_sigma_partial_ffT(SigArgs a,
         const float t = rv[u] * r;
         sl += t;
         dl = fmaf(t, r, dl);
+      }
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < FFT_U; ++u) rv[u] = rn[u];
       }
     }
     for (int m = m0 + lane; m < nS; m += 32) {
