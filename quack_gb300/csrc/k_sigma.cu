@@ -593,11 +593,21 @@ __global__ void __launch_bounds__(NEWT_WARPS * 32) k_qp_newton_ff(NewtFF a, QPSt
         const float* Rq = Rp + (long long)nS * q;
         float sl = 0.f, dl = 0.f;
         int m0 = 0;
-        // batches of NEWT_U coalesced warp loads issued before their arithmetic
-        for (; m0 + 32 * NEWT_U <= nS; m0 += 32 * NEWT_U) {
-          float rv[NEWT_U];
+        // batches of NEWT_U coalesced warp loads, the next batch issued before the current one
+        // is used (each lane still takes its m in increasing order)
+        const int nfull = nS / (32 * NEWT_U);
+        float rv[NEWT_U];
+        if (nfull > 0) {
 #pragma unroll
-          for (int u = 0; u < NEWT_U; ++u) rv[u] = __ldg(Rq + m0 + 32 * u + lane);
+          for (int u = 0; u < NEWT_U; ++u) rv[u] = __ldg(Rq + 32 * u + lane);
+        }
+        for (int b = 0; b < nfull; ++b, m0 += 32 * NEWT_U) {
+          float rn[NEWT_U];
+          const bool more = b + 1 < nfull;
+          if (more) {
+#pragma unroll
+            for (int u = 0; u < NEWT_U; ++u) rn[u] = __ldg(Rq + m0 + 32 * NEWT_U + 32 * u + lane);
+          }
 #pragma unroll
           for (int u = 0; u < NEWT_U; ++u) {
             const int m = m0 + 32 * u + lane;
@@ -608,6 +618,10 @@ __global__ void __launch_bounds__(NEWT_WARPS * 32) k_qp_newton_ff(NewtFF a, QPSt
             const float t = rv[u] * r;
             sl += t;
             dl = fmaf(t, r, dl);
+          }
+          if (more) {
+#pragma unroll
+            for (int u = 0; u < NEWT_U; ++u) rv[u] = rn[u];
           }
         }
         for (int m = m0 + lane; m < nS; m += 32) {
