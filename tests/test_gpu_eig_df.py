@@ -11,7 +11,8 @@ the context setting "dsyev_df" = 1 and hold it to:
 - bitwise repetition (the same exact mat-vec accumulators as the FP64 kernel);
 - any magnitude: the matrix is scaled by a power of two before it goes to double-float;
 - the grouped launch of the batched driver in the mixed tier: its results repeat bitwise for any
-  grouping.
+  grouping;
+- a size whose per-CTA vectors live in global memory (n = 6900), for both kernels.
 """
 import numpy as np
 import pytest
@@ -109,3 +110,19 @@ def test_mixed_batched_grouped_df_repeatable(ctx):
         outs.append(dG.cpu().numpy())
     for o in outs[1:]:
         assert np.array_equal(o, outs[0], equal_nan=True)
+
+
+def test_df_vectors_in_global_memory(ctx):
+    """n = 6900: the three vectors of every CTA no longer fit in shared memory beside the tiles,
+    so both kernels keep them in global memory (the FP64 kernel from n ~ 3800 on); eigenvalues
+    against LAPACK's."""
+    n = 6900
+    rng = np.random.default_rng(17)
+    A = rng.standard_normal((n, n))
+    A = A + A.T
+    w_ref = np.linalg.eigvalsh(A)
+    scale = np.abs(w_ref).max()
+    w_df, _ = _dsyev(ctx, A, True, want_vectors=False)
+    assert np.max(np.abs(w_df - w_ref)) < 1e-11 * scale
+    w_64, _ = _dsyev(ctx, A, False, want_vectors=False)
+    assert np.max(np.abs(w_64 - w_ref)) < 1e-11 * scale
